@@ -1,0 +1,423 @@
+/*
+ * s2let_gpu.h — C ABI of libs2let_gpu.so, a GB300 (sm_103a) implementation of
+ * S2LET's scale-discretised wavelet transforms on McEwen–Wiaux (MW) sampling.
+ *
+ * Drop-in boundary.  Every s2let_* function below has the name, argument list,
+ * argument meaning and coefficient layout of the reference C API
+ * (the include/s2let headers of S2LET 2.2.7), so that a caller of the reference relinks
+ * against this library unchanged.  Each declaration cites the reference
+ * declaration it replaces.  Buffers are HOST memory, allocated by the caller
+ * (e.g. with the s2let_allocate_* helpers); complex arrays are interleaved
+ * (re, im) doubles, as C99 `double complex` and C++ `std::complex<double>` lay
+ * them out.  Calls are synchronous.
+ *
+ * Errors.  The reference prints and calls exit(1) on an invalid sampling scheme
+ * (include/s2let/s2let_error.h:13-27) and validates nothing else.  This library
+ * never exits the host process: an invalid argument or a CUDA failure leaves
+ * the outputs untouched, records a status readable with s2let_gpu_last_error()
+ * / s2let_gpu_last_error_string(), and prints one line to stderr.  Setting the
+ * environment variable S2LET_GPU_ABORT_ON_ERROR=1 restores the reference's
+ * exit(1) behaviour.
+ *
+ * Sampling.  Only S2LET_SAMPLING_MW is implemented on the GPU; MW_SS returns
+ * S2LET_GPU_ERR_UNSUPPORTED.
+ *
+ * Extensions (no reference counterpart) are prefixed s2let_gpu_: precision
+ * selection, device-pointer batched entry points on a caller stream, and the
+ * status query.
+ */
+#ifndef S2LET_GPU_H
+#define S2LET_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#include <complex>
+#define S2LET_COMPLEX(TYPE) std::complex<TYPE>
+extern "C" {
+#else
+#include <complex.h>
+#define S2LET_COMPLEX(TYPE) TYPE complex
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Types (layout identical to include/s2let/s2let_types.h:18-137)           */
+/* ------------------------------------------------------------------------ */
+
+#ifndef S2LET_GPU_NO_SSHT_TYPES
+/* Wigner recursion selector of SSHT; accepted and ignored (results are the
+ * same linear map either way).  int-sized enum as in SSHT. */
+typedef enum { SSHT_DL_RISBO = 0, SSHT_DL_TRAPANI = 1 } ssht_dl_method_t;
+#endif
+
+/* include/s2let/s2let_types.h:18-38 */
+typedef enum {
+  S2LET_SAMPLING_MW,
+  S2LET_SAMPLING_MW_SS,
+  S2LET_SAMPLING_SIZE
+} s2let_sampling_t;
+
+/* include/s2let/s2let_types.h:56-137 — field order and types must not change. */
+typedef struct {
+  int verbosity;
+  int reality;
+  int upsample;
+  double B;
+  int L;
+  int J_min;
+  int N;
+  int spin;
+  int original_spin;
+  s2let_sampling_t sampling_scheme;
+  ssht_dl_method_t dl_method;
+} s2let_parameters_t;
+
+/* ------------------------------------------------------------------------ */
+/* Tiling (host FP64; src/c/s2let_tiling.c)                                 */
+/* ------------------------------------------------------------------------ */
+
+void s2let_switch_wavtype(int typenum);                                   /* s2let_tiling.h:14 */
+int s2let_bandlimit(int j, const s2let_parameters_t *parameters);          /* s2let_tiling.h:16 */
+int s2let_L0(int j, const s2let_parameters_t *parameters);                 /* s2let_tiling.h:18 */
+int s2let_j_max(const s2let_parameters_t *parameters);                     /* s2let_tiling.h:20 */
+void s2let_tiling_axisym_allocate(double **kappa, double **kappa0,
+                                  const s2let_parameters_t *parameters);    /* s2let_tiling.h:22 */
+void s2let_tiling_axisym(double *kappa, double *kappa0,
+                         const s2let_parameters_t *parameters);             /* s2let_tiling.h:24 */
+void s2let_tiling_direction_allocate(S2LET_COMPLEX(double) **s_elm,
+                                     const s2let_parameters_t *parameters); /* s2let_tiling.h:26 */
+void s2let_tiling_direction(S2LET_COMPLEX(double) *s_elm,
+                            const s2let_parameters_t *parameters);          /* s2let_tiling.h:28 */
+void s2let_tiling_wavelet_allocate(S2LET_COMPLEX(double) **psi, double **phi,
+                                   const s2let_parameters_t *parameters);   /* s2let_tiling.h:30 */
+void s2let_tiling_wavelet(S2LET_COMPLEX(double) *psi, double *phi,
+                          const s2let_parameters_t *parameters);            /* s2let_tiling.h:32 */
+double s2let_tiling_axisym_check_identity(double *kappa, double *kappa0,
+                                          const s2let_parameters_t *parameters);  /* :34 */
+double s2let_tiling_direction_check_identity(S2LET_COMPLEX(double) *s_elm,
+                                             const s2let_parameters_t *parameters); /* :36 */
+double s2let_tiling_wavelet_check_identity(S2LET_COMPLEX(double) *psi, double *phi,
+                                           const s2let_parameters_t *parameters);   /* :38 */
+
+/* math helpers (include/s2let/s2let_math.h) */
+double s2let_math_kappa0_quadtrap_s2dw(double a, double b, int n, double B);
+double s2let_math_kappa0_quadtrap_needlet(double a, double b, int n);
+double s2let_math_spline_scalingfct(double x, double y);
+unsigned long binomial_coefficient(int n, int k, int exact);
+
+/* ------------------------------------------------------------------------ */
+/* Sizes and allocation (src/c/s2let_helper.c, src/c/s2let_alloc.c)        */
+/* ------------------------------------------------------------------------ */
+
+int s2let_n_phi(const s2let_parameters_t *parameters);      /* s2let_helper.h:8  */
+int s2let_n_theta(const s2let_parameters_t *parameters);    /* s2let_helper.h:9  */
+int s2let_n_px(const s2let_parameters_t *parameters);       /* s2let_helper.h:10 */
+int s2let_n_lm(const s2let_parameters_t *parameters);       /* s2let_helper.h:11 */
+int s2let_n_lm_scal(const s2let_parameters_t *parameters);  /* s2let_helper.h:12 */
+int s2let_n_lmn_wav(const s2let_parameters_t *parameters);  /* s2let_helper.h:13 */
+int s2let_n_gamma(const s2let_parameters_t *parameters);    /* s2let_helper.h:14 */
+int s2let_n_scal(const s2let_parameters_t *parameters);     /* s2let_helper.h:15 */
+int s2let_n_wav(const s2let_parameters_t *parameters);      /* s2let_helper.h:16 */
+int s2let_n_wav_j(int j, const s2let_parameters_t *parameters); /* s2let_helper.h:17 */
+
+void s2let_allocate_mw(S2LET_COMPLEX(double) **f, int L);              /* s2let_alloc.h:16 */
+void s2let_allocate_mw_real(double **f, int L);                        /* s2let_alloc.h:18 */
+void s2let_allocate_mwss(S2LET_COMPLEX(double) **f, int L);            /* s2let_alloc.h:20 */
+void s2let_allocate_mwss_real(double **f, int L);                      /* s2let_alloc.h:22 */
+void s2let_allocate_lm(S2LET_COMPLEX(double) **flm, int L);            /* s2let_alloc.h:24 */
+void s2let_allocate_lmn_f_wav(S2LET_COMPLEX(double) **f_wav_lmn, S2LET_COMPLEX(double) **f_scal_lm,
+                              const s2let_parameters_t *parameters);   /* s2let_alloc.h:26 */
+void s2let_allocate_f_wav(S2LET_COMPLEX(double) **f_wav, S2LET_COMPLEX(double) **f_scal,
+                          const s2let_parameters_t *parameters);       /* s2let_alloc.h:31 */
+void s2let_allocate_f_wav_real(double **f_wav, double **f_scal,
+                               const s2let_parameters_t *parameters);  /* s2let_alloc.h:36 */
+void s2let_allocate_f_wav_manual(S2LET_COMPLEX(double) **f_wav, S2LET_COMPLEX(double) **f_scal,
+                                 int *wav_bandlimits, int scal_bandlimit, int N, int J,
+                                 const s2let_parameters_t *parameters); /* s2let_alloc.h:41 */
+
+/* ------------------------------------------------------------------------ */
+/* Directional analysis (src/c/s2let_analysis.c; s2let_analysis.h:16-77)   */
+/* ------------------------------------------------------------------------ */
+
+void s2let_analysis_lm2lmn(S2LET_COMPLEX(double) *f_wav_lmn, S2LET_COMPLEX(double) *f_scal_lm,
+                           const S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *wav_lm,
+                           const double *scal_l, const s2let_parameters_t *parameters); /* :16 */
+void s2let_analysis_lm2lmn_real(S2LET_COMPLEX(double) *f_wav_lmn, S2LET_COMPLEX(double) *f_scal_lm,
+                                const S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *wav_lm,
+                                const double *scal_l, const s2let_parameters_t *parameters); /* :24 */
+void s2let_analysis_lm2wav_manual(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
+                                  const S2LET_COMPLEX(double) *flm, const double *scal_l,
+                                  const S2LET_COMPLEX(double) *wav_lm, const int scal_bandlimit,
+                                  const int *wav_bandlimits, int J, int L, int spin, int N); /* :32 */
+void s2let_analysis_lm2wav(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
+                           const S2LET_COMPLEX(double) *flm,
+                           const s2let_parameters_t *parameters);                /* :45 */
+void s2let_analysis_lm2wav_real(double *f_wav, double *f_scal, const S2LET_COMPLEX(double) *flm,
+                                const s2let_parameters_t *parameters);           /* :52 */
+void s2let_analysis_px2wav(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
+                           const S2LET_COMPLEX(double) *f,
+                           const s2let_parameters_t *parameters);                /* :59 */
+void s2let_analysis_px2wav_real(double *f_wav, double *f_scal, const double *f,
+                                const s2let_parameters_t *parameters);           /* :66 */
+
+/* ------------------------------------------------------------------------ */
+/* Directional synthesis (src/c/s2let_synthesis.c; s2let_synthesis.h:16-77) */
+/* ------------------------------------------------------------------------ */
+
+void s2let_synthesis_lmn2lm(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav_lmn,
+                            const S2LET_COMPLEX(double) *f_scal_lm, const S2LET_COMPLEX(double) *wav_lm,
+                            const double *scal_l, const s2let_parameters_t *parameters); /* :16 */
+void s2let_synthesis_lmn2lm_real(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav_lmn,
+                                 const S2LET_COMPLEX(double) *f_scal_lm,
+                                 const S2LET_COMPLEX(double) *wav_lm, const double *scal_l,
+                                 const s2let_parameters_t *parameters);          /* :24 */
+void s2let_synthesis_wav2lm_manual(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav,
+                                   const S2LET_COMPLEX(double) *f_scal, const double *scal_l,
+                                   const S2LET_COMPLEX(double) *wav_lm, const int scal_bandlimit,
+                                   const int *wav_bandlimits, int J, int L, int spin, int N); /* :32 */
+void s2let_synthesis_wav2lm(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav,
+                            const S2LET_COMPLEX(double) *f_scal,
+                            const s2let_parameters_t *parameters);               /* :45 */
+void s2let_synthesis_wav2lm_real(S2LET_COMPLEX(double) *flm, const double *f_wav,
+                                 const double *f_scal, const s2let_parameters_t *parameters); /* :52 */
+void s2let_synthesis_wav2px(S2LET_COMPLEX(double) *f, const S2LET_COMPLEX(double) *f_wav,
+                            const S2LET_COMPLEX(double) *f_scal,
+                            const s2let_parameters_t *parameters);               /* :59 */
+void s2let_synthesis_wav2px_real(double *f, const double *f_wav, const double *f_scal,
+                                 const s2let_parameters_t *parameters);          /* :66 */
+
+/* ------------------------------------------------------------------------ */
+/* Adjoints (src/c/s2let_analysis_adjoint.c, src/c/s2let_synthesis_adjoint.c) */
+/* ------------------------------------------------------------------------ */
+
+void s2let_analysis_adjoint_lmn2lm(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav_lmn,
+                                   const S2LET_COMPLEX(double) *f_scal_lm,
+                                   const S2LET_COMPLEX(double) *wav_lm, const double *scal_l,
+                                   const s2let_parameters_t *parameters);        /* s2let_analysis_adjoint.h:16 */
+void s2let_analysis_adjoint_lmn2lm_real(S2LET_COMPLEX(double) *flm,
+                                        const S2LET_COMPLEX(double) *f_wav_lmn,
+                                        const S2LET_COMPLEX(double) *f_scal_lm,
+                                        const S2LET_COMPLEX(double) *wav_lm, const double *scal_l,
+                                        const s2let_parameters_t *parameters);   /* :24 */
+void s2let_analysis_adjoint_wav2lm_manual(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav,
+                                          const S2LET_COMPLEX(double) *f_scal, const double *scal_l,
+                                          const S2LET_COMPLEX(double) *wav_lm,
+                                          const int scal_bandlimit, const int *wav_bandlimits,
+                                          int J, int L, int spin, int N);        /* :48 */
+void s2let_analysis_adjoint_wav2lm(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav,
+                                   const S2LET_COMPLEX(double) *f_scal,
+                                   const s2let_parameters_t *parameters);        /* :61 */
+void s2let_analysis_adjoint_wav2lm_real(S2LET_COMPLEX(double) *flm, const double *f_wav,
+                                        const double *f_scal,
+                                        const s2let_parameters_t *parameters);   /* :67 */
+void s2let_analysis_adjoint_wav2px(S2LET_COMPLEX(double) *f, const S2LET_COMPLEX(double) *f_wav,
+                                   const S2LET_COMPLEX(double) *f_scal,
+                                   const s2let_parameters_t *parameters);        /* :73 */
+void s2let_analysis_adjoint_wav2px_real(double *f, const double *f_wav, const double *f_scal,
+                                        const s2let_parameters_t *parameters);   /* :79 */
+
+void s2let_synthesis_adjoint_lm2lmn(S2LET_COMPLEX(double) *f_wav_lmn, S2LET_COMPLEX(double) *f_scal_lm,
+                                    const S2LET_COMPLEX(double) *flm,
+                                    const S2LET_COMPLEX(double) *wav_lm, const double *scal_l,
+                                    const s2let_parameters_t *parameters);       /* s2let_synthesis_adjoint.h:16 */
+void s2let_synthesis_adjoint_lm2lmn_real(S2LET_COMPLEX(double) *f_wav_lmn,
+                                         S2LET_COMPLEX(double) *f_scal_lm,
+                                         const S2LET_COMPLEX(double) *flm,
+                                         const S2LET_COMPLEX(double) *wav_lm, const double *scal_l,
+                                         const s2let_parameters_t *parameters);  /* :24 */
+void s2let_synthesis_adjoint_lm2wav_manual(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
+                                           const S2LET_COMPLEX(double) *flm, const double *scal_l,
+                                           const S2LET_COMPLEX(double) *wav_lm,
+                                           const int scal_bandlimit, const int *wav_bandlimits,
+                                           int J, int L, int spin, int N);       /* :48 */
+void s2let_synthesis_adjoint_lm2wav(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
+                                    const S2LET_COMPLEX(double) *flm,
+                                    const s2let_parameters_t *parameters);       /* :61 */
+void s2let_synthesis_adjoint_lm2wav_real(double *f_wav, double *f_scal,
+                                         const S2LET_COMPLEX(double) *flm,
+                                         const s2let_parameters_t *parameters);  /* :67 */
+void s2let_synthesis_adjoint_px2wav(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
+                                    const S2LET_COMPLEX(double) *f,
+                                    const s2let_parameters_t *parameters);       /* :73 */
+void s2let_synthesis_adjoint_px2wav_real(double *f_wav, double *f_scal, const double *f,
+                                         const s2let_parameters_t *parameters);  /* :79 */
+
+/* ------------------------------------------------------------------------ */
+/* Axisymmetric wavelets (src/c/s2let_transform_axisym_lm.c, _mw.c)         */
+/* ------------------------------------------------------------------------ */
+
+void s2let_transform_axisym_lm_allocate_f_wav(S2LET_COMPLEX(double) **f_wav_lm,
+                                              S2LET_COMPLEX(double) **f_scal_lm,
+                                              const s2let_parameters_t *parameters); /* s2let_transform_axisym_lm.h:14 */
+void s2let_transform_axisym_lm_allocate_f_wav_multires(S2LET_COMPLEX(double) **f_wav_lm,
+                                                       S2LET_COMPLEX(double) **f_scal_lm,
+                                                       const s2let_parameters_t *parameters); /* :19 */
+void s2let_transform_axisym_lm_allocate_wav(double **wav_lm, double **scal_lm,
+                                            const s2let_parameters_t *parameters); /* :24 */
+void s2let_transform_axisym_lm_wav(double *wav_lm, double *scal_lm,
+                                   const s2let_parameters_t *parameters);          /* :27 */
+void s2let_transform_axisym_lm_wav_analysis(S2LET_COMPLEX(double) *f_wav_lm,
+                                            S2LET_COMPLEX(double) *f_scal_lm,
+                                            const S2LET_COMPLEX(double) *flm, const double *wav_lm,
+                                            const double *scal_lm,
+                                            const s2let_parameters_t *parameters);   /* :30 */
+void s2let_transform_axisym_lm_wav_synthesis(S2LET_COMPLEX(double) *flm,
+                                             const S2LET_COMPLEX(double) *f_wav_lm,
+                                             const S2LET_COMPLEX(double) *f_scal_lm,
+                                             const double *wav_lm, const double *scal_lm,
+                                             const s2let_parameters_t *parameters);  /* :37 */
+void s2let_transform_axisym_lm_wav_analysis_multires(S2LET_COMPLEX(double) *f_wav_lm,
+                                                     S2LET_COMPLEX(double) *f_scal_lm,
+                                                     const S2LET_COMPLEX(double) *flm,
+                                                     const double *wav_lm, const double *scal_lm,
+                                                     const s2let_parameters_t *parameters); /* :44 */
+void s2let_transform_axisym_lm_wav_synthesis_multires(S2LET_COMPLEX(double) *flm,
+                                                      const S2LET_COMPLEX(double) *f_wav_lm,
+                                                      const S2LET_COMPLEX(double) *f_scal_lm,
+                                                      const double *wav_lm, const double *scal_lm,
+                                                      const s2let_parameters_t *parameters); /* :51 */
+
+void s2let_transform_axisym_allocate_mw_f_wav(S2LET_COMPLEX(double) **f_wav, S2LET_COMPLEX(double) **f_scal,
+                                              const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:13 */
+void s2let_transform_axisym_allocate_mw_f_wav_multires(S2LET_COMPLEX(double) **f_wav,
+                                                       S2LET_COMPLEX(double) **f_scal,
+                                                       const s2let_parameters_t *parameters); /* :14 */
+void s2let_transform_axisym_allocate_mw_f_wav_real(double **f_wav, double **f_scal,
+                                                   const s2let_parameters_t *parameters); /* :15 */
+void s2let_transform_axisym_allocate_mw_f_wav_multires_real(double **f_wav, double **f_scal,
+                                                            const s2let_parameters_t *parameters); /* :16 */
+void s2let_transform_axisym_wav_analysis_mw(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
+                                            const S2LET_COMPLEX(double) *f,
+                                            const s2let_parameters_t *parameters); /* :18 */
+void s2let_transform_axisym_wav_analysis_adjoint_mw(S2LET_COMPLEX(double) *f,
+                                                    const S2LET_COMPLEX(double) *f_wav,
+                                                    const S2LET_COMPLEX(double) *f_scal,
+                                                    const s2let_parameters_t *parameters); /* :19 */
+void s2let_transform_axisym_wav_synthesis_mw(S2LET_COMPLEX(double) *f, const S2LET_COMPLEX(double) *f_wav,
+                                             const S2LET_COMPLEX(double) *f_scal,
+                                             const s2let_parameters_t *parameters); /* :20 */
+void s2let_transform_axisym_wav_synthesis_adjoint_mw(S2LET_COMPLEX(double) *f_wav,
+                                                     S2LET_COMPLEX(double) *f_scal,
+                                                     const S2LET_COMPLEX(double) *f,
+                                                     const s2let_parameters_t *parameters); /* :21 */
+void s2let_transform_axisym_wav_analysis_mw_multires(S2LET_COMPLEX(double) *f_wav,
+                                                     S2LET_COMPLEX(double) *f_scal,
+                                                     const S2LET_COMPLEX(double) *f,
+                                                     const s2let_parameters_t *parameters); /* :23 */
+void s2let_transform_axisym_wav_analysis_adjoint_mw_multires(S2LET_COMPLEX(double) *f,
+                                                             const S2LET_COMPLEX(double) *f_wav,
+                                                             const S2LET_COMPLEX(double) *f_scal,
+                                                             const s2let_parameters_t *parameters); /* :24 */
+void s2let_transform_axisym_wav_synthesis_mw_multires(S2LET_COMPLEX(double) *f,
+                                                      const S2LET_COMPLEX(double) *f_wav,
+                                                      const S2LET_COMPLEX(double) *f_scal,
+                                                      const s2let_parameters_t *parameters); /* :25 */
+void s2let_transform_axisym_wav_synthesis_adjoint_mw_multires(S2LET_COMPLEX(double) *f_wav,
+                                                              S2LET_COMPLEX(double) *f_scal,
+                                                              const S2LET_COMPLEX(double) *f,
+                                                              const s2let_parameters_t *parameters); /* :26 */
+void s2let_transform_axisym_wav_analysis_mw_real(double *f_wav, double *f_scal, const double *f,
+                                                 const s2let_parameters_t *parameters); /* :28 */
+void s2let_transform_axisym_wav_analysis_adjoint_mw_real(double *f, const double *f_wav,
+                                                         const double *f_scal,
+                                                         const s2let_parameters_t *parameters); /* :29 */
+void s2let_transform_axisym_wav_synthesis_mw_real(double *f, const double *f_wav, const double *f_scal,
+                                                  const s2let_parameters_t *parameters); /* :30 */
+void s2let_transform_axisym_wav_synthesis_adjoint_mw_real(double *f_wav, double *f_scal, const double *f,
+                                                          const s2let_parameters_t *parameters); /* :31 */
+void s2let_transform_axisym_wav_analysis_mw_multires_real(double *f_wav, double *f_scal,
+                                                          const double *f,
+                                                          const s2let_parameters_t *parameters); /* :33 */
+void s2let_transform_axisym_wav_analysis_adjoint_mw_multires_real(double *f, const double *f_wav,
+                                                                  const double *f_scal,
+                                                                  const s2let_parameters_t *parameters); /* :34 */
+void s2let_transform_axisym_wav_synthesis_mw_multires_real(double *f, const double *f_wav,
+                                                           const double *f_scal,
+                                                           const s2let_parameters_t *parameters); /* :35 */
+void s2let_transform_axisym_wav_synthesis_adjoint_mw_multires_real(double *f_wav, double *f_scal,
+                                                                   const double *f,
+                                                                   const s2let_parameters_t *parameters); /* :36 */
+void s2let_transform_axisym_wav_hardthreshold_real(double *g_wav, const double *threshold,
+                                                   const s2let_parameters_t *parameters); /* :38 */
+void s2let_transform_axisym_wav_hardthreshold_multires_real(double *g_wav, const double *threshold,
+                                                            const s2let_parameters_t *parameters); /* :39 */
+
+/* ------------------------------------------------------------------------ */
+/* Plain MW spherical-harmonic transforms (src/c/s2let_mw.c; s2let_mw.h)    */
+/* ------------------------------------------------------------------------ */
+
+void s2let_mw_map2alm_real(S2LET_COMPLEX(double) *flm, const double *f, int L);          /* :15 */
+void s2let_mw_alm2map_real(double *f, const S2LET_COMPLEX(double) *flm, int L);          /* :16 */
+void s2let_mw_alm2map(S2LET_COMPLEX(double) *f, const S2LET_COMPLEX(double) *flm, int L, int spin); /* :17 */
+void s2let_mw_map2alm(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f, int L, int spin); /* :18 */
+double s2let_mw_power(S2LET_COMPLEX(double) *flm, int L);                                /* :20 */
+double s2let_mw_power_real(double *flm, int L);                                          /* :21 */
+double s2let_lm_power(S2LET_COMPLEX(double) *flm, int L);                                /* s2let_lm.h:15 */
+
+/* ------------------------------------------------------------------------ */
+/* GB300 extensions (no reference counterpart)                              */
+/* ------------------------------------------------------------------------ */
+
+enum {
+  S2LET_GPU_OK = 0,
+  S2LET_GPU_ERR_INVALID = 1,     /* bad parameter (L<1, N<1, B<=1, |spin|>=L, ...) */
+  S2LET_GPU_ERR_UNSUPPORTED = 2, /* e.g. MW_SS sampling, spline/needlet kernels on GPU paths */
+  S2LET_GPU_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  S2LET_GPU_ERR_NOMEM = 4,       /* device or host allocation failed */
+  S2LET_GPU_ERR_NO_DEVICE = 5    /* no usable CUDA device */
+};
+
+/* Status of the last call made on this thread (0 = success). */
+int s2let_gpu_last_error(void);
+const char *s2let_gpu_last_error_string(void);
+
+/* Arithmetic used by subsequent calls of this thread.
+ *   0 = FP64 throughout (default);
+ *   1 = mixed: FP64 Wigner tables and tiling, split-precision tensor-core Legendre
+ *       contraction with FP32 accumulation and FP64 combination. */
+int s2let_gpu_set_precision(int mode);
+int s2let_gpu_get_precision(void);
+
+/* Drops cached plans (Wigner tables, FFT chirps) and frees their device memory. */
+void s2let_gpu_release_plans(void);
+/* Bytes of device memory currently held by cached plans. */
+size_t s2let_gpu_plan_bytes(void);
+
+/*
+ * Batched device-pointer entry points.  All pointers are DEVICE pointers; `stream`
+ * is a cudaStream_t (NULL = default stream).  `nbatch` maps share one parameter
+ * set; map b starts at b*stride of each array, strides being the single-map sizes
+ * (s2let_n_px, s2let_n_wav, s2let_n_scal elements).  Asynchronous with respect to
+ * the host; the status covers launch-time errors.  Real-signal layouts as the
+ * _real host functions.
+ */
+int s2let_gpu_analysis_px2wav_real_batch(double *f_wav, double *f_scal, const double *f, int nbatch,
+                                         const s2let_parameters_t *parameters, void *stream);
+int s2let_gpu_synthesis_wav2px_real_batch(double *f, const double *f_wav, const double *f_scal,
+                                          int nbatch, const s2let_parameters_t *parameters,
+                                          void *stream);
+int s2let_gpu_analysis_px2wav_batch(void *f_wav, void *f_scal, const void *f, int nbatch,
+                                    const s2let_parameters_t *parameters, void *stream);
+int s2let_gpu_synthesis_wav2px_batch(void *f, const void *f_wav, const void *f_scal, int nbatch,
+                                     const s2let_parameters_t *parameters, void *stream);
+/* Exact adjoints (backward of the autograd op), same conventions. */
+int s2let_gpu_analysis_adjoint_wav2px_real_batch(double *f, const double *f_wav, const double *f_scal,
+                                                 int nbatch, const s2let_parameters_t *parameters,
+                                                 void *stream);
+int s2let_gpu_synthesis_adjoint_px2wav_real_batch(double *f_wav, double *f_scal, const double *f,
+                                                  int nbatch, const s2let_parameters_t *parameters,
+                                                  void *stream);
+int s2let_gpu_analysis_adjoint_wav2px_batch(void *f, const void *f_wav, const void *f_scal,
+                                            int nbatch, const s2let_parameters_t *parameters,
+                                            void *stream);
+int s2let_gpu_synthesis_adjoint_px2wav_batch(void *f_wav, void *f_scal, const void *f, int nbatch,
+                                             const s2let_parameters_t *parameters, void *stream);
+
+/* Number of this library's kernel launches since load (instrumentation). */
+uint64_t s2let_gpu_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* S2LET_GPU_H */
