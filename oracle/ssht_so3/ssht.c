@@ -122,14 +122,16 @@ void oracle_wigner_d_column(double *out, int L, int m, int n, double theta) {
   int ka, kb;
   double sign = 1.0;
   int k; /* binomial C(2 l0, k) */
+  /* closed forms of d^{l0}: second index = l0 gives sqrt(C(2l0, l0+m)) c^{l0+m} s^{l0-m};
+   * the others follow from d_{mn} = (-1)^{m-n} d_{nm} and d_{-m,-n} = (-1)^{m-n} d_{mn} */
   if (l0 == m) {
-    ka = m + n; kb = m - n; k = m + n;
+    ka = m + n; kb = m - n; k = m + n; sign = neg1(l0 - n);
   } else if (l0 == -m) {
-    ka = l0 - n; kb = l0 + n; k = l0 - n; sign = neg1(l0 + n);
+    ka = l0 - n; kb = l0 + n; k = l0 - n;
   } else if (l0 == n) {
-    ka = l0 + m; kb = l0 - m; k = l0 + m; sign = neg1(l0 - m);
+    ka = l0 + m; kb = l0 - m; k = l0 + m;
   } else {
-    ka = l0 - m; kb = l0 + m; k = l0 - m;
+    ka = l0 - m; kb = l0 + m; k = l0 - m; sign = neg1(m + l0);
   }
   double lg = 0.5 * (lgamma(2.0 * l0 + 1) - lgamma(k + 1.0) - lgamma(2.0 * l0 - k + 1.0));
   double lv = lg + (ka ? ka * log(fabs(c)) : 0.0) + (kb ? kb * log(fabs(s)) : 0.0);

@@ -1,0 +1,1008 @@
+// Executors: the reference's wavelet entry points composed from the FP64
+// kernels (ring DFTs, Wigner contractions, gamma DFTs, tiling merge), plus the
+// C ABI wrappers (host-pointer drop-ins and device-pointer batch extensions).
+//
+// Data flow of one directional analysis at scale j (all maps of a batch at once):
+//   flm --(l->t contraction, table D_n, weight conj psi_j(l,n))--> G_n[t][m]
+//       --(gamma synthesis over n)--> spectra_g[t][m] --(inverse ring DFT)--> f_wav_j
+// which fuses s2let_analysis_lm2lmn (src/c/s2let_analysis.c:28-89) with the SO3
+// inverse (so3_core_inverse_direct, called at src/c/s2let_analysis.c:348): the
+// normalisations 8pi^2/(2l+1), (2l+1)/(8pi^2), (-1)^n and sqrt((2l+1)/4pi)
+// cancel, leaving conj(psi_j(l,n)) as the only per-l weight.  Synthesis runs the
+// mirror image with the forward tables Q_n and merges all (j, n) in one kernel.
+// The axisymmetric transforms are the same machinery with one direction (n = 0)
+// per scale and the axisymmetric kernels as weights.
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "host_layer.h"
+#include "kernels.h"
+#include "plan.h"
+#include "runtime.h"
+
+namespace s2g {
+
+std::atomic<uint64_t> g_launches{0};
+int current_kernel_type();  // host_layer.cpp
+
+namespace {
+
+thread_local int t_status = 0;
+thread_local std::string t_message;
+thread_local int t_precision = 0;
+
+template <class T>
+T *upload(const std::vector<T> &v) {
+  T *d = nullptr;
+  S2G_CUDA(cudaMalloc(&d, sizeof(T) * std::max<size_t>(1, v.size())));
+  if (!v.empty()) S2G_CUDA(cudaMemcpy(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return d;
+}
+
+// ---------------------------------------------------------------------------
+// wavelet plan: one tiling (standard, manual or axisymmetric) of one signal type
+// ---------------------------------------------------------------------------
+struct Scale {
+  int bl = 1, Nj = 1, ng = 1;
+  int64_t woff = 0;              // offset of the scale in f_wav
+  std::vector<int> ns;           // directions visited
+  int *d_ns = nullptr;
+  std::vector<int64_t> w_pair;   // per direction: [w(l,n) | w(l,-n)], 2*bl entries (merge weights)
+  std::vector<int64_t> w_split;  // per direction: split weight, bl entries
+  std::vector<int64_t> z_off;    // per direction: z block (bl^2) inside one map
+  int64_t w_axi = -1;            // axisymmetric: per-l kernel weight (bl entries)
+};
+
+struct WavPlan {
+  int L = 0, s = 0;
+  bool real = false, axisym = false;
+  int bl_scal = 1, scal_lmin = 0;
+  std::vector<Scale> sc;
+  double2 *d_w = nullptr;
+  int64_t w_phi = 0, w_cl = 0;
+  MergePair *d_pairs = nullptr;
+  int npairs = 0;
+  int64_t z_per_map = 0;
+  int max_bl = 1, max_nn = 1, max_ng = 1;
+  void release() {
+    cudaFree(d_w);
+    cudaFree(d_pairs);
+    for (auto &x : sc) cudaFree(x.d_ns);
+    d_w = nullptr;
+    d_pairs = nullptr;
+  }
+};
+
+// Inputs of plan construction.
+struct PlanSpec {
+  int L = 0, spin = 0;
+  bool real = false, axisym = false;
+  int bl_scal = 1, scal_lmin = 0;
+  std::vector<int> jrow, bl, Nj;  // per scale: psi row (or axisym kernel row), band-limits
+  std::vector<int64_t> woff;      // per scale f_wav offsets
+  const cplx *psi = nullptr;      // rows of L^2 (directional)
+  const double *axi = nullptr;    // rows of L (axisymmetric kernels)
+  const double *phi = nullptr;    // scaling weights, length L
+  bool split_conj = true;         // split multiplies by conj(psi) (else psi)
+  bool merge_conj = false;        // merge multiplies by conj(psi) (else psi)
+};
+
+std::unique_ptr<WavPlan> build_plan(const PlanSpec &ps) {
+  auto P = std::make_unique<WavPlan>();
+  P->L = ps.L;
+  P->s = ps.real ? 0 : ps.spin;
+  P->real = ps.real;
+  P->axisym = ps.axisym;
+  P->bl_scal = ps.bl_scal;
+  P->scal_lmin = ps.scal_lmin;
+  const int L = ps.L;
+  std::vector<double2> w;
+  auto push = [&w](double re, double im) { w.push_back(make_double2(re, im)); };
+  P->w_phi = 0;
+  for (int l = 0; l < L; ++l) push(ps.phi[l], 0.0);
+  P->w_cl = (int64_t)w.size();
+  for (int l = 0; l < L; ++l) push(((P->s & 1) ? -1.0 : 1.0) * sqrt((2.0 * l + 1.0) / (4.0 * kPi)), 0.0);
+  std::vector<MergePair> pairs;
+  const int nsc = (int)ps.bl.size();
+  P->sc.resize(nsc);
+  for (int k = 0; k < nsc; ++k) {
+    Scale &sd = P->sc[k];
+    sd.bl = ps.bl[k];
+    sd.Nj = ps.Nj[k];
+    sd.woff = ps.woff[k];
+    const int bl = sd.bl, jr = ps.jrow[k];
+    if (ps.axisym) {
+      sd.ns = {0};
+      sd.ng = 1;
+      sd.w_axi = (int64_t)w.size();
+      for (int l = 0; l < bl; ++l) push(ps.axi[(size_t)jr * L + l], 0.0);
+    } else {
+      sd.ng = 2 * sd.Nj - 1;
+      if (ps.real)
+        for (int n = 1 - sd.Nj % 2; n < sd.Nj; n += 2) sd.ns.push_back(n);
+      else
+        for (int n = -sd.Nj + 1; n < sd.Nj; n += 2) sd.ns.push_back(n);
+    }
+    for (int n : sd.ns) {
+      sd.w_pair.push_back((int64_t)w.size());
+      for (int sgn = 0; sgn < 2; ++sgn) {
+        const int nn = sgn == 0 ? n : -n;
+        for (int l = 0; l < bl; ++l) {
+          cplx v = 1.0;
+          if (!ps.axisym) {
+            v = (std::abs(nn) <= l) ? ps.psi[(size_t)jr * L * L + l * l + l + nn] : cplx(0.0);
+            if (ps.merge_conj) v = std::conj(v);
+          }
+          push(v.real(), v.imag());
+        }
+      }
+      sd.w_split.push_back((int64_t)w.size());
+      for (int l = 0; l < bl; ++l) {
+        cplx v = 1.0;
+        if (!ps.axisym) {
+          v = (std::abs(n) <= l) ? ps.psi[(size_t)jr * L * L + l * l + l + n] : cplx(0.0);
+          if (ps.split_conj) v = std::conj(v);
+        }
+        push(v.real(), v.imag());
+      }
+      sd.z_off.push_back(P->z_per_map);
+      MergePair mp;
+      mp.off = P->z_per_map;
+      mp.bl = bl;
+      mp.n = n;
+      mp.lmin = (ps.real || ps.axisym) ? 0 : std::abs(ps.spin);
+      mp.woff = sd.w_pair.back();
+      pairs.push_back(mp);
+      P->z_per_map += (int64_t)bl * bl;
+    }
+    P->max_bl = std::max(P->max_bl, bl);
+    P->max_nn = std::max(P->max_nn, (int)sd.ns.size());
+    P->max_ng = std::max(P->max_ng, sd.ng);
+  }
+  P->npairs = (int)pairs.size();
+  P->d_w = upload(w);
+  P->d_pairs = upload(pairs);
+  for (auto &sd : P->sc) sd.d_ns = upload(sd.ns);
+  // build the Wigner tables and FFT data now, outside the transforms' timing
+  wigner_table(L, std::abs(P->s));
+  wigner_table(ps.bl_scal, 0);
+  for (auto &sd : P->sc)
+    for (int n : sd.ns) wigner_table(sd.bl, std::abs(n));
+  ring_fft(2 * L - 1);
+  ring_fft(2 * ps.bl_scal - 1);
+  for (auto &sd : P->sc) ring_fft(2 * sd.bl - 1);
+  return P;
+}
+
+// standard (tiling from the parameters), cached per parameter set ------------
+struct PlanKey {
+  int L, J_min, N, spin, original_spin, upsample, reality, real, axisym, multires, kernel;
+  double B;
+  bool operator<(const PlanKey &o) const { return std::memcmp(this, &o, sizeof(PlanKey)) < 0; }
+};
+std::mutex g_plan_mu;
+std::map<PlanKey, std::unique_ptr<WavPlan>> g_plans;
+
+const WavPlan &directional_plan(const s2let_parameters_t &p, bool real) {
+  PlanKey key;
+  std::memset(&key, 0, sizeof key);
+  key.L = p.L;
+  key.J_min = p.J_min;
+  key.N = p.N;
+  key.spin = real ? 0 : p.spin;
+  key.original_spin = p.original_spin;
+  key.upsample = p.upsample;
+  key.reality = p.reality;
+  key.real = real;
+  key.kernel = current_kernel_type();
+  key.B = p.B;
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  auto it = g_plans.find(key);
+  if (it != g_plans.end()) return *it->second;
+  s2let_parameters_t q = p;
+  if (real) {
+    q.reality = 1;
+    q.spin = 0;
+  }
+  const Layout g = make_layout(q, real);
+  const int L = p.L;
+  std::vector<cplx> psi((size_t)(g.J + 1) * L * L, 0.0);
+  std::vector<double> phi(L, 0.0);
+  tiling_wavelet(psi.data(), phi.data(), q);
+  PlanSpec ps;
+  ps.L = L;
+  ps.spin = q.spin;
+  ps.real = real;
+  ps.bl_scal = g.bl_scal;
+  ps.jrow = g.j;
+  ps.bl = g.bl;
+  ps.Nj = g.Nj;
+  ps.woff.assign(g.woff.begin(), g.woff.end() - 1);
+  ps.psi = psi.data();
+  ps.phi = phi.data();
+  auto P = build_plan(ps);
+  const WavPlan &ref = *P;
+  g_plans.emplace(key, std::move(P));
+  return ref;
+}
+
+const WavPlan &axisym_plan(const s2let_parameters_t &p, bool real, bool multires) {
+  PlanKey key;
+  std::memset(&key, 0, sizeof key);
+  key.L = p.L;
+  key.J_min = p.J_min;
+  key.real = real;
+  key.axisym = 1;
+  key.multires = multires;
+  key.kernel = current_kernel_type();
+  key.B = p.B;
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  auto it = g_plans.find(key);
+  if (it != g_plans.end()) return *it->second;
+  const int L = p.L, J = j_max(p);
+  std::vector<double> wav((size_t)(J + 1) * L, 0.0), scal(L, 0.0);
+  axisym_kernels(wav.data(), scal.data(), p);
+  PlanSpec ps;
+  ps.L = L;
+  ps.spin = 0;
+  ps.real = real;
+  ps.axisym = true;
+  ps.bl_scal = multires ? std::min(bandlimit(p.J_min - 1, p), L) : L;
+  int64_t off = 0;
+  for (int j = p.J_min; j <= J; ++j) {
+    const int bl = multires ? std::min(bandlimit(j, p), L) : L;
+    ps.jrow.push_back(j);
+    ps.bl.push_back(bl);
+    ps.Nj.push_back(1);
+    ps.woff.push_back(off);
+    off += (int64_t)bl * (2 * bl - 1);
+  }
+  ps.axi = wav.data();
+  ps.phi = scal.data();
+  auto P = build_plan(ps);
+  const WavPlan &ref = *P;
+  g_plans.emplace(key, std::move(P));
+  return ref;
+}
+
+// ---------------------------------------------------------------------------
+// full-band spin-s spherical-harmonic transforms (MW)
+// ---------------------------------------------------------------------------
+
+struct Sht {
+  int L, s;
+  bool real;
+  const double2 *cl;  // (-1)^s sqrt((2l+1)/4pi), l < L (device)
+};
+Sht sht_of(const WavPlan &P) { return Sht{P.L, P.s, P.real, P.d_w + P.w_cl}; }
+
+// flm (nb x L^2, zero outside the computed range) <- forward transform of maps
+// (or the adjoint of the inverse)
+void sht_forward(const Sht &H, const void *f, int64_t fstride, double2 *flm, int nb, Scratch &S,
+                 bool adjoint_of_inverse) {
+  const int L = H.L, s = H.s, K = 2 * L - 1;
+  const bool real = H.real;
+  const int sw = real ? L : K, mlo = real ? 0 : -(L - 1);
+  double2 *spec = S.get<double2>((int64_t)nb * L * sw);
+  ring_forward(f, K, fstride, L, spec, sw, sw, mlo, nb * L, L, real, S.st);
+  S2G_CUDA(cudaMemsetAsync(flm, 0, sizeof(double2) * nb * L * L, S.st));
+  T2L a{};
+  a.tb = &wigner_table(L, std::abs(s));
+  a.n = -s;
+  a.use_q = !adjoint_of_inverse;
+  a.mlo = mlo;
+  a.mhi = L - 1;
+  a.in = spec;
+  a.is = (int64_t)L * sw;
+  a.iw = sw;
+  a.imlo = mlo;
+  a.w = H.cl;
+  a.wscale = adjoint_of_inverse ? 1.0 : 2.0 * kPi / K;
+  a.lmin = std::abs(s);
+  a.y = flm;
+  a.ys = (int64_t)L * L;
+  a.nb = nb;
+  contract_t2l(a, S.st);
+}
+
+// maps <- inverse transform (or adjoint of the forward) of flm
+void sht_inverse(const Sht &H, const double2 *flm, bool flm_half, void *f, int64_t fstride, int nb,
+                 Scratch &S, bool adjoint_of_forward) {
+  const int L = H.L, s = H.s, K = 2 * L - 1;
+  const bool real = H.real;
+  const int sw = real ? L : K, mlo = real ? 0 : -(L - 1);
+  double2 *spec = S.get<double2>((int64_t)nb * L * sw);
+  L2T a{};
+  a.tb = &wigner_table(L, std::abs(s));
+  a.n = -s;
+  a.use_q = adjoint_of_forward;
+  a.mlo = mlo;
+  a.mhi = L - 1;
+  a.x = flm;
+  a.xs = (int64_t)L * L;
+  a.xL = L;
+  a.x_half = flm_half;
+  a.w = H.cl;
+  a.wscale = adjoint_of_forward ? 2.0 * kPi / K : 1.0;
+  a.lmin = std::abs(s);
+  a.out = spec;
+  a.os = (int64_t)L * sw;
+  a.ow = sw;
+  a.omlo = mlo;
+  a.nb = nb;
+  contract_l2t(a, S.st);
+  ring_inverse(spec, sw, sw, mlo, f, K, fstride, L, nb * L, L, real, S.st);
+}
+
+// ---------------------------------------------------------------------------
+// harmonic <-> wavelet space
+// ---------------------------------------------------------------------------
+
+enum SplitMode { SPLIT_ANALYSIS, SPLIT_SYNTH_ADJ };
+enum MergeMode { MERGE_SYNTHESIS, MERGE_ANALYSIS_ADJ };
+const double kSqrt2Pi = 2.5066282746310005024;
+
+// flm -> (f_wav, f_scal).  SPLIT_ANALYSIS: lm2wav.  SPLIT_SYNTH_ADJ: adjoint of wav2lm.
+void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_half, void *f_wav,
+               int64_t wstride, void *f_scal, int64_t sstride, int nb, Scratch &S) {
+  const bool real = P.real;
+  const int L = P.L;
+  const size_t esz = real ? sizeof(double) : sizeof(double2);
+  const bool adj = (mode == SPLIT_SYNTH_ADJ);
+  // scaling function: spin-0 transform at bl_scal
+  {
+    const int bs = P.bl_scal, Ks = 2 * bs - 1;
+    const int sw = real ? bs : Ks, mlo = real ? 0 : -(bs - 1);
+    double2 *spec = S.get<double2>((int64_t)nb * bs * sw);
+    L2T a{};
+    a.tb = &wigner_table(bs, 0);
+    a.n = 0;
+    a.use_q = adj;
+    a.mlo = mlo;
+    a.mhi = bs - 1;
+    a.x = flm;
+    a.xs = (int64_t)L * L;
+    a.xL = L;
+    a.x_half = flm_half;
+    a.w = P.d_w + P.w_phi;
+    a.wscale = adj ? 2.0 * kPi / Ks : 1.0;
+    a.lmin = P.scal_lmin;
+    a.out = spec;
+    a.os = (int64_t)bs * sw;
+    a.ow = sw;
+    a.omlo = mlo;
+    a.nb = nb;
+    contract_l2t(a, S.st);
+    ring_inverse(spec, sw, sw, mlo, f_scal, Ks, sstride, bs, nb * bs, bs, real, S.st);
+  }
+  const int64_t Wmax = 2 * P.max_bl - 1;
+  double2 *G = S.get<double2>((int64_t)nb * P.max_nn * P.max_bl * Wmax);
+  double2 *spec = S.get<double2>((int64_t)nb * P.max_ng * P.max_bl * Wmax);
+  for (const Scale &sd : P.sc) {
+    const int bl = sd.bl, W = 2 * bl - 1, ng = sd.ng, nn = (int)sd.ns.size();
+    for (int i = 0; i < nn; ++i) {
+      const int n = sd.ns[i];
+      L2T a{};
+      a.tb = &wigner_table(bl, std::abs(n));
+      a.n = n;
+      a.use_q = adj;
+      a.mlo = (real && n == 0) ? 0 : -(bl - 1);
+      a.mhi = bl - 1;
+      a.x = flm;
+      a.xs = (int64_t)L * L;
+      a.xL = L;
+      a.x_half = flm_half;
+      if (P.axisym) {
+        a.w = P.d_w + sd.w_axi;
+        a.wscale = adj ? 2.0 * kPi / W * kSqrt2Pi : 1.0 / kSqrt2Pi;
+      } else {
+        a.w = P.d_w + sd.w_split[i];
+        a.wscale = adj ? 4.0 * kPi * kPi / W : 1.0;
+      }
+      a.lmin = real ? 0 : std::abs(P.s);
+      if (P.axisym) a.lmin = 0;
+      a.out = G + (int64_t)i * bl * W;
+      a.os = (int64_t)nn * bl * W;
+      a.ow = W;
+      a.omlo = -(bl - 1);
+      a.nb = nb;
+      contract_l2t(a, S.st);
+    }
+    const int sw = real ? bl : W, mlo = real ? 0 : -(bl - 1);
+    gamma_synthesis(G, spec, sd.d_ns, nn, ng, bl, nb, real, adj && !P.axisym ? 1.0 / ng : 1.0, S.st);
+    char *out = (char *)f_wav + (size_t)sd.woff * esz;
+    ring_inverse(spec, sw, sw, mlo, out, W, wstride, ng * bl, nb * ng * bl, bl, real, S.st);
+  }
+}
+
+// (f_wav, f_scal) -> flm.  MERGE_SYNTHESIS: wav2lm.  MERGE_ANALYSIS_ADJ: adjoint of lm2wav.
+// For real signals flm holds m >= 0 only.  accumulate: add to flm instead of overwriting.
+void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstride, const void *f_scal,
+               int64_t sstride, double2 *flm, int nb, Scratch &S, bool accumulate = false) {
+  const bool real = P.real;
+  const int L = P.L;
+  const size_t esz = real ? sizeof(double) : sizeof(double2);
+  const bool adj = (mode == MERGE_ANALYSIS_ADJ);
+  double2 *z = S.get<double2>((int64_t)nb * std::max<int64_t>(1, P.z_per_map));
+  const int bs = P.bl_scal, Ks = 2 * bs - 1;
+  double2 *zs = S.get<double2>((int64_t)nb * bs * bs);
+  {
+    const int sw = real ? bs : Ks, mlo = real ? 0 : -(bs - 1);
+    double2 *spec = S.get<double2>((int64_t)nb * bs * sw);
+    ring_forward(f_scal, Ks, sstride, bs, spec, sw, sw, mlo, nb * bs, bs, real, S.st);
+    if (P.scal_lmin > 0) S2G_CUDA(cudaMemsetAsync(zs, 0, sizeof(double2) * nb * bs * bs, S.st));
+    T2L a{};
+    a.tb = &wigner_table(bs, 0);
+    a.n = 0;
+    a.use_q = !adj;
+    a.mlo = mlo;
+    a.mhi = bs - 1;
+    a.in = spec;
+    a.is = (int64_t)bs * sw;
+    a.iw = sw;
+    a.imlo = mlo;
+    a.w = P.d_w + P.w_phi;
+    a.wscale = adj ? 1.0 : 2.0 * kPi / Ks;
+    a.lmin = P.scal_lmin;
+    a.y = zs;
+    a.ys = (int64_t)bs * bs;
+    a.nb = nb;
+    contract_t2l(a, S.st);
+  }
+  const int64_t Wmax = 2 * P.max_bl - 1;
+  double2 *G = S.get<double2>((int64_t)nb * P.max_nn * P.max_bl * Wmax);
+  double2 *spec = S.get<double2>((int64_t)nb * P.max_ng * P.max_bl * Wmax);
+  for (const Scale &sd : P.sc) {
+    const int bl = sd.bl, W = 2 * bl - 1, ng = sd.ng, nn = (int)sd.ns.size();
+    const int sw = real ? bl : W, mlo = real ? 0 : -(bl - 1);
+    const char *in = (const char *)f_wav + (size_t)sd.woff * esz;
+    ring_forward(in, W, wstride, ng * bl, spec, sw, sw, mlo, nb * ng * bl, bl, real, S.st);
+    gamma_analysis(spec, G, sd.d_ns, nn, ng, bl, nb, real, (adj || P.axisym) ? 1.0 : 1.0 / ng, S.st);
+    for (int i = 0; i < nn; ++i) {
+      const int n = sd.ns[i];
+      T2L a{};
+      a.tb = &wigner_table(bl, std::abs(n));
+      a.n = n;
+      a.use_q = !adj;
+      a.mlo = (real && n == 0) ? 0 : -(bl - 1);
+      a.mhi = bl - 1;
+      a.in = G + (int64_t)i * bl * W;
+      a.is = (int64_t)nn * bl * W;
+      a.iw = W;
+      a.imlo = -(bl - 1);
+      if (P.axisym) {
+        a.w = P.d_w + sd.w_axi;
+        a.wscale = adj ? 1.0 / kSqrt2Pi : 2.0 * kPi / W * kSqrt2Pi;
+        a.lmin = 0;
+      } else {
+        a.w = nullptr;
+        a.wscale = adj ? 1.0 : 4.0 * kPi * kPi / W;
+        a.lmin = real ? 0 : std::abs(P.s);
+      }
+      a.y = z + sd.z_off[i];
+      a.ys = P.z_per_map;
+      a.nb = nb;
+      contract_t2l(a, S.st);
+    }
+  }
+  merge_lmn(flm, L, (int64_t)L * L, z, P.z_per_map, P.d_pairs, P.npairs, P.d_w, zs, (int64_t)bs * bs, bs,
+            real, accumulate, nb, S.st);
+}
+
+// (-1)^s sqrt((2l+1)/4pi) on the device, cached per (L, s)
+const double2 *cl_weights(int L, int s) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, double2 *> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(L, s);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  std::vector<double2> w(L);
+  for (int l = 0; l < L; ++l) w[l] = make_double2(((s & 1) ? -1.0 : 1.0) * sqrt((2.0 * l + 1.0) / (4.0 * kPi)), 0.0);
+  double2 *d = upload(w);
+  cache[key] = d;
+  return d;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// status / runtime helpers (declared in runtime.h)
+// ---------------------------------------------------------------------------
+
+void set_status(int code, const std::string &msg) {
+  t_status = code;
+  t_message = msg;
+}
+void report_failure() {
+  fprintf(stderr, "s2let_gpu: %s\n", t_message.c_str());
+  const char *ab = getenv("S2LET_GPU_ABORT_ON_ERROR");
+  if (ab && ab[0] == '1') exit(1);
+}
+int last_status() { return t_status; }
+
+void ensure_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  S2G_REQUIRE(e == cudaSuccess && n > 0, ERR_NO_DEVICE, "no CUDA device available");
+  static std::once_flag f;
+  std::call_once(f, [] {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;  // keep freed scratch cached in the pool
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+  });
+}
+
+cudaStream_t host_stream() {
+  static thread_local cudaStream_t st = nullptr;
+  if (!st) S2G_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  return st;
+}
+
+namespace {
+}  // namespace
+
+// ===========================================================================
+// executors (device pointers, one stream)
+// ===========================================================================
+
+enum Op { OP_PX2WAV, OP_WAV2PX, OP_ADJ_WAV2PX, OP_ADJ_PX2WAV, OP_LM2WAV, OP_WAV2LM, OP_ADJ_WAV2LM,
+          OP_ADJ_LM2WAV };
+
+// One wavelet transform of `nb` maps with plan P.  Pixel maps, wavelet and
+// scaling arrays are batched with their single-map sizes as strides.
+void run_plan(Op op, const WavPlan &P, void *px, void *lm, void *wav, int64_t nw, void *scal, int64_t ns,
+              int nb, cudaStream_t st, bool accumulate_lm = false) {
+  if (nb <= 0) return;
+  Scratch S(st);
+  const int L = P.L;
+  const bool real = P.real;
+  const int64_t npx = (int64_t)L * (2 * L - 1);
+  const bool lm_api = (op == OP_LM2WAV || op == OP_WAV2LM || op == OP_ADJ_WAV2LM || op == OP_ADJ_LM2WAV);
+  double2 *flm = lm_api ? (double2 *)lm : S.get<double2>((int64_t)nb * L * L);
+  switch (op) {
+  case OP_PX2WAV:
+    sht_forward(sht_of(P), px, npx, flm, nb, S, false);
+    wav_split(P, SPLIT_ANALYSIS, flm, real, wav, nw, scal, ns, nb, S);
+    break;
+  case OP_LM2WAV:
+    wav_split(P, SPLIT_ANALYSIS, flm, false, wav, nw, scal, ns, nb, S);
+    break;
+  case OP_ADJ_PX2WAV:
+    sht_forward(sht_of(P), px, npx, flm, nb, S, true);
+    wav_split(P, SPLIT_SYNTH_ADJ, flm, real, wav, nw, scal, ns, nb, S);
+    break;
+  case OP_ADJ_LM2WAV:
+    wav_split(P, SPLIT_SYNTH_ADJ, flm, false, wav, nw, scal, ns, nb, S);
+    break;
+  case OP_WAV2PX:
+    wav_merge(P, MERGE_SYNTHESIS, wav, nw, scal, ns, flm, nb, S);
+    sht_inverse(sht_of(P), flm, real, px, npx, nb, S, false);
+    break;
+  case OP_WAV2LM:
+    wav_merge(P, MERGE_SYNTHESIS, wav, nw, scal, ns, flm, nb, S, accumulate_lm);
+    if (real) symmetrize_flm(flm, L, (int64_t)L * L, nb, st);
+    break;
+  case OP_ADJ_WAV2PX:
+    wav_merge(P, MERGE_ANALYSIS_ADJ, wav, nw, scal, ns, flm, nb, S);
+    sht_inverse(sht_of(P), flm, real, px, npx, nb, S, true);
+    break;
+  case OP_ADJ_WAV2LM:
+    wav_merge(P, MERGE_ANALYSIS_ADJ, wav, nw, scal, ns, flm, nb, S, accumulate_lm);
+    if (real) symmetrize_flm(flm, L, (int64_t)L * L, nb, st);
+    break;
+  }
+}
+
+void run_directional(Op op, const s2let_parameters_t &p, bool real, void *px, void *lm, void *wav,
+                     void *scal, int nb, cudaStream_t st) {
+  validate(&p);
+  const WavPlan &P = directional_plan(p, real);
+  run_plan(op, P, px, lm, wav, s2let_n_wav(&p), scal, s2let_n_scal(&p), nb, st);
+}
+
+// Plain MW spherical-harmonic transform on device buffers.
+// dir: 0 forward (map -> flm), 1 inverse, 2 adjoint of forward (flm -> map),
+// 3 adjoint of inverse (map -> flm).  Real signals: flm returned complete.
+void run_sht(int dir, int L, int spin, bool real, void *f, double2 *flm, int nb, cudaStream_t st) {
+  S2G_REQUIRE(L >= 1 && L <= 8192, ERR_INVALID, "L must lie in [1, 8192]");
+  S2G_REQUIRE(std::abs(spin) < L, ERR_INVALID, "|spin| must be < L");
+  if (real) S2G_REQUIRE(spin == 0, ERR_INVALID, "real signals are spin 0");
+  Scratch S(st);
+  const Sht H{L, real ? 0 : spin, real, cl_weights(L, real ? 0 : spin)};
+  wigner_table(L, std::abs(H.s));
+  const int64_t npx = (int64_t)L * (2 * L - 1);
+  if (dir == 0 || dir == 3) {
+    sht_forward(H, f, npx, flm, nb, S, dir == 3);
+    if (real) symmetrize_flm(flm, L, (int64_t)L * L, nb, st);
+  } else {
+    sht_inverse(H, flm, false, f, npx, nb, S, dir == 2);
+  }
+}
+
+}  // namespace s2g
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+using s2g::cplx;
+
+namespace {
+
+int host_directional(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool real, void *px,
+                     void *lm, void *wav, void *scal) {
+  return s2g::guarded(fn, [&] {
+    s2g::validate(p);
+    s2g::ensure_device();
+    cudaStream_t st = s2g::host_stream();
+    s2g::Scratch S(st);
+    s2g::Staged io(S);
+    const int L = p->L;
+    const int64_t npx = (int64_t)L * (2 * L - 1), nw = s2let_n_wav(p), ns = s2let_n_scal(p);
+    const int64_t dd = real ? 1 : 2;  // doubles per sample
+    void *dpx = nullptr, *dlm = nullptr, *dwav = nullptr, *dscal = nullptr;
+    using namespace s2g;
+    const bool px_in = (op == OP_PX2WAV || op == OP_ADJ_PX2WAV);
+    const bool px_out = (op == OP_WAV2PX || op == OP_ADJ_WAV2PX);
+    const bool lm_in = (op == OP_LM2WAV || op == OP_ADJ_LM2WAV);
+    const bool lm_out = (op == OP_WAV2LM || op == OP_ADJ_WAV2LM);
+    const bool wav_in = px_out || lm_out;
+    if (px_in) dpx = io.in<double>(px, npx * dd);
+    if (px_out) dpx = io.out<double>(px, npx * dd);
+    if (lm_in) dlm = io.in<double2>(lm, (int64_t)L * L);
+    if (lm_out) dlm = io.out<double2>(lm, (int64_t)L * L);
+    if (wav_in) {
+      dwav = io.in<double>(wav, nw * dd);
+      dscal = io.in<double>(scal, ns * dd);
+    } else {
+      dwav = io.out<double>(wav, nw * dd);
+      dscal = io.out<double>(scal, ns * dd);
+    }
+    run_directional(op, *p, real, dpx, dlm, dwav, dscal, 1, st);
+    io.finish();
+  });
+}
+
+void host_sht(const char *fn, int dir, int L, int spin, bool real, void *f, void *flm) {
+  s2g::guarded(fn, [&] {
+    s2g::ensure_device();
+    cudaStream_t st = s2g::host_stream();
+    s2g::Scratch S(st);
+    s2g::Staged io(S);
+    const int64_t npx = (int64_t)L * (2 * L - 1) * (real ? 1 : 2);
+    void *df;
+    double2 *dlm;
+    if (dir == 0 || dir == 3) {
+      df = io.in<double>(f, npx);
+      dlm = io.out<double2>(flm, (int64_t)L * L);
+    } else {
+      dlm = io.in<double2>(flm, (int64_t)L * L);
+      df = io.out<double>(f, npx);
+    }
+    s2g::run_sht(dir, L, spin, real, df, dlm, 1, st);
+    io.finish();
+  });
+}
+
+int batch_directional(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool real, void *px,
+                      void *wav, void *scal, int nb, void *stream) {
+  return s2g::guarded(fn, [&] {
+    s2g::validate(p);
+    s2g::ensure_device();
+    s2g::run_directional(op, *p, real, px, nullptr, wav, scal, nb, (cudaStream_t)stream);
+  });
+}
+
+// ---- axisymmetric pixel-space transforms (src/c/s2let_transform_axisym_mw.c:124-1171)
+void host_axisym(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool real, bool multires,
+                 void *f, void *wav, void *scal) {
+  s2g::guarded(fn, [&] {
+    S2G_REQUIRE(p != nullptr, s2g::ERR_INVALID, "parameters is NULL");
+    s2let_parameters_t q = *p;
+    q.spin = 0;  // the axisymmetric transforms are spin 0 (src/c/s2let_transform_axisym_mw.c:132)
+    q.N = 1;
+    s2g::validate(&q, false);
+    s2g::ensure_device();
+    cudaStream_t st = s2g::host_stream();
+    s2g::Scratch S(st);
+    s2g::Staged io(S);
+    const s2g::WavPlan &P = s2g::axisym_plan(q, real, multires);
+    const int L = q.L;
+    const int64_t npx = (int64_t)L * (2 * L - 1);
+    int64_t nw = 0;
+    for (const auto &sd : P.sc) nw += (int64_t)sd.bl * (2 * sd.bl - 1);
+    const int64_t ns = (int64_t)P.bl_scal * (2 * P.bl_scal - 1);
+    const int64_t dd = real ? 1 : 2;
+    using namespace s2g;
+    void *dpx, *dwav, *dscal;
+    if (op == OP_PX2WAV || op == OP_ADJ_PX2WAV) {
+      dpx = io.in<double>(f, npx * dd);
+      dwav = io.out<double>(wav, nw * dd);
+      dscal = io.out<double>(scal, ns * dd);
+    } else {
+      dpx = io.out<double>(f, npx * dd);
+      dwav = io.in<double>(wav, nw * dd);
+      dscal = io.in<double>(scal, ns * dd);
+    }
+    s2g::run_plan(op, P, dpx, nullptr, dwav, nw, dscal, ns, 1, st);
+    io.finish();
+  });
+}
+
+// ---- manual tilings (src/c/s2let_analysis.c:188-276 and the three siblings)
+void host_manual(const char *fn, s2g::Op op, cplx *flm, cplx *f_wav, cplx *f_scal, const double *scal_l,
+                 const cplx *wav_lm, int scal_bl, const int *wav_bl, int J, int L, int spin, int N) {
+  s2g::guarded(fn, [&] {
+    S2G_REQUIRE(L >= 1 && N >= 1 && J >= 0 && std::abs(spin) < L, s2g::ERR_INVALID, "bad manual parameters");
+    S2G_REQUIRE(scal_l && wav_lm && wav_bl, s2g::ERR_INVALID, "NULL tiling array");
+    s2g::ensure_device();
+    using namespace s2g;
+    s2g::PlanSpec ps;
+    ps.L = L;
+    ps.spin = spin;
+    ps.real = false;
+    ps.bl_scal = std::min(scal_bl, L);
+    ps.scal_lmin = std::abs(spin);
+    int64_t off = 0;
+    for (int j = 0; j <= J; ++j) {
+      const int bl = std::min(wav_bl[j], L);
+      int Nj = std::min(N, bl);
+      Nj += (Nj + N) % 2;
+      ps.jrow.push_back(j);
+      ps.bl.push_back(bl);
+      ps.Nj.push_back(Nj);
+      ps.woff.push_back(off);
+      off += (int64_t)(2 * Nj - 1) * bl * (2 * bl - 1);
+    }
+    ps.psi = wav_lm;
+    ps.phi = scal_l;
+    // the reference's adjoint manual paths multiply by conj(psi) / psi where the
+    // exact adjoint would use psi / conj(psi); reproduced as specified there
+    // (src/c/s2let_analysis_adjoint.c:278, src/c/s2let_synthesis_adjoint.c:266)
+    ps.split_conj = (op == OP_LM2WAV);
+    ps.merge_conj = (op == OP_ADJ_WAV2LM);
+    auto P = s2g::build_plan(ps);
+    if (op == OP_ADJ_LM2WAV) {  // src/c/s2let_synthesis_adjoint.c:215-218
+      printf("J = %i\n", J);
+      printf("B = %g\n", pow(L, 1.0 / (float)(J + 2)));
+      printf("N = %i\n", N);
+      printf("L = %i\n", L);
+    }
+    cudaStream_t st = s2g::host_stream();
+    {
+      s2g::Scratch S(st);
+      s2g::Staged io(S);
+      const int64_t ns = (int64_t)ps.bl_scal * (2 * ps.bl_scal - 1);
+      double2 *dlm, *dw, *dsc;
+      if (op == OP_LM2WAV || op == OP_ADJ_LM2WAV) {
+        dlm = io.in<double2>(flm, (int64_t)L * L);
+        dw = io.out<double2>(f_wav, off);
+        dsc = io.out<double2>(f_scal, ns);
+      } else {  // these two accumulate into flm (src/c/s2let_synthesis.c:254,281)
+        dlm = io.inout<double2>(flm, (int64_t)L * L);
+        dw = io.in<double2>(f_wav, off);
+        dsc = io.in<double2>(f_scal, ns);
+      }
+      s2g::run_plan(op, *P, nullptr, dlm, dw, off, dsc, ns, 1, st, true);
+      io.finish();
+    }
+    P->release();
+  });
+}
+
+}  // namespace
+
+extern "C" {
+
+int s2let_gpu_last_error(void) { return s2g::t_status; }
+const char *s2let_gpu_last_error_string(void) { return s2g::t_message.c_str(); }
+int s2let_gpu_set_precision(int mode) {
+  if (mode != 0 && mode != 1) {
+    s2g::set_status(s2g::ERR_INVALID, "precision mode must be 0 (FP64) or 1 (mixed)");
+    return s2g::ERR_INVALID;
+  }
+  s2g::t_precision = mode;
+  return 0;
+}
+int s2let_gpu_get_precision(void) { return s2g::t_precision; }
+void s2let_gpu_release_plans(void) {
+  s2g::guarded("s2let_gpu_release_plans", [] {
+    {
+      std::lock_guard<std::mutex> lk(s2g::g_plan_mu);
+      cudaDeviceSynchronize();
+      for (auto &kv : s2g::g_plans) kv.second->release();
+      s2g::g_plans.clear();
+    }
+    s2g::release_plans();
+  });
+}
+size_t s2let_gpu_plan_bytes(void) { return s2g::plan_bytes(); }
+uint64_t s2let_gpu_launch_count(void) { return s2g::g_launches.load(); }
+
+// ---- pixel-space directional transforms
+void s2let_analysis_px2wav(cplx *f_wav, cplx *f_scal, const cplx *f, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_PX2WAV, p, false, (void *)f, nullptr, f_wav, f_scal);
+}
+void s2let_analysis_px2wav_real(double *f_wav, double *f_scal, const double *f, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_PX2WAV, p, true, (void *)f, nullptr, f_wav, f_scal);
+}
+void s2let_synthesis_wav2px(cplx *f, const cplx *f_wav, const cplx *f_scal, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_WAV2PX, p, false, f, nullptr, (void *)f_wav, (void *)f_scal);
+}
+void s2let_synthesis_wav2px_real(double *f, const double *f_wav, const double *f_scal, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_WAV2PX, p, true, f, nullptr, (void *)f_wav, (void *)f_scal);
+}
+void s2let_analysis_adjoint_wav2px(cplx *f, const cplx *f_wav, const cplx *f_scal, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_ADJ_WAV2PX, p, false, f, nullptr, (void *)f_wav, (void *)f_scal);
+}
+void s2let_analysis_adjoint_wav2px_real(double *f, const double *f_wav, const double *f_scal,
+                                        const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_ADJ_WAV2PX, p, true, f, nullptr, (void *)f_wav, (void *)f_scal);
+}
+void s2let_synthesis_adjoint_px2wav(cplx *f_wav, cplx *f_scal, const cplx *f, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_ADJ_PX2WAV, p, false, (void *)f, nullptr, f_wav, f_scal);
+}
+void s2let_synthesis_adjoint_px2wav_real(double *f_wav, double *f_scal, const double *f,
+                                         const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_ADJ_PX2WAV, p, true, (void *)f, nullptr, f_wav, f_scal);
+}
+
+// ---- harmonic-space directional transforms
+void s2let_analysis_lm2wav(cplx *f_wav, cplx *f_scal, const cplx *flm, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_LM2WAV, p, false, nullptr, (void *)flm, f_wav, f_scal);
+}
+void s2let_analysis_lm2wav_real(double *f_wav, double *f_scal, const cplx *flm, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_LM2WAV, p, true, nullptr, (void *)flm, f_wav, f_scal);
+}
+void s2let_synthesis_wav2lm(cplx *flm, const cplx *f_wav, const cplx *f_scal, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_WAV2LM, p, false, nullptr, flm, (void *)f_wav, (void *)f_scal);
+}
+void s2let_synthesis_wav2lm_real(cplx *flm, const double *f_wav, const double *f_scal, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_WAV2LM, p, true, nullptr, flm, (void *)f_wav, (void *)f_scal);
+}
+void s2let_analysis_adjoint_wav2lm(cplx *flm, const cplx *f_wav, const cplx *f_scal, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_ADJ_WAV2LM, p, false, nullptr, flm, (void *)f_wav, (void *)f_scal);
+}
+void s2let_analysis_adjoint_wav2lm_real(cplx *flm, const double *f_wav, const double *f_scal,
+                                        const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_ADJ_WAV2LM, p, true, nullptr, flm, (void *)f_wav, (void *)f_scal);
+}
+void s2let_synthesis_adjoint_lm2wav(cplx *f_wav, cplx *f_scal, const cplx *flm, const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_ADJ_LM2WAV, p, false, nullptr, (void *)flm, f_wav, f_scal);
+}
+void s2let_synthesis_adjoint_lm2wav_real(double *f_wav, double *f_scal, const cplx *flm,
+                                         const s2let_parameters_t *p) {
+  host_directional(__func__, s2g::OP_ADJ_LM2WAV, p, true, nullptr, (void *)flm, f_wav, f_scal);
+}
+
+// ---- manual tilings
+void s2let_analysis_lm2wav_manual(cplx *f_wav, cplx *f_scal, const cplx *flm, const double *scal_l,
+                                  const cplx *wav_lm, const int scal_bandlimit, const int *wav_bandlimits,
+                                  int J, int L, int spin, int N) {
+  host_manual(__func__, s2g::OP_LM2WAV, (cplx *)flm, f_wav, f_scal, scal_l, wav_lm, scal_bandlimit,
+              wav_bandlimits, J, L, spin, N);
+}
+void s2let_synthesis_wav2lm_manual(cplx *flm, const cplx *f_wav, const cplx *f_scal, const double *scal_l,
+                                   const cplx *wav_lm, const int scal_bandlimit, const int *wav_bandlimits,
+                                   int J, int L, int spin, int N) {
+  host_manual(__func__, s2g::OP_WAV2LM, flm, (cplx *)f_wav, (cplx *)f_scal, scal_l, wav_lm, scal_bandlimit,
+              wav_bandlimits, J, L, spin, N);
+}
+void s2let_analysis_adjoint_wav2lm_manual(cplx *flm, const cplx *f_wav, const cplx *f_scal,
+                                          const double *scal_l, const cplx *wav_lm, const int scal_bandlimit,
+                                          const int *wav_bandlimits, int J, int L, int spin, int N) {
+  host_manual(__func__, s2g::OP_ADJ_WAV2LM, flm, (cplx *)f_wav, (cplx *)f_scal, scal_l, wav_lm,
+              scal_bandlimit, wav_bandlimits, J, L, spin, N);
+}
+void s2let_synthesis_adjoint_lm2wav_manual(cplx *f_wav, cplx *f_scal, const cplx *flm, const double *scal_l,
+                                           const cplx *wav_lm, const int scal_bandlimit,
+                                           const int *wav_bandlimits, int J, int L, int spin, int N) {
+  host_manual(__func__, s2g::OP_ADJ_LM2WAV, (cplx *)flm, f_wav, f_scal, scal_l, wav_lm, scal_bandlimit,
+              wav_bandlimits, J, L, spin, N);
+}
+
+// ---- axisymmetric pixel-space transforms
+#define S2G_AXI(name, op, mr, re, TA, TB, TC)                                                     \
+  void name(TA *a, TB *b, TC *c, const s2let_parameters_t *p) {                                  \
+    if (op == s2g::OP_PX2WAV || op == s2g::OP_ADJ_PX2WAV)                                        \
+      host_axisym(#name, op, p, re, mr, (void *)c, (void *)a, (void *)b);                       \
+    else                                                                                         \
+      host_axisym(#name, op, p, re, mr, (void *)a, (void *)b, (void *)c);                       \
+  }
+// analysis / synthesis-adjoint: (f_wav, f_scal, f);  synthesis / analysis-adjoint: (f, f_wav, f_scal)
+S2G_AXI(s2let_transform_axisym_wav_analysis_mw, s2g::OP_PX2WAV, false, false, cplx, cplx, const cplx)
+S2G_AXI(s2let_transform_axisym_wav_analysis_mw_multires, s2g::OP_PX2WAV, true, false, cplx, cplx, const cplx)
+S2G_AXI(s2let_transform_axisym_wav_analysis_mw_real, s2g::OP_PX2WAV, false, true, double, double, const double)
+S2G_AXI(s2let_transform_axisym_wav_analysis_mw_multires_real, s2g::OP_PX2WAV, true, true, double, double,
+        const double)
+S2G_AXI(s2let_transform_axisym_wav_synthesis_adjoint_mw, s2g::OP_ADJ_PX2WAV, false, false, cplx, cplx, const cplx)
+S2G_AXI(s2let_transform_axisym_wav_synthesis_adjoint_mw_multires, s2g::OP_ADJ_PX2WAV, true, false, cplx, cplx,
+        const cplx)
+S2G_AXI(s2let_transform_axisym_wav_synthesis_adjoint_mw_real, s2g::OP_ADJ_PX2WAV, false, true, double, double,
+        const double)
+S2G_AXI(s2let_transform_axisym_wav_synthesis_adjoint_mw_multires_real, s2g::OP_ADJ_PX2WAV, true, true, double,
+        double, const double)
+S2G_AXI(s2let_transform_axisym_wav_synthesis_mw, s2g::OP_WAV2PX, false, false, cplx, const cplx, const cplx)
+S2G_AXI(s2let_transform_axisym_wav_synthesis_mw_multires, s2g::OP_WAV2PX, true, false, cplx, const cplx, const cplx)
+S2G_AXI(s2let_transform_axisym_wav_synthesis_mw_real, s2g::OP_WAV2PX, false, true, double, const double,
+        const double)
+S2G_AXI(s2let_transform_axisym_wav_synthesis_mw_multires_real, s2g::OP_WAV2PX, true, true, double, const double,
+        const double)
+S2G_AXI(s2let_transform_axisym_wav_analysis_adjoint_mw, s2g::OP_ADJ_WAV2PX, false, false, cplx, const cplx,
+        const cplx)
+S2G_AXI(s2let_transform_axisym_wav_analysis_adjoint_mw_multires, s2g::OP_ADJ_WAV2PX, true, false, cplx,
+        const cplx, const cplx)
+S2G_AXI(s2let_transform_axisym_wav_analysis_adjoint_mw_real, s2g::OP_ADJ_WAV2PX, false, true, double,
+        const double, const double)
+S2G_AXI(s2let_transform_axisym_wav_analysis_adjoint_mw_multires_real, s2g::OP_ADJ_WAV2PX, true, true, double,
+        const double, const double)
+#undef S2G_AXI
+
+// ---- plain MW spherical-harmonic transforms (src/c/s2let_mw.c:21-94)
+void s2let_mw_alm2map(cplx *f, const cplx *flm, int L, int spin) { host_sht(__func__, 1, L, spin, false, f, (void *)flm); }
+void s2let_mw_map2alm(cplx *flm, const cplx *f, int L, int spin) { host_sht(__func__, 0, L, spin, false, (void *)f, flm); }
+void s2let_mw_alm2map_real(double *f, const cplx *flm, int L) { host_sht(__func__, 1, L, 0, true, f, (void *)flm); }
+void s2let_mw_map2alm_real(cplx *flm, const double *f, int L) { host_sht(__func__, 0, L, 0, true, (void *)f, flm); }
+double s2let_mw_power(cplx *f, int L) {
+  std::vector<cplx> flm((size_t)L * L);
+  s2let_mw_map2alm(flm.data(), f, L, 0);
+  return s2let_lm_power(flm.data(), L);
+}
+double s2let_mw_power_real(double *f, int L) {
+  std::vector<cplx> flm((size_t)L * L);
+  s2let_mw_map2alm_real(flm.data(), f, L);
+  return s2let_lm_power(flm.data(), L);
+}
+// Adjoints of the plain transforms (SSHT adjoints that S2LET uses internally).
+void s2let_gpu_mw_adjoint_map2alm(cplx *f, const cplx *flm, int L, int spin) {
+  host_sht(__func__, 2, L, spin, false, f, (void *)flm);
+}
+void s2let_gpu_mw_adjoint_alm2map(cplx *flm, const cplx *f, int L, int spin) {
+  host_sht(__func__, 3, L, spin, false, (void *)f, flm);
+}
+
+// ---- batched device-pointer extensions
+int s2let_gpu_analysis_px2wav_real_batch(double *f_wav, double *f_scal, const double *f, int nb,
+                                         const s2let_parameters_t *p, void *stream) {
+  return batch_directional(__func__, s2g::OP_PX2WAV, p, true, (void *)f, f_wav, f_scal, nb, stream);
+}
+int s2let_gpu_synthesis_wav2px_real_batch(double *f, const double *f_wav, const double *f_scal, int nb,
+                                          const s2let_parameters_t *p, void *stream) {
+  return batch_directional(__func__, s2g::OP_WAV2PX, p, true, f, (void *)f_wav, (void *)f_scal, nb, stream);
+}
+int s2let_gpu_analysis_px2wav_batch(void *f_wav, void *f_scal, const void *f, int nb,
+                                    const s2let_parameters_t *p, void *stream) {
+  return batch_directional(__func__, s2g::OP_PX2WAV, p, false, (void *)f, f_wav, f_scal, nb, stream);
+}
+int s2let_gpu_synthesis_wav2px_batch(void *f, const void *f_wav, const void *f_scal, int nb,
+                                     const s2let_parameters_t *p, void *stream) {
+  return batch_directional(__func__, s2g::OP_WAV2PX, p, false, f, (void *)f_wav, (void *)f_scal, nb, stream);
+}
+int s2let_gpu_analysis_adjoint_wav2px_real_batch(double *f, const double *f_wav, const double *f_scal, int nb,
+                                                 const s2let_parameters_t *p, void *stream) {
+  return batch_directional(__func__, s2g::OP_ADJ_WAV2PX, p, true, f, (void *)f_wav, (void *)f_scal, nb, stream);
+}
+int s2let_gpu_synthesis_adjoint_px2wav_real_batch(double *f_wav, double *f_scal, const double *f, int nb,
+                                                  const s2let_parameters_t *p, void *stream) {
+  return batch_directional(__func__, s2g::OP_ADJ_PX2WAV, p, true, (void *)f, f_wav, f_scal, nb, stream);
+}
+int s2let_gpu_analysis_adjoint_wav2px_batch(void *f, const void *f_wav, const void *f_scal, int nb,
+                                            const s2let_parameters_t *p, void *stream) {
+  return batch_directional(__func__, s2g::OP_ADJ_WAV2PX, p, false, f, (void *)f_wav, (void *)f_scal, nb, stream);
+}
+int s2let_gpu_synthesis_adjoint_px2wav_batch(void *f_wav, void *f_scal, const void *f, int nb,
+                                             const s2let_parameters_t *p, void *stream) {
+  return batch_directional(__func__, s2g::OP_ADJ_PX2WAV, p, false, (void *)f, f_wav, f_scal, nb, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,805 @@
+// Transform kernels, FP64 path.
+//
+//  k_ring      batched Bluestein DFT of MW rings (length 2bl-1, odd) in shared
+//              memory: chirp premultiply, radix-2 DIT FFT of the padded length,
+//              pointwise multiply by the chirp-kernel spectrum, DIF inverse FFT,
+//              chirp postmultiply.  Two real rings share one complex FFT.
+//  k_contract  per-m Legendre/Wigner contraction against the cached d-tables,
+//              tiled through shared memory (table tiles loaded coalesced along
+//              their contiguous axis, coefficient tiles broadcast).
+//  k_gamma_*   DFT over the 2N-1 gamma samples of the rotation group.
+//  k_merge     harmonic tiling merge (lmn -> lm) fused over scales/directions.
+#include "common.h"
+#include "kernels.h"
+
+namespace s2g {
+
+namespace {
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cmulc(double2 a, double2 b) {  // a * conj(b)
+  return make_double2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ double2 conj2(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 add2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 sub2(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 scl2(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__device__ __forceinline__ int brev(int k, int logP) {
+  return logP == 0 ? 0 : (int)(__brev((unsigned)k) >> (32 - logP));
+}
+
+// ---------------------------------------------------------------------------
+// Ring DFT (Bluestein)
+// ---------------------------------------------------------------------------
+
+struct RingArgs {
+  const void *rings;
+  double2 *rings_out;  // inverse: output rings (as double2 or double)
+  int64_t ring_stride;  // between rings of one map
+  int64_t map_stride;   // between maps
+  int rpm;              // rings per map
+  const double2 *spec_in;
+  double2 *spec_out;
+  int64_t spec_stride;
+  int sw, mlo;
+  int nrings, bl, K, P, logP;
+  const double2 *chirp, *bhat, *tw;
+};
+
+// element offset of ring r (rings of a map are ring_stride apart, maps map_stride)
+__device__ __forceinline__ int64_t ring_base(const RingArgs &a, int r) {
+  return (int64_t)(r / a.rpm) * a.map_stride + (int64_t)(r % a.rpm) * a.ring_stride;
+}
+
+// In-place transforms on the shared buffer.
+__device__ void fft_dit(double2 *buf, const double2 *__restrict__ tw, int P, int logP) {
+  for (int s = 1; s <= logP; ++s) {
+    const int half = 1 << (s - 1);
+    for (int i = threadIdx.x; i < P / 2; i += blockDim.x) {
+      const int j = i & (half - 1);
+      const int i0 = ((i >> (s - 1)) << s) + j, i1 = i0 + half;
+      const double2 w = __ldg(&tw[j << (logP - s)]);
+      const double2 u = buf[i0], v = cmul(buf[i1], w);
+      buf[i0] = add2(u, v);
+      buf[i1] = sub2(u, v);
+    }
+    __syncthreads();
+  }
+}
+__device__ void ifft_dif(double2 *buf, const double2 *__restrict__ tw, int P, int logP) {
+  for (int s = logP; s >= 1; --s) {
+    const int half = 1 << (s - 1);
+    for (int i = threadIdx.x; i < P / 2; i += blockDim.x) {
+      const int j = i & (half - 1);
+      const int i0 = ((i >> (s - 1)) << s) + j, i1 = i0 + half;
+      const double2 w = conj2(__ldg(&tw[j << (logP - s)]));
+      const double2 u = buf[i0], v = buf[i1];
+      buf[i0] = add2(u, v);
+      buf[i1] = cmul(sub2(u, v), w);
+    }
+    __syncthreads();
+  }
+}
+
+// Bluestein core: buf holds a_j (bit-reversed positions) on entry; on exit
+// buf[brev(k)] holds P * y_k where y = a (*) chirp-kernel.
+__device__ void bluestein_core(double2 *buf, const RingArgs &a) {
+  __syncthreads();
+  fft_dit(buf, a.tw, a.P, a.logP);
+  for (int k = threadIdx.x; k < a.P; k += blockDim.x) buf[k] = cmul(buf[k], __ldg(&a.bhat[k]));
+  __syncthreads();
+  ifft_dif(buf, a.tw, a.P, a.logP);
+}
+
+template <bool REAL>
+__global__ void __launch_bounds__(512) k_ring_forward(RingArgs a) {
+  extern __shared__ double2 buf[];
+  const int K = a.K, P = a.P, logP = a.logP;
+  const int r0 = REAL ? 2 * blockIdx.x : blockIdx.x;
+  const bool has1 = REAL && (r0 + 1 < a.nrings);
+  for (int j = threadIdx.x; j < P; j += blockDim.x) {
+    double2 z = make_double2(0.0, 0.0);
+    if (j < K) {
+      if (REAL) {
+        z.x = ((const double *)a.rings)[ring_base(a, r0) + j];
+        if (has1) z.y = ((const double *)a.rings)[ring_base(a, r0 + 1) + j];
+      } else {
+        z = ((const double2 *)a.rings)[ring_base(a, r0) + j];
+      }
+      z = cmulc(z, __ldg(&a.chirp[j]));  // x_j conj(c_j)
+    }
+    buf[brev(j, logP)] = z;
+  }
+  bluestein_core(buf, a);
+  const double inv = 1.0 / (double)P;
+  if (!REAL) {
+    double2 *out = a.spec_out + (int64_t)r0 * a.spec_stride;
+    for (int c = threadIdx.x; c < a.sw; c += blockDim.x) {
+      const int m = a.mlo + c;
+      const int k = ((m % K) + K) % K;
+      out[c] = scl2(cmulc(buf[brev(k, logP)], __ldg(&a.chirp[k])), inv);
+    }
+  } else {
+    double2 *out0 = a.spec_out + (int64_t)r0 * a.spec_stride;
+    for (int m = threadIdx.x; m < a.sw; m += blockDim.x) {
+      const int km = (K - m) % K;
+      const double2 zm = scl2(cmulc(buf[brev(m, logP)], __ldg(&a.chirp[m])), inv);
+      const double2 zk = scl2(cmulc(buf[brev(km, logP)], __ldg(&a.chirp[km])), inv);
+      const double2 zc = conj2(zk);
+      // A = (Z_m + conj Z_{-m})/2,  B = (Z_m - conj Z_{-m})/(2i)
+      out0[m] = make_double2(0.5 * (zm.x + zc.x), 0.5 * (zm.y + zc.y));
+      if (has1) {
+        const double2 d = sub2(zm, zc);
+        out0[a.spec_stride + m] = make_double2(0.5 * d.y, -0.5 * d.x);
+      }
+    }
+  }
+}
+
+template <bool REAL>
+__global__ void __launch_bounds__(512) k_ring_inverse(RingArgs a) {
+  extern __shared__ double2 buf[];
+  const int K = a.K, P = a.P, logP = a.logP, bl = a.bl;
+  const int r0 = REAL ? 2 * blockIdx.x : blockIdx.x;
+  const bool has1 = REAL && (r0 + 1 < a.nrings);
+  const double2 *s0 = a.spec_in + (int64_t)r0 * a.spec_stride;
+  for (int j = threadIdx.x; j < P; j += blockDim.x) {
+    double2 z = make_double2(0.0, 0.0);
+    if (j < K) {
+      const int m = (j < bl) ? j : j - K;  // frequency of DFT bin j
+      if (REAL) {
+        const int am = m < 0 ? -m : m;
+        if (am < a.sw) {
+          double2 A = s0[am];
+          double2 B = has1 ? s0[a.spec_stride + am] : make_double2(0.0, 0.0);
+          if (m < 0) {
+            A = conj2(A);
+            B = conj2(B);
+          }
+          z = make_double2(A.x - B.y, A.y + B.x);  // A + i B
+        }
+      } else {
+        const int c = m - a.mlo;
+        if (c >= 0 && c < a.sw) z = s0[c];
+      }
+      // inverse DFT = conj(forward(conj z)):  a_j = conj(z_j) conj(c_j)
+      z = conj2(cmul(z, __ldg(&a.chirp[j])));
+    }
+    buf[brev(j, logP)] = z;
+  }
+  bluestein_core(buf, a);
+  const double inv = 1.0 / (double)P;
+  for (int p = threadIdx.x; p < K; p += blockDim.x) {
+    // f_p = conj(conj(c_p) y_p) = c_p conj(y_p)
+    const double2 y = scl2(buf[brev(p, logP)], inv);
+    const double2 f = cmul(__ldg(&a.chirp[p]), conj2(y));
+    if (REAL) {
+      ((double *)a.rings_out)[ring_base(a, r0) + p] = f.x;
+      if (has1) ((double *)a.rings_out)[ring_base(a, r0 + 1) + p] = f.y;
+    } else {
+      a.rings_out[ring_base(a, r0) + p] = f;
+    }
+  }
+}
+
+RingArgs ring_args(const RingFFT &rf, int bl, int nrings) {
+  RingArgs a{};
+  a.K = rf.K;
+  a.P = rf.P;
+  a.logP = rf.logP;
+  a.bl = bl;
+  a.nrings = nrings;
+  a.chirp = rf.chirp;
+  a.bhat = rf.bhat;
+  a.tw = rf.tw;
+  return a;
+}
+
+int ring_threads(int P) { return P / 2 >= 512 ? 512 : (P / 2 >= 32 ? P / 2 : 32); }
+
+// ---------------------------------------------------------------------------
+// Contractions
+// ---------------------------------------------------------------------------
+
+constexpr int CT_M = 128;  // rows (t or l) per CTA
+constexpr int CT_K = 32;   // reduction tile
+
+struct TableRef {
+  int mi;       // m index inside the table
+  double sign;  // (-1)^{m+|n|} when read through the n -> -n mirror
+};
+__device__ __forceinline__ TableRef table_ref(int mlo_table, int n, int m) {
+  TableRef r;
+  if (n > 0 || (n == 0 && m >= 0)) {
+    r.mi = m - mlo_table;
+    r.sign = 1.0;
+  } else {
+    const int an = n < 0 ? -n : n;
+    r.mi = -m - mlo_table;
+    r.sign = ((m + an) & 1) ? -1.0 : 1.0;
+  }
+  return r;
+}
+
+struct ContractArgs {
+  const double *table;
+  const int64_t *off;
+  int bl, an, tmlo, n, mlo, lmin;
+  const double2 *w;
+  double wscale;
+  int wconj;
+  // l->t: x source / spectra dest;  t->l: spectra source / y dest
+  const double2 *src;
+  int64_t ss;
+  int sw_or_xL;  // t->l: spectrum row width; l->t: x band-limit
+  int s_mlo;     // t->l: m of spectrum column 0
+  int x_half;
+  double2 *dst;
+  int64_t ds;
+  int dw, d_mlo;  // l->t: spectrum row width / m of column 0
+  int nb;
+};
+
+__device__ __forceinline__ double2 weight_at(const ContractArgs &a, int l) {
+  double2 w = a.w ? a.w[l] : make_double2(1.0, 0.0);
+  if (a.wconj) w.y = -w.y;
+  return scl2(w, a.wscale);
+}
+
+// MODE 0: l->t with D (A[t][l] = D[t][l-l0])     MODE 1: l->t with Q^T (A[t][l] = Q[l-l0][t])
+// MODE 2: t->l with Q (A[l][t] = Q[l-l0][t])     MODE 3: t->l with D^T (A[l][t] = D[t][l-l0])
+template <int MODE, int NBT>
+__global__ void __launch_bounds__(CT_M) k_contract(ContractArgs a) {
+  __shared__ double sA[CT_M][CT_K + 1];
+  __shared__ double2 sX[CT_K][NBT];
+  const int m = a.mlo + blockIdx.x;
+  const int am = m < 0 ? -m : m;
+  const int l0 = am > a.an ? am : a.an;
+  const int bl = a.bl;
+  const int nl = bl - l0;
+  const int lst = l0 > a.lmin ? l0 : a.lmin;
+  constexpr bool L2T = (MODE == 0 || MODE == 1);
+  // l -> t with no admissible l still writes its (zero) output rows
+  if (!L2T && lst >= bl) return;
+  const TableRef tr = table_ref(a.tmlo, a.n, m);
+  const double *T = (lst < bl) ? a.table + a.off[tr.mi] : a.table;
+  const int b0 = blockIdx.z * NBT;
+  const int r = threadIdx.x;
+  // rows of this CTA
+  const int row0 = blockIdx.y * CT_M;
+  const int rows_total = L2T ? bl : (bl - lst);
+  if (row0 >= rows_total) return;
+  const int kbeg = L2T ? lst : 0, kend = bl;  // reduction range (l for L2T, t for T2L)
+
+  double2 acc[NBT];
+#pragma unroll
+  for (int b = 0; b < NBT; ++b) acc[b] = make_double2(0.0, 0.0);
+
+  for (int k0 = kbeg; k0 < kend; k0 += CT_K) {
+    // coefficient tile
+    for (int i = threadIdx.x; i < CT_K * NBT; i += CT_M) {
+      const int kk = i / NBT, b = i % NBT, k = k0 + kk;
+      double2 v = make_double2(0.0, 0.0);
+      if (k < kend && b0 + b < a.nb) {
+        if (L2T) {  // x(l = k, m) * w(l)
+          const int64_t base = (int64_t)(b0 + b) * a.ss + (int64_t)k * k + k;
+          if (a.x_half && m < 0) {
+            v = conj2(a.src[base - m]);
+            if (am & 1) v = scl2(v, -1.0);
+          } else {
+            v = a.src[base + m];
+          }
+          v = cmul(v, weight_at(a, k));
+        } else {  // spectrum(t = k, m)
+          v = a.src[(int64_t)(b0 + b) * a.ss + (int64_t)k * a.sw_or_xL + (m - a.s_mlo)];
+        }
+      }
+      sX[kk][b] = v;
+    }
+    // table tile sA[row][kk]
+    if (MODE == 0 || MODE == 2) {
+      // contiguous along the reduction axis: D[t][l-l0] (MODE 0) or Q[l-l0][t] (MODE 2)
+      for (int i = threadIdx.x; i < CT_M * CT_K; i += CT_M) {
+        const int rr = i / CT_K, kk = i % CT_K;
+        const int row = row0 + rr, k = k0 + kk;
+        double v = 0.0;
+        if (row < rows_total && k < kend) {
+          if (MODE == 0)
+            v = T[(int64_t)row * nl + (k - l0)];
+          else
+            v = T[(int64_t)(lst + row - l0) * bl + k];
+        }
+        sA[rr][kk] = v;
+      }
+    } else {
+      // contiguous along the row axis: Q[l-l0][t] read as A[t][l] (MODE 1),
+      // D[t][l-l0] read as A[l][t] (MODE 3)
+      for (int i = threadIdx.x; i < CT_M * CT_K; i += CT_M) {
+        const int kk = i / CT_M, rr = i % CT_M;
+        const int row = row0 + rr, k = k0 + kk;
+        double v = 0.0;
+        if (row < rows_total && k < kend) {
+          if (MODE == 1)
+            v = T[(int64_t)(k - l0) * bl + row];
+          else
+            v = T[(int64_t)k * nl + (lst + row - l0)];
+        }
+        sA[rr][kk] = v;
+      }
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < CT_K; ++kk) {
+      const double av = sA[r][kk];
+#pragma unroll
+      for (int b = 0; b < NBT; ++b) {
+        const double2 x = sX[kk][b];
+        acc[b].x = fma(av, x.x, acc[b].x);
+        acc[b].y = fma(av, x.y, acc[b].y);
+      }
+    }
+    __syncthreads();
+  }
+  const int row = row0 + r;
+  if (row >= rows_total) return;
+#pragma unroll
+  for (int b = 0; b < NBT; ++b) {
+    if (b0 + b >= a.nb) break;
+    double2 v = scl2(acc[b], tr.sign);
+    if (L2T) {
+      a.dst[(int64_t)(b0 + b) * a.ds + (int64_t)row * a.dw + (m - a.d_mlo)] = v;
+    } else {
+      const int l = lst + row;
+      v = cmul(v, weight_at(a, l));
+      a.dst[(int64_t)(b0 + b) * a.ds + (int64_t)l * l + l + m] = v;
+    }
+  }
+}
+
+template <int MODE>
+void launch_contract(const ContractArgs &a, int nm, int rows, cudaStream_t st) {
+  const int nbt = a.nb >= 8 ? 8 : (a.nb >= 4 ? 4 : (a.nb >= 2 ? 2 : 1));
+  dim3 grid(nm, ceil_div(rows, CT_M), ceil_div(a.nb, nbt));
+  switch (nbt) {
+  case 8: k_contract<MODE, 8><<<grid, CT_M, 0, st>>>(a); break;
+  case 4: k_contract<MODE, 4><<<grid, CT_M, 0, st>>>(a); break;
+  case 2: k_contract<MODE, 2><<<grid, CT_M, 0, st>>>(a); break;
+  default: k_contract<MODE, 1><<<grid, CT_M, 0, st>>>(a); break;
+  }
+  S2G_LAUNCHED();
+}
+
+// ---------------------------------------------------------------------------
+// gamma DFTs
+// ---------------------------------------------------------------------------
+
+__global__ void k_gamma_synth(const double2 *__restrict__ G, double2 *__restrict__ spec,
+                              const int *__restrict__ ns, int nn, int ng, int bl, int nb, int real,
+                              double c) {
+  const int W = 2 * bl - 1;
+  const int sw = real ? bl : W, smlo = real ? 0 : -(bl - 1);
+  const int64_t total = (int64_t)nb * bl * sw;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const int col = (int)(gid % sw);
+  const int t = (int)((gid / sw) % bl);
+  const int b = (int)(gid / ((int64_t)sw * bl));
+  const int m = smlo + col;
+  const int64_t gb = (int64_t)b * nn * bl * W;
+  for (int g = 0; g < ng; ++g) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int k = 0; k < nn; ++k) {
+      const int n = ns[k];
+      double sn, cs;
+      sincospi(2.0 * (double)((n * g) % ng) / (double)ng, &sn, &cs);
+      const double2 e = make_double2(cs, sn);
+      const double2 *Gk = G + gb + (int64_t)k * bl * W + (int64_t)t * W;
+      acc = add2(acc, cmul(e, Gk[m + bl - 1]));
+      if (real && n > 0) acc = add2(acc, cmul(conj2(e), conj2(Gk[-m + bl - 1])));
+    }
+    spec[((int64_t)b * ng + g) * bl * sw + (int64_t)t * sw + col] = scl2(acc, c);
+  }
+}
+
+__global__ void k_gamma_anal(const double2 *__restrict__ spec, double2 *__restrict__ G,
+                             const int *__restrict__ ns, int nn, int ng, int bl, int nb, int real,
+                             double c) {
+  const int W = 2 * bl - 1;
+  const int sw = real ? bl : W, smlo = real ? 0 : -(bl - 1);
+  const int64_t total = (int64_t)nb * bl * W;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const int col = (int)(gid % W);
+  const int t = (int)((gid / W) % bl);
+  const int b = (int)(gid / ((int64_t)W * bl));
+  const int m = col - (bl - 1);
+  for (int k = 0; k < nn; ++k) {
+    const int n = ns[k];
+    double2 acc = make_double2(0.0, 0.0);
+    for (int g = 0; g < ng; ++g) {
+      double2 s;
+      const double2 *sg = spec + ((int64_t)b * ng + g) * bl * sw + (int64_t)t * sw;
+      if (real) {
+        s = m >= 0 ? sg[m] : conj2(sg[-m]);
+      } else {
+        s = sg[m - smlo];
+      }
+      double sn, cs;
+      sincospi(2.0 * (double)((n * g) % ng) / (double)ng, &sn, &cs);
+      acc = add2(acc, cmul(make_double2(cs, -sn), s));
+    }
+    G[((int64_t)b * nn + k) * bl * W + (int64_t)t * W + col] = scl2(acc, c);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// lmn -> lm merge
+// ---------------------------------------------------------------------------
+
+__global__ void k_merge(double2 *__restrict__ flm, int L, int64_t fs, const double2 *__restrict__ z,
+                        int64_t zs, const MergePair *__restrict__ pairs, int npairs,
+                        const double2 *__restrict__ wts, const double2 *__restrict__ zscal, int64_t zss,
+                        int bl_scal, int real, int accumulate, int nb) {
+  const int64_t L2 = (int64_t)L * L;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= nb * L2) return;
+  const int b = (int)(gid / L2);
+  const int i = (int)(gid % L2);
+  int l2 = (int)sqrt((double)i);
+  while (l2 * l2 > i) --l2;
+  while ((l2 + 1) * (l2 + 1) <= i) ++l2;
+  const int m = i - l2 * l2 - l2;
+  if (real && m < 0) return;
+  double2 acc = accumulate ? flm[(int64_t)b * fs + i] : make_double2(0.0, 0.0);
+  const double2 *zb = z + (int64_t)b * zs;
+  for (int p = 0; p < npairs; ++p) {
+    const MergePair pr = pairs[p];
+    if (l2 >= pr.bl || l2 < pr.lmin) continue;
+    const int an = pr.n < 0 ? -pr.n : pr.n;
+    if (l2 < an) continue;
+    const double2 *zp = zb + pr.off;
+    const int64_t li = (int64_t)l2 * l2 + l2;
+    acc = add2(acc, cmul(wts[pr.woff + l2], zp[li + m]));
+    if (real && pr.n > 0) {
+      double2 v = cmul(conj2(zp[li - m]), wts[pr.woff + pr.bl + l2]);
+      if ((m + pr.n) & 1) v = scl2(v, -1.0);
+      acc = add2(acc, v);
+    }
+  }
+  if (zscal && l2 < bl_scal) acc = add2(acc, zscal[(int64_t)b * zss + i]);
+  flm[(int64_t)b * fs + i] = acc;
+}
+
+__global__ void k_symmetrize(double2 *flm, int L, int64_t fs, int nb) {
+  const int64_t L2 = (int64_t)L * L;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= nb * L2) return;
+  const int b = (int)(gid / L2);
+  const int i = (int)(gid % L2);
+  int l = (int)sqrt((double)i);
+  while (l * l > i) --l;
+  while ((l + 1) * (l + 1) <= i) ++l;
+  const int m = i - l * l - l;
+  if (m <= 0) return;
+  double2 v = conj2(flm[(int64_t)b * fs + i]);
+  if (m & 1) v = scl2(v, -1.0);
+  flm[(int64_t)b * fs + l * l + l - m] = v;
+}
+
+__global__ void k_scale_copy(const double *x, double *y, int64_t n, double s) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = x[i] * s;
+}
+
+}  // namespace
+
+// ===========================================================================
+// wrappers
+// ===========================================================================
+
+void ring_forward(const void *rings, int64_t ring_stride, int64_t map_stride, int rpm, double2 *spec,
+                  int64_t spec_stride, int sw, int mlo, int nrings, int bl, bool real, cudaStream_t st) {
+  if (nrings <= 0) return;
+  const RingFFT &rf = ring_fft(2 * bl - 1);
+  RingArgs a = ring_args(rf, bl, nrings);
+  a.rings = rings;
+  a.ring_stride = ring_stride;
+  a.map_stride = map_stride;
+  a.rpm = rpm;
+  a.spec_out = spec;
+  a.spec_stride = spec_stride;
+  a.sw = sw;
+  a.mlo = mlo;
+  const int nblk = real ? (nrings + 1) / 2 : nrings;
+  const size_t smem = sizeof(double2) * rf.P;
+  if (real) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_ring_forward<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
+  } else {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_ring_forward<false><<<nblk, ring_threads(rf.P), smem, st>>>(a);
+  }
+  S2G_LAUNCHED();
+}
+
+void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, void *rings,
+                  int64_t ring_stride, int64_t map_stride, int rpm, int nrings, int bl, bool real,
+                  cudaStream_t st) {
+  if (nrings <= 0) return;
+  const RingFFT &rf = ring_fft(2 * bl - 1);
+  RingArgs a = ring_args(rf, bl, nrings);
+  a.spec_in = spec;
+  a.spec_stride = spec_stride;
+  a.sw = sw;
+  a.mlo = mlo;
+  a.rings_out = (double2 *)rings;
+  a.ring_stride = ring_stride;
+  a.map_stride = map_stride;
+  a.rpm = rpm;
+  const int nblk = real ? (nrings + 1) / 2 : nrings;
+  const size_t smem = sizeof(double2) * rf.P;
+  if (real) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_inverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_ring_inverse<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
+  } else {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_inverse<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_ring_inverse<false><<<nblk, ring_threads(rf.P), smem, st>>>(a);
+  }
+  S2G_LAUNCHED();
+}
+
+void contract_l2t(const L2T &p, cudaStream_t st) {
+  if (p.nb <= 0 || p.mhi < p.mlo) return;
+  ContractArgs a{};
+  a.table = p.use_q ? p.tb->Q : p.tb->D;
+  a.off = p.tb->d_off;
+  a.bl = p.tb->bl;
+  a.an = p.tb->an;
+  a.tmlo = p.tb->mlo;
+  a.n = p.n;
+  a.mlo = p.mlo;
+  a.lmin = p.lmin;
+  a.w = p.w;
+  a.wscale = p.wscale;
+  a.wconj = p.wconj;
+  a.src = p.x;
+  a.ss = p.xs;
+  a.sw_or_xL = p.xL;
+  a.x_half = p.x_half;
+  a.dst = p.out;
+  a.ds = p.os;
+  a.dw = p.ow;
+  a.d_mlo = p.omlo;
+  a.nb = p.nb;
+  const int nm = p.mhi - p.mlo + 1;
+  if (p.use_q)
+    launch_contract<1>(a, nm, a.bl, st);
+  else
+    launch_contract<0>(a, nm, a.bl, st);
+}
+
+void contract_t2l(const T2L &p, cudaStream_t st) {
+  if (p.nb <= 0 || p.mhi < p.mlo) return;
+  ContractArgs a{};
+  a.table = p.use_q ? p.tb->Q : p.tb->D;
+  a.off = p.tb->d_off;
+  a.bl = p.tb->bl;
+  a.an = p.tb->an;
+  a.tmlo = p.tb->mlo;
+  a.n = p.n;
+  a.mlo = p.mlo;
+  a.lmin = p.lmin;
+  a.w = p.w;
+  a.wscale = p.wscale;
+  a.wconj = p.wconj;
+  a.src = p.in;
+  a.ss = p.is;
+  a.sw_or_xL = p.iw;
+  a.s_mlo = p.imlo;
+  a.dst = p.y;
+  a.ds = p.ys;
+  a.nb = p.nb;
+  const int nm = p.mhi - p.mlo + 1;
+  if (p.use_q)
+    launch_contract<2>(a, nm, a.bl, st);
+  else
+    launch_contract<3>(a, nm, a.bl, st);
+}
+
+void gamma_synthesis(const double2 *G, double2 *spec, const int *ns, int nn, int ng, int bl, int nb,
+                     bool real, double c, cudaStream_t st) {
+  const int sw = real ? bl : 2 * bl - 1;
+  const int64_t total = (int64_t)nb * bl * sw;
+  if (total <= 0) return;
+  k_gamma_synth<<<ceil_div(total, 256), 256, 0, st>>>(G, spec, ns, nn, ng, bl, nb, real, c);
+  S2G_LAUNCHED();
+}
+
+void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int ng, int bl, int nb,
+                    bool real, double c, cudaStream_t st) {
+  const int64_t total = (int64_t)nb * bl * (2 * bl - 1);
+  if (total <= 0) return;
+  k_gamma_anal<<<ceil_div(total, 256), 256, 0, st>>>(spec, G, ns, nn, ng, bl, nb, real, c);
+  S2G_LAUNCHED();
+}
+
+void merge_lmn(double2 *flm, int L, int64_t fs, const double2 *z, int64_t zs, const MergePair *pairs,
+               int npairs, const double2 *wts, const double2 *zscal, int64_t zss, int bl_scal,
+               bool real, bool accumulate, int nb, cudaStream_t st) {
+  const int64_t total = (int64_t)nb * L * L;
+  if (total <= 0) return;
+  k_merge<<<ceil_div(total, 256), 256, 0, st>>>(flm, L, fs, z, zs, pairs, npairs, wts, zscal, zss,
+                                               bl_scal, real, accumulate, nb);
+  S2G_LAUNCHED();
+}
+
+void symmetrize_flm(double2 *flm, int L, int64_t fs, int nb, cudaStream_t st) {
+  const int64_t total = (int64_t)nb * L * L;
+  if (total <= 0) return;
+  k_symmetrize<<<ceil_div(total, 256), 256, 0, st>>>(flm, L, fs, nb);
+  S2G_LAUNCHED();
+}
+
+void scale_copy(const double *x, double *y, int64_t n, double s, cudaStream_t st) {
+  if (n <= 0) return;
+  k_scale_copy<<<ceil_div(n, 256), 256, 0, st>>>(x, y, n, s);
+  S2G_LAUNCHED();
+}
+
+}  // namespace s2g
+
+// ===========================================================================
+// Wigner-layout tiling multiplies, axisymmetric multiplies, thresholding
+// ===========================================================================
+
+namespace s2g {
+
+namespace {
+
+__device__ __forceinline__ int64_t sumsq(int64_t k) { return k < 0 ? 0 : k * (k + 1) * (2 * k + 1) / 6; }
+
+// SO3 compact storage index (src of the layout: so3_sampling_elmn2ind for
+// SO3_STORAGE_COMPACT / SO3_N_ORDER_NEGATIVE_FIRST)
+__device__ __forceinline__ int64_t so3_index(int l, int m, int n, int L, int N, bool real) {
+  const int64_t L2 = (int64_t)L * L;
+  if (real) return (int64_t)n * L2 - sumsq(n - 1) + (int64_t)l * l - (int64_t)n * n + l + m;
+  const int64_t drop = (n <= 0) ? sumsq(N - 1) - sumsq(-n) : sumsq(N - 1) + sumsq(n - 1);
+  return (int64_t)(n + N - 1) * L2 - drop + (int64_t)l * l - (int64_t)n * n + l + m;
+}
+
+__device__ __forceinline__ void lm_of(int i, int &l, int &m) {
+  int q = (int)sqrt((double)i);
+  while (q * q > i) --q;
+  while ((q + 1) * (q + 1) <= i) ++q;
+  l = q;
+  m = i - q * q - q;
+}
+
+__global__ void k_lmn_split(double2 *flmn, double2 *fscal, const double2 *__restrict__ flm,
+                            const double2 *__restrict__ psi, const double *__restrict__ phi,
+                            const LmnScale *__restrict__ scales, int nscale, int L, int bl_scal, int spin,
+                            int real, int mode) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L * L) return;
+  int l, m;
+  lm_of(i, l, m);
+  const int k = blockIdx.y, zi = blockIdx.z;
+  if (k == nscale) {  // scaling part
+    if (zi != 0 || l >= bl_scal || l < (real ? 0 : (spin < 0 ? -spin : spin))) return;
+    fscal[i] = scl2(flm[i], sqrt(4.0 * kPi / (2 * l + 1)) * phi[l]);
+    return;
+  }
+  const LmnScale sc = scales[k];
+  if (l >= sc.bl) return;
+  const int n = real ? (1 - sc.Nj % 2) + 2 * zi : -sc.Nj + 1 + 2 * zi;
+  if (n >= sc.Nj) return;
+  const int an = n < 0 ? -n : n, as = spin < 0 ? -spin : spin;
+  const int lmin = real ? n : (as > an ? as : an);
+  if (l < lmin) return;
+  double2 w = conj2(psi[(int64_t)sc.j * L * L + (int64_t)l * l + l + n]);
+  if (mode == 0) w = scl2(w, 8.0 * kPi * kPi / (2 * l + 1));
+  flmn[sc.loff + so3_index(l, m, n, sc.bl, sc.Nj, real)] = cmul(flm[i], w);
+}
+
+__global__ void k_lmn_merge(double2 *flm, const double2 *__restrict__ flmn, const double2 *__restrict__ fscal,
+                            const double2 *__restrict__ psi, const double *__restrict__ phi,
+                            const LmnScale *__restrict__ scales, int nscale, int L, int bl_scal, int spin,
+                            int real, int mode) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L * L) return;
+  int l, m;
+  lm_of(i, l, m);
+  const int as = spin < 0 ? -spin : spin;
+  double2 acc = make_double2(0.0, 0.0);
+  const double sc8 = (mode == 1) ? 8.0 * kPi * kPi / (2 * l + 1) : 1.0;
+  for (int k = 0; k < nscale; ++k) {
+    const LmnScale sc = scales[k];
+    if (l >= sc.bl) continue;
+    const int n0 = real ? 1 - sc.Nj % 2 : -sc.Nj + 1;
+    for (int n = n0; n < sc.Nj; n += 2) {
+      const int an = n < 0 ? -n : n;
+      const int lmin = real ? n : (as > an ? as : an);
+      if (l < lmin) continue;
+      const double2 *ps = psi + (int64_t)sc.j * L * L + (int64_t)l * l + l;
+      acc = add2(acc, cmul(flmn[sc.loff + so3_index(l, m, n, sc.bl, sc.Nj, real)], scl2(ps[n], sc8)));
+      if (real && n) {
+        double2 v = cmul(conj2(flmn[sc.loff + so3_index(l, -m, n, sc.bl, sc.Nj, real)]), scl2(ps[-n], sc8));
+        if ((m + n) & 1) v = scl2(v, -1.0);
+        acc = add2(acc, v);
+      }
+    }
+  }
+  if (l < bl_scal && l >= (real ? 0 : as)) acc = add2(acc, scl2(fscal[i], sqrt(4.0 * kPi / (2 * l + 1)) * phi[l]));
+  flm[i] = acc;
+}
+
+__global__ void k_axi_lm(double2 *flm, double2 *fwav, double2 *fscal, const double *__restrict__ wav_lm,
+                         const double *__restrict__ scal_lm, const int *__restrict__ bl,
+                         const int64_t *__restrict__ off, int J_min, int nscale, int L, int bl_scal, int synth) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L * L) return;
+  int l, m;
+  lm_of(i, l, m);
+  const double nl = sqrt((4.0 * kPi) / (2.0 * l + 1.0));
+  if (!synth) {
+    for (int k = 0; k < nscale; ++k)
+      if (l < bl[k]) fwav[off[k] + i] = scl2(flm[i], nl * wav_lm[(int64_t)(J_min + k) * L + l]);
+    if (l < bl_scal) fscal[i] = scl2(flm[i], nl * scal_lm[l]);
+  } else {
+    double2 acc = flm[i];
+    for (int k = 0; k < nscale; ++k)
+      if (l < bl[k]) acc = add2(acc, scl2(fwav[off[k] + i], nl * wav_lm[(int64_t)(J_min + k) * L + l]));
+    if (l < bl_scal) acc = add2(acc, scl2(fscal[i], nl * scal_lm[l]));
+    flm[i] = acc;
+  }
+}
+
+__global__ void k_threshold(double *g, const double *__restrict__ thr, const int64_t *__restrict__ off,
+                            int nscale, int64_t total) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  int k = 0;
+  while (k + 1 < nscale && off[k + 1] <= i) ++k;
+  const double v = g[i];
+  // the reference compares abs() of an int-converted double (truncation toward zero)
+  const long long t = (fabs(v) < 9.2e18) ? (long long)v : 0x7fffffffffffffffLL;
+  const long long a = t < 0 ? -t : t;
+  if ((double)a < thr[k]) g[i] = 0.0;
+}
+
+}  // namespace
+
+void lmn_split(double2 *flmn, double2 *fscal, const double2 *flm, const double2 *psi, const double *phi,
+               const LmnScale *scales, int nscale, int Nmax, int L, int bl_scal, int spin, bool real,
+               int mode, cudaStream_t st) {
+  dim3 grid(ceil_div((int64_t)L * L, 128), nscale + 1, Nmax > 0 ? Nmax : 1);
+  k_lmn_split<<<grid, 128, 0, st>>>(flmn, fscal, flm, psi, phi, scales, nscale, L, bl_scal, spin, real, mode);
+  S2G_LAUNCHED();
+}
+
+void lmn_merge(double2 *flm, const double2 *flmn, const double2 *fscal, const double2 *psi,
+               const double *phi, const LmnScale *scales, int nscale, int L, int bl_scal, int spin,
+               bool real, int mode, cudaStream_t st) {
+  k_lmn_merge<<<ceil_div((int64_t)L * L, 128), 128, 0, st>>>(flm, flmn, fscal, psi, phi, scales, nscale, L,
+                                                              bl_scal, spin, real, mode);
+  S2G_LAUNCHED();
+}
+
+void axisym_lm(double2 *flm, double2 *fwav, double2 *fscal, const double *wav_lm, const double *scal_lm,
+               const int *bl, const int64_t *off, int J_min, int nscale, int L, int bl_scal, int synth,
+               cudaStream_t st) {
+  k_axi_lm<<<ceil_div((int64_t)L * L, 128), 128, 0, st>>>(flm, fwav, fscal, wav_lm, scal_lm, bl, off, J_min,
+                                                           nscale, L, bl_scal, synth);
+  S2G_LAUNCHED();
+}
+
+void hard_threshold(double *g, const double *thr, const int64_t *off, int nscale, int64_t total,
+                    cudaStream_t st) {
+  if (total <= 0) return;
+  k_threshold<<<ceil_div(total, 256), 256, 0, st>>>(g, thr, off, nscale, total);
+  S2G_LAUNCHED();
+}
+
+}  // namespace s2g

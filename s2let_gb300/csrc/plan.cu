@@ -1,0 +1,387 @@
+// Plan construction: Wigner-d tables (FP64 scaled three-term recursion on the
+// GPU), the exact MW forward-quadrature operator W_eps, the forward tables
+// Q = D^T W / K^2 (FP64 GEMM on the GPU), and Bluestein FFT data.
+#include <cmath>
+#include <complex>
+#include <map>
+#include <mutex>
+
+#include "common.h"
+#include "plan.h"
+
+namespace s2g {
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// d^l_{m,an}(theta_t), l = l0..bl-1, for one (m, t) per thread.
+//
+// Start value at l0 = max(|m|, an) (closed forms of d^{l0}):
+//   l0 = m  >= an : (-1)^{l0-an} sqrt(C(2l0, l0+an)) c^{l0+an} s^{l0-an}
+//   l0 = -m >= an : sqrt(C(2l0, l0-an)) c^{l0-an} s^{l0+an}
+//   l0 = an > |m| : sqrt(C(2l0, l0+m)) c^{l0+m} s^{l0-m}
+// c = cos(theta/2), s = sin(theta/2).  sqrt(C) arrives from the host as
+// mant * 2^e; the powers are formed in log space; the recursion
+//   d^{l+1} = [(2l+1)(l(l+1) cos - m an) d^l - (l+1) sqrt((l^2-m^2)(l^2-an^2)) d^{l-1}]
+//             / [l sqrt(((l+1)^2-m^2)((l+1)^2-an^2))]
+// runs on a mantissa with a separate power-of-two exponent so that starts far
+// below the double range stay exact.
+// ---------------------------------------------------------------------------
+__global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ off, int bl, int an,
+                           int mlo, int nm, const double *__restrict__ start_mant,
+                           const int *__restrict__ start_exp) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (int64_t)nm * bl) return;
+  const int mi = (int)(gid / bl), t = (int)(gid % bl);
+  const int m = mlo + mi;
+  const int am = m < 0 ? -m : m;
+  const int l0 = am > an ? am : an;
+  const int nl = bl - l0;
+  if (nl <= 0) return;
+  const int K = 2 * bl - 1;
+  // theta/2 = pi (2t+1)/(2K) in (0, pi/2]: evaluated with sincospi on the exact
+  // rational so that theta = pi at t = bl-1 gives c = 0 exactly (never c < 0)
+  double s, c, ct, st_;
+  sincospi((double)(2 * t + 1) / (double)(2 * K), &s, &c);
+  sincospi((double)(2 * t + 1) / (double)K, &st_, &ct);
+  int ka, kb;
+  double sign = 1.0;
+  if (m >= 0 && m >= an) {
+    ka = l0 + an; kb = l0 - an; sign = ((l0 - an) & 1) ? -1.0 : 1.0;
+  } else if (m < 0 && am >= an) {
+    ka = l0 - an; kb = l0 + an;
+  } else {
+    ka = l0 + m; kb = l0 - m;
+  }
+  double v;
+  int E;
+  if ((ka > 0 && c == 0.0) || (kb > 0 && s == 0.0)) {
+    v = 0.0;  // the closed form vanishes; so does the whole recursion
+    E = 0;
+  } else {
+    const double lv = (ka ? ka * log(c) : 0.0) + (kb ? kb * log(s) : 0.0);
+    E = (int)floor(lv * 1.4426950408889634074);
+    v = sign * start_mant[mi] * exp(lv - E * 0.69314718055994530942);
+    E += start_exp[mi];
+  }
+  double vp = 0.0;
+  double *row = D + off[mi] + (int64_t)t * nl;
+  row[0] = ldexp(v, E);
+  const double mn = (double)m * (double)an, m2 = (double)m * m, n2 = (double)an * an;
+  int l = l0;
+  if (l0 == 0 && nl > 1) { /* m = an = 0: d^1_{00} = cos(theta) */
+    vp = v;
+    v = ct * v;
+    row[1] = ldexp(v, E);
+    l = 1;
+  }
+  for (; l + 1 < bl; ++l) {
+    const double dl = (double)l;
+    const double a = (2.0 * dl + 1.0) * (dl * (dl + 1.0) * ct - mn);
+    const double b = (dl + 1.0) * sqrt((dl * dl - m2) * (dl * dl - n2));
+    const double q = dl * sqrt(((dl + 1.0) * (dl + 1.0) - m2) * ((dl + 1.0) * (dl + 1.0) - n2));
+    const double vn = (a * v - b * vp) / q;
+    vp = v;
+    v = vn;
+    if (fabs(v) > 0x1p500) {
+      v = ldexp(v, -500);
+      vp = ldexp(vp, -500);
+      E += 500;
+    }
+    row[l + 1 - l0] = ldexp(v, E);
+  }
+}
+
+// w(p) = int_0^pi e^{ipt} sin t dt  (complex: +-i pi/2 at p = +-1)
+__device__ inline double2 wsin(int p) {
+  if (p == 1) return make_double2(0.0, 0.5 * kPi);
+  if (p == -1) return make_double2(0.0, -0.5 * kPi);
+  if (p & 1) return make_double2(0.0, 0.0);
+  return make_double2(2.0 / (1.0 - (double)p * (double)p), 0.0);
+}
+
+// A[m'][t] = e^{-i m' theta_t} + [t < bl-1] eps e^{i m' theta_t}   (m' in [-(bl-1), bl-1])
+__device__ inline double2 fold_basis(int mp, int t, int bl, int eps) {
+  const int K = 2 * bl - 1;
+  double sn, cs;
+  // angle m' * pi (2t+1)/K reduced modulo 2K for accuracy
+  long q = ((long)mp * (2 * t + 1)) % (2L * K);
+  sincospi((double)q / (double)K, &sn, &cs);
+  double2 r = make_double2(cs, -sn);
+  if (t < bl - 1) {
+    r.x += eps * cs;
+    r.y += eps * sn;
+  }
+  return r;
+}
+
+// TA[m''][t'] = sum_{m'} w(m' + m'') A[m'][t']
+__global__ void k_wmat_ta(double2 *__restrict__ TA, int bl, int eps) {
+  const int K = 2 * bl - 1;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (int64_t)K * bl) return;
+  const int mpp = (int)(gid / bl) - (bl - 1), tp = (int)(gid % bl);
+  double2 acc = make_double2(0.0, 0.0);
+  for (int mp = -(bl - 1); mp <= bl - 1; ++mp) {
+    const int p = mp + mpp;
+    if ((p & 1) && p != 1 && p != -1) continue;
+    const double2 w = wsin(p), a = fold_basis(mp, tp, bl, eps);
+    acc.x += w.x * a.x - w.y * a.y;
+    acc.y += w.x * a.y + w.y * a.x;
+  }
+  TA[gid] = acc;
+}
+
+// W[t][t'] = Re sum_{m''} A[m''][t] TA[m''][t'] / K^2
+__global__ void k_wmat_w(double *__restrict__ W, const double2 *__restrict__ TA, int bl, int eps) {
+  const int K = 2 * bl - 1;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (int64_t)bl * bl) return;
+  const int t = (int)(gid / bl), tp = (int)(gid % bl);
+  double acc = 0.0;
+  for (int mpp = -(bl - 1); mpp <= bl - 1; ++mpp) {
+    const double2 a = fold_basis(mpp, t, bl, eps);
+    const double2 b = TA[(int64_t)(mpp + bl - 1) * bl + tp];
+    acc += a.x * b.x - a.y * b.y;
+  }
+  W[gid] = acc / ((double)K * (double)K);
+}
+
+// Q_m[l][t'] = sum_t D_m[t][l] W_eps(m)[t][t'], tiled FP64 GEMM per m (grid.z = m).
+constexpr int QG_T = 64, QG_K = 16;
+__global__ void __launch_bounds__(256) k_qgemm(double *__restrict__ Q, const double *__restrict__ D,
+                                               const int64_t *__restrict__ off,
+                                               const double *__restrict__ Wp,
+                                               const double *__restrict__ Wm, int bl, int an,
+                                               int mlo) {
+  const int mi = blockIdx.z, m = mlo + mi;
+  const int am = m < 0 ? -m : m;
+  const int l0 = am > an ? am : an, nl = bl - l0;
+  const int row0 = blockIdx.y * QG_T, col0 = blockIdx.x * QG_T;  // rows: l-l0, cols: t'
+  if (row0 >= nl) return;
+  const double *W = (((m + an) & 1) == 0) ? Wp : Wm;
+  const double *Dm = D + off[mi];
+  double *Qm = Q + off[mi];
+  __shared__ double sA[QG_K][QG_T + 1];  // [t][l]
+  __shared__ double sB[QG_K][QG_T + 1];  // [t][t']
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4] = {};
+  for (int k0 = 0; k0 < bl; k0 += QG_K) {
+    for (int i = threadIdx.x; i < QG_K * QG_T; i += 256) {
+      const int kk = i / QG_T, c = i % QG_T;
+      const int t = k0 + kk;
+      sA[kk][c] = (t < bl && row0 + c < nl) ? Dm[(int64_t)t * nl + row0 + c] : 0.0;
+      sB[kk][c] = (t < bl && col0 + c < bl) ? W[(int64_t)t * bl + col0 + c] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < QG_K; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = sA[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = sB[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = row0 + ty * 4 + i;
+    if (r >= nl) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = col0 + tx * 4 + j;
+      if (c < bl) Qm[(int64_t)r * bl + c] = acc[i][j];
+    }
+  }
+}
+
+// host FFT (radix-2) for the Bluestein kernel spectrum
+void host_fft(std::vector<std::complex<double>> &x) {
+  const size_t n = x.size();
+  for (size_t i = 1, j = 0; i < n; ++i) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) std::swap(x[i], x[j]);
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    for (size_t i = 0; i < n; i += len)
+      for (size_t k = 0; k < len / 2; ++k) {
+        const double a = -2.0 * kPi * (double)k / (double)len;
+        std::complex<double> w(cos(a), sin(a));
+        auto u = x[i + k], v = x[i + k + len / 2] * w;
+        x[i + k] = u + v;
+        x[i + k + len / 2] = u - v;
+      }
+  }
+}
+
+std::mutex g_plan_mu;
+std::map<std::pair<int, int>, std::unique_ptr<WignerTable>> g_tables;
+std::map<int, std::unique_ptr<RingFFT>> g_rings;
+size_t g_bytes = 0;
+
+template <class T>
+T *dev_alloc(size_t n) {
+  T *p = nullptr;
+  S2G_CUDA(cudaMalloc(&p, sizeof(T) * (n ? n : 1)));
+  g_bytes += sizeof(T) * (n ? n : 1);
+  return p;
+}
+
+std::unique_ptr<WignerTable> build_table(int bl, int an) {
+  auto tb = std::make_unique<WignerTable>();
+  tb->bl = bl;
+  tb->an = an;
+  tb->mlo = an == 0 ? 0 : -(bl - 1);
+  tb->nm = bl - tb->mlo;
+  tb->off.assign(tb->nm + 1, 0);
+  std::vector<double> mant(tb->nm);
+  std::vector<int> ex(tb->nm);
+  for (int mi = 0; mi < tb->nm; ++mi) {
+    const int m = tb->mlo + mi;
+    const int l0 = tb->l0(m);
+    const int64_t nl = std::max(0, bl - l0);
+    tb->off[mi + 1] = tb->off[mi] + nl * bl;
+    // sqrt(C(2 l0, ka)) in extended precision, split into mantissa * 2^e
+    int ka;
+    const int am = std::abs(m);
+    if (m >= 0 && m >= an) ka = l0 + an;
+    else if (m < 0 && am >= an) ka = l0 - an;
+    else ka = l0 + m;
+    long double lc = 0.0L;
+    const int kk = std::min(ka, 2 * l0 - ka);
+    for (int i = 1; i <= kk; ++i) lc += logl((long double)(2 * l0 - kk + i)) - logl((long double)i);
+    lc *= 0.5L;
+    const long double ln2 = 0.693147180559945309417232121458176568L;
+    const int e = (int)floorl(lc / ln2);
+    mant[mi] = (double)expl(lc - e * ln2);
+    ex[mi] = e;
+  }
+  const int64_t n = tb->elems();
+  tb->D = dev_alloc<double>(n);
+  tb->Q = dev_alloc<double>(n);
+  tb->d_off = dev_alloc<int64_t>(tb->nm + 1);
+  S2G_CUDA(cudaMemcpy(tb->d_off, tb->off.data(), sizeof(int64_t) * (tb->nm + 1), cudaMemcpyHostToDevice));
+  double *d_mant = nullptr;
+  int *d_ex = nullptr;
+  S2G_CUDA(cudaMalloc(&d_mant, sizeof(double) * tb->nm));
+  S2G_CUDA(cudaMalloc(&d_ex, sizeof(int) * tb->nm));
+  S2G_CUDA(cudaMemcpy(d_mant, mant.data(), sizeof(double) * tb->nm, cudaMemcpyHostToDevice));
+  S2G_CUDA(cudaMemcpy(d_ex, ex.data(), sizeof(int) * tb->nm, cudaMemcpyHostToDevice));
+  {
+    const int64_t nthr = (int64_t)tb->nm * bl;
+    k_wigner_d<<<ceil_div(nthr, 128), 128>>>(tb->D, tb->d_off, bl, an, tb->mlo, tb->nm, d_mant, d_ex);
+    S2G_LAUNCHED();
+  }
+  // W_+ and W_- (exact forward quadrature operators), then Q = D^T W per m
+  const int K = 2 * bl - 1;
+  double2 *TA = nullptr;
+  double *W[2] = {nullptr, nullptr};
+  S2G_CUDA(cudaMalloc(&TA, sizeof(double2) * (size_t)K * bl));
+  for (int e = 0; e < 2; ++e) {
+    S2G_CUDA(cudaMalloc(&W[e], sizeof(double) * (size_t)bl * bl));
+    const int eps = e == 0 ? 1 : -1;
+    k_wmat_ta<<<ceil_div((int64_t)K * bl, 128), 128>>>(TA, bl, eps);
+    S2G_LAUNCHED();
+    k_wmat_w<<<ceil_div((int64_t)bl * bl, 128), 128>>>(W[e], TA, bl, eps);
+    S2G_LAUNCHED();
+  }
+  {
+    dim3 grid(ceil_div(bl, QG_T), ceil_div(bl, QG_T), tb->nm);
+    k_qgemm<<<grid, 256>>>(tb->Q, tb->D, tb->d_off, W[0], W[1], bl, an, tb->mlo);
+    S2G_LAUNCHED();
+  }
+  S2G_CUDA(cudaDeviceSynchronize());
+  cudaFree(TA);
+  cudaFree(W[0]);
+  cudaFree(W[1]);
+  cudaFree(d_mant);
+  cudaFree(d_ex);
+  return tb;
+}
+
+std::unique_ptr<RingFFT> build_ring(int K) {
+  auto r = std::make_unique<RingFFT>();
+  r->K = K;
+  int P = 1, logP = 0;
+  while (P < 2 * K - 1) {
+    P <<= 1;
+    ++logP;
+  }
+  r->P = P;
+  r->logP = logP;
+  std::vector<std::complex<double>> chirp(K), b(P, 0.0), tw(std::max(1, P / 2));
+  for (long k = 0; k < K; ++k) {
+    long q = (k * k) % (2L * K);
+    const double a = kPi * (double)q / (double)K;
+    chirp[k] = {cos(a), sin(a)};
+  }
+  b[0] = chirp[0];
+  for (int k = 1; k < K; ++k) b[k] = b[P - k] = chirp[k];
+  host_fft(b);
+  for (int k = 0; k < P / 2; ++k) {
+    const double a = -2.0 * kPi * (double)k / (double)P;
+    tw[k] = {cos(a), sin(a)};
+  }
+  r->chirp = dev_alloc<double2>(K);
+  r->bhat = dev_alloc<double2>(P);
+  r->tw = dev_alloc<double2>(std::max(1, P / 2));
+  S2G_CUDA(cudaMemcpy(r->chirp, chirp.data(), sizeof(double2) * K, cudaMemcpyHostToDevice));
+  S2G_CUDA(cudaMemcpy(r->bhat, b.data(), sizeof(double2) * P, cudaMemcpyHostToDevice));
+  S2G_CUDA(cudaMemcpy(r->tw, tw.data(), sizeof(double2) * std::max(1, P / 2), cudaMemcpyHostToDevice));
+  return r;
+}
+
+}  // namespace
+
+const WignerTable &wigner_table(int bl, int an) {
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  auto key = std::make_pair(bl, an);
+  auto it = g_tables.find(key);
+  if (it != g_tables.end()) return *it->second;
+  auto tb = build_table(bl, an);
+  const WignerTable &ref = *tb;
+  g_tables.emplace(key, std::move(tb));
+  return ref;
+}
+
+const RingFFT &ring_fft(int K) {
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  auto it = g_rings.find(K);
+  if (it != g_rings.end()) return *it->second;
+  auto r = build_ring(K);
+  const RingFFT &ref = *r;
+  g_rings.emplace(K, std::move(r));
+  return ref;
+}
+
+void release_plans() {
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  cudaDeviceSynchronize();
+  for (auto &kv : g_tables) {
+    cudaFree(kv.second->D);
+    cudaFree(kv.second->Q);
+    cudaFree(kv.second->d_off);
+  }
+  for (auto &kv : g_rings) {
+    cudaFree(kv.second->chirp);
+    cudaFree(kv.second->bhat);
+    cudaFree(kv.second->tw);
+  }
+  g_tables.clear();
+  g_rings.clear();
+  g_bytes = 0;
+}
+
+size_t plan_bytes() {
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  return g_bytes;
+}
+
+}  // namespace s2g

@@ -1,0 +1,46 @@
+// Cached device-side plans: Wigner tables per (band-limit, |n|) and Bluestein
+// FFT data per ring length.  Built once, kept until s2let_gpu_release_plans().
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+namespace s2g {
+
+// Wigner-d table of one band-limit bl and direction an = |n| >= 0 on the MW
+// theta grid theta_t = pi (2t+1)/(2bl-1), t < bl, for m in [mlo, bl-1]
+// (mlo = 0 when an = 0, else -(bl-1)); per m the l-range is
+// [l0(m), bl), l0 = max(|m|, an), nl = bl - l0.
+//   D (inverse)  block m: row-major [t][l - l0]      value d^l_{m,an}(theta_t)
+//   Q (forward)  block m: row-major [l - l0][t']     value sum_t d^l_{m,an}(theta_t) W_eps[t][t'] / (2bl-1)^2
+// where W_eps (eps = (-1)^{m+an}) is the exact MW quadrature operator: extension
+// of a ring signal to the full circle with parity eps, Fourier transform,
+// convolution with w(p) = int_0^pi e^{ipt} sin t dt, and folding back.
+// Entries for n < 0 are read from the |n| table at -m with sign (-1)^{m+|n|}.
+struct WignerTable {
+  int bl = 0, an = 0, mlo = 0, nm = 0;
+  std::vector<int64_t> off;  // host copy, nm+1 entries (elements)
+  int64_t *d_off = nullptr;
+  double *D = nullptr;
+  double *Q = nullptr;
+  int64_t elems() const { return off.empty() ? 0 : off.back(); }
+  int l0(int m) const { return (m < 0 ? -m : m) > an ? (m < 0 ? -m : m) : an; }
+};
+
+// Bluestein data for ring length K (odd or even), padded FFT size P = 2^logP >= 2K-1.
+struct RingFFT {
+  int K = 0, P = 0, logP = 0;
+  double2 *chirp = nullptr;  // K entries, exp(i pi k^2 / K)
+  double2 *bhat = nullptr;   // P entries, FFT_P of the wrapped chirp
+  double2 *tw = nullptr;     // P/2 entries, exp(-2 pi i k / P)
+};
+
+const WignerTable &wigner_table(int bl, int an);
+const RingFFT &ring_fft(int K);
+void release_plans();
+size_t plan_bytes();
+
+}  // namespace s2g
