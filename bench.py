@@ -1,0 +1,382 @@
+#!/usr/bin/env python3
+"""Benchmark: px2wav + wav2px round trips (maps/s) of real spin-0 maps at
+L=1024, N=4, B=2, J_min=2, upsample=0 on McEwen-Wiaux sampling.
+
+One step = analysis (s2let_analysis_px2wav_real) and synthesis
+(s2let_synthesis_wav2px_real) of one batch of maps already resident in HBM,
+through the batched device-pointer entry points of libs2let_gpu.so.
+
+Prints one JSON line (rank 0).  Fields beyond the headline:
+  e2e           same metric through the drop-in host-pointer C ABI, host<->device
+                copies inside the timed region
+  roofline      dominant kernel, measured live with CUDA events on its stream
+  cpu_baseline  the CPU oracle (C restatement of the reference path, OpenMP) on
+                the host cores, one map of the same workload
+  clocks        nvidia-smi samples taken during the timed region
+
+`--impl reference` times the reference path's CPU implementation instead (the
+oracle port, all host threads) and prints the same metric.
+Multi-GPU (torchrun): independent replicas, one batch per rank, max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "px2wav+wav2px maps/s at L=1024,N=4: mixed vs FP64 GPU at stated max err"
+NOMINAL_FP64_TFLOPS = 1.25  # GB300 FP64 (vendor nominal; no measured FP64 peak is available)
+
+
+def args_():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=8, help="maps per step per GPU")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--L", type=int, default=1024)
+    ap.add_argument("--N", type=int, default=4)
+    ap.add_argument("--B", type=float, default=2.0)
+    ap.add_argument("--J_min", type=int, default=2)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(a):
+    return dict(workload=f"real spin-0 maps, L={a.L}, N={a.N}, B={a.B:g}, J_min={a.J_min}, upsample=0, "
+                         "MW sampling, px2wav+wav2px",
+                L=a.L, N=a.N, B=a.B, J_min=a.J_min, spin=0, upsample=0, reality=1)
+
+
+def power_law_real_flm(rng, L):
+    """Gaussian flm with C_l ∝ (l+1)^-2, real-field symmetry, f_00 = 0."""
+    l = np.repeat(np.arange(L), 2 * np.arange(L) + 1)
+    m = np.concatenate([np.arange(-k, k + 1) for k in range(L)])
+    amp = 1.0 / (l + 1.0)
+    z = (rng.normal(size=L * L) + 1j * rng.normal(size=L * L)) * amp / np.sqrt(2.0)
+    z[m == 0] = rng.normal(size=L) / (np.arange(L) + 1.0)
+    neg = m < 0
+    ipos = l[neg] ** 2 + l[neg] - m[neg]
+    z[neg] = np.where(m[neg] % 2 == 0, 1.0, -1.0) * np.conj(z[ipos])
+    z[0] = 0.0
+    return z
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.dev)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profile_traffic(precision):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh).get(precision)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline_sample(p_args, f0):
+    """The oracle (C restatement of the reference path, OpenMP on all host cores):
+    one map through px2wav_real + wav2px_real.  Returns (seconds, f_wav, f_scal)."""
+    from oracle import oracle
+    from s2let_gb300.capi import make_parameters
+
+    port = oracle.port()
+    p = make_parameters(p_args.L, p_args.B, p_args.J_min, p_args.N, 0, 0)
+    t0 = time.perf_counter()
+    w, s = port.px2wav(f0, p, real=True)
+    port.wav2px(w, s, p, real=True)
+    return time.perf_counter() - t0, w, s
+
+
+def run_reference(a, rank):
+    if rank != 0:
+        return
+    rng = np.random.default_rng(0)
+    from oracle import oracle
+
+    port = oracle.port()
+    from s2let_gb300.capi import make_parameters
+
+    p = make_parameters(a.L, a.B, a.J_min, a.N, 0, 0)
+    f0 = port.alm2map(power_law_real_flm(rng, a.L), a.L, real=True)
+    times = []
+    for i in range(a.warmup + a.steps):
+        t0 = time.perf_counter()
+        w, s = port.px2wav(f0, p, real=True)
+        port.wav2px(w, s, p, real=True)
+        if i >= a.warmup:
+            times.append(time.perf_counter() - t0)
+    sec = sum(times) / len(times)
+    cores = os.cpu_count()
+    val = 1.0 / sec
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "maps/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload(a),
+        "cpu_baseline": {"value": val, "unit": "maps/s", "cores": cores, "kind": "port",
+                         "sample": "one map per step (px2wav_real + wav2px_real), CPU oracle: C restatement "
+                                   "of the reference S2LET layer over a restated SSHT/SO3, OpenMP on all cores"},
+        "e2e": {"value": val, "unit": "maps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    a = args_()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        run_reference(a, rank)
+        return
+
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import s2let_gb300
+    from s2let_gb300.capi import make_parameters
+
+    api = s2let_gb300.api()
+    lib = api.lib
+    lib.s2let_gpu_set_precision(1 if a.precision == "mixed" else 0)
+    p = make_parameters(a.L, a.B, a.J_min, a.N, 0, 0)
+    sz = api.sizes(p)
+    nb = a.batch
+    npx, nw, ns = sz["n_px"], sz["n_wav"], sz["n_scal"]
+
+    # seeded band-limited inputs, synthesised on the GPU from power-law flm
+    rng = np.random.default_rng(1000 + rank)
+    f_host = np.stack([api.alm2map(power_law_real_flm(rng, a.L), a.L, real=True) for _ in range(nb)])
+    s2let_gb300.check(lib, "alm2map_real")
+    f = torch.tensor(f_host, device=dev)
+    w = torch.zeros((nb, nw), dtype=torch.float64, device=dev)
+    sc = torch.zeros((nb, ns), dtype=torch.float64, device=dev)
+    fr = torch.zeros_like(f)
+    stream = torch.cuda.current_stream(dev)
+    st = C.c_void_p(stream.cuda_stream)
+    vp = lambda t: C.c_void_p(t.data_ptr())
+
+    def step():
+        rc = lib.s2let_gpu_analysis_px2wav_real_batch(vp(w), vp(sc), vp(f), nb, C.byref(p), st)
+        rc |= lib.s2let_gpu_synthesis_wav2px_real_batch(vp(fr), vp(w), vp(sc), nb, C.byref(p), st)
+        if rc:
+            raise RuntimeError(lib.s2let_gpu_last_error_string().decode())
+
+    t0 = time.perf_counter()
+    step()  # builds the plan (Wigner tables, FFT data)
+    torch.cuda.synchronize()
+    plan_s = time.perf_counter() - t0
+    for _ in range(max(a.warmup - 1, 0)):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region (device-resident inputs) ----
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    launches0 = lib.s2let_gpu_launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = lib.s2let_gpu_launch_count() - launches0
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / a.steps
+    ms_max = ms
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * nb * 1000.0 / ms_max
+
+    # round-trip fidelity on the band-limited inputs
+    rt_err = float(((fr - f).abs().max() / f.abs().max()).item())
+
+    # ---- roofline: one instrumented step, CUDA events around each launch ----
+    lib.s2let_gpu_timing_enable(1)
+    step()
+    torch.cuda.synchronize()
+    rep = (C.c_double * 24)()
+    lib.s2let_gpu_timing_report(rep, 6)
+    lib.s2let_gpu_timing_enable(0)
+    cats = ["fp64_contraction", "ring_dft", "gamma_dft", "tiling_merge", "tensor_contraction", "other"]
+    kernels = {c: {"launches": int(rep[4 * i]), "ms": rep[4 * i + 1], "flops": rep[4 * i + 2],
+                   "bytes": rep[4 * i + 3]} for i, c in enumerate(cats)}
+    dom = max(kernels, key=lambda c: kernels[c]["ms"])
+    kd = kernels[dom]
+    peaks, peak_kind = measured_peaks()
+    step_ms_instr = sum(k["ms"] for k in kernels.values())
+    if dom == "tensor_contraction":
+        ach = kd["flops"] / (kd["ms"] * 1e-3) / 1e12
+        peak = peaks.get("bf16_tflops")
+        roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak}
+    else:
+        ach = kd["bytes"] / (kd["ms"] * 1e-3) / 1e9
+        peak = peaks.get("hbm_gbs")
+        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak}
+    tr = profile_traffic(a.precision)
+    roof.update({
+        "kernel": dom, "peak_source": peak_kind, "launches_per_step": kd["launches"],
+        "avg_launch_ms": kd["ms"] / max(kd["launches"], 1),
+        "traffic": tr,
+        "share_of_step": kd["ms"] / step_ms_instr if step_ms_instr else None,
+        "fp64": {"achieved_tflops": kd["flops"] / (kd["ms"] * 1e-3) / 1e12 if kd["ms"] else None,
+                 "nominal_peak_tflops": NOMINAL_FP64_TFLOPS,
+                 "frac_of_nominal": (kd["flops"] / (kd["ms"] * 1e-3) / 1e12) / NOMINAL_FP64_TFLOPS
+                 if kd["ms"] else None},
+        "per_kernel_ms_per_step": {c: k["ms"] for c, k in kernels.items() if k["launches"]},
+    })
+
+    # ---- e2e through the drop-in host-pointer C ABI ----
+    e2e = None
+    if not a.no_e2e:
+        fh = torch.empty((nb, npx), dtype=torch.float64, pin_memory=True)
+        fh.copy_(torch.tensor(f_host))
+        wh = torch.empty((nb, nw), dtype=torch.float64, pin_memory=True)
+        sh = torch.empty((nb, ns), dtype=torch.float64, pin_memory=True)
+        frh = torch.empty((nb, npx), dtype=torch.float64, pin_memory=True)
+
+        def e2e_step():
+            for b in range(nb):
+                lib.s2let_analysis_px2wav_real(vp(wh[b]), vp(sh[b]), vp(fh[b]), C.byref(p))
+                lib.s2let_synthesis_wav2px_real(vp(frh[b]), vp(wh[b]), vp(sh[b]), C.byref(p))
+            s2let_gb300.check(lib, "host API")
+
+        e2e_step()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            e2e_step()
+        e2e_s = (time.perf_counter() - t0) / a.steps
+        if dist:
+            t = torch.tensor([e2e_s], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": world * nb / e2e_s, "unit": "maps/s",
+               "h2d_bytes_per_step": nb * (npx + nw + ns) * 8, "d2h_bytes_per_step": nb * (nw + ns + npx) * 8,
+               "api": "s2let_analysis_px2wav_real + s2let_synthesis_wav2px_real, pinned host buffers"}
+
+    # ---- CPU baseline (rank 0, N=1) and the error against it ----
+    cpu = None
+    err_vs_oracle = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        sec, w_o, s_o = cpu_baseline_sample(a, f_host[0])
+        cpu = {"value": 1.0 / sec, "unit": "maps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"1 map (px2wav_real + wav2px_real) of the same workload, {sec:.1f} s; CPU oracle = C "
+                         "restatement of the reference S2LET layer over restated SSHT/SO3, OpenMP"}
+        wg = w[0].cpu().numpy()
+        sg = sc[0].cpu().numpy()
+        err_vs_oracle = max(float(np.abs(wg - w_o).max() / np.abs(w_o).max()),
+                            float(np.abs(sg - s_o).max() / np.abs(s_o).max()))
+
+    if rank != 0:
+        return
+    cfg = workload(a)
+    cfg.update({"batch_per_gpu": nb, "precision": a.precision, "parallelism": f"replicas x{world}",
+                "l2_policy": "inputs larger than L2: f 16.8 MB + f_wav 274 MB per map, no flush needed",
+                "plan_build_s": plan_s})
+    out = {
+        "metric": METRIC, "value": value, "unit": "maps/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if a.precision == "fp64" else "bf16-split/f32-acc/f64",
+        "data": "synthetic: Gaussian flm, C_l ∝ (l+1)^-2, real-field symmetry, seeded; maps by GPU alm2map",
+        "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        "gpu_launches": launches,
+        "max_rel_err_vs_oracle": err_vs_oracle, "roundtrip_rel_err": rt_err,
+    }
+    print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

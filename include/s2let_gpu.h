@@ -379,6 +379,16 @@ const char *s2let_gpu_last_error_string(void);
 int s2let_gpu_set_precision(int mode);
 int s2let_gpu_get_precision(void);
 
+/* Adjoints of the plain MW transforms (host buffers): the adjoint of
+ * s2let_mw_map2alm maps flm to pixels, the adjoint of s2let_mw_alm2map maps
+ * pixels to flm.  These are the SSHT adjoints the reference calls internally
+ * (ssht_adjoint_mw_forward_sov_sym / ssht_adjoint_mw_inverse_sov_sym at
+ * src/c/s2let_analysis_adjoint.c:506 and src/c/s2let_synthesis_adjoint.c:480). */
+void s2let_gpu_mw_adjoint_map2alm(S2LET_COMPLEX(double) *f, const S2LET_COMPLEX(double) *flm, int L,
+                                  int spin);
+void s2let_gpu_mw_adjoint_alm2map(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f, int L,
+                                  int spin);
+
 /* Drops cached plans (Wigner tables, FFT chirps) and frees their device memory. */
 void s2let_gpu_release_plans(void);
 /* Bytes of device memory currently held by cached plans. */
@@ -416,6 +426,14 @@ int s2let_gpu_synthesis_adjoint_px2wav_batch(void *f_wav, void *f_scal, const vo
 
 /* Number of this library's kernel launches since load (instrumentation). */
 uint64_t s2let_gpu_launch_count(void);
+
+/* Optional per-kernel timing with CUDA events on the launching stream.
+ * enable(1) clears previous records; report fills out[c*4 + {0,1,2,3}] =
+ * {launches, milliseconds, algorithmic flops, algorithmic bytes} for kernel
+ * category c < ncat (0 FP64 contraction, 1 ring DFT, 2 gamma DFT, 3 tiling
+ * merge, 4 split-precision tensor-core contraction, 5 other). */
+int s2let_gpu_timing_enable(int on);
+int s2let_gpu_timing_report(double *out, int ncat);
 
 #ifdef __cplusplus
 }

@@ -150,6 +150,7 @@ static void inverse_any(void *fout, const complex double *flmn, const so3_parame
   oracle_ssht_inverse_multi(maps, (const complex double **)x, spin, rl, nn, L);
   for (int g = 0; g < ng; ++g) {
     double gam = 2.0 * SPI * g / ng;
+#pragma omp parallel for schedule(static) if (npx >= 4096)
     for (size_t i = 0; i < npx; ++i) {
       complex double acc = 0;
       for (int k = 0; k < nn; ++k) {
@@ -210,6 +211,7 @@ static void forward_any(complex double *flmn, const void *fin, const so3_paramet
     rl[k] = real && n == 0;
     y[k] = (complex double *)xcalloc((size_t)L * L, sizeof(complex double));
     maps[k] = rl[k] ? xcalloc(npx, sizeof(double)) : xcalloc(npx, sizeof(complex double));
+#pragma omp parallel for schedule(static) if (npx >= 4096)
     for (size_t i = 0; i < npx; ++i) {
       complex double acc = 0;
       for (int g = 0; g < ng; ++g) {
@@ -274,6 +276,7 @@ static void adjoint_inverse_any(complex double *flmn, const void *fin, const so3
     rl[k] = real && n == 0;
     y[k] = (complex double *)xcalloc((size_t)L * L, sizeof(complex double));
     maps[k] = rl[k] ? xcalloc(npx, sizeof(double)) : xcalloc(npx, sizeof(complex double));
+#pragma omp parallel for schedule(static) if (npx >= 4096)
     for (size_t i = 0; i < npx; ++i) {
       complex double acc = 0;
       for (int g = 0; g < ng; ++g) {
@@ -347,6 +350,7 @@ static void adjoint_forward_any(void *fout, const complex double *flmn, const so
   oracle_ssht_adjoint_forward_multi(maps, (const complex double **)x, spin, rl, nn, L);
   for (int g = 0; g < ng; ++g) {
     double gam = 2.0 * SPI * g / ng;
+#pragma omp parallel for schedule(static) if (npx >= 4096)
     for (size_t i = 0; i < npx; ++i) {
       complex double acc = 0;
       for (int k = 0; k < nn; ++k) {

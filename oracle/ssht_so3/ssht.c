@@ -65,11 +65,14 @@ void oracle_delta_quadrant(double *D, int l) {
   }
   double *a = (double *)xcalloc(w + 1, sizeof(double));
   double *b = (double *)xcalloc(w + 1, sizeof(double));
+  double *sv = (double *)xcalloc(w, sizeof(double));
+  int *se = (int *)xcalloc(w, sizeof(int));
   for (int n = 1; n <= l; ++n) {
     a[n] = sqrt((double)(l - n) * (double)(l + n + 1));
     b[n] = sqrt((double)(l + n) * (double)(l - n + 1));
   }
-  /* r(0) = C(2l,l)/4^l as mantissa*2^exponent */
+  /* start values sqrt(C(2l, l+mp)/4^l) = sv[mp] * 2^se[mp], from r(0) = C(2l,l)/4^l
+   * and r(mp)/r(mp-1) = (l-mp+1)/(l+mp), kept as mantissa * 2^exponent */
   double rm = 1.0;
   int re = 0;
   for (int k = 1; k <= l; ++k) {
@@ -83,18 +86,20 @@ void oracle_delta_quadrant(double *D, int l) {
       rm = frexp(rm * ((double)(l - mp + 1) / (double)(l + mp)), &e);
       re += e;
     }
-    /* start = sqrt(rm * 2^re) = v * 2^E */
-    double v;
-    int E;
     if (re & 1) {
-      v = sqrt(rm * 2.0);
-      E = (re - 1) / 2;
+      sv[mp] = sqrt(rm * 2.0);
+      se[mp] = (re - 1) / 2;
     } else {
-      v = sqrt(rm);
-      E = re / 2;
+      sv[mp] = sqrt(rm);
+      se[mp] = re / 2;
     }
+  }
+  /* three-term recursion in the second index, downward from n = l */
+#pragma omp parallel for schedule(static) if (l >= 64)
+  for (int mp = 0; mp <= l; ++mp) {
     double *row = D + (size_t)mp * w;
-    double vn = v, vn1 = 0.0;
+    double vn = sv[mp], vn1 = 0.0;
+    int E = se[mp];
     row[l] = ldexp(vn, E);
     for (int n = l; n >= 1; --n) {
       double vm = (-2.0 * mp * vn - a[n] * vn1) / b[n];
@@ -110,6 +115,8 @@ void oracle_delta_quadrant(double *D, int l) {
   }
   free(a);
   free(b);
+  free(sv);
+  free(se);
 }
 
 void oracle_wigner_d_column(double *out, int L, int m, int n, double theta) {
@@ -271,6 +278,7 @@ static void harm_to_mm(complex double **F, const complex double **flm, const int
       delta_column(Pn, D, l, n);
       for (int mp = 0; mp <= l; ++mp) Pa[mp] = neg1(mp) * Pn[mp];
       const int m0 = mlo > -l ? mlo : -l;
+#pragma omp parallel for schedule(static) if (l >= 64)
       for (int m = m0; m <= l; ++m) {
         complex double a = flm[j][l * l + l + m];
         if (a == 0) continue;
@@ -319,6 +327,7 @@ static void mm_to_harm(complex double **flm, complex double **G, const int *spin
       delta_column(Pn, D, l, n);
       for (int mp = 0; mp <= l; ++mp) Pa[mp] = neg1(mp) * Pn[mp];
       const int m0 = mlo > -l ? mlo : -l;
+#pragma omp parallel for schedule(static) if (l >= 64)
       for (int m = m0; m <= l; ++m) {
         const complex double *row = G[j] + (size_t)(m + L - 1) * L;
         const double *drow = D + (size_t)abs(m) * w;
@@ -349,8 +358,11 @@ static void mm_to_harm(complex double **flm, complex double **G, const int *spin
 static void mm_to_map(complex double *fc, double *fr, const complex double *F, int L, int s,
                       int mlo) {
   const int K = 2 * L - 1, n = -s;
-  complex double *x = (complex double *)xcalloc(K, sizeof(complex double));
   complex double *ring = (complex double *)xcalloc((size_t)L * K, sizeof(complex double));
+#pragma omp parallel if (L >= 64)
+  {
+  complex double *x = (complex double *)xcalloc(K, sizeof(complex double));
+#pragma omp for schedule(static)
   for (int m = mlo; m <= L - 1; ++m) {
     const complex double *row = F + (size_t)(m + L - 1) * L;
     memset(x, 0, sizeof(complex double) * K);
@@ -363,6 +375,9 @@ static void mm_to_map(complex double *fc, double *fr, const complex double *F, i
     offt_dft(x, K, +1);
     for (int t = 0; t < L; ++t) ring[(size_t)t * K + modk(m, K)] = x[t];
   }
+  free(x);
+  }
+#pragma omp parallel for schedule(static) if (L >= 64)
   for (int t = 0; t < L; ++t) {
     complex double *r = ring + (size_t)t * K;
     if (mlo == 0) /* Hermitian completion for a real signal */
@@ -375,7 +390,6 @@ static void mm_to_map(complex double *fc, double *fr, const complex double *F, i
         fc[(size_t)t * K + p] = r[p];
     }
   }
-  free(x);
   free(ring);
 }
 
@@ -424,24 +438,31 @@ void ssht_core_mw_inverse_sov_sym_real(double *f, const complex double *flm, int
 /* map -> per-m ring spectra Fm[mi*L + t] (unnormalised phi-DFT). */
 static void map_to_rings(complex double *Fm, const complex double *fc, const double *fr, int L) {
   const int K = 2 * L - 1;
-  complex double *x = (complex double *)xcalloc(K, sizeof(complex double));
-  for (int t = 0; t < L; ++t) {
-    for (int p = 0; p < K; ++p) x[p] = fr ? fr[(size_t)t * K + p] : fc[(size_t)t * K + p];
-    offt_dft(x, K, -1);
-    for (int m = -(L - 1); m <= L - 1; ++m) Fm[(size_t)(m + L - 1) * L + t] = x[modk(m, K)];
+#pragma omp parallel if (L >= 64)
+  {
+    complex double *x = (complex double *)xcalloc(K, sizeof(complex double));
+#pragma omp for schedule(static)
+    for (int t = 0; t < L; ++t) {
+      for (int p = 0; p < K; ++p) x[p] = fr ? fr[(size_t)t * K + p] : fc[(size_t)t * K + p];
+      offt_dft(x, K, -1);
+      for (int m = -(L - 1); m <= L - 1; ++m) Fm[(size_t)(m + L - 1) * L + t] = x[modk(m, K)];
+    }
+    free(x);
   }
-  free(x);
 }
 
 /* per-m ring spectra -> G (mp >= 0, symmetrised) for the forward contraction */
 static void rings_to_G(complex double *G, const complex double *Fm, int L, int s, int mlo) {
   const int K = 2 * L - 1, n = -s;
+  memset(G, 0, sizeof(complex double) * (size_t)K * L);
+#pragma omp parallel if (L >= 64)
+  {
   conv_plan *cp = get_conv(L);
   complex double *ext = (complex double *)xcalloc(K, sizeof(complex double));
   complex double *Fh = (complex double *)xcalloc(K, sizeof(complex double));
   complex double *Gf = (complex double *)xcalloc(K, sizeof(complex double));
   complex double *scr = (complex double *)xcalloc(cp->P, sizeof(complex double));
-  memset(G, 0, sizeof(complex double) * (size_t)K * L);
+#pragma omp for schedule(static)
   for (int m = mlo; m <= L - 1; ++m) {
     const complex double *Fr = Fm + (size_t)(m + L - 1) * L;
     double eps = neg1(m + s);
@@ -461,6 +482,7 @@ static void rings_to_G(complex double *G, const complex double *Fm, int L, int s
   free(Fh);
   free(Gf);
   free(scr);
+  }
 }
 
 void oracle_ssht_forward_multi(complex double **flm, const void **f, const int *spin,
@@ -515,8 +537,11 @@ void ssht_core_mw_forward_sov_conv_sym_real(complex double *flm, const double *f
 
 static void rings_to_H(complex double *H, const complex double *Fm, int L, int s, int mlo) {
   const int K = 2 * L - 1, n = -s;
-  complex double *x = (complex double *)xcalloc(K, sizeof(complex double));
   memset(H, 0, sizeof(complex double) * (size_t)K * L);
+#pragma omp parallel if (L >= 64)
+  {
+  complex double *x = (complex double *)xcalloc(K, sizeof(complex double));
+#pragma omp for schedule(static)
   for (int m = mlo; m <= L - 1; ++m) {
     const complex double *Fr = Fm + (size_t)(m + L - 1) * L;
     memset(x, 0, sizeof(complex double) * K);
@@ -535,6 +560,7 @@ static void rings_to_H(complex double *H, const complex double *Fm, int L, int s
     }
   }
   free(x);
+  }
 }
 
 void oracle_ssht_adjoint_inverse_multi(complex double **flm, const void **f, const int *spin,
@@ -590,12 +616,15 @@ void ssht_adjoint_mw_inverse_sov_sym_real(complex double *flm, const double *f, 
 static void G_to_map_adj(complex double *fc, double *fr, const complex double *Gs, int L, int s,
                          int mlo) {
   const int K = 2 * L - 1, n = -s;
+  complex double *ring = (complex double *)xcalloc((size_t)L * K, sizeof(complex double));
+#pragma omp parallel if (L >= 64)
+  {
   conv_plan *cp = get_conv(L);
   complex double *Gf = (complex double *)xcalloc(K, sizeof(complex double));
   complex double *Fh = (complex double *)xcalloc(K, sizeof(complex double));
   complex double *x = (complex double *)xcalloc(K, sizeof(complex double));
   complex double *scr = (complex double *)xcalloc(cp->P, sizeof(complex double));
-  complex double *ring = (complex double *)xcalloc((size_t)L * K, sizeof(complex double));
+#pragma omp for schedule(static)
   for (int m = mlo; m <= L - 1; ++m) {
     const complex double *g = Gs + (size_t)(m + L - 1) * L;
     double sym = neg1(m + n);
@@ -617,6 +646,12 @@ static void G_to_map_adj(complex double *fc, double *fr, const complex double *G
       ring[(size_t)t * K + modk(m, K)] = v;
     }
   }
+  free(Gf);
+  free(Fh);
+  free(x);
+  free(scr);
+  }
+#pragma omp parallel for schedule(static) if (L >= 64)
   for (int t = 0; t < L; ++t) {
     complex double *r = ring + (size_t)t * K;
     offt_dft(r, K, +1);
@@ -627,10 +662,6 @@ static void G_to_map_adj(complex double *fc, double *fr, const complex double *G
         fc[(size_t)t * K + p] = r[p];
     }
   }
-  free(Gf);
-  free(Fh);
-  free(x);
-  free(scr);
   free(ring);
 }
 

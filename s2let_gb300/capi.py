@@ -122,6 +122,8 @@ GPU_SIGNATURES = {
     "s2let_gpu_release_plans": (None, []),
     "s2let_gpu_plan_bytes": (C.c_size_t, []),
     "s2let_gpu_launch_count": (C.c_uint64, []),
+    "s2let_gpu_timing_enable": (I, [I]),
+    "s2let_gpu_timing_report": (I, [V, I]),
     "s2let_gpu_mw_adjoint_map2alm": (None, [V, V, I, I]),
     "s2let_gpu_mw_adjoint_alm2map": (None, [V, V, I, I]),
     "s2let_gpu_analysis_px2wav_real_batch": (I, [V, V, V, I, P, V]),

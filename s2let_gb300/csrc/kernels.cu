@@ -11,6 +11,7 @@
 //  k_merge     harmonic tiling merge (lmn -> lm) fused over scales/directions.
 #include "common.h"
 #include "kernels.h"
+#include "timing.h"
 
 namespace s2g {
 
@@ -358,9 +359,29 @@ __global__ void __launch_bounds__(CT_M) k_contract(ContractArgs a) {
   }
 }
 
+// algorithmic work of one contraction launch: one complex x real MAC (4 flops)
+// per (l, m, t) per map; bytes = table entries read once + coefficient/spectrum I/O
+void contract_work(const ContractArgs &a, int nm, double *flops, double *bytes) {
+  double macs = 0, tab = 0, io = 0;
+  for (int i = 0; i < nm; ++i) {
+    const int m = a.mlo + i, am = m < 0 ? -m : m;
+    const int l0 = am > a.an ? am : a.an, lst = l0 > a.lmin ? l0 : a.lmin;
+    const int nl = a.bl - lst;
+    if (nl <= 0) continue;
+    macs += (double)nl * a.bl;
+    tab += (double)nl * a.bl;
+    io += (double)nl + a.bl;
+  }
+  *flops = 4.0 * macs * a.nb;
+  *bytes = 8.0 * tab + 16.0 * io * a.nb;
+}
+
 template <int MODE>
 void launch_contract(const ContractArgs &a, int nm, int rows, cudaStream_t st) {
   const int nbt = a.nb >= 8 ? 8 : (a.nb >= 4 ? 4 : (a.nb >= 2 ? 2 : 1));
+  double fl = 0, by = 0;
+  if (timing_enabled()) contract_work(a, nm, &fl, &by);
+  KTimer kt(KC_CONTRACT, st, fl, by);
   dim3 grid(nm, ceil_div(rows, CT_M), ceil_div(a.nb, nbt));
   switch (nbt) {
   case 8: k_contract<MODE, 8><<<grid, CT_M, 0, st>>>(a); break;
@@ -514,6 +535,7 @@ void ring_forward(const void *rings, int64_t ring_stride, int64_t map_stride, in
   a.mlo = mlo;
   const int nblk = real ? (nrings + 1) / 2 : nrings;
   const size_t smem = sizeof(double2) * rf.P;
+  KTimer kt(KC_RING, st, 0.0, (double)nrings * (2 * bl - 1) * (real ? 8.0 : 16.0) + (double)nrings * sw * 16.0);
   if (real) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_ring_forward<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
@@ -540,6 +562,7 @@ void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, voi
   a.rpm = rpm;
   const int nblk = real ? (nrings + 1) / 2 : nrings;
   const size_t smem = sizeof(double2) * rf.P;
+  KTimer kt(KC_RING, st, 0.0, (double)nrings * (2 * bl - 1) * (real ? 8.0 : 16.0) + (double)nrings * sw * 16.0);
   if (real) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_inverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_ring_inverse<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
@@ -613,6 +636,7 @@ void gamma_synthesis(const double2 *G, double2 *spec, const int *ns, int nn, int
   const int sw = real ? bl : 2 * bl - 1;
   const int64_t total = (int64_t)nb * bl * sw;
   if (total <= 0) return;
+  KTimer kt(KC_GAMMA, st, 0.0, 0.0);
   k_gamma_synth<<<ceil_div(total, 256), 256, 0, st>>>(G, spec, ns, nn, ng, bl, nb, real, c);
   S2G_LAUNCHED();
 }
@@ -621,6 +645,7 @@ void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int 
                     bool real, double c, cudaStream_t st) {
   const int64_t total = (int64_t)nb * bl * (2 * bl - 1);
   if (total <= 0) return;
+  KTimer kt(KC_GAMMA, st, 0.0, 0.0);
   k_gamma_anal<<<ceil_div(total, 256), 256, 0, st>>>(spec, G, ns, nn, ng, bl, nb, real, c);
   S2G_LAUNCHED();
 }
@@ -630,6 +655,7 @@ void merge_lmn(double2 *flm, int L, int64_t fs, const double2 *z, int64_t zs, co
                bool real, bool accumulate, int nb, cudaStream_t st) {
   const int64_t total = (int64_t)nb * L * L;
   if (total <= 0) return;
+  KTimer kt(KC_MERGE, st, 0.0, 0.0);
   k_merge<<<ceil_div(total, 256), 256, 0, st>>>(flm, L, fs, z, zs, pairs, npairs, wts, zscal, zss,
                                                bl_scal, real, accumulate, nb);
   S2G_LAUNCHED();
@@ -638,6 +664,7 @@ void merge_lmn(double2 *flm, int L, int64_t fs, const double2 *z, int64_t zs, co
 void symmetrize_flm(double2 *flm, int L, int64_t fs, int nb, cudaStream_t st) {
   const int64_t total = (int64_t)nb * L * L;
   if (total <= 0) return;
+  KTimer kt(KC_MERGE, st, 0.0, 0.0);
   k_symmetrize<<<ceil_div(total, 256), 256, 0, st>>>(flm, L, fs, nb);
   S2G_LAUNCHED();
 }

@@ -1,0 +1,32 @@
+// Optional per-kernel timing: CUDA events recorded on the launching stream
+// around each instrumented launch, with the launch's algorithmic work (flops,
+// bytes) attached.  Off by default; s2let_gpu_timing_enable() switches it on.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace s2g {
+
+enum KCat {
+  KC_CONTRACT = 0,  // FP64 Wigner/Legendre contractions
+  KC_RING = 1,      // Bluestein ring DFTs
+  KC_GAMMA = 2,     // gamma DFTs
+  KC_MERGE = 3,     // tiling merge / split / symmetrise
+  KC_MIXED = 4,     // split-precision tensor-core contractions
+  KC_OTHER = 5,
+  KC_N = 6
+};
+
+bool timing_enabled();
+
+class KTimer {
+ public:
+  KTimer(int cat, cudaStream_t st, double flops, double bytes);
+  ~KTimer();
+
+ private:
+  int slot_ = -1;
+  cudaStream_t st_ = nullptr;
+};
+
+}  // namespace s2g
