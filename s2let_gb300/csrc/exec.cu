@@ -648,7 +648,16 @@ int host_directional(const char *fn, s2g::Op op, const s2let_parameters_t *p, bo
     s2g::Scratch S(st);
     s2g::Staged io(S);
     const int L = p->L;
-    const int64_t npx = (int64_t)L * (2 * L - 1), nw = s2let_n_wav(p), ns = s2let_n_scal(p);
+    const int64_t npx = (int64_t)L * (2 * L - 1), ns = s2let_n_scal(p);
+    // the transforms advance scale offsets with N_j; when some N_j < N the end of
+    // the s2let_n_wav-sized buffer is never touched (src/c/s2let_analysis.c:340-350),
+    // so only the used prefix crosses the bus
+    s2let_parameters_t q = *p;
+    if (real) {
+      q.reality = 1;
+      q.spin = 0;
+    }
+    const int64_t nw = s2g::make_layout(q, real).woff.back();
     const int64_t dd = real ? 1 : 2;  // doubles per sample
     void *dpx = nullptr, *dlm = nullptr, *dwav = nullptr, *dscal = nullptr;
     using namespace s2g;
@@ -777,6 +786,7 @@ void host_manual(const char *fn, s2g::Op op, cplx *flm, cplx *f_wav, cplx *f_sca
       printf("B = %g\n", pow(L, 1.0 / (float)(J + 2)));
       printf("N = %i\n", N);
       printf("L = %i\n", L);
+      fflush(stdout);
     }
     cudaStream_t st = s2g::host_stream();
     {

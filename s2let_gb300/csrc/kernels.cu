@@ -396,9 +396,20 @@ void launch_contract(const ContractArgs &a, int nm, int rows, cudaStream_t st) {
 // gamma DFTs
 // ---------------------------------------------------------------------------
 
+// e^{i n_k gamma_g} for all (g, k) of one call, gamma_g = 2 pi g / ng
+constexpr int kMaxGammaTw = 512;
+
 __global__ void k_gamma_synth(const double2 *__restrict__ G, double2 *__restrict__ spec,
                               const int *__restrict__ ns, int nn, int ng, int bl, int nb, int real,
                               double c) {
+  __shared__ double2 tw[kMaxGammaTw];  // tw[g * nn + k]
+  for (int i = threadIdx.x; i < ng * nn; i += blockDim.x) {
+    const int g = i / nn, k = i % nn;
+    double sn, cs;
+    sincospi(2.0 * (double)((ns[k] * g) % ng) / (double)ng, &sn, &cs);
+    tw[i] = make_double2(cs, sn);
+  }
+  __syncthreads();
   const int W = 2 * bl - 1;
   const int sw = real ? bl : W, smlo = real ? 0 : -(bl - 1);
   const int64_t total = (int64_t)nb * bl * sw;
@@ -409,16 +420,18 @@ __global__ void k_gamma_synth(const double2 *__restrict__ G, double2 *__restrict
   const int b = (int)(gid / ((int64_t)sw * bl));
   const int m = smlo + col;
   const int64_t gb = (int64_t)b * nn * bl * W;
+  double2 gv[16], gm[16];
+  for (int k = 0; k < nn; ++k) {
+    const double2 *Gk = G + gb + (int64_t)k * bl * W + (int64_t)t * W;
+    gv[k] = Gk[m + bl - 1];
+    gm[k] = (real && ns[k] > 0) ? conj2(Gk[-m + bl - 1]) : make_double2(0.0, 0.0);
+  }
   for (int g = 0; g < ng; ++g) {
     double2 acc = make_double2(0.0, 0.0);
     for (int k = 0; k < nn; ++k) {
-      const int n = ns[k];
-      double sn, cs;
-      sincospi(2.0 * (double)((n * g) % ng) / (double)ng, &sn, &cs);
-      const double2 e = make_double2(cs, sn);
-      const double2 *Gk = G + gb + (int64_t)k * bl * W + (int64_t)t * W;
-      acc = add2(acc, cmul(e, Gk[m + bl - 1]));
-      if (real && n > 0) acc = add2(acc, cmul(conj2(e), conj2(Gk[-m + bl - 1])));
+      const double2 e = tw[g * nn + k];
+      acc = add2(acc, cmul(e, gv[k]));
+      if (real && ns[k] > 0) acc = add2(acc, cmul(conj2(e), gm[k]));
     }
     spec[((int64_t)b * ng + g) * bl * sw + (int64_t)t * sw + col] = scl2(acc, c);
   }
@@ -427,6 +440,14 @@ __global__ void k_gamma_synth(const double2 *__restrict__ G, double2 *__restrict
 __global__ void k_gamma_anal(const double2 *__restrict__ spec, double2 *__restrict__ G,
                              const int *__restrict__ ns, int nn, int ng, int bl, int nb, int real,
                              double c) {
+  __shared__ double2 tw[kMaxGammaTw];  // tw[g * nn + k] = e^{-i n_k gamma_g}
+  for (int i = threadIdx.x; i < ng * nn; i += blockDim.x) {
+    const int g = i / nn, k = i % nn;
+    double sn, cs;
+    sincospi(2.0 * (double)((ns[k] * g) % ng) / (double)ng, &sn, &cs);
+    tw[i] = make_double2(cs, -sn);
+  }
+  __syncthreads();
   const int W = 2 * bl - 1;
   const int sw = real ? bl : W, smlo = real ? 0 : -(bl - 1);
   const int64_t total = (int64_t)nb * bl * W;
@@ -436,23 +457,18 @@ __global__ void k_gamma_anal(const double2 *__restrict__ spec, double2 *__restri
   const int t = (int)((gid / W) % bl);
   const int b = (int)(gid / ((int64_t)W * bl));
   const int m = col - (bl - 1);
-  for (int k = 0; k < nn; ++k) {
-    const int n = ns[k];
-    double2 acc = make_double2(0.0, 0.0);
-    for (int g = 0; g < ng; ++g) {
-      double2 s;
-      const double2 *sg = spec + ((int64_t)b * ng + g) * bl * sw + (int64_t)t * sw;
-      if (real) {
-        s = m >= 0 ? sg[m] : conj2(sg[-m]);
-      } else {
-        s = sg[m - smlo];
-      }
-      double sn, cs;
-      sincospi(2.0 * (double)((n * g) % ng) / (double)ng, &sn, &cs);
-      acc = add2(acc, cmul(make_double2(cs, -sn), s));
-    }
-    G[((int64_t)b * nn + k) * bl * W + (int64_t)t * W + col] = scl2(acc, c);
+  double2 acc[16];
+  for (int k = 0; k < nn; ++k) acc[k] = make_double2(0.0, 0.0);
+  for (int g = 0; g < ng; ++g) {
+    const double2 *sg = spec + ((int64_t)b * ng + g) * bl * sw + (int64_t)t * sw;
+    double2 s;
+    if (real)
+      s = m >= 0 ? sg[m] : conj2(sg[-m]);
+    else
+      s = sg[m - smlo];
+    for (int k = 0; k < nn; ++k) acc[k] = add2(acc[k], cmul(tw[g * nn + k], s));
   }
+  for (int k = 0; k < nn; ++k) G[((int64_t)b * nn + k) * bl * W + (int64_t)t * W + col] = scl2(acc[k], c);
 }
 
 // ---------------------------------------------------------------------------
@@ -633,6 +649,7 @@ void contract_t2l(const T2L &p, cudaStream_t st) {
 
 void gamma_synthesis(const double2 *G, double2 *spec, const int *ns, int nn, int ng, int bl, int nb,
                      bool real, double c, cudaStream_t st) {
+  S2G_REQUIRE(nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
   const int sw = real ? bl : 2 * bl - 1;
   const int64_t total = (int64_t)nb * bl * sw;
   if (total <= 0) return;
@@ -643,6 +660,7 @@ void gamma_synthesis(const double2 *G, double2 *spec, const int *ns, int nn, int
 
 void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int ng, int bl, int nb,
                     bool real, double c, cudaStream_t st) {
+  S2G_REQUIRE(nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
   const int64_t total = (int64_t)nb * bl * (2 * bl - 1);
   if (total <= 0) return;
   KTimer kt(KC_GAMMA, st, 0.0, 0.0);

@@ -14,22 +14,104 @@ namespace s2g {
 namespace {
 
 // ---------------------------------------------------------------------------
-// d^l_{m,an}(theta_t), l = l0..bl-1, for one (m, t) per thread.
+// double-double arithmetic (pairs hi + lo, |lo| <= ulp(hi)/2), used where the
+// Wigner tables are built so that the stored doubles are correctly rounded
+// ---------------------------------------------------------------------------
+struct dd {
+  double hi, lo;
+};
+__device__ __forceinline__ dd dd_quick(double a, double b) {
+  const double s = a + b;
+  return dd{s, b - (s - a)};
+}
+__device__ __forceinline__ dd dd_add(dd a, dd b) {
+  const double s = a.hi + b.hi, bb = s - a.hi;
+  const double e = (a.hi - (s - bb)) + (b.hi - bb) + a.lo + b.lo;
+  return dd_quick(s, e);
+}
+__device__ __forceinline__ dd dd_neg(dd a) { return dd{-a.hi, -a.lo}; }
+__device__ __forceinline__ dd dd_mul(dd a, dd b) {
+  const double p = a.hi * b.hi;
+  double e = fma(a.hi, b.hi, -p);
+  e = fma(a.hi, b.lo, e);
+  e = fma(a.lo, b.hi, e);
+  return dd_quick(p, e);
+}
+__device__ __forceinline__ dd dd_mul_d(dd a, double b) {
+  const double p = a.hi * b;
+  double e = fma(a.hi, b, -p);
+  e = fma(a.lo, b, e);
+  return dd_quick(p, e);
+}
+__device__ __forceinline__ dd dd_div(dd a, dd b) {
+  const double q1 = a.hi / b.hi;
+  dd r = dd_add(a, dd_neg(dd_mul_d(b, q1)));
+  const double q2 = r.hi / b.hi;
+  r = dd_add(r, dd_neg(dd_mul_d(b, q2)));
+  const double q3 = r.hi / b.hi;
+  return dd_add(dd_quick(q1, q2), dd{q3, 0.0});
+}
+// sqrt of an exactly representable double, to double-double accuracy
+__device__ __forceinline__ dd dd_sqrt_d(double x) {
+  const double r = sqrt(x);
+  if (r == 0.0) return dd{0.0, 0.0};
+  return dd_quick(r, fma(-r, r, x) / (2.0 * r));
+}
+__device__ __forceinline__ void dd_renorm(dd &a, int &E) {
+  int e;
+  frexp(a.hi, &e);
+  a.hi = ldexp(a.hi, -e);
+  a.lo = ldexp(a.lo, -e);
+  E += e;
+}
+// x^k as mantissa * 2^E (x > 0), square-and-multiply with renormalisation
+__device__ dd dd_pow(dd x, int k, int &E) {
+  dd r{1.0, 0.0};
+  E = 0;
+  int Eb = 0;
+  dd_renorm(x, Eb);
+  while (k) {
+    if (k & 1) {
+      r = dd_mul(r, x);
+      E += Eb;
+      dd_renorm(r, E);
+    }
+    k >>= 1;
+    if (k) {
+      x = dd_mul(x, x);
+      Eb *= 2;
+      dd_renorm(x, Eb);
+    }
+  }
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// d^l_{m,an}(theta_t), l = l0..bl-1, for one (m, t) per thread, in double-double.
 //
 // Start value at l0 = max(|m|, an) (closed forms of d^{l0}):
 //   l0 = m  >= an : (-1)^{l0-an} sqrt(C(2l0, l0+an)) c^{l0+an} s^{l0-an}
 //   l0 = -m >= an : sqrt(C(2l0, l0-an)) c^{l0-an} s^{l0+an}
 //   l0 = an > |m| : sqrt(C(2l0, l0+m)) c^{l0+m} s^{l0-m}
-// c = cos(theta/2), s = sin(theta/2).  sqrt(C) arrives from the host as
-// mant * 2^e; the powers are formed in log space; the recursion
-//   d^{l+1} = [(2l+1)(l(l+1) cos - m an) d^l - (l+1) sqrt((l^2-m^2)(l^2-an^2)) d^{l-1}]
-//             / [l sqrt(((l+1)^2-m^2)((l+1)^2-an^2))]
-// runs on a mantissa with a separate power-of-two exponent so that starts far
-// below the double range stay exact.
+// c = cos(theta/2), s = sin(theta/2), both supplied by the host in double-double
+// from the exact rational theta_t = pi (2t+1)/(2bl-1); sqrt(C) arrives as
+// double-double mantissa * 2^e.  Three-term recursion in l:
+//   d^{l+1} = [(2l+1)(l(l+1) x - m an) d^l - (l+1) sqrt((l^2-m^2)(l^2-an^2)) d^{l-1}]
+//             / [l sqrt(((l+1)^2-m^2)((l+1)^2-an^2))],     x = cos(theta).
+// x is never formed (its rounding is amplified by l^2 near the poles):
+//   l(l+1) x - m an = (l(l+1) - m an) - l(l+1) u,   u = 2 s^2   (northern half)
+//                   = l(l+1) v - (l(l+1) + m an),   v = 2 c^2   (southern half)
+// with exact integer parts.  The mantissa carries a separate power-of-two
+// exponent so that starts far below the double range stay exact.
 // ---------------------------------------------------------------------------
+struct AngleDD {
+  double s_hi, s_lo, c_hi, c_lo, u_hi, u_lo;  // u = 2 s^2 (north) or 2 c^2 (south)
+};
+
 __global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ off, int bl, int an,
-                           int mlo, int nm, const double *__restrict__ start_mant,
-                           const int *__restrict__ start_exp) {
+                           int mlo, int nm, const double *__restrict__ start_hi,
+                           const double *__restrict__ start_lo, const int *__restrict__ start_exp,
+                           const AngleDD *__restrict__ ang) {
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= (int64_t)nm * bl) return;
   const int mi = (int)(gid / bl), t = (int)(gid % bl);
@@ -39,11 +121,9 @@ __global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ o
   const int nl = bl - l0;
   if (nl <= 0) return;
   const int K = 2 * bl - 1;
-  // theta/2 = pi (2t+1)/(2K) in (0, pi/2]: evaluated with sincospi on the exact
-  // rational so that theta = pi at t = bl-1 gives c = 0 exactly (never c < 0)
-  double s, c, ct, st_;
-  sincospi((double)(2 * t + 1) / (double)(2 * K), &s, &c);
-  sincospi((double)(2 * t + 1) / (double)K, &st_, &ct);
+  const AngleDD A = ang[t];
+  const dd s{A.s_hi, A.s_lo}, c{A.c_hi, A.c_lo}, u{A.u_hi, A.u_lo};
+  const bool north = (2 * (2 * t + 1) <= K);
   int ka, kb;
   double sign = 1.0;
   if (m >= 0 && m >= an) {
@@ -53,42 +133,54 @@ __global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ o
   } else {
     ka = l0 + m; kb = l0 - m;
   }
-  double v;
-  int E;
-  if ((ka > 0 && c == 0.0) || (kb > 0 && s == 0.0)) {
-    v = 0.0;  // the closed form vanishes; so does the whole recursion
-    E = 0;
-  } else {
-    const double lv = (ka ? ka * log(c) : 0.0) + (kb ? kb * log(s) : 0.0);
-    E = (int)floor(lv * 1.4426950408889634074);
-    v = sign * start_mant[mi] * exp(lv - E * 0.69314718055994530942);
-    E += start_exp[mi];
-  }
-  double vp = 0.0;
   double *row = D + off[mi] + (int64_t)t * nl;
-  row[0] = ldexp(v, E);
+  if ((ka > 0 && c.hi == 0.0) || (kb > 0 && s.hi == 0.0)) {
+    // the closed form vanishes (theta = pi); so does the whole recursion
+    for (int i = 0; i < nl; ++i) row[i] = 0.0;
+    return;
+  }
+  int E = start_exp[mi], e1 = 0, e2 = 0;
+  dd v{start_hi[mi], start_lo[mi]};
+  if (ka) {
+    v = dd_mul(v, dd_pow(c, ka, e1));
+    E += e1;
+  }
+  if (kb) {
+    v = dd_mul(v, dd_pow(s, kb, e2));
+    E += e2;
+  }
+  v.hi *= sign;
+  v.lo *= sign;
+  dd vp{0.0, 0.0};
+  row[0] = ldexp(v.hi, E);
   const double mn = (double)m * (double)an, m2 = (double)m * m, n2 = (double)an * an;
   int l = l0;
   if (l0 == 0 && nl > 1) { /* m = an = 0: d^1_{00} = cos(theta) */
+    const dd x = north ? dd_add(dd{1.0, 0.0}, dd_neg(u)) : dd_add(u, dd{-1.0, 0.0});
     vp = v;
-    v = ct * v;
-    row[1] = ldexp(v, E);
+    v = dd_mul(x, v);
+    row[1] = ldexp(v.hi, E);
     l = 1;
   }
   for (; l + 1 < bl; ++l) {
     const double dl = (double)l;
-    const double a = (2.0 * dl + 1.0) * (dl * (dl + 1.0) * ct - mn);
-    const double b = (dl + 1.0) * sqrt((dl * dl - m2) * (dl * dl - n2));
-    const double q = dl * sqrt(((dl + 1.0) * (dl + 1.0) - m2) * ((dl + 1.0) * (dl + 1.0) - n2));
-    const double vn = (a * v - b * vp) / q;
+    const double ll1 = dl * (dl + 1.0);
+    const dd lu = dd_mul_d(u, ll1);
+    const dd xterm = north ? dd_add(dd{ll1 - mn, 0.0}, dd_neg(lu)) : dd_add(lu, dd{-(ll1 + mn), 0.0});
+    const dd a = dd_mul_d(xterm, 2.0 * dl + 1.0);
+    const dd b = dd_mul_d(dd_sqrt_d((dl * dl - m2) * (dl * dl - n2)), dl + 1.0);
+    const dd q = dd_mul_d(dd_sqrt_d(((dl + 1.0) * (dl + 1.0) - m2) * ((dl + 1.0) * (dl + 1.0) - n2)), dl);
+    const dd vn = dd_div(dd_add(dd_mul(a, v), dd_neg(dd_mul(b, vp))), q);
     vp = v;
     v = vn;
-    if (fabs(v) > 0x1p500) {
-      v = ldexp(v, -500);
-      vp = ldexp(vp, -500);
+    if (fabs(v.hi) > 0x1p500) {
+      v.hi = ldexp(v.hi, -500);
+      v.lo = ldexp(v.lo, -500);
+      vp.hi = ldexp(vp.hi, -500);
+      vp.lo = ldexp(vp.lo, -500);
       E += 500;
     }
-    row[l + 1 - l0] = ldexp(v, E);
+    row[l + 1 - l0] = ldexp(v.hi, E);
   }
 }
 
@@ -241,14 +333,15 @@ std::unique_ptr<WignerTable> build_table(int bl, int an) {
   tb->mlo = an == 0 ? 0 : -(bl - 1);
   tb->nm = bl - tb->mlo;
   tb->off.assign(tb->nm + 1, 0);
-  std::vector<double> mant(tb->nm);
+  std::vector<double> st_hi(tb->nm), st_lo(tb->nm);
   std::vector<int> ex(tb->nm);
+  const long double ln2 = 0.693147180559945309417232121458176568L;
   for (int mi = 0; mi < tb->nm; ++mi) {
     const int m = tb->mlo + mi;
     const int l0 = tb->l0(m);
     const int64_t nl = std::max(0, bl - l0);
     tb->off[mi + 1] = tb->off[mi] + nl * bl;
-    // sqrt(C(2 l0, ka)) in extended precision, split into mantissa * 2^e
+    // sqrt(C(2 l0, ka)) in extended precision, split into (hi + lo) * 2^e
     int ka;
     const int am = std::abs(m);
     if (m >= 0 && m >= an) ka = l0 + an;
@@ -258,25 +351,57 @@ std::unique_ptr<WignerTable> build_table(int bl, int an) {
     const int kk = std::min(ka, 2 * l0 - ka);
     for (int i = 1; i <= kk; ++i) lc += logl((long double)(2 * l0 - kk + i)) - logl((long double)i);
     lc *= 0.5L;
-    const long double ln2 = 0.693147180559945309417232121458176568L;
     const int e = (int)floorl(lc / ln2);
-    mant[mi] = (double)expl(lc - e * ln2);
+    const long double mant = expl(lc - e * ln2);
+    st_hi[mi] = (double)mant;
+    st_lo[mi] = (double)(mant - (long double)st_hi[mi]);
     ex[mi] = e;
+  }
+  // half-angles of the MW rings, theta_t / 2 = pi (2t+1) / (2(2bl-1)), in extended precision
+  std::vector<AngleDD> ang(bl);
+  {
+    const long double pi_l = 3.141592653589793238462643383279502884197L;
+    const int K = 2 * bl - 1;
+    auto split = [](long double x, double &hi, double &lo) {
+      hi = (double)x;
+      lo = (double)(x - (long double)hi);
+    };
+    for (int t = 0; t < bl; ++t) {
+      long double sl, cl;
+      if (2 * t + 1 == K) {
+        sl = 1.0L;
+        cl = 0.0L;  // theta = pi exactly
+      } else {
+        const long double h = pi_l * (long double)(2 * t + 1) / (long double)(2 * K);
+        sl = sinl(h);
+        cl = cosl(h);
+      }
+      const bool north = (2 * (2 * t + 1) <= K);
+      const long double u = north ? 2.0L * sl * sl : 2.0L * cl * cl;
+      split(sl, ang[t].s_hi, ang[t].s_lo);
+      split(cl, ang[t].c_hi, ang[t].c_lo);
+      split(u, ang[t].u_hi, ang[t].u_lo);
+    }
   }
   const int64_t n = tb->elems();
   tb->D = dev_alloc<double>(n);
   tb->Q = dev_alloc<double>(n);
   tb->d_off = dev_alloc<int64_t>(tb->nm + 1);
   S2G_CUDA(cudaMemcpy(tb->d_off, tb->off.data(), sizeof(int64_t) * (tb->nm + 1), cudaMemcpyHostToDevice));
-  double *d_mant = nullptr;
+  double *d_hi = nullptr, *d_lo = nullptr;
   int *d_ex = nullptr;
-  S2G_CUDA(cudaMalloc(&d_mant, sizeof(double) * tb->nm));
+  AngleDD *d_ang = nullptr;
+  S2G_CUDA(cudaMalloc(&d_hi, sizeof(double) * tb->nm));
+  S2G_CUDA(cudaMalloc(&d_lo, sizeof(double) * tb->nm));
   S2G_CUDA(cudaMalloc(&d_ex, sizeof(int) * tb->nm));
-  S2G_CUDA(cudaMemcpy(d_mant, mant.data(), sizeof(double) * tb->nm, cudaMemcpyHostToDevice));
+  S2G_CUDA(cudaMalloc(&d_ang, sizeof(AngleDD) * bl));
+  S2G_CUDA(cudaMemcpy(d_hi, st_hi.data(), sizeof(double) * tb->nm, cudaMemcpyHostToDevice));
+  S2G_CUDA(cudaMemcpy(d_lo, st_lo.data(), sizeof(double) * tb->nm, cudaMemcpyHostToDevice));
   S2G_CUDA(cudaMemcpy(d_ex, ex.data(), sizeof(int) * tb->nm, cudaMemcpyHostToDevice));
+  S2G_CUDA(cudaMemcpy(d_ang, ang.data(), sizeof(AngleDD) * bl, cudaMemcpyHostToDevice));
   {
     const int64_t nthr = (int64_t)tb->nm * bl;
-    k_wigner_d<<<ceil_div(nthr, 128), 128>>>(tb->D, tb->d_off, bl, an, tb->mlo, tb->nm, d_mant, d_ex);
+    k_wigner_d<<<ceil_div(nthr, 128), 128>>>(tb->D, tb->d_off, bl, an, tb->mlo, tb->nm, d_hi, d_lo, d_ex, d_ang);
     S2G_LAUNCHED();
   }
   // W_+ and W_- (exact forward quadrature operators), then Q = D^T W per m
@@ -301,8 +426,10 @@ std::unique_ptr<WignerTable> build_table(int bl, int an) {
   cudaFree(TA);
   cudaFree(W[0]);
   cudaFree(W[1]);
-  cudaFree(d_mant);
+  cudaFree(d_hi);
+  cudaFree(d_lo);
   cudaFree(d_ex);
+  cudaFree(d_ang);
   return tb;
 }
 

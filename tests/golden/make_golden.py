@@ -1,0 +1,77 @@
+"""Generates tests/golden/*.npz from the reference's own S2LET C sources compiled
+in place (oracle/_ref/libs2let_ref.so, see oracle/Makefile) over the project's
+SSHT/SO3 restatement.  Inputs are seeded numpy draws stored with the outputs, so
+the fixtures pin the oracle port (oracle/s2let_port.c) without the reference.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle  # noqa: E402
+from s2let_gb300.capi import make_parameters  # noqa: E402
+
+CASES = {
+    # name: (L, N, B, J_min, spin, upsample)
+    "dir_L16_N4_s0_multires": (16, 4, 2.0, 2, 0, 0),
+    "dir_L16_N4_s0_fullres": (16, 4, 2.0, 2, 0, 1),
+    "dir_L16_N4_s2_multires": (16, 4, 2.0, 2, 2, 0),
+    "dir_L16_N4_s2_fullres": (16, 4, 2.0, 2, 2, 1),
+    "dir_L17_N3_B2.5_s1": (17, 3, 2.5, 1, 1, 0),
+    "dir_L12_N5_Jmin0": (12, 5, 2.0, 0, 0, 0),
+    "dir_L24_N5_s2_Jmin3": (24, 5, 2.0, 3, 2, 0),
+}
+AXI = {"axi_L16_J0": (16, 2.0, 0), "axi_L32_B3_J1": (32, 3.0, 1)}
+
+
+def main():
+    oracle.build(ref=True)
+    R = oracle.ref()
+    rng = np.random.default_rng(20261203)
+    for name, (L, N, B, J_min, spin, up) in CASES.items():
+        p = make_parameters(L, B, J_min, N, spin, up)
+        npx = L * (2 * L - 1)
+        out = {"params": np.array([L, N, B, J_min, spin, up], dtype=np.float64)}
+        f = rng.normal(size=npx) + 1j * rng.normal(size=npx)
+        flm = rng.normal(size=L * L) + 1j * rng.normal(size=L * L)
+        out["f"] = f
+        out["flm"] = flm
+        out["px2wav_wav"], out["px2wav_scal"] = R.px2wav(f, p)
+        out["wav2px"] = R.wav2px(out["px2wav_wav"], out["px2wav_scal"], p)
+        out["adj_wav2px"] = R.analysis_adjoint_wav2px(out["px2wav_wav"], out["px2wav_scal"], p)
+        out["adj_px2wav_wav"], out["adj_px2wav_scal"] = R.synthesis_adjoint_px2wav(f, p)
+        out["lm2wav_wav"], out["lm2wav_scal"] = R.lm2wav(flm, p)
+        out["wav2lm"] = R.wav2lm(out["lm2wav_wav"], out["lm2wav_scal"], p)
+        out["lm2lmn"], out["lm2lmn_scal"] = R.lm2lmn(flm, p)
+        out["lmn2lm"] = R.lmn2lm(out["lm2lmn"], out["lm2lmn_scal"], p)
+        psi, phi = R.tiling(p)
+        out["psi"], out["phi"] = psi, phi
+        if spin == 0:
+            fr = rng.normal(size=npx)
+            out["f_real"] = fr
+            out["px2wav_real_wav"], out["px2wav_real_scal"] = R.px2wav(fr, p, real=True)
+            out["wav2px_real"] = R.wav2px(out["px2wav_real_wav"], out["px2wav_real_scal"], p, real=True)
+            out["adj_wav2px_real"] = R.analysis_adjoint_wav2px(out["px2wav_real_wav"], out["px2wav_real_scal"], p,
+                                                               real=True)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    for name, (L, B, J_min) in AXI.items():
+        p = make_parameters(L, B, J_min, 1, 0, 0)
+        npx = L * (2 * L - 1)
+        f = rng.normal(size=npx)
+        out = {"params": np.array([L, B, J_min], dtype=np.float64), "f": f}
+        for mr in (0, 1):
+            w, s = R.axisym("analysis", [f], p, bool(mr), True)
+            out[f"ana_mr{mr}_wav"], out[f"ana_mr{mr}_scal"] = w, s
+            out[f"syn_mr{mr}"] = R.axisym("synthesis", [w, s], p, bool(mr), True)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", len(CASES) + len(AXI), "fixtures")
+
+
+if __name__ == "__main__":
+    main()

@@ -111,3 +111,49 @@ def test_lm2wav_wav2lm(gpu, oracle_port, case):
         w_g, s_g = gpu.lm2wav(flr, p, real=True)
         assert rel_err(w_g, w_o) < TOL and rel_err(s_g, s_o) < TOL
         assert rel_err(gpu.wav2lm(w_o, s_o, p, real=True), oracle_port.wav2lm(w_o, s_o, p, real=True)) < TOL
+
+
+import glob  # noqa: E402
+import os  # noqa: E402
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "dir_*.npz")))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_gpu_matches_reference_golden(gpu, path):
+    """GPU outputs against vectors produced by the reference's own S2LET sources."""
+    g = np.load(path)
+    L, N, B, J_min, spin, up = g["params"]
+    p = make_parameters(int(L), B, int(J_min), int(N), int(spin), int(up))
+    w, s = gpu.px2wav(g["f"], p)
+    assert rel_err(w, g["px2wav_wav"]) < TOL and rel_err(s, g["px2wav_scal"]) < TOL
+    assert rel_err(gpu.wav2px(g["px2wav_wav"], g["px2wav_scal"], p), g["wav2px"]) < TOL
+    assert rel_err(gpu.analysis_adjoint_wav2px(g["px2wav_wav"], g["px2wav_scal"], p), g["adj_wav2px"]) < TOL
+    a, b = gpu.synthesis_adjoint_px2wav(g["f"], p)
+    assert rel_err(a, g["adj_px2wav_wav"]) < TOL and rel_err(b, g["adj_px2wav_scal"]) < TOL
+    w, s = gpu.lm2wav(g["flm"], p)
+    assert rel_err(w, g["lm2wav_wav"]) < TOL and rel_err(s, g["lm2wav_scal"]) < TOL
+    lmn, sc = gpu.lm2lmn(g["flm"], p)
+    n = len(g["lm2lmn"])
+    assert rel_err(lmn[:n], g["lm2lmn"]) < TOL
+    if "f_real" in g.files:
+        w, s = gpu.px2wav(g["f_real"], p, real=True)
+        assert rel_err(w, g["px2wav_real_wav"]) < TOL and rel_err(s, g["px2wav_real_scal"]) < TOL
+        assert rel_err(gpu.wav2px(w, s, p, real=True), g["wav2px_real"]) < TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L", [256, 1024])
+def test_full_size_properties(gpu, L):
+    """Size-independent checks at the benchmark size: exact round trip on a
+    band-limited map, and linearity px2wav(a f + b g) = a px2wav(f) + b px2wav(g)."""
+    p = make_parameters(L, 2.0, 2, 4, 0, 0)
+    rng = np.random.default_rng(21)
+    f = gpu.alm2map(random_flm(rng, L, real=True, power=lambda l: 1.0 / (l + 1)), L, real=True)
+    g2 = gpu.alm2map(random_flm(rng, L, real=True, power=lambda l: 1.0 / (l + 1)), L, real=True)
+    w, s = gpu.px2wav(f, p, real=True)
+    assert rel_err(gpu.wav2px(w, s, p, real=True), f) < 1e-12
+    w2, s2 = gpu.px2wav(g2, p, real=True)
+    w3, s3 = gpu.px2wav(2.0 * f - 0.5 * g2, p, real=True)
+    assert rel_err(w3, 2.0 * w - 0.5 * w2) < 1e-13
