@@ -342,6 +342,13 @@ void s2let_transform_axisym_wav_hardthreshold_real(double *g_wav, const double *
                                                    const s2let_parameters_t *parameters); /* :38 */
 void s2let_transform_axisym_wav_hardthreshold_multires_real(double *g_wav, const double *threshold,
                                                             const s2let_parameters_t *parameters); /* :39 */
+/* No counterpart in the reference.  The hard threshold above (multires = 0:
+ * _real, 1: _multires_real) with no device allocation: staging lives in one
+ * 8 MiB static device array shared by every call, so calls that overlap on the
+ * GPU (two host threads at once) race.  Requests above 8 MiB (maps + 2 x 256 B
+ * of scale tables) return S2LET_GPU_ERR_INVALID.  Returns the status. */
+int s2let_gpu_axisym_wav_hardthreshold_real_noalloc(double *g_wav, const double *threshold,
+                                                    const s2let_parameters_t *parameters, int multires);
 
 /* ------------------------------------------------------------------------ */
 /* Plain MW spherical-harmonic transforms (src/c/s2let_mw.c; s2let_mw.h)    */

@@ -124,6 +124,7 @@ GPU_SIGNATURES = {
     "s2let_gpu_launch_count": (C.c_uint64, []),
     "s2let_gpu_timing_enable": (I, [I]),
     "s2let_gpu_timing_report": (I, [V, I]),
+    "s2let_gpu_axisym_wav_hardthreshold_real_noalloc": (I, [V, V, P, I]),
     "s2let_gpu_mw_adjoint_map2alm": (None, [V, V, I, I]),
     "s2let_gpu_mw_adjoint_alm2map": (None, [V, V, I, I]),
     "s2let_gpu_analysis_px2wav_real_batch": (I, [V, V, V, I, P, V]),
