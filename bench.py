@@ -138,14 +138,16 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def profile_traffic(precision):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
-    try:
-        with open(path) as fh:
-            return json.load(fh).get(precision)
-    except (OSError, ValueError):
-        return None
+# DRAM traffic / algorithmic bytes of the dominant kernel, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum over the bytes the launch must
+# move); profiles/fp64_contraction_L512_N4_batch8.md.  Traffic grows with the
+# table size, so the ratio carries to the L=1024 launches.
+TRAFFIC_RATIO = {"fp64_contraction": 1.126}
+
+
+def profile_traffic(kernel, alg_bytes_per_launch):
+    r = TRAFFIC_RATIO.get(kernel)
+    return None if r is None else r * alg_bytes_per_launch
 
 
 def cpu_baseline_sample(p_args, f0):
@@ -302,7 +304,7 @@ def main():
         ach = kd["bytes"] / (kd["ms"] * 1e-3) / 1e9
         peak = peaks.get("hbm_gbs")
         roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak}
-    tr = profile_traffic(a.precision)
+    tr = profile_traffic(dom, kd["bytes"] / max(kd["launches"], 1))
     roof.update({
         "kernel": dom, "peak_source": peak_kind, "launches_per_step": kd["launches"],
         "avg_launch_ms": kd["ms"] / max(kd["launches"], 1),
@@ -362,7 +364,8 @@ def main():
         return
     cfg = workload(a)
     cfg.update({"batch_per_gpu": nb, "precision": a.precision, "parallelism": f"replicas x{world}",
-                "l2_policy": "inputs larger than L2: f 16.8 MB + f_wav 274 MB per map, no flush needed",
+                "l2_policy": f"inputs larger than L2 (129 MB): f {npx * 8 / 1e6:.1f} MB + f_wav {nw * 8 / 1e6:.0f} MB "
+                             f"per map x {nb} maps, no flush needed",
                 "plan_build_s": plan_s})
     out = {
         "metric": METRIC, "value": value, "unit": "maps/s", "n_gpus": world, "steps": a.steps,

@@ -94,11 +94,11 @@ void s2let_tiling_wavelet_allocate(S2LET_COMPLEX(double) **psi, double **phi,
 void s2let_tiling_wavelet(S2LET_COMPLEX(double) *psi, double *phi,
                           const s2let_parameters_t *parameters);            /* s2let_tiling.h:32 */
 double s2let_tiling_axisym_check_identity(double *kappa, double *kappa0,
-                                          const s2let_parameters_t *parameters);  /* :34 */
+                                          const s2let_parameters_t *parameters);  /* s2let_tiling.h:34 */
 double s2let_tiling_direction_check_identity(S2LET_COMPLEX(double) *s_elm,
-                                             const s2let_parameters_t *parameters); /* :36 */
+                                             const s2let_parameters_t *parameters); /* s2let_tiling.h:36 */
 double s2let_tiling_wavelet_check_identity(S2LET_COMPLEX(double) *psi, double *phi,
-                                           const s2let_parameters_t *parameters);   /* :38 */
+                                           const s2let_parameters_t *parameters);   /* s2let_tiling.h:38 */
 
 /* math helpers (include/s2let/s2let_math.h) */
 double s2let_math_kappa0_quadtrap_s2dw(double a, double b, int n, double B);
@@ -113,28 +113,28 @@ unsigned long binomial_coefficient(int n, int k, int exact);
 int s2let_n_phi(const s2let_parameters_t *parameters);      /* s2let_helper.h:8  */
 int s2let_n_theta(const s2let_parameters_t *parameters);    /* s2let_helper.h:9  */
 int s2let_n_px(const s2let_parameters_t *parameters);       /* s2let_helper.h:10 */
-int s2let_n_lm(const s2let_parameters_t *parameters);       /* s2let_helper.h:11 */
-int s2let_n_lm_scal(const s2let_parameters_t *parameters);  /* s2let_helper.h:12 */
-int s2let_n_lmn_wav(const s2let_parameters_t *parameters);  /* s2let_helper.h:13 */
-int s2let_n_gamma(const s2let_parameters_t *parameters);    /* s2let_helper.h:14 */
-int s2let_n_scal(const s2let_parameters_t *parameters);     /* s2let_helper.h:15 */
-int s2let_n_wav(const s2let_parameters_t *parameters);      /* s2let_helper.h:16 */
-int s2let_n_wav_j(int j, const s2let_parameters_t *parameters); /* s2let_helper.h:17 */
+int s2let_n_lm(const s2let_parameters_t *parameters);       /* s2let_helper.h:12 */
+int s2let_n_lm_scal(const s2let_parameters_t *parameters);  /* s2let_helper.h:14 */
+int s2let_n_lmn_wav(const s2let_parameters_t *parameters);  /* s2let_helper.h:15 */
+int s2let_n_gamma(const s2let_parameters_t *parameters);    /* s2let_helper.h:17 */
+int s2let_n_scal(const s2let_parameters_t *parameters);     /* s2let_helper.h:18 */
+int s2let_n_wav(const s2let_parameters_t *parameters);      /* s2let_helper.h:19 */
+int s2let_n_wav_j(int j, const s2let_parameters_t *parameters); /* s2let_helper.h:21 */
 
 void s2let_allocate_mw(S2LET_COMPLEX(double) **f, int L);              /* s2let_alloc.h:16 */
-void s2let_allocate_mw_real(double **f, int L);                        /* s2let_alloc.h:18 */
-void s2let_allocate_mwss(S2LET_COMPLEX(double) **f, int L);            /* s2let_alloc.h:20 */
-void s2let_allocate_mwss_real(double **f, int L);                      /* s2let_alloc.h:22 */
+void s2let_allocate_mw_real(double **f, int L);                        /* s2let_alloc.h:17 */
+void s2let_allocate_mwss(S2LET_COMPLEX(double) **f, int L);            /* s2let_alloc.h:19 */
+void s2let_allocate_mwss_real(double **f, int L);                      /* s2let_alloc.h:20 */
 void s2let_allocate_lm(S2LET_COMPLEX(double) **flm, int L);            /* s2let_alloc.h:24 */
 void s2let_allocate_lmn_f_wav(S2LET_COMPLEX(double) **f_wav_lmn, S2LET_COMPLEX(double) **f_scal_lm,
-                              const s2let_parameters_t *parameters);   /* s2let_alloc.h:26 */
+                              const s2let_parameters_t *parameters);   /* s2let_alloc.h:28 */
 void s2let_allocate_f_wav(S2LET_COMPLEX(double) **f_wav, S2LET_COMPLEX(double) **f_scal,
-                          const s2let_parameters_t *parameters);       /* s2let_alloc.h:31 */
+                          const s2let_parameters_t *parameters);       /* s2let_alloc.h:35 */
 void s2let_allocate_f_wav_real(double **f_wav, double **f_scal,
-                               const s2let_parameters_t *parameters);  /* s2let_alloc.h:36 */
+                               const s2let_parameters_t *parameters);  /* s2let_alloc.h:40 */
 void s2let_allocate_f_wav_manual(S2LET_COMPLEX(double) **f_wav, S2LET_COMPLEX(double) **f_scal,
                                  int *wav_bandlimits, int scal_bandlimit, int N, int J,
-                                 const s2let_parameters_t *parameters); /* s2let_alloc.h:41 */
+                                 const s2let_parameters_t *parameters); /* s2let_alloc.h:45 */
 
 /* ------------------------------------------------------------------------ */
 /* Directional analysis (src/c/s2let_analysis.c; s2let_analysis.h:16-77)   */
@@ -142,24 +142,24 @@ void s2let_allocate_f_wav_manual(S2LET_COMPLEX(double) **f_wav, S2LET_COMPLEX(do
 
 void s2let_analysis_lm2lmn(S2LET_COMPLEX(double) *f_wav_lmn, S2LET_COMPLEX(double) *f_scal_lm,
                            const S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *wav_lm,
-                           const double *scal_l, const s2let_parameters_t *parameters); /* :16 */
+                           const double *scal_l, const s2let_parameters_t *parameters); /* s2let_analysis.h:16 */
 void s2let_analysis_lm2lmn_real(S2LET_COMPLEX(double) *f_wav_lmn, S2LET_COMPLEX(double) *f_scal_lm,
                                 const S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *wav_lm,
-                                const double *scal_l, const s2let_parameters_t *parameters); /* :24 */
+                                const double *scal_l, const s2let_parameters_t *parameters); /* s2let_analysis.h:26 */
 void s2let_analysis_lm2wav_manual(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
                                   const S2LET_COMPLEX(double) *flm, const double *scal_l,
                                   const S2LET_COMPLEX(double) *wav_lm, const int scal_bandlimit,
-                                  const int *wav_bandlimits, int J, int L, int spin, int N); /* :32 */
+                                  const int *wav_bandlimits, int J, int L, int spin, int N); /* s2let_analysis.h:36 */
 void s2let_analysis_lm2wav(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
                            const S2LET_COMPLEX(double) *flm,
-                           const s2let_parameters_t *parameters);                /* :45 */
+                           const s2let_parameters_t *parameters);                /* s2let_analysis.h:49 */
 void s2let_analysis_lm2wav_real(double *f_wav, double *f_scal, const S2LET_COMPLEX(double) *flm,
-                                const s2let_parameters_t *parameters);           /* :52 */
+                                const s2let_parameters_t *parameters);           /* s2let_analysis.h:57 */
 void s2let_analysis_px2wav(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
                            const S2LET_COMPLEX(double) *f,
-                           const s2let_parameters_t *parameters);                /* :59 */
+                           const s2let_parameters_t *parameters);                /* s2let_analysis.h:65 */
 void s2let_analysis_px2wav_real(double *f_wav, double *f_scal, const double *f,
-                                const s2let_parameters_t *parameters);           /* :66 */
+                                const s2let_parameters_t *parameters);           /* s2let_analysis.h:73 */
 
 /* ------------------------------------------------------------------------ */
 /* Directional synthesis (src/c/s2let_synthesis.c; s2let_synthesis.h:16-77) */
@@ -167,25 +167,25 @@ void s2let_analysis_px2wav_real(double *f_wav, double *f_scal, const double *f,
 
 void s2let_synthesis_lmn2lm(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav_lmn,
                             const S2LET_COMPLEX(double) *f_scal_lm, const S2LET_COMPLEX(double) *wav_lm,
-                            const double *scal_l, const s2let_parameters_t *parameters); /* :16 */
+                            const double *scal_l, const s2let_parameters_t *parameters); /* s2let_synthesis.h:16 */
 void s2let_synthesis_lmn2lm_real(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav_lmn,
                                  const S2LET_COMPLEX(double) *f_scal_lm,
                                  const S2LET_COMPLEX(double) *wav_lm, const double *scal_l,
-                                 const s2let_parameters_t *parameters);          /* :24 */
+                                 const s2let_parameters_t *parameters);          /* s2let_synthesis.h:26 */
 void s2let_synthesis_wav2lm_manual(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav,
                                    const S2LET_COMPLEX(double) *f_scal, const double *scal_l,
                                    const S2LET_COMPLEX(double) *wav_lm, const int scal_bandlimit,
-                                   const int *wav_bandlimits, int J, int L, int spin, int N); /* :32 */
+                                   const int *wav_bandlimits, int J, int L, int spin, int N); /* s2let_synthesis.h:36 */
 void s2let_synthesis_wav2lm(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav,
                             const S2LET_COMPLEX(double) *f_scal,
-                            const s2let_parameters_t *parameters);               /* :45 */
+                            const s2let_parameters_t *parameters);               /* s2let_synthesis.h:49 */
 void s2let_synthesis_wav2lm_real(S2LET_COMPLEX(double) *flm, const double *f_wav,
-                                 const double *f_scal, const s2let_parameters_t *parameters); /* :52 */
+                                 const double *f_scal, const s2let_parameters_t *parameters); /* s2let_synthesis.h:57 */
 void s2let_synthesis_wav2px(S2LET_COMPLEX(double) *f, const S2LET_COMPLEX(double) *f_wav,
                             const S2LET_COMPLEX(double) *f_scal,
-                            const s2let_parameters_t *parameters);               /* :59 */
+                            const s2let_parameters_t *parameters);               /* s2let_synthesis.h:65 */
 void s2let_synthesis_wav2px_real(double *f, const double *f_wav, const double *f_scal,
-                                 const s2let_parameters_t *parameters);          /* :66 */
+                                 const s2let_parameters_t *parameters);          /* s2let_synthesis.h:73 */
 
 /* ------------------------------------------------------------------------ */
 /* Adjoints (src/c/s2let_analysis_adjoint.c, src/c/s2let_synthesis_adjoint.c) */
@@ -194,54 +194,54 @@ void s2let_synthesis_wav2px_real(double *f, const double *f_wav, const double *f
 void s2let_analysis_adjoint_lmn2lm(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav_lmn,
                                    const S2LET_COMPLEX(double) *f_scal_lm,
                                    const S2LET_COMPLEX(double) *wav_lm, const double *scal_l,
-                                   const s2let_parameters_t *parameters);        /* s2let_analysis_adjoint.h:16 */
+                                   const s2let_parameters_t *parameters);        /* s2let_analysis_adjoint.h:31 */
 void s2let_analysis_adjoint_lmn2lm_real(S2LET_COMPLEX(double) *flm,
                                         const S2LET_COMPLEX(double) *f_wav_lmn,
                                         const S2LET_COMPLEX(double) *f_scal_lm,
                                         const S2LET_COMPLEX(double) *wav_lm, const double *scal_l,
-                                        const s2let_parameters_t *parameters);   /* :24 */
+                                        const s2let_parameters_t *parameters);   /* s2let_analysis_adjoint.h:58 */
 void s2let_analysis_adjoint_wav2lm_manual(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav,
                                           const S2LET_COMPLEX(double) *f_scal, const double *scal_l,
                                           const S2LET_COMPLEX(double) *wav_lm,
                                           const int scal_bandlimit, const int *wav_bandlimits,
-                                          int J, int L, int spin, int N);        /* :48 */
+                                          int J, int L, int spin, int N);        /* s2let_analysis_adjoint.h:96 */
 void s2let_analysis_adjoint_wav2lm(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f_wav,
                                    const S2LET_COMPLEX(double) *f_scal,
-                                   const s2let_parameters_t *parameters);        /* :61 */
+                                   const s2let_parameters_t *parameters);        /* s2let_analysis_adjoint.h:125 */
 void s2let_analysis_adjoint_wav2lm_real(S2LET_COMPLEX(double) *flm, const double *f_wav,
                                         const double *f_scal,
-                                        const s2let_parameters_t *parameters);   /* :67 */
+                                        const s2let_parameters_t *parameters);   /* s2let_analysis_adjoint.h:147 */
 void s2let_analysis_adjoint_wav2px(S2LET_COMPLEX(double) *f, const S2LET_COMPLEX(double) *f_wav,
                                    const S2LET_COMPLEX(double) *f_scal,
-                                   const s2let_parameters_t *parameters);        /* :73 */
+                                   const s2let_parameters_t *parameters);        /* s2let_analysis_adjoint.h:168 */
 void s2let_analysis_adjoint_wav2px_real(double *f, const double *f_wav, const double *f_scal,
-                                        const s2let_parameters_t *parameters);   /* :79 */
+                                        const s2let_parameters_t *parameters);   /* s2let_analysis_adjoint.h:188 */
 
 void s2let_synthesis_adjoint_lm2lmn(S2LET_COMPLEX(double) *f_wav_lmn, S2LET_COMPLEX(double) *f_scal_lm,
                                     const S2LET_COMPLEX(double) *flm,
                                     const S2LET_COMPLEX(double) *wav_lm, const double *scal_l,
-                                    const s2let_parameters_t *parameters);       /* s2let_synthesis_adjoint.h:16 */
+                                    const s2let_parameters_t *parameters);       /* s2let_synthesis_adjoint.h:29 */
 void s2let_synthesis_adjoint_lm2lmn_real(S2LET_COMPLEX(double) *f_wav_lmn,
                                          S2LET_COMPLEX(double) *f_scal_lm,
                                          const S2LET_COMPLEX(double) *flm,
                                          const S2LET_COMPLEX(double) *wav_lm, const double *scal_l,
-                                         const s2let_parameters_t *parameters);  /* :24 */
+                                         const s2let_parameters_t *parameters);  /* s2let_synthesis_adjoint.h:56 */
 void s2let_synthesis_adjoint_lm2wav_manual(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
                                            const S2LET_COMPLEX(double) *flm, const double *scal_l,
                                            const S2LET_COMPLEX(double) *wav_lm,
                                            const int scal_bandlimit, const int *wav_bandlimits,
-                                           int J, int L, int spin, int N);       /* :48 */
+                                           int J, int L, int spin, int N);       /* s2let_synthesis_adjoint.h:94 */
 void s2let_synthesis_adjoint_lm2wav(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
                                     const S2LET_COMPLEX(double) *flm,
-                                    const s2let_parameters_t *parameters);       /* :61 */
+                                    const s2let_parameters_t *parameters);       /* s2let_synthesis_adjoint.h:124 */
 void s2let_synthesis_adjoint_lm2wav_real(double *f_wav, double *f_scal,
                                          const S2LET_COMPLEX(double) *flm,
-                                         const s2let_parameters_t *parameters);  /* :67 */
+                                         const s2let_parameters_t *parameters);  /* s2let_synthesis_adjoint.h:147 */
 void s2let_synthesis_adjoint_px2wav(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
                                     const S2LET_COMPLEX(double) *f,
-                                    const s2let_parameters_t *parameters);       /* :73 */
+                                    const s2let_parameters_t *parameters);       /* s2let_synthesis_adjoint.h:170 */
 void s2let_synthesis_adjoint_px2wav_real(double *f_wav, double *f_scal, const double *f,
-                                         const s2let_parameters_t *parameters);  /* :79 */
+                                         const s2let_parameters_t *parameters);  /* s2let_synthesis_adjoint.h:193 */
 
 /* ------------------------------------------------------------------------ */
 /* Axisymmetric wavelets (src/c/s2let_transform_axisym_lm.c, _mw.c)         */
@@ -252,96 +252,96 @@ void s2let_transform_axisym_lm_allocate_f_wav(S2LET_COMPLEX(double) **f_wav_lm,
                                               const s2let_parameters_t *parameters); /* s2let_transform_axisym_lm.h:14 */
 void s2let_transform_axisym_lm_allocate_f_wav_multires(S2LET_COMPLEX(double) **f_wav_lm,
                                                        S2LET_COMPLEX(double) **f_scal_lm,
-                                                       const s2let_parameters_t *parameters); /* :19 */
+                                                       const s2let_parameters_t *parameters); /* s2let_transform_axisym_lm.h:19 */
 void s2let_transform_axisym_lm_allocate_wav(double **wav_lm, double **scal_lm,
-                                            const s2let_parameters_t *parameters); /* :24 */
+                                            const s2let_parameters_t *parameters); /* s2let_transform_axisym_lm.h:24 */
 void s2let_transform_axisym_lm_wav(double *wav_lm, double *scal_lm,
-                                   const s2let_parameters_t *parameters);          /* :27 */
+                                   const s2let_parameters_t *parameters);          /* s2let_transform_axisym_lm.h:25 */
 void s2let_transform_axisym_lm_wav_analysis(S2LET_COMPLEX(double) *f_wav_lm,
                                             S2LET_COMPLEX(double) *f_scal_lm,
                                             const S2LET_COMPLEX(double) *flm, const double *wav_lm,
                                             const double *scal_lm,
-                                            const s2let_parameters_t *parameters);   /* :30 */
+                                            const s2let_parameters_t *parameters);   /* s2let_transform_axisym_lm.h:27 */
 void s2let_transform_axisym_lm_wav_synthesis(S2LET_COMPLEX(double) *flm,
                                              const S2LET_COMPLEX(double) *f_wav_lm,
                                              const S2LET_COMPLEX(double) *f_scal_lm,
                                              const double *wav_lm, const double *scal_lm,
-                                             const s2let_parameters_t *parameters);  /* :37 */
+                                             const s2let_parameters_t *parameters);  /* s2let_transform_axisym_lm.h:34 */
 void s2let_transform_axisym_lm_wav_analysis_multires(S2LET_COMPLEX(double) *f_wav_lm,
                                                      S2LET_COMPLEX(double) *f_scal_lm,
                                                      const S2LET_COMPLEX(double) *flm,
                                                      const double *wav_lm, const double *scal_lm,
-                                                     const s2let_parameters_t *parameters); /* :44 */
+                                                     const s2let_parameters_t *parameters); /* s2let_transform_axisym_lm.h:42 */
 void s2let_transform_axisym_lm_wav_synthesis_multires(S2LET_COMPLEX(double) *flm,
                                                       const S2LET_COMPLEX(double) *f_wav_lm,
                                                       const S2LET_COMPLEX(double) *f_scal_lm,
                                                       const double *wav_lm, const double *scal_lm,
-                                                      const s2let_parameters_t *parameters); /* :51 */
+                                                      const s2let_parameters_t *parameters); /* s2let_transform_axisym_lm.h:49 */
 
 void s2let_transform_axisym_allocate_mw_f_wav(S2LET_COMPLEX(double) **f_wav, S2LET_COMPLEX(double) **f_scal,
                                               const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:13 */
 void s2let_transform_axisym_allocate_mw_f_wav_multires(S2LET_COMPLEX(double) **f_wav,
                                                        S2LET_COMPLEX(double) **f_scal,
-                                                       const s2let_parameters_t *parameters); /* :14 */
+                                                       const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:14 */
 void s2let_transform_axisym_allocate_mw_f_wav_real(double **f_wav, double **f_scal,
-                                                   const s2let_parameters_t *parameters); /* :15 */
+                                                   const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:15 */
 void s2let_transform_axisym_allocate_mw_f_wav_multires_real(double **f_wav, double **f_scal,
-                                                            const s2let_parameters_t *parameters); /* :16 */
+                                                            const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:16 */
 void s2let_transform_axisym_wav_analysis_mw(S2LET_COMPLEX(double) *f_wav, S2LET_COMPLEX(double) *f_scal,
                                             const S2LET_COMPLEX(double) *f,
-                                            const s2let_parameters_t *parameters); /* :18 */
+                                            const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:18 */
 void s2let_transform_axisym_wav_analysis_adjoint_mw(S2LET_COMPLEX(double) *f,
                                                     const S2LET_COMPLEX(double) *f_wav,
                                                     const S2LET_COMPLEX(double) *f_scal,
-                                                    const s2let_parameters_t *parameters); /* :19 */
+                                                    const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:19 */
 void s2let_transform_axisym_wav_synthesis_mw(S2LET_COMPLEX(double) *f, const S2LET_COMPLEX(double) *f_wav,
                                              const S2LET_COMPLEX(double) *f_scal,
-                                             const s2let_parameters_t *parameters); /* :20 */
+                                             const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:20 */
 void s2let_transform_axisym_wav_synthesis_adjoint_mw(S2LET_COMPLEX(double) *f_wav,
                                                      S2LET_COMPLEX(double) *f_scal,
                                                      const S2LET_COMPLEX(double) *f,
-                                                     const s2let_parameters_t *parameters); /* :21 */
+                                                     const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:21 */
 void s2let_transform_axisym_wav_analysis_mw_multires(S2LET_COMPLEX(double) *f_wav,
                                                      S2LET_COMPLEX(double) *f_scal,
                                                      const S2LET_COMPLEX(double) *f,
-                                                     const s2let_parameters_t *parameters); /* :23 */
+                                                     const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:23 */
 void s2let_transform_axisym_wav_analysis_adjoint_mw_multires(S2LET_COMPLEX(double) *f,
                                                              const S2LET_COMPLEX(double) *f_wav,
                                                              const S2LET_COMPLEX(double) *f_scal,
-                                                             const s2let_parameters_t *parameters); /* :24 */
+                                                             const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:24 */
 void s2let_transform_axisym_wav_synthesis_mw_multires(S2LET_COMPLEX(double) *f,
                                                       const S2LET_COMPLEX(double) *f_wav,
                                                       const S2LET_COMPLEX(double) *f_scal,
-                                                      const s2let_parameters_t *parameters); /* :25 */
+                                                      const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:25 */
 void s2let_transform_axisym_wav_synthesis_adjoint_mw_multires(S2LET_COMPLEX(double) *f_wav,
                                                               S2LET_COMPLEX(double) *f_scal,
                                                               const S2LET_COMPLEX(double) *f,
-                                                              const s2let_parameters_t *parameters); /* :26 */
+                                                              const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:26 */
 void s2let_transform_axisym_wav_analysis_mw_real(double *f_wav, double *f_scal, const double *f,
-                                                 const s2let_parameters_t *parameters); /* :28 */
+                                                 const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:28 */
 void s2let_transform_axisym_wav_analysis_adjoint_mw_real(double *f, const double *f_wav,
                                                          const double *f_scal,
-                                                         const s2let_parameters_t *parameters); /* :29 */
+                                                         const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:29 */
 void s2let_transform_axisym_wav_synthesis_mw_real(double *f, const double *f_wav, const double *f_scal,
-                                                  const s2let_parameters_t *parameters); /* :30 */
+                                                  const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:30 */
 void s2let_transform_axisym_wav_synthesis_adjoint_mw_real(double *f_wav, double *f_scal, const double *f,
-                                                          const s2let_parameters_t *parameters); /* :31 */
+                                                          const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:31 */
 void s2let_transform_axisym_wav_analysis_mw_multires_real(double *f_wav, double *f_scal,
                                                           const double *f,
-                                                          const s2let_parameters_t *parameters); /* :33 */
+                                                          const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:33 */
 void s2let_transform_axisym_wav_analysis_adjoint_mw_multires_real(double *f, const double *f_wav,
                                                                   const double *f_scal,
-                                                                  const s2let_parameters_t *parameters); /* :34 */
+                                                                  const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:34 */
 void s2let_transform_axisym_wav_synthesis_mw_multires_real(double *f, const double *f_wav,
                                                            const double *f_scal,
-                                                           const s2let_parameters_t *parameters); /* :35 */
+                                                           const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:35 */
 void s2let_transform_axisym_wav_synthesis_adjoint_mw_multires_real(double *f_wav, double *f_scal,
                                                                    const double *f,
-                                                                   const s2let_parameters_t *parameters); /* :36 */
+                                                                   const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:36 */
 void s2let_transform_axisym_wav_hardthreshold_real(double *g_wav, const double *threshold,
-                                                   const s2let_parameters_t *parameters); /* :38 */
+                                                   const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:38 */
 void s2let_transform_axisym_wav_hardthreshold_multires_real(double *g_wav, const double *threshold,
-                                                            const s2let_parameters_t *parameters); /* :39 */
+                                                            const s2let_parameters_t *parameters); /* s2let_transform_axisym_mw.h:39 */
 /* No counterpart in the reference.  The hard threshold above (multires = 0:
  * _real, 1: _multires_real) with no device allocation: staging lives in one
  * 8 MiB static device array shared by every call, so calls that overlap on the
@@ -354,13 +354,13 @@ int s2let_gpu_axisym_wav_hardthreshold_real_noalloc(double *g_wav, const double 
 /* Plain MW spherical-harmonic transforms (src/c/s2let_mw.c; s2let_mw.h)    */
 /* ------------------------------------------------------------------------ */
 
-void s2let_mw_map2alm_real(S2LET_COMPLEX(double) *flm, const double *f, int L);          /* :15 */
-void s2let_mw_alm2map_real(double *f, const S2LET_COMPLEX(double) *flm, int L);          /* :16 */
-void s2let_mw_alm2map(S2LET_COMPLEX(double) *f, const S2LET_COMPLEX(double) *flm, int L, int spin); /* :17 */
-void s2let_mw_map2alm(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f, int L, int spin); /* :18 */
-double s2let_mw_power(S2LET_COMPLEX(double) *flm, int L);                                /* :20 */
-double s2let_mw_power_real(double *flm, int L);                                          /* :21 */
-double s2let_lm_power(S2LET_COMPLEX(double) *flm, int L);                                /* s2let_lm.h:15 */
+void s2let_mw_map2alm_real(S2LET_COMPLEX(double) *flm, const double *f, int L);          /* s2let_mw.h:15 */
+void s2let_mw_alm2map_real(double *f, const S2LET_COMPLEX(double) *flm, int L);          /* s2let_mw.h:16 */
+void s2let_mw_alm2map(S2LET_COMPLEX(double) *f, const S2LET_COMPLEX(double) *flm, int L, int spin); /* s2let_mw.h:17 */
+void s2let_mw_map2alm(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f, int L, int spin); /* s2let_mw.h:18 */
+double s2let_mw_power(S2LET_COMPLEX(double) *flm, int L);                                /* s2let_mw.h:21 */
+double s2let_mw_power_real(double *flm, int L);                                          /* s2let_mw.h:22 */
+double s2let_lm_power(S2LET_COMPLEX(double) *flm, int L);                                /* s2let_lm.h:14 */
 
 /* ------------------------------------------------------------------------ */
 /* GB300 extensions (no reference counterpart)                              */
