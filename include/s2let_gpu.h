@@ -431,6 +431,11 @@ int s2let_gpu_analysis_adjoint_wav2px_batch(void *f, const void *f_wav, const vo
 int s2let_gpu_synthesis_adjoint_px2wav_batch(void *f_wav, void *f_scal, const void *f, int nbatch,
                                              const s2let_parameters_t *parameters, void *stream);
 
+/* Reads and clears the device-side fault flag of the split-precision
+ * tensor-core contraction: non-zero when one of its bounded waits expired since
+ * the last call (the affected outputs are invalid).  0 when all went well. */
+int s2let_gpu_device_fault(void);
+
 /* Number of this library's kernel launches since load (instrumentation). */
 uint64_t s2let_gpu_launch_count(void);
 

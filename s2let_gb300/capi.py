@@ -122,6 +122,7 @@ GPU_SIGNATURES = {
     "s2let_gpu_release_plans": (None, []),
     "s2let_gpu_plan_bytes": (C.c_size_t, []),
     "s2let_gpu_launch_count": (C.c_uint64, []),
+    "s2let_gpu_device_fault": (I, []),
     "s2let_gpu_timing_enable": (I, [I]),
     "s2let_gpu_timing_report": (I, [V, I]),
     "s2let_gpu_axisym_wav_hardthreshold_real_noalloc": (I, [V, V, P, I]),

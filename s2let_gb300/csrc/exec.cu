@@ -22,6 +22,7 @@
 #include "common.h"
 #include "host_layer.h"
 #include "kernels.h"
+#include "mixed.h"
 #include "plan.h"
 #include "runtime.h"
 
@@ -29,12 +30,12 @@ namespace s2g {
 
 std::atomic<uint64_t> g_launches{0};
 int current_kernel_type();  // host_layer.cpp
+thread_local int t_precision = 0;
 
 namespace {
 
 thread_local int t_status = 0;
 thread_local std::string t_message;
-thread_local int t_precision = 0;
 
 template <class T>
 T *upload(const std::vector<T> &v) {
@@ -833,10 +834,16 @@ void s2let_gpu_release_plans(void) {
       for (auto &kv : s2g::g_plans) kv.second->release();
       s2g::g_plans.clear();
     }
+    s2g::release_sliced_tables();
     s2g::release_plans();
   });
 }
-size_t s2let_gpu_plan_bytes(void) { return s2g::plan_bytes(); }
+size_t s2let_gpu_plan_bytes(void) { return s2g::plan_bytes() + s2g::sliced_table_bytes(); }
+int s2let_gpu_device_fault(void) {
+  int v = 0;
+  s2g::guarded("s2let_gpu_device_fault", [&] { v = s2g::mixed_error_flag_read_and_clear(); });
+  return v;
+}
 uint64_t s2let_gpu_launch_count(void) { return s2g::g_launches.load(); }
 
 // ---- pixel-space directional transforms

@@ -11,6 +11,7 @@
 //  k_merge     harmonic tiling merge (lmn -> lm) fused over scales/directions.
 #include "common.h"
 #include "kernels.h"
+#include "mixed.h"
 #include "timing.h"
 
 namespace s2g {
@@ -591,6 +592,7 @@ void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, voi
 
 void contract_l2t(const L2T &p, cudaStream_t st) {
   if (p.nb <= 0 || p.mhi < p.mlo) return;
+  if (t_precision == 1 && contract_l2t_mixed(p, st)) return;
   ContractArgs a{};
   a.table = p.use_q ? p.tb->Q : p.tb->D;
   a.off = p.tb->d_off;
@@ -621,6 +623,7 @@ void contract_l2t(const L2T &p, cudaStream_t st) {
 
 void contract_t2l(const T2L &p, cudaStream_t st) {
   if (p.nb <= 0 || p.mhi < p.mlo) return;
+  if (t_precision == 1 && contract_t2l_mixed(p, st)) return;
   ContractArgs a{};
   a.table = p.use_q ? p.tb->Q : p.tb->D;
   a.off = p.tb->d_off;

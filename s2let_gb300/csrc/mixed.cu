@@ -1,0 +1,902 @@
+// Split-precision contraction on tcgen05 (see mixed.h for the number format).
+//
+// Layout in HBM
+//   Sliced table, one per (band-limit, |n|, D or Q): for each table m, for each
+//   128-row tile rt, for each 64-wide K-chunk kc, for each digit slice j, a
+//   16 KB panel [128 rows][64 bf16] in the 128-byte-swizzled K-major image that
+//   tcgen05 reads from shared memory; rows and K are zero-padded to the panel.
+//   Row exponents eA (int8) per (m, row).
+//   Sliced coefficients, per call and per problem m: for each kc one 14 KB
+//   panel [7 slices x 16 columns][64 bf16] (16 real columns = 8 complex maps),
+//   column exponents eX (int32) per (m, column).
+//
+// Kernel k_contract_mx: persistent, one CTA per SM, 6 warps.
+//   warp 0    producer: cp.async.bulk of panels into a 10-deep ring of 16 KB
+//             table stages and a 2-deep ring of 14 KB coefficient stages.
+//   warp 1    MMA issuer: per K-chunk and digit slice j, one 128 x N x 64
+//             product (4 tcgen05.mma of K=16) of table slice j against the
+//             first 7-j coefficient slices, written to the accumulator columns
+//             of classes j..6 (N = 16 (7-j)); two TMEM accumulators alternate
+//             between tiles.
+//   warps 2-5 epilogue: tcgen05.ld of the 7 class accumulators, FP64 combine,
+//             row/column exponents, sign, per-l weight, store.
+// Every wait is bounded (about 2 s); on expiry the kernel raises an error flag,
+// drains its own copies and MMAs, frees TMEM and returns.
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "common.h"
+#include "kernels.h"
+#include "mixed.h"
+#include "plan.h"
+#include "timing.h"
+
+namespace s2g {
+
+namespace {
+
+constexpr int kS = 7;                  // digit slices per operand
+constexpr int kB0 = 6;                 // bits of the first digit (later digits: 7)
+constexpr int kPK = 64;                // K per panel
+constexpr int kPM = 128;               // rows per panel
+constexpr int kNC = 16;                // real coefficient columns per CTA
+constexpr int kPanelA = kPM * kPK;     // 8192 elements, 16 KB
+constexpr int kPanelX = kS * kNC * kPK;  // 7168 elements, 14 KB
+constexpr int kAST = 10, kXST = 2;     // pipeline depths
+constexpr int kAccCols = kS * kNC;     // 112 TMEM columns per accumulator
+constexpr int kTmemCols = 256;
+constexpr int kThreads = 192;
+constexpr int kMinBl = 128;            // below this the FP64 kernel is used
+constexpr long long kWaitCycles = 4000000000LL;
+
+constexpr size_t kSmemA = (size_t)kAST * kPanelA * 2;
+constexpr size_t kSmemX = (size_t)kXST * kPanelX * 2;
+constexpr int kNumBars = 2 * kAST + 2 * kXST + 4 + 1;
+constexpr size_t kSmemBytes = 1024 + kSmemA + kSmemX + kNumBars * 8 + 16;
+
+struct Geom {
+  int l0, nl, rows, K, nkc, nrt;
+};
+__host__ __device__ inline Geom geom(int bl, int an, int m, bool q) {
+  Geom g;
+  const int am = m < 0 ? -m : m;
+  g.l0 = am > an ? am : an;
+  g.nl = bl - g.l0 > 0 ? bl - g.l0 : 0;
+  g.rows = q ? g.nl : bl;
+  g.K = q ? bl : g.nl;
+  g.nkc = g.nl > 0 ? (g.K + kPK - 1) / kPK : 0;
+  g.nrt = (g.rows + kPM - 1) / kPM;  // l -> t keeps its rows (written as zeros) when nl = 0
+  return g;
+}
+
+// element index of (row, col) inside a [rows][64] bf16 K-major panel with the
+// 128-byte swizzle: 16-byte chunk index XOR (row mod 8), 8-row atoms of 1024 B
+__host__ __device__ inline int swz(int row, int col) {
+  const int chunk = (col >> 3) ^ (row & 7);
+  return (row >> 3) * 512 + (row & 7) * 64 + chunk * 8 + (col & 7);
+}
+
+__device__ __forceinline__ uint16_t digit_bf16(double d) {
+  // |d| <= 64 is an integer: exact in bf16 (top half of the fp32 pattern)
+  return (uint16_t)(__float_as_uint((float)d) >> 16);
+}
+
+// digits of r = v 2^-e, |r| <= 1
+__device__ __forceinline__ void split_digits(double r, uint16_t *out) {
+  double d = rint(r * 64.0);
+  out[0] = digit_bf16(d);
+  r = r * 64.0 - d;
+#pragma unroll
+  for (int j = 1; j < kS; ++j) {
+    d = rint(r * 128.0);
+    out[j] = digit_bf16(d);
+    r = r * 128.0 - d;
+  }
+}
+
+__device__ __forceinline__ int exponent_of(double mx) { return mx > 0.0 ? ilogb(mx) + 1 : 0; }
+
+struct TableRefM {
+  int mi;
+  double sign;
+};
+__device__ __forceinline__ TableRefM table_ref_m(int tmlo, int n, int m) {
+  TableRefM r;
+  if (n > 0 || (n == 0 && m >= 0)) {
+    r.mi = m - tmlo;
+    r.sign = 1.0;
+  } else {
+    const int an = n < 0 ? -n : n;
+    r.mi = -m - tmlo;
+    r.sign = ((m + an) & 1) ? -1.0 : 1.0;
+  }
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// table slicing (plan time)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(128) k_slice_table(const double *__restrict__ T,
+                                                     const int64_t *__restrict__ off, int bl, int an,
+                                                     int tmlo, int q, uint16_t *__restrict__ panels,
+                                                     const int64_t *__restrict__ pan_off,
+                                                     int8_t *__restrict__ eA,
+                                                     const int64_t *__restrict__ e_off) {
+  const int mi = blockIdx.x, rt = blockIdx.y;
+  const Geom g = geom(bl, an, tmlo + mi, q != 0);
+  if (rt >= g.nrt) return;
+  const double *Tm = T + off[mi];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int kpad = g.nkc * kPK;
+  for (int rr = warp; rr < kPM; rr += 4) {
+    const int row = rt * kPM + rr;
+    const bool live = row < g.rows;
+    double mx = 0.0;
+    if (live)
+      for (int k = lane; k < g.K; k += 32) mx = fmax(mx, fabs(Tm[(int64_t)row * g.K + k]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = exponent_of(mx);
+    e = e < -126 ? -126 : (e > 126 ? 126 : e);
+    if (lane == 0) eA[e_off[mi] + row] = (int8_t)e;
+    for (int k = lane; k < kpad; k += 32) {
+      const double v = (live && k < g.K) ? Tm[(int64_t)row * g.K + k] : 0.0;
+      uint16_t dg[kS];
+      split_digits(ldexp(v, -e), dg);
+      const int kc = k / kPK;
+      uint16_t *p = panels + pan_off[mi] + (int64_t)(rt * g.nkc + kc) * kS * kPanelA;
+      const int idx = swz(rr, k % kPK);
+#pragma unroll
+      for (int j = 0; j < kS; ++j) p[(int64_t)j * kPanelA + idx] = dg[j];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// coefficient slicing (per call)
+// ---------------------------------------------------------------------------
+
+struct XArgs {
+  int q;  // 0: l -> t (K = l - l0), 1: t -> l (K = t)
+  int bl, an, mlo, lmin;
+  const double2 *src;
+  int64_t ss;
+  int sw, s_mlo, x_half;
+  const double2 *w;
+  double wscale;
+  int wconj;
+  int nb, b0;
+  const int64_t *xoff;
+  uint16_t *xpan;
+  int *eX;
+};
+
+__device__ __forceinline__ double2 weight_of(const double2 *w, double wscale, int wconj, int l) {
+  double2 v = w ? w[l] : make_double2(1.0, 0.0);
+  if (wconj) v.y = -v.y;
+  return make_double2(v.x * wscale, v.y * wscale);
+}
+
+__device__ __forceinline__ double x_value(const XArgs &a, int m, int am, const Geom &g, int lst, int k,
+                                          int c) {
+  const int b = a.b0 + (c >> 1);
+  if (b >= a.nb) return 0.0;
+  double2 v;
+  if (!a.q) {
+    const int l = g.l0 + k;
+    if (l < lst || l >= a.bl) return 0.0;
+    const int64_t base = (int64_t)b * a.ss + (int64_t)l * l + l;
+    if (a.x_half && m < 0) {
+      v = a.src[base - m];
+      v.y = -v.y;
+      if (am & 1) v = make_double2(-v.x, -v.y);
+    } else {
+      v = a.src[base + m];
+    }
+    const double2 wt = weight_of(a.w, a.wscale, a.wconj, l);
+    v = make_double2(v.x * wt.x - v.y * wt.y, v.x * wt.y + v.y * wt.x);
+  } else {
+    if (k >= a.bl) return 0.0;
+    v = a.src[(int64_t)b * a.ss + (int64_t)k * a.sw + (m - a.s_mlo)];
+  }
+  return (c & 1) ? v.y : v.x;
+}
+
+__global__ void __launch_bounds__(256) k_slice_x(XArgs a) {
+  const int pm = blockIdx.x, m = a.mlo + pm, am = m < 0 ? -m : m;
+  const Geom g = geom(a.bl, a.an, m, a.q != 0);
+  const int c = threadIdx.x >> 4, sub = threadIdx.x & 15;
+  if (g.nkc == 0) {
+    if (sub == 0) a.eX[pm * kNC + c] = 0;
+    return;
+  }
+  const int lst = g.l0 > a.lmin ? g.l0 : a.lmin;
+  int kc0 = 0;
+  if (!a.q) kc0 = lst >= a.bl ? g.nkc : (lst - g.l0) / kPK;
+  double mx = 0.0;
+  for (int k = kc0 * kPK + sub; k < g.nkc * kPK; k += 16) mx = fmax(mx, fabs(x_value(a, m, am, g, lst, k, c)));
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const int e = exponent_of(mx);
+  if (sub == 0) a.eX[pm * kNC + c] = e;
+  uint16_t *base = a.xpan + a.xoff[pm];
+  for (int k = kc0 * kPK + sub; k < g.nkc * kPK; k += 16) {
+    uint16_t dg[kS];
+    split_digits(ldexp(x_value(a, m, am, g, lst, k, c), -e), dg);
+    uint16_t *p = base + (int64_t)(k / kPK) * kPanelX;
+#pragma unroll
+    for (int j = 0; j < kS; ++j) p[swz(j * kNC + c, k % kPK)] = dg[j];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// tcgen05 / mbarrier / bulk-copy primitives
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t saddr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void bar_init(uint64_t *b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(uint64_t *b) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(saddr(b))
+               : "memory");
+}
+__device__ __forceinline__ void bar_expect_tx(uint64_t *b, uint32_t bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                   saddr(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool bar_try(uint64_t *b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, "
+      "p;\n\t}"
+      : "=r"(ok)
+      : "r"(saddr(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait that ignores the abort flag (draining before TMEM release).
+__device__ __noinline__ bool bar_wait_timed(uint64_t *b, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!bar_try(b, parity))
+    if (clock64() - t0 > kWaitCycles) return false;
+  return true;
+}
+// Bounded wait; false when the CTA is aborting or the wait expired (then it
+// raises the CTA abort flag and the global error flag).
+__device__ __noinline__ bool bar_wait(uint64_t *b, uint32_t parity, volatile int *abort_flag, int *err) {
+  const long long t0 = clock64();
+  for (uint32_t it = 0;; ++it) {
+    if (bar_try(b, parity)) return true;
+    if ((it & 255u) == 255u) {
+      if (*abort_flag) return false;
+      if (clock64() - t0 > kWaitCycles) {
+        *abort_flag = 1;
+        atomicExch(err, 1);
+        return false;
+      }
+    }
+  }
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   saddr(dst)),
+               "l"(src), "r"(bytes), "r"(saddr(bar))
+               : "memory");
+}
+__device__ __forceinline__ uint64_t sw128_desc(const void *p) {
+  const uint32_t a = saddr(p);
+  uint64_t d = 0;
+  d |= (uint64_t)((a >> 4) & 0x3FFFu);  // start address
+  d |= (uint64_t)1 << 16;               // leading byte offset (unused with 128B swizzle)
+  d |= (uint64_t)(1024 >> 4) << 32;     // stride byte offset: 8-row groups 1024 B apart
+  d |= (uint64_t)1 << 46;               // descriptor version
+  d |= (uint64_t)2 << 61;               // 128-byte swizzle
+  return d;
+}
+__device__ __forceinline__ uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4)                    // D: f32
+         | (1u << 7) | (1u << 10)     // A, B: bf16
+         | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);  // K-major A and B
+}
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, "
+      "p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---------------------------------------------------------------------------
+// the contraction
+// ---------------------------------------------------------------------------
+
+struct MxArgs {
+  int q;  // 0: l -> t with D, 1: t -> l with Q
+  const uint16_t *panels;
+  const int64_t *pan_off;
+  const int8_t *eA;
+  const int64_t *e_off;
+  int bl, an, tmlo, n, mlo, lmin;
+  const uint16_t *xpan;
+  const int64_t *xoff;
+  const int *eX;
+  const int2 *tiles;
+  int ntiles;
+  double2 *dst;
+  int64_t ds;
+  int dw, d_mlo;
+  const double2 *w;
+  double wscale;
+  int wconj;
+  int nb, b0;
+  int *err;
+};
+
+struct TileInfo {
+  int pm, m, mi, rt, kc0, nkc, l0, lst;
+  double sign;
+};
+__device__ __forceinline__ TileInfo tile_info(const MxArgs &a, int t) {
+  TileInfo ti;
+  const int2 tl = a.tiles[t];
+  ti.pm = tl.x;
+  ti.rt = tl.y;
+  ti.m = a.mlo + ti.pm;
+  const TableRefM r = table_ref_m(a.tmlo, a.n, ti.m);
+  ti.mi = r.mi;
+  ti.sign = r.sign;
+  const Geom g = geom(a.bl, a.an, ti.m, a.q != 0);
+  ti.l0 = g.l0;
+  ti.nkc = g.nkc;
+  ti.lst = g.l0 > a.lmin ? g.l0 : a.lmin;
+  ti.kc0 = 0;
+  if (!a.q) ti.kc0 = ti.lst >= a.bl ? g.nkc : (ti.lst - g.l0) / kPK;
+  return ti;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint16_t *sA = (uint16_t *)smem;
+  uint16_t *sX = (uint16_t *)(smem + kSmemA);
+  uint64_t *bars = (uint64_t *)(smem + kSmemA + kSmemX);
+  uint64_t *fullA = bars, *emptyA = bars + kAST, *fullX = bars + 2 * kAST, *emptyX = bars + 2 * kAST + kXST;
+  uint64_t *tfull = bars + 2 * kAST + 2 * kXST, *tempty = tfull + 2, *mma_done = tfull + 4;
+  volatile int *abort_flag = (volatile int *)(bars + kNumBars);
+  uint32_t *tmem_slot = (uint32_t *)(bars + kNumBars) + 1;
+  int *cons = (int *)(bars + kNumBars) + 2;  // [2]: table / coefficient stages consumed
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kAST; ++i) {
+      bar_init(&fullA[i], 1);
+      bar_init(&emptyA[i], 1);
+    }
+    for (int i = 0; i < kXST; ++i) {
+      bar_init(&fullX[i], 1);
+      bar_init(&emptyX[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      bar_init(&tfull[i], 1);
+      bar_init(&tempty[i], 128);
+    }
+    bar_init(mma_done, 1);
+    *abort_flag = 0;
+    cons[0] = cons[1] = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  int issuedA = 0, issuedX = 0;
+  if (warp == 0 && lane == 0) {
+    // ---------------- producer ----------------
+    bool ok = true;
+    for (int t = blockIdx.x; ok && t < a.ntiles; t += gridDim.x) {
+      const TileInfo ti = tile_info(a, t);
+      const uint16_t *pan = a.panels + a.pan_off[ti.mi] + (int64_t)ti.rt * ti.nkc * kS * kPanelA;
+      const uint16_t *xp = a.xpan + a.xoff[ti.pm];
+      for (int kc = ti.kc0; ok && kc < ti.nkc; ++kc) {
+        const int xs = issuedX % kXST;
+        if (!(ok = bar_wait(&emptyX[xs], ((issuedX / kXST) & 1) ^ 1, abort_flag, a.err))) break;
+        bar_expect_tx(&fullX[xs], kPanelX * 2);
+        bulk_g2s(sX + (size_t)xs * kPanelX, xp + (int64_t)kc * kPanelX, kPanelX * 2, &fullX[xs]);
+        ++issuedX;
+        for (int j = 0; j < kS; ++j) {
+          const int as = issuedA % kAST;
+          if (!(ok = bar_wait(&emptyA[as], ((issuedA / kAST) & 1) ^ 1, abort_flag, a.err))) break;
+          bar_expect_tx(&fullA[as], kPanelA * 2);
+          bulk_g2s(sA + (size_t)as * kPanelA, pan + ((int64_t)kc * kS + j) * kPanelA, kPanelA * 2, &fullA[as]);
+          ++issuedA;
+        }
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer ----------------
+    int ca = 0, cx = 0, ti_n = 0;
+    bool ok = true, any = false;
+    for (int t = blockIdx.x; ok && t < a.ntiles; t += gridDim.x, ++ti_n) {
+      const TileInfo ti = tile_info(a, t);
+      const int ab = ti_n & 1;
+      if (!(ok = bar_wait(&tempty[ab], ((ti_n >> 1) & 1) ^ 1, abort_flag, a.err))) break;
+      tc_fence_after();
+      const uint32_t d0 = tmem + (uint32_t)(ab * kAccCols);
+      if (ti.kc0 >= ti.nkc) {
+        bar_arrive(&tfull[ab]);  // nothing to accumulate: the epilogue writes zeros
+        continue;
+      }
+      for (int kc = ti.kc0; ok && kc < ti.nkc; ++kc) {
+        const int xs = cx % kXST;
+        if (!(ok = bar_wait(&fullX[xs], (cx / kXST) & 1, abort_flag, a.err))) break;
+        tc_fence_after();
+        const uint64_t bdesc = sw128_desc(sX + (size_t)xs * kPanelX);
+        for (int j = 0; j < kS; ++j) {
+          const int as = ca % kAST;
+          if (!(ok = bar_wait(&fullA[as], (ca / kAST) & 1, abort_flag, a.err))) break;
+          tc_fence_after();
+          const uint64_t adesc = sw128_desc(sA + (size_t)as * kPanelA);
+          const uint32_t idesc = idesc_bf16(kPM, kNC * (kS - j));
+#pragma unroll
+          for (int k = 0; k < kPK / 16; ++k) {
+            // K advance of 16 bf16 = 32 bytes inside the swizzle atom
+            mma_bf16(d0 + (uint32_t)(kNC * j), adesc + (uint64_t)(2 * k), bdesc + (uint64_t)(2 * k), idesc,
+                     (kc == ti.kc0 && j == 0 && k == 0) ? 0u : 1u);
+          }
+          any = true;
+          mma_commit(&emptyA[as]);
+          ++ca;
+        }
+        if (!ok) break;
+        mma_commit(&emptyX[xs]);
+        ++cx;
+      }
+      if (!ok) break;
+      mma_commit(&tfull[ab]);
+    }
+    cons[0] = ca;
+    cons[1] = cx;
+    if (any) {  // every MMA of this thread has completed before TMEM is released
+      mma_commit(mma_done);
+      if (!bar_wait_timed(mma_done, 0)) atomicExch(a.err, 2);
+    }
+  } else if (warp >= 2) {
+    // ---------------- epilogue ----------------
+    const int quarter = warp & 3;
+    const int rr = quarter * 32 + lane;
+    int ti_n = 0;
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++ti_n) {
+      const TileInfo ti = tile_info(a, t);
+      const int ab = ti_n & 1;
+      // warp-uniform outcome: tcgen05.ld below is .sync.aligned
+      if (!__all_sync(0xffffffffu, bar_wait(&tfull[ab], (ti_n >> 1) & 1, abort_flag, a.err))) break;
+      tc_fence_after();
+      double y[kNC];
+      if (ti.kc0 < ti.nkc) {
+        float acc[kS][kNC];
+        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * kAccCols);
+#pragma unroll
+        for (int c = 0; c < kS; ++c) tmem_ld16(taddr + (uint32_t)(c * kNC), acc[c]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        tc_fence_before();
+        bar_arrive(&tempty[ab]);
+        const int rowg = ti.rt * kPM + rr;
+        const int ea = a.eA[a.e_off[ti.mi] + rowg];
+#pragma unroll
+        for (int col = 0; col < kNC; ++col) {
+          double s = 0.0;
+#pragma unroll
+          for (int c = kS - 1; c >= 0; --c) s = s * (1.0 / 128.0) + (double)acc[c][col];
+          y[col] = ldexp(s, ea + a.eX[ti.pm * kNC + col] - 2 * kB0) * ti.sign;
+        }
+      } else {
+        tc_fence_before();
+        bar_arrive(&tempty[ab]);
+#pragma unroll
+        for (int col = 0; col < kNC; ++col) y[col] = 0.0;
+      }
+      if (!a.q) {
+        const int t_row = ti.rt * kPM + rr;
+        if (t_row < a.bl) {
+#pragma unroll
+          for (int bb = 0; bb < kNC / 2; ++bb) {
+            const int b = a.b0 + bb;
+            if (b < a.nb)
+              a.dst[(int64_t)b * a.ds + (int64_t)t_row * a.dw + (ti.m - a.d_mlo)] =
+                  make_double2(y[2 * bb], y[2 * bb + 1]);
+          }
+        }
+      } else {
+        const int l = ti.l0 + ti.rt * kPM + rr;
+        if (l >= ti.lst && l < a.bl) {
+          const double2 wt = weight_of(a.w, a.wscale, a.wconj, l);
+#pragma unroll
+          for (int bb = 0; bb < kNC / 2; ++bb) {
+            const int b = a.b0 + bb;
+            if (b < a.nb) {
+              const double yr = y[2 * bb], yi = y[2 * bb + 1];
+              a.dst[(int64_t)b * a.ds + (int64_t)l * l + l + ti.m] =
+                  make_double2(yr * wt.x - yi * wt.y, yr * wt.y + yi * wt.x);
+            }
+          }
+        }
+      }
+    }
+  }
+
+  // producer: on abort, wait (bounded) for its own copies still in flight
+  __syncthreads();
+  if (warp == 0 && lane == 0 && *abort_flag) {
+    const long long t0 = clock64();
+    for (int i = cons[0]; i < issuedA; ++i)
+      while (!bar_try(&fullA[i % kAST], (i / kAST) & 1) && clock64() - t0 < kWaitCycles) {
+      }
+    for (int i = cons[1]; i < issuedX; ++i)
+      while (!bar_try(&fullX[i % kXST], (i / kXST) & 1) && clock64() - t0 < kWaitCycles) {
+      }
+    (void)t0;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// host side: sliced-table cache, tile lists, launches
+// ---------------------------------------------------------------------------
+
+struct TileList {
+  int2 *d_tiles = nullptr;
+  int ntiles = 0;
+  int64_t *d_xoff = nullptr;
+  int64_t x_elems = 0;
+  int64_t work_entries = 0;  // table entries streamed per launch (all tiles)
+};
+
+struct SlicedTable {
+  int bl = 0, an = 0, mlo = 0, nm = 0;
+  bool q = false;
+  uint16_t *panels = nullptr;
+  int8_t *eA = nullptr;
+  int64_t *d_pan_off = nullptr, *d_e_off = nullptr;
+  size_t bytes = 0;
+  std::map<std::tuple<int, int, int, int>, TileList> lists;  // (n, mlo, mhi, lmin)
+};
+
+std::mutex g_mx_mu;
+std::map<std::tuple<int, int, int>, std::unique_ptr<SlicedTable>> g_sliced;
+size_t g_mx_bytes = 0;
+int *g_err = nullptr;
+
+template <class T>
+T *dev_alloc(size_t n, size_t *acc) {
+  void *p = nullptr;
+  S2G_CUDA(cudaMalloc(&p, sizeof(T) * (n ? n : 1)));
+  *acc += sizeof(T) * (n ? n : 1);
+  return (T *)p;
+}
+
+SlicedTable &sliced(const WignerTable &tb, bool q, cudaStream_t st) {
+  auto key = std::make_tuple(tb.bl, tb.an, q ? 1 : 0);
+  auto it = g_sliced.find(key);
+  if (it != g_sliced.end()) return *it->second;
+  auto s = std::make_unique<SlicedTable>();
+  s->bl = tb.bl;
+  s->an = tb.an;
+  s->mlo = tb.mlo;
+  s->nm = tb.nm;
+  s->q = q;
+  std::vector<int64_t> po(tb.nm), eo(tb.nm);
+  int64_t ptot = 0, etot = 0;
+  for (int mi = 0; mi < tb.nm; ++mi) {
+    const Geom g = geom(tb.bl, tb.an, tb.mlo + mi, q);
+    po[mi] = ptot;
+    eo[mi] = etot;
+    ptot += (int64_t)g.nrt * g.nkc * kS * kPanelA;
+    etot += (int64_t)g.nrt * kPM;
+  }
+  size_t by = 0;
+  s->panels = dev_alloc<uint16_t>((size_t)ptot, &by);
+  s->eA = dev_alloc<int8_t>((size_t)etot, &by);
+  s->d_pan_off = dev_alloc<int64_t>(tb.nm, &by);
+  s->d_e_off = dev_alloc<int64_t>(tb.nm, &by);
+  S2G_CUDA(cudaMemcpyAsync(s->d_pan_off, po.data(), sizeof(int64_t) * tb.nm, cudaMemcpyHostToDevice, st));
+  S2G_CUDA(cudaMemcpyAsync(s->d_e_off, eo.data(), sizeof(int64_t) * tb.nm, cudaMemcpyHostToDevice, st));
+  int nrt_max = (tb.bl + kPM - 1) / kPM;
+  dim3 grid(tb.nm, nrt_max);
+  k_slice_table<<<grid, 128, 0, st>>>(q ? tb.Q : tb.D, tb.d_off, tb.bl, tb.an, tb.mlo, q ? 1 : 0, s->panels,
+                                      s->d_pan_off, s->eA, s->d_e_off);
+  S2G_LAUNCHED();
+  S2G_CUDA(cudaStreamSynchronize(st));
+  s->bytes = by;
+  g_mx_bytes += by;
+  SlicedTable &ref = *s;
+  g_sliced.emplace(key, std::move(s));
+  return ref;
+}
+
+const TileList &tile_list(SlicedTable &s, int n, int mlo, int mhi, int lmin, cudaStream_t st) {
+  auto key = std::make_tuple(n, mlo, mhi, lmin);
+  auto it = s.lists.find(key);
+  if (it != s.lists.end()) return it->second;
+  TileList L;
+  std::vector<int2> tiles;
+  std::vector<int64_t> xoff(mhi - mlo + 1);
+  int64_t xe = 0, work = 0;
+  for (int m = mlo; m <= mhi; ++m) {
+    const Geom g = geom(s.bl, s.an, m, s.q);
+    xoff[m - mlo] = xe;
+    xe += (int64_t)g.nkc * kPanelX;
+    if (g.nl <= 0) continue;
+    const int lst = g.l0 > lmin ? g.l0 : lmin;
+    int rt0 = 0, kc0 = 0;
+    if (s.q) {
+      if (lst >= s.bl) continue;
+      rt0 = (lst - g.l0) / kPM;
+    } else {
+      kc0 = lst >= s.bl ? g.nkc : (lst - g.l0) / kPK;
+    }
+    for (int rt = rt0; rt < g.nrt; ++rt) {
+      tiles.push_back(make_int2(m - mlo, rt));
+      work += (int64_t)(g.nkc - kc0) * kPK * kPM;
+    }
+  }
+  size_t by = 0;
+  L.ntiles = (int)tiles.size();
+  L.d_tiles = dev_alloc<int2>(tiles.size(), &by);
+  L.d_xoff = dev_alloc<int64_t>(xoff.size(), &by);
+  L.x_elems = xe;
+  L.work_entries = work;
+  if (!tiles.empty())
+    S2G_CUDA(cudaMemcpyAsync(L.d_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, st));
+  S2G_CUDA(cudaMemcpyAsync(L.d_xoff, xoff.data(), sizeof(int64_t) * xoff.size(), cudaMemcpyHostToDevice, st));
+  S2G_CUDA(cudaStreamSynchronize(st));
+  g_mx_bytes += by;
+  s.bytes += by;
+  return s.lists.emplace(key, L).first->second;
+}
+
+int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    S2G_CUDA(cudaGetDevice(&dev));
+    S2G_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return n;
+}
+
+int *error_flag() {
+  if (!g_err) {
+    S2G_CUDA(cudaMalloc(&g_err, sizeof(int)));
+    S2G_CUDA(cudaMemset(g_err, 0, sizeof(int)));
+  }
+  return g_err;
+}
+
+struct Problem {
+  bool q;
+  const WignerTable *tb;
+  int n, mlo, mhi, lmin;
+  const double2 *src;
+  int64_t ss;
+  int sw, s_mlo, x_half;
+  const double2 *w;
+  double wscale;
+  int wconj;
+  double2 *dst;
+  int64_t ds;
+  int dw, d_mlo;
+  int nb;
+};
+
+void run_mixed(const Problem &p, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    S2G_CUDA(cudaFuncSetAttribute(k_contract_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
+    attr = true;
+  }
+  SlicedTable *s;
+  const TileList *L;
+  int *err;
+  {
+    std::lock_guard<std::mutex> lk(g_mx_mu);
+    s = &sliced(*p.tb, p.q, st);
+    L = &tile_list(*s, p.n, p.mlo, p.mhi, p.lmin, st);
+    err = error_flag();
+  }
+  const int nmp = p.mhi - p.mlo + 1;
+  const int ngroups = (p.nb + kNC / 2 - 1) / (kNC / 2);
+  uint16_t *xpan = nullptr;
+  int *eX = nullptr;
+  S2G_CUDA(cudaMallocAsync((void **)&xpan, sizeof(uint16_t) * (size_t)(L->x_elems ? L->x_elems : 1), st));
+  S2G_CUDA(cudaMallocAsync((void **)&eX, sizeof(int) * (size_t)nmp * kNC, st));
+  // algorithmic work: 4 flop per (entry, complex map); bytes: 14 B per table
+  // entry streamed + coefficient panels + FP64 outputs
+  const double entries = (double)L->work_entries;
+  for (int g = 0; g < ngroups; ++g) {
+    const int b0 = g * (kNC / 2);
+    const int nbg = p.nb - b0 < kNC / 2 ? p.nb - b0 : kNC / 2;
+    double fl = 0, by = 0;
+    if (timing_enabled()) {
+      fl = 4.0 * entries * nbg;
+      by = entries * 2.0 * kS + (double)L->x_elems * 2.0 + 16.0 * nbg * (double)p.tb->bl * nmp;
+    }
+    KTimer kt(KC_MIXED, st, fl, by);
+    XArgs xa{};
+    xa.q = p.q ? 1 : 0;
+    xa.bl = p.tb->bl;
+    xa.an = p.tb->an;
+    xa.mlo = p.mlo;
+    xa.lmin = p.lmin;
+    xa.src = p.src;
+    xa.ss = p.ss;
+    xa.sw = p.sw;
+    xa.s_mlo = p.s_mlo;
+    xa.x_half = p.x_half;
+    xa.w = p.w;
+    xa.wscale = p.wscale;
+    xa.wconj = p.wconj;
+    xa.nb = p.nb;
+    xa.b0 = b0;
+    xa.xoff = L->d_xoff;
+    xa.xpan = xpan;
+    xa.eX = eX;
+    k_slice_x<<<nmp, 256, 0, st>>>(xa);
+    S2G_LAUNCHED();
+    if (L->ntiles == 0) continue;
+    MxArgs ma{};
+    ma.q = xa.q;
+    ma.panels = s->panels;
+    ma.pan_off = s->d_pan_off;
+    ma.eA = s->eA;
+    ma.e_off = s->d_e_off;
+    ma.bl = p.tb->bl;
+    ma.an = p.tb->an;
+    ma.tmlo = p.tb->mlo;
+    ma.n = p.n;
+    ma.mlo = p.mlo;
+    ma.lmin = p.lmin;
+    ma.xpan = xpan;
+    ma.xoff = L->d_xoff;
+    ma.eX = eX;
+    ma.tiles = L->d_tiles;
+    ma.ntiles = L->ntiles;
+    ma.dst = p.dst;
+    ma.ds = p.ds;
+    ma.dw = p.dw;
+    ma.d_mlo = p.d_mlo;
+    ma.w = p.w;
+    ma.wscale = p.wscale;
+    ma.wconj = p.wconj;
+    ma.nb = p.nb;
+    ma.b0 = b0;
+    ma.err = err;
+    const int grid = L->ntiles < num_sms() ? L->ntiles : num_sms();
+    k_contract_mx<<<grid, kThreads, kSmemBytes, st>>>(ma);
+    S2G_LAUNCHED();
+  }
+  cudaFreeAsync(xpan, st);
+  cudaFreeAsync(eX, st);
+}
+
+}  // namespace
+
+bool contract_l2t_mixed(const L2T &a, cudaStream_t st) {
+  if (a.use_q || a.tb->bl < kMinBl || a.nb <= 0 || a.mhi < a.mlo) return false;
+  Problem p{};
+  p.q = false;
+  p.tb = a.tb;
+  p.n = a.n;
+  p.mlo = a.mlo;
+  p.mhi = a.mhi;
+  p.lmin = a.lmin;
+  p.src = a.x;
+  p.ss = a.xs;
+  p.x_half = a.x_half ? 1 : 0;
+  p.w = a.w;
+  p.wscale = a.wscale;
+  p.wconj = a.wconj ? 1 : 0;
+  p.dst = a.out;
+  p.ds = a.os;
+  p.dw = a.ow;
+  p.d_mlo = a.omlo;
+  p.nb = a.nb;
+  run_mixed(p, st);
+  return true;
+}
+
+bool contract_t2l_mixed(const T2L &a, cudaStream_t st) {
+  if (!a.use_q || a.tb->bl < kMinBl || a.nb <= 0 || a.mhi < a.mlo) return false;
+  Problem p{};
+  p.q = true;
+  p.tb = a.tb;
+  p.n = a.n;
+  p.mlo = a.mlo;
+  p.mhi = a.mhi;
+  p.lmin = a.lmin;
+  p.src = a.in;
+  p.ss = a.is;
+  p.sw = a.iw;
+  p.s_mlo = a.imlo;
+  p.w = a.w;
+  p.wscale = a.wscale;
+  p.wconj = a.wconj ? 1 : 0;
+  p.dst = a.y;
+  p.ds = a.ys;
+  p.nb = a.nb;
+  run_mixed(p, st);
+  return true;
+}
+
+void release_sliced_tables() {
+  std::lock_guard<std::mutex> lk(g_mx_mu);
+  for (auto &kv : g_sliced) {
+    SlicedTable &s = *kv.second;
+    cudaFree(s.panels);
+    cudaFree(s.eA);
+    cudaFree(s.d_pan_off);
+    cudaFree(s.d_e_off);
+    for (auto &l : s.lists) {
+      cudaFree(l.second.d_tiles);
+      cudaFree(l.second.d_xoff);
+    }
+  }
+  g_sliced.clear();
+  g_mx_bytes = 0;
+}
+
+size_t sliced_table_bytes() {
+  std::lock_guard<std::mutex> lk(g_mx_mu);
+  return g_mx_bytes;
+}
+
+int mixed_error_flag_read_and_clear() {
+  std::lock_guard<std::mutex> lk(g_mx_mu);
+  if (!g_err) return 0;
+  int v = 0;
+  S2G_CUDA(cudaMemcpy(&v, g_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) S2G_CUDA(cudaMemset(g_err, 0, sizeof(int)));
+  return v;
+}
+
+}  // namespace s2g
