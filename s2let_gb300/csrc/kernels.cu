@@ -48,6 +48,7 @@ struct RingArgs {
   int sw, mlo;
   int nrings, bl, K, P, logP;
   const double2 *chirp, *bhat, *tw;
+  const float4 *chirp_df, *bhat_df, *tw_df;
 };
 
 // element offset of ring r (rings of a map are ring_stride apart, maps map_stride)
@@ -186,6 +187,246 @@ __global__ void __launch_bounds__(512) k_ring_inverse(RingArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Ring DFT in double-float arithmetic (split-precision path)
+//
+// Values are unevaluated sums hi + lo of two floats (48-bit significand, unit
+// roundoff 2^-48, error-free transformations of Dekker/Knuth: two-sum,
+// two-product by FMA).  Every operation is an explicit round-to-nearest
+// intrinsic so that no multiply-add is contracted.  The same Bluestein steps
+// as the FP64 kernels run on the FP32 pipe; each ring (pair) is scaled by a
+// power of two first so that the float exponent range never limits accuracy.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float v = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
+  return make_float2(s, e);
+}
+__device__ __forceinline__ float2 df_fast(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  float2 s = df_two_sum(a.x, b.x);
+  s.y = __fadd_rn(s.y, __fadd_rn(a.y, b.y));
+  return df_fast(s.x, s.y);
+}
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+// a*b + c*d (double-float in, double-float out)
+__device__ __forceinline__ float2 df_dot2(float2 a, float2 b, float2 c, float2 d) {
+  const float p1 = __fmul_rn(a.x, b.x);
+  const float e1 = __fmaf_rn(a.x, b.x, -p1);
+  const float p2 = __fmul_rn(c.x, d.x);
+  const float e2 = __fmaf_rn(c.x, d.x, -p2);
+  const float2 s = df_two_sum(p1, p2);
+  float e = __fadd_rn(s.y, __fadd_rn(e1, e2));
+  e = __fmaf_rn(a.x, b.y, e);
+  e = __fmaf_rn(a.y, b.x, e);
+  e = __fmaf_rn(c.x, d.y, e);
+  e = __fmaf_rn(c.y, d.x, e);
+  return df_fast(s.x, e);
+}
+// complex double-float as float4 (re.hi, re.lo, im.hi, im.lo)
+__device__ __forceinline__ float2 dre(float4 z) { return make_float2(z.x, z.y); }
+__device__ __forceinline__ float2 dim_(float4 z) { return make_float2(z.z, z.w); }
+__device__ __forceinline__ float4 dmk(float2 re, float2 im) { return make_float4(re.x, re.y, im.x, im.y); }
+__device__ __forceinline__ float4 dc_mul(float4 a, float4 b) {
+  return dmk(df_dot2(dre(a), dre(b), df_neg(dim_(a)), dim_(b)), df_dot2(dre(a), dim_(b), dim_(a), dre(b)));
+}
+__device__ __forceinline__ float4 dc_mulc(float4 a, float4 b) {  // a * conj(b)
+  return dmk(df_dot2(dre(a), dre(b), dim_(a), dim_(b)), df_dot2(dim_(a), dre(b), df_neg(dre(a)), dim_(b)));
+}
+__device__ __forceinline__ float4 dc_add(float4 a, float4 b) {
+  return dmk(df_add(dre(a), dre(b)), df_add(dim_(a), dim_(b)));
+}
+__device__ __forceinline__ float4 dc_sub(float4 a, float4 b) {
+  return dmk(df_add(dre(a), df_neg(dre(b))), df_add(dim_(a), df_neg(dim_(b))));
+}
+__device__ __forceinline__ float4 dc_conj(float4 a) { return make_float4(a.x, a.y, -a.z, -a.w); }
+__device__ __forceinline__ float2 df_from(double v) {
+  const float h = __double2float_rn(v);
+  return make_float2(h, __double2float_rn(v - (double)h));
+}
+__device__ __forceinline__ float4 dc_from(double2 v) { return dmk(df_from(v.x), df_from(v.y)); }
+__device__ __forceinline__ double2 dc_to(float4 z, int e) {
+  return make_double2(ldexp((double)z.x + (double)z.y, e), ldexp((double)z.z + (double)z.w, e));
+}
+
+__device__ void fft_dit_df(float4 *buf, const float4 *__restrict__ tw, int P, int logP) {
+  for (int s = 1; s <= logP; ++s) {
+    const int half = 1 << (s - 1);
+    for (int i = threadIdx.x; i < P / 2; i += blockDim.x) {
+      const int j = i & (half - 1);
+      const int i0 = ((i >> (s - 1)) << s) + j, i1 = i0 + half;
+      const float4 w = __ldg(&tw[j << (logP - s)]);
+      const float4 u = buf[i0], v = dc_mul(buf[i1], w);
+      buf[i0] = dc_add(u, v);
+      buf[i1] = dc_sub(u, v);
+    }
+    __syncthreads();
+  }
+}
+__device__ void ifft_dif_df(float4 *buf, const float4 *__restrict__ tw, int P, int logP) {
+  for (int s = logP; s >= 1; --s) {
+    const int half = 1 << (s - 1);
+    for (int i = threadIdx.x; i < P / 2; i += blockDim.x) {
+      const int j = i & (half - 1);
+      const int i0 = ((i >> (s - 1)) << s) + j, i1 = i0 + half;
+      const float4 w = __ldg(&tw[j << (logP - s)]);
+      const float4 u = buf[i0], v = buf[i1];
+      buf[i0] = dc_add(u, v);
+      buf[i1] = dc_mulc(dc_sub(u, v), w);
+    }
+    __syncthreads();
+  }
+}
+
+// block-wide max of v over all threads (blockDim.x <= 1024)
+__device__ double block_max(double v) {
+  __shared__ double red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double m = 0.0;
+  for (int i = 0; i < (int)((blockDim.x + 31) >> 5); ++i) m = fmax(m, red[i]);
+  return m;
+}
+
+__device__ __forceinline__ int pow2_exponent(double mx) { return mx > 0.0 ? ilogb(mx) + 1 : 0; }
+
+template <bool REAL>
+__global__ void __launch_bounds__(512) k_ring_forward_df(RingArgs a) {
+  extern __shared__ float4 bufd[];
+  const int K = a.K, P = a.P, logP = a.logP;
+  const int r0 = REAL ? 2 * blockIdx.x : blockIdx.x;
+  const bool has1 = REAL && (r0 + 1 < a.nrings);
+  double mx = 0.0;
+  for (int j = threadIdx.x; j < K; j += blockDim.x) {
+    if (REAL) {
+      mx = fmax(mx, fabs(((const double *)a.rings)[ring_base(a, r0) + j]));
+      if (has1) mx = fmax(mx, fabs(((const double *)a.rings)[ring_base(a, r0 + 1) + j]));
+    } else {
+      const double2 z = ((const double2 *)a.rings)[ring_base(a, r0) + j];
+      mx = fmax(mx, fmax(fabs(z.x), fabs(z.y)));
+    }
+  }
+  const int e = pow2_exponent(block_max(mx));
+  for (int j = threadIdx.x; j < P; j += blockDim.x) {
+    float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (j < K) {
+      double2 v;
+      if (REAL) {
+        v.x = ((const double *)a.rings)[ring_base(a, r0) + j];
+        v.y = has1 ? ((const double *)a.rings)[ring_base(a, r0 + 1) + j] : 0.0;
+      } else {
+        v = ((const double2 *)a.rings)[ring_base(a, r0) + j];
+      }
+      z = dc_mulc(dc_from(make_double2(ldexp(v.x, -e), ldexp(v.y, -e))), __ldg(&a.chirp_df[j]));
+    }
+    bufd[brev(j, logP)] = z;
+  }
+  __syncthreads();
+  fft_dit_df(bufd, a.tw_df, P, logP);
+  for (int k = threadIdx.x; k < P; k += blockDim.x) bufd[k] = dc_mul(bufd[k], __ldg(&a.bhat_df[k]));
+  __syncthreads();
+  ifft_dif_df(bufd, a.tw_df, P, logP);
+  const int eo = e - logP;  // undo the ring scaling and the 1/P of the unnormalised transforms
+  if (!REAL) {
+    double2 *out = a.spec_out + (int64_t)r0 * a.spec_stride;
+    for (int c = threadIdx.x; c < a.sw; c += blockDim.x) {
+      const int m = a.mlo + c;
+      const int k = ((m % K) + K) % K;
+      out[c] = dc_to(dc_mulc(bufd[brev(k, logP)], __ldg(&a.chirp_df[k])), eo);
+    }
+  } else {
+    double2 *out0 = a.spec_out + (int64_t)r0 * a.spec_stride;
+    for (int m = threadIdx.x; m < a.sw; m += blockDim.x) {
+      const int km = (K - m) % K;
+      const float4 zm = dc_mulc(bufd[brev(m, logP)], __ldg(&a.chirp_df[m]));
+      const float4 zc = dc_conj(dc_mulc(bufd[brev(km, logP)], __ldg(&a.chirp_df[km])));
+      // A = (Z_m + conj Z_{-m})/2,  B = (Z_m - conj Z_{-m})/(2i)
+      const double2 s = dc_to(dc_add(zm, zc), eo - 1);
+      out0[m] = s;
+      if (has1) {
+        const double2 d = dc_to(dc_sub(zm, zc), eo - 1);
+        out0[a.spec_stride + m] = make_double2(d.y, -d.x);
+      }
+    }
+  }
+}
+
+template <bool REAL>
+__global__ void __launch_bounds__(512) k_ring_inverse_df(RingArgs a) {
+  extern __shared__ float4 bufd[];
+  const int K = a.K, P = a.P, logP = a.logP, bl = a.bl;
+  const int r0 = REAL ? 2 * blockIdx.x : blockIdx.x;
+  const bool has1 = REAL && (r0 + 1 < a.nrings);
+  const double2 *s0 = a.spec_in + (int64_t)r0 * a.spec_stride;
+  double mx = 0.0;
+  for (int c = threadIdx.x; c < a.sw; c += blockDim.x) {
+    const double2 A = s0[c];
+    mx = fmax(mx, fmax(fabs(A.x), fabs(A.y)));
+    if (has1) {
+      const double2 B = s0[a.spec_stride + c];
+      mx = fmax(mx, fmax(fabs(B.x), fabs(B.y)));
+    }
+  }
+  const int e = pow2_exponent(block_max(mx));
+  for (int j = threadIdx.x; j < P; j += blockDim.x) {
+    double2 z = make_double2(0.0, 0.0);
+    bool live = false;
+    if (j < K) {
+      const int m = (j < bl) ? j : j - K;
+      if (REAL) {
+        const int am = m < 0 ? -m : m;
+        if (am < a.sw) {
+          double2 A = s0[am];
+          double2 B = has1 ? s0[a.spec_stride + am] : make_double2(0.0, 0.0);
+          if (m < 0) {
+            A = conj2(A);
+            B = conj2(B);
+          }
+          z = make_double2(A.x - B.y, A.y + B.x);  // A + i B, exact up to one rounding per part
+          live = true;
+        }
+      } else {
+        const int c = m - a.mlo;
+        if (c >= 0 && c < a.sw) {
+          z = s0[c];
+          live = true;
+        }
+      }
+    }
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (j < K) {
+      // inverse DFT = conj(forward(conj z)):  a_j = conj(z_j) conj(c_j)
+      const float4 zz = live ? dc_from(make_double2(ldexp(z.x, -e), ldexp(z.y, -e))) : v;
+      v = dc_conj(dc_mul(zz, __ldg(&a.chirp_df[j])));
+    }
+    bufd[brev(j, logP)] = v;
+  }
+  __syncthreads();
+  fft_dit_df(bufd, a.tw_df, P, logP);
+  for (int k = threadIdx.x; k < P; k += blockDim.x) bufd[k] = dc_mul(bufd[k], __ldg(&a.bhat_df[k]));
+  __syncthreads();
+  ifft_dif_df(bufd, a.tw_df, P, logP);
+  const int eo = e - logP;
+  for (int p = threadIdx.x; p < K; p += blockDim.x) {
+    // f_p = c_p conj(y_p)
+    const double2 f = dc_to(dc_mul(__ldg(&a.chirp_df[p]), dc_conj(bufd[brev(p, logP)])), eo);
+    if (REAL) {
+      ((double *)a.rings_out)[ring_base(a, r0) + p] = f.x;
+      if (has1) ((double *)a.rings_out)[ring_base(a, r0 + 1) + p] = f.y;
+    } else {
+      a.rings_out[ring_base(a, r0) + p] = f;
+    }
+  }
+}
+
 RingArgs ring_args(const RingFFT &rf, int bl, int nrings) {
   RingArgs a{};
   a.K = rf.K;
@@ -196,6 +437,9 @@ RingArgs ring_args(const RingFFT &rf, int bl, int nrings) {
   a.chirp = rf.chirp;
   a.bhat = rf.bhat;
   a.tw = rf.tw;
+  a.chirp_df = rf.chirp_df;
+  a.bhat_df = rf.bhat_df;
+  a.tw_df = rf.tw_df;
   return a;
 }
 
@@ -553,7 +797,15 @@ void ring_forward(const void *rings, int64_t ring_stride, int64_t map_stride, in
   const int nblk = real ? (nrings + 1) / 2 : nrings;
   const size_t smem = sizeof(double2) * rf.P;
   KTimer kt(KC_RING, st, 0.0, (double)nrings * (2 * bl - 1) * (real ? 8.0 : 16.0) + (double)nrings * sw * 16.0);
-  if (real) {
+  if (t_precision == 1) {
+    if (real) {
+      if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_forward_df<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_ring_forward_df<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
+    } else {
+      if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_forward_df<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_ring_forward_df<false><<<nblk, ring_threads(rf.P), smem, st>>>(a);
+    }
+  } else if (real) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_ring_forward<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
   } else {
@@ -580,7 +832,15 @@ void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, voi
   const int nblk = real ? (nrings + 1) / 2 : nrings;
   const size_t smem = sizeof(double2) * rf.P;
   KTimer kt(KC_RING, st, 0.0, (double)nrings * (2 * bl - 1) * (real ? 8.0 : 16.0) + (double)nrings * sw * 16.0);
-  if (real) {
+  if (t_precision == 1) {
+    if (real) {
+      if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_inverse_df<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_ring_inverse_df<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
+    } else {
+      if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_inverse_df<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_ring_inverse_df<false><<<nblk, ring_threads(rf.P), smem, st>>>(a);
+    }
+  } else if (real) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_inverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_ring_inverse<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
   } else {

@@ -462,6 +462,21 @@ std::unique_ptr<RingFFT> build_ring(int K) {
   S2G_CUDA(cudaMemcpy(r->chirp, chirp.data(), sizeof(double2) * K, cudaMemcpyHostToDevice));
   S2G_CUDA(cudaMemcpy(r->bhat, b.data(), sizeof(double2) * P, cudaMemcpyHostToDevice));
   S2G_CUDA(cudaMemcpy(r->tw, tw.data(), sizeof(double2) * std::max(1, P / 2), cudaMemcpyHostToDevice));
+  auto to_df = [](const std::vector<std::complex<double>> &v) {
+    std::vector<float4> o(v.size());
+    for (size_t i = 0; i < v.size(); ++i) {
+      const float rh = (float)v[i].real(), ih = (float)v[i].imag();
+      o[i] = make_float4(rh, (float)(v[i].real() - (double)rh), ih, (float)(v[i].imag() - (double)ih));
+    }
+    return o;
+  };
+  const auto cdf = to_df(chirp), bdf = to_df(b), tdf = to_df(tw);
+  r->chirp_df = dev_alloc<float4>(K);
+  r->bhat_df = dev_alloc<float4>(P);
+  r->tw_df = dev_alloc<float4>(std::max(1, P / 2));
+  S2G_CUDA(cudaMemcpy(r->chirp_df, cdf.data(), sizeof(float4) * K, cudaMemcpyHostToDevice));
+  S2G_CUDA(cudaMemcpy(r->bhat_df, bdf.data(), sizeof(float4) * P, cudaMemcpyHostToDevice));
+  S2G_CUDA(cudaMemcpy(r->tw_df, tdf.data(), sizeof(float4) * std::max(1, P / 2), cudaMemcpyHostToDevice));
   return r;
 }
 
@@ -500,6 +515,9 @@ void release_plans() {
     cudaFree(kv.second->chirp);
     cudaFree(kv.second->bhat);
     cudaFree(kv.second->tw);
+    cudaFree(kv.second->chirp_df);
+    cudaFree(kv.second->bhat_df);
+    cudaFree(kv.second->tw_df);
   }
   g_tables.clear();
   g_rings.clear();

@@ -36,6 +36,9 @@ struct RingFFT {
   double2 *chirp = nullptr;  // K entries, exp(i pi k^2 / K)
   double2 *bhat = nullptr;   // P entries, FFT_P of the wrapped chirp
   double2 *tw = nullptr;     // P/2 entries, exp(-2 pi i k / P)
+  // the same three arrays as double-float pairs (re.hi, re.lo, im.hi, im.lo)
+  // for the FP32-pipe transform of the split-precision path
+  float4 *chirp_df = nullptr, *bhat_df = nullptr, *tw_df = nullptr;
 };
 
 const WignerTable &wigner_table(int bl, int an);
