@@ -223,7 +223,7 @@ def main():
 
     api = s2let_gb300.api()
     lib = api.lib
-    lib.s2let_gpu_set_precision(1 if a.precision == "mixed" else 0)
+    lib.s2let_gpu_set_precision(0)  # inputs are synthesised on the FP64 path
     p = make_parameters(a.L, a.B, a.J_min, a.N, 0, 0)
     sz = api.sizes(p)
     nb = a.batch
@@ -234,6 +234,7 @@ def main():
     f_host = np.stack([api.alm2map(power_law_real_flm(rng, a.L), a.L, real=True) for _ in range(nb)])
     s2let_gb300.check(lib, "alm2map_real")
     f = torch.tensor(f_host, device=dev)
+    lib.s2let_gpu_set_precision(1 if a.precision == "mixed" else 0)
     w = torch.zeros((nb, nw), dtype=torch.float64, device=dev)
     sc = torch.zeros((nb, ns), dtype=torch.float64, device=dev)
     fr = torch.zeros_like(f)

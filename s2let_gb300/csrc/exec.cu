@@ -57,6 +57,9 @@ struct Scale {
   std::vector<int64_t> w_split;  // per direction: split weight, bl entries
   std::vector<int64_t> z_off;    // per direction: z block (bl^2) inside one map
   int64_t w_axi = -1;            // axisymmetric: per-l kernel weight (bl entries)
+  // per direction: first l with a non-zero split / merge weight; terms below
+  // are exact zeros and are skipped
+  std::vector<int> lsup_split, lsup_merge;
 };
 
 struct WavPlan {
@@ -151,12 +154,29 @@ std::unique_ptr<WavPlan> build_plan(const PlanSpec &ps) {
         }
         push(v.real(), v.imag());
       }
+      // weight supports: split = w_split, merge = w_pair halves (axisym: the kernel)
+      auto first_nonzero = [&w, bl](int64_t off, int nrows) {
+        for (int l = 0; l < bl; ++l)
+          for (int r = 0; r < nrows; ++r) {
+            const double2 v = w[off + (int64_t)r * bl + l];
+            if (v.x != 0.0 || v.y != 0.0) return l;
+          }
+        return bl;
+      };
+      if (ps.axisym) {
+        const int la = first_nonzero(sd.w_axi, 1);
+        sd.lsup_split.push_back(la);
+        sd.lsup_merge.push_back(la);
+      } else {
+        sd.lsup_split.push_back(first_nonzero(sd.w_split.back(), 1));
+        sd.lsup_merge.push_back(first_nonzero(sd.w_pair.back(), 2));
+      }
       sd.z_off.push_back(P->z_per_map);
       MergePair mp;
       mp.off = P->z_per_map;
       mp.bl = bl;
       mp.n = n;
-      mp.lmin = (ps.real || ps.axisym) ? 0 : std::abs(ps.spin);
+      mp.lmin = std::max((ps.real || ps.axisym) ? 0 : std::abs(ps.spin), sd.lsup_merge.back());
       mp.woff = sd.w_pair.back();
       pairs.push_back(mp);
       P->z_per_map += (int64_t)bl * bl;
@@ -382,42 +402,57 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
     ring_inverse(spec, sw, sw, mlo, f_scal, Ks, sstride, bs, nb * bs, bs, real, S.st);
   }
   const int64_t Wmax = 2 * P.max_bl - 1;
-  double2 *G = S.get<double2>((int64_t)nb * P.max_nn * P.max_bl * Wmax);
+  const int64_t gsz = (int64_t)nb * P.max_nn * P.max_bl * Wmax;
+  double2 *Gbuf = S.get<double2>(2 * gsz);
   double2 *spec = S.get<double2>((int64_t)nb * P.max_ng * P.max_bl * Wmax);
-  for (const Scale &sd : P.sc) {
-    const int bl = sd.bl, W = 2 * bl - 1, ng = sd.ng, nn = (int)sd.ns.size();
+  for (size_t k0 = 0; k0 < P.sc.size();) {
+    // scales sharing band-limit and directions share each table pass
+    size_t k1 = k0 + 1;
+    if (k1 < P.sc.size() && P.sc[k1].bl == P.sc[k0].bl && P.sc[k1].ns == P.sc[k0].ns) ++k1;
+    const int ngrp = (int)(k1 - k0);
+    const int bl = P.sc[k0].bl, W = 2 * bl - 1, nn = (int)P.sc[k0].ns.size();
     for (int i = 0; i < nn; ++i) {
-      const int n = sd.ns[i];
-      L2T a{};
-      a.tb = &wigner_table(bl, std::abs(n));
-      a.n = n;
-      a.use_q = adj;
-      a.mlo = (real && n == 0) ? 0 : -(bl - 1);
-      a.mhi = bl - 1;
-      a.x = flm;
-      a.xs = (int64_t)L * L;
-      a.xL = L;
-      a.x_half = flm_half;
-      if (P.axisym) {
-        a.w = P.d_w + sd.w_axi;
-        a.wscale = adj ? 2.0 * kPi / W * kSqrt2Pi : 1.0 / kSqrt2Pi;
-      } else {
-        a.w = P.d_w + sd.w_split[i];
-        a.wscale = adj ? 4.0 * kPi * kPi / W : 1.0;
+      L2T grp[2];
+      for (int q = 0; q < ngrp; ++q) {
+        const Scale &sd = P.sc[k0 + q];
+        const int n = sd.ns[i];
+        L2T &a = grp[q];
+        a = L2T{};
+        a.tb = &wigner_table(bl, std::abs(n));
+        a.n = n;
+        a.use_q = adj;
+        a.mlo = (real && n == 0) ? 0 : -(bl - 1);
+        a.mhi = bl - 1;
+        a.x = flm;
+        a.xs = (int64_t)L * L;
+        a.xL = L;
+        a.x_half = flm_half;
+        if (P.axisym) {
+          a.w = P.d_w + sd.w_axi;
+          a.wscale = adj ? 2.0 * kPi / W * kSqrt2Pi : 1.0 / kSqrt2Pi;
+        } else {
+          a.w = P.d_w + sd.w_split[i];
+          a.wscale = adj ? 4.0 * kPi * kPi / W : 1.0;
+        }
+        a.lmin = std::max((real || P.axisym) ? 0 : std::abs(P.s), sd.lsup_split[i]);
+        a.out = Gbuf + q * gsz + (int64_t)i * bl * W;
+        a.os = (int64_t)nn * bl * W;
+        a.ow = W;
+        a.omlo = -(bl - 1);
+        a.nb = nb;
       }
-      a.lmin = real ? 0 : std::abs(P.s);
-      if (P.axisym) a.lmin = 0;
-      a.out = G + (int64_t)i * bl * W;
-      a.os = (int64_t)nn * bl * W;
-      a.ow = W;
-      a.omlo = -(bl - 1);
-      a.nb = nb;
-      contract_l2t(a, S.st);
+      contract_l2t_group(grp, ngrp, S.st);
     }
-    const int sw = real ? bl : W, mlo = real ? 0 : -(bl - 1);
-    gamma_synthesis(G, spec, sd.d_ns, nn, ng, bl, nb, real, adj && !P.axisym ? 1.0 / ng : 1.0, S.st);
-    char *out = (char *)f_wav + (size_t)sd.woff * esz;
-    ring_inverse(spec, sw, sw, mlo, out, W, wstride, ng * bl, nb * ng * bl, bl, real, S.st);
+    for (int q = 0; q < ngrp; ++q) {
+      const Scale &sd = P.sc[k0 + q];
+      const int ng = sd.ng;
+      const int sw = real ? bl : W, mlo = real ? 0 : -(bl - 1);
+      gamma_synthesis(Gbuf + q * gsz, spec, sd.d_ns, nn, ng, bl, nb, real, adj && !P.axisym ? 1.0 / ng : 1.0,
+                      S.st);
+      char *out = (char *)f_wav + (size_t)sd.woff * esz;
+      ring_inverse(spec, sw, sw, mlo, out, W, wstride, ng * bl, nb * ng * bl, bl, real, S.st);
+    }
+    k0 = k1;
   }
 }
 
@@ -456,40 +491,55 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
     contract_t2l(a, S.st);
   }
   const int64_t Wmax = 2 * P.max_bl - 1;
-  double2 *G = S.get<double2>((int64_t)nb * P.max_nn * P.max_bl * Wmax);
+  const int64_t gsz = (int64_t)nb * P.max_nn * P.max_bl * Wmax;
+  double2 *Gbuf = S.get<double2>(2 * gsz);
   double2 *spec = S.get<double2>((int64_t)nb * P.max_ng * P.max_bl * Wmax);
-  for (const Scale &sd : P.sc) {
-    const int bl = sd.bl, W = 2 * bl - 1, ng = sd.ng, nn = (int)sd.ns.size();
+  for (size_t k0 = 0; k0 < P.sc.size();) {
+    size_t k1 = k0 + 1;
+    if (k1 < P.sc.size() && P.sc[k1].bl == P.sc[k0].bl && P.sc[k1].ns == P.sc[k0].ns) ++k1;
+    const int ngrp = (int)(k1 - k0);
+    const int bl = P.sc[k0].bl, W = 2 * bl - 1, nn = (int)P.sc[k0].ns.size();
     const int sw = real ? bl : W, mlo = real ? 0 : -(bl - 1);
-    const char *in = (const char *)f_wav + (size_t)sd.woff * esz;
-    ring_forward(in, W, wstride, ng * bl, spec, sw, sw, mlo, nb * ng * bl, bl, real, S.st);
-    gamma_analysis(spec, G, sd.d_ns, nn, ng, bl, nb, real, (adj || P.axisym) ? 1.0 : 1.0 / ng, S.st);
-    for (int i = 0; i < nn; ++i) {
-      const int n = sd.ns[i];
-      T2L a{};
-      a.tb = &wigner_table(bl, std::abs(n));
-      a.n = n;
-      a.use_q = !adj;
-      a.mlo = (real && n == 0) ? 0 : -(bl - 1);
-      a.mhi = bl - 1;
-      a.in = G + (int64_t)i * bl * W;
-      a.is = (int64_t)nn * bl * W;
-      a.iw = W;
-      a.imlo = -(bl - 1);
-      if (P.axisym) {
-        a.w = P.d_w + sd.w_axi;
-        a.wscale = adj ? 1.0 / kSqrt2Pi : 2.0 * kPi / W * kSqrt2Pi;
-        a.lmin = 0;
-      } else {
-        a.w = nullptr;
-        a.wscale = adj ? 1.0 : 4.0 * kPi * kPi / W;
-        a.lmin = real ? 0 : std::abs(P.s);
-      }
-      a.y = z + sd.z_off[i];
-      a.ys = P.z_per_map;
-      a.nb = nb;
-      contract_t2l(a, S.st);
+    for (int q = 0; q < ngrp; ++q) {
+      const Scale &sd = P.sc[k0 + q];
+      const int ng = sd.ng;
+      const char *in = (const char *)f_wav + (size_t)sd.woff * esz;
+      ring_forward(in, W, wstride, ng * bl, spec, sw, sw, mlo, nb * ng * bl, bl, real, S.st);
+      gamma_analysis(spec, Gbuf + q * gsz, sd.d_ns, nn, ng, bl, nb, real, (adj || P.axisym) ? 1.0 : 1.0 / ng,
+                     S.st);
     }
+    for (int i = 0; i < nn; ++i) {
+      T2L grp[2];
+      for (int q = 0; q < ngrp; ++q) {
+        const Scale &sd = P.sc[k0 + q];
+        const int n = sd.ns[i];
+        T2L &a = grp[q];
+        a = T2L{};
+        a.tb = &wigner_table(bl, std::abs(n));
+        a.n = n;
+        a.use_q = !adj;
+        a.mlo = (real && n == 0) ? 0 : -(bl - 1);
+        a.mhi = bl - 1;
+        a.in = Gbuf + q * gsz + (int64_t)i * bl * W;
+        a.is = (int64_t)nn * bl * W;
+        a.iw = W;
+        a.imlo = -(bl - 1);
+        if (P.axisym) {
+          a.w = P.d_w + sd.w_axi;
+          a.wscale = adj ? 1.0 / kSqrt2Pi : 2.0 * kPi / W * kSqrt2Pi;
+          a.lmin = sd.lsup_merge[i];
+        } else {
+          a.w = nullptr;
+          a.wscale = adj ? 1.0 : 4.0 * kPi * kPi / W;
+          a.lmin = std::max(real ? 0 : std::abs(P.s), sd.lsup_merge[i]);
+        }
+        a.y = z + sd.z_off[i];
+        a.ys = P.z_per_map;
+        a.nb = nb;
+      }
+      contract_t2l_group(grp, ngrp, S.st);
+    }
+    k0 = k1;
   }
   merge_lmn(flm, L, (int64_t)L * L, z, P.z_per_map, P.d_pairs, P.npairs, P.d_w, zs, (int64_t)bs * bs, bs,
             real, accumulate, nb, S.st);

@@ -644,12 +644,13 @@ void launch_contract(const ContractArgs &a, int nm, int rows, cudaStream_t st) {
 // e^{i n_k gamma_g} for all (g, k) of one call, gamma_g = 2 pi g / ng
 constexpr int kMaxGammaTw = 512;
 
+// NN = number of n values (compile time, so that the per-n values live in registers)
+template <int NN>
 __global__ void k_gamma_synth(const double2 *__restrict__ G, double2 *__restrict__ spec,
-                              const int *__restrict__ ns, int nn, int ng, int bl, int nb, int real,
-                              double c) {
-  __shared__ double2 tw[kMaxGammaTw];  // tw[g * nn + k]
-  for (int i = threadIdx.x; i < ng * nn; i += blockDim.x) {
-    const int g = i / nn, k = i % nn;
+                              const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+  __shared__ double2 tw[kMaxGammaTw];  // tw[g * NN + k]
+  for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
+    const int g = i / NN, k = i % NN;
     double sn, cs;
     sincospi(2.0 * (double)((ns[k] * g) % ng) / (double)ng, &sn, &cs);
     tw[i] = make_double2(cs, sn);
@@ -664,30 +665,38 @@ __global__ void k_gamma_synth(const double2 *__restrict__ G, double2 *__restrict
   const int t = (int)((gid / sw) % bl);
   const int b = (int)(gid / ((int64_t)sw * bl));
   const int m = smlo + col;
-  const int64_t gb = (int64_t)b * nn * bl * W;
-  double2 gv[16], gm[16];
-  for (int k = 0; k < nn; ++k) {
+  const int64_t gb = (int64_t)b * NN * bl * W;
+  // real signals: the -n term is conj of G_n at -m, folded in as
+  // e G_n(m) + conj(e) conj(G_n(-m)) = e.re (G + H) + i e.im (G - H),  H = conj(G_n(-m))
+  double2 S[NN], D[NN];
+#pragma unroll
+  for (int k = 0; k < NN; ++k) {
     const double2 *Gk = G + gb + (int64_t)k * bl * W + (int64_t)t * W;
-    gv[k] = Gk[m + bl - 1];
-    gm[k] = (real && ns[k] > 0) ? conj2(Gk[-m + bl - 1]) : make_double2(0.0, 0.0);
+    const double2 gv = Gk[m + bl - 1];
+    const double2 gm = (real && ns[k] > 0) ? conj2(Gk[-m + bl - 1]) : make_double2(0.0, 0.0);
+    S[k] = add2(gv, gm);
+    D[k] = sub2(gv, gm);
   }
+  double2 *out = spec + (int64_t)b * ng * bl * sw + (int64_t)t * sw + col;
   for (int g = 0; g < ng; ++g) {
     double2 acc = make_double2(0.0, 0.0);
-    for (int k = 0; k < nn; ++k) {
-      const double2 e = tw[g * nn + k];
-      acc = add2(acc, cmul(e, gv[k]));
-      if (real && ns[k] > 0) acc = add2(acc, cmul(conj2(e), gm[k]));
+#pragma unroll
+    for (int k = 0; k < NN; ++k) {
+      const double2 e = tw[g * NN + k];
+      // e.re * S + i e.im * D
+      acc.x = fma(e.x, S[k].x, fma(-e.y, D[k].y, acc.x));
+      acc.y = fma(e.x, S[k].y, fma(e.y, D[k].x, acc.y));
     }
-    spec[((int64_t)b * ng + g) * bl * sw + (int64_t)t * sw + col] = scl2(acc, c);
+    out[(int64_t)g * bl * sw] = scl2(acc, c);
   }
 }
 
+template <int NN>
 __global__ void k_gamma_anal(const double2 *__restrict__ spec, double2 *__restrict__ G,
-                             const int *__restrict__ ns, int nn, int ng, int bl, int nb, int real,
-                             double c) {
-  __shared__ double2 tw[kMaxGammaTw];  // tw[g * nn + k] = e^{-i n_k gamma_g}
-  for (int i = threadIdx.x; i < ng * nn; i += blockDim.x) {
-    const int g = i / nn, k = i % nn;
+                             const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+  __shared__ double2 tw[kMaxGammaTw];  // tw[g * NN + k] = e^{-i n_k gamma_g}
+  for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
+    const int g = i / NN, k = i % NN;
     double sn, cs;
     sincospi(2.0 * (double)((ns[k] * g) % ng) / (double)ng, &sn, &cs);
     tw[i] = make_double2(cs, -sn);
@@ -702,18 +711,25 @@ __global__ void k_gamma_anal(const double2 *__restrict__ spec, double2 *__restri
   const int t = (int)((gid / W) % bl);
   const int b = (int)(gid / ((int64_t)W * bl));
   const int m = col - (bl - 1);
-  double2 acc[16];
-  for (int k = 0; k < nn; ++k) acc[k] = make_double2(0.0, 0.0);
-  for (int g = 0; g < ng; ++g) {
-    const double2 *sg = spec + ((int64_t)b * ng + g) * bl * sw + (int64_t)t * sw;
+  double2 acc[NN];
+#pragma unroll
+  for (int k = 0; k < NN; ++k) acc[k] = make_double2(0.0, 0.0);
+  const double2 *sg = spec + (int64_t)b * ng * bl * sw + (int64_t)t * sw;
+  for (int g = 0; g < ng; ++g, sg += (int64_t)bl * sw) {
     double2 s;
     if (real)
       s = m >= 0 ? sg[m] : conj2(sg[-m]);
     else
       s = sg[m - smlo];
-    for (int k = 0; k < nn; ++k) acc[k] = add2(acc[k], cmul(tw[g * nn + k], s));
+#pragma unroll
+    for (int k = 0; k < NN; ++k) {
+      const double2 e = tw[g * NN + k];
+      acc[k].x = fma(e.x, s.x, fma(-e.y, s.y, acc[k].x));
+      acc[k].y = fma(e.x, s.y, fma(e.y, s.x, acc[k].y));
+    }
   }
-  for (int k = 0; k < nn; ++k) G[((int64_t)b * nn + k) * bl * W + (int64_t)t * W + col] = scl2(acc[k], c);
+#pragma unroll
+  for (int k = 0; k < NN; ++k) G[((int64_t)b * NN + k) * bl * W + (int64_t)t * W + col] = scl2(acc[k], c);
 }
 
 // ---------------------------------------------------------------------------
@@ -852,7 +868,7 @@ void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, voi
 
 void contract_l2t(const L2T &p, cudaStream_t st) {
   if (p.nb <= 0 || p.mhi < p.mlo) return;
-  if (t_precision == 1 && contract_l2t_mixed(p, st)) return;
+  if (t_precision == 1 && contract_l2t_mixed(&p, 1, st)) return;
   ContractArgs a{};
   a.table = p.use_q ? p.tb->Q : p.tb->D;
   a.off = p.tb->d_off;
@@ -883,7 +899,7 @@ void contract_l2t(const L2T &p, cudaStream_t st) {
 
 void contract_t2l(const T2L &p, cudaStream_t st) {
   if (p.nb <= 0 || p.mhi < p.mlo) return;
-  if (t_precision == 1 && contract_t2l_mixed(p, st)) return;
+  if (t_precision == 1 && contract_t2l_mixed(&p, 1, st)) return;
   ContractArgs a{};
   a.table = p.use_q ? p.tb->Q : p.tb->D;
   a.off = p.tb->d_off;
@@ -910,24 +926,53 @@ void contract_t2l(const T2L &p, cudaStream_t st) {
     launch_contract<3>(a, nm, a.bl, st);
 }
 
+void contract_l2t_group(const L2T *a, int n, cudaStream_t st) {
+  if (n <= 0) return;
+  if (t_precision == 1 && n <= 2 && contract_l2t_mixed(a, n, st)) return;
+  for (int i = 0; i < n; ++i) contract_l2t(a[i], st);
+}
+
+void contract_t2l_group(const T2L *a, int n, cudaStream_t st) {
+  if (n <= 0) return;
+  if (t_precision == 1 && n <= 2 && contract_t2l_mixed(a, n, st)) return;
+  for (int i = 0; i < n; ++i) contract_t2l(a[i], st);
+}
+
 void gamma_synthesis(const double2 *G, double2 *spec, const int *ns, int nn, int ng, int bl, int nb,
                      bool real, double c, cudaStream_t st) {
-  S2G_REQUIRE(nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
+  S2G_REQUIRE(nn >= 1 && nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
   const int sw = real ? bl : 2 * bl - 1;
   const int64_t total = (int64_t)nb * bl * sw;
   if (total <= 0) return;
-  KTimer kt(KC_GAMMA, st, 0.0, 0.0);
-  k_gamma_synth<<<ceil_div(total, 256), 256, 0, st>>>(G, spec, ns, nn, ng, bl, nb, real, c);
+  KTimer kt(KC_GAMMA, st, 0.0, (double)nb * bl * ((real ? 2.0 : 1.0) * nn + ng) * sw * 16.0);
+  const unsigned grid = (unsigned)ceil_div(total, 256);
+  switch (nn) {
+#define S2G_GS(N) \
+  case N: k_gamma_synth<N><<<grid, 256, 0, st>>>(G, spec, ns, ng, bl, nb, real, c); break;
+    S2G_GS(1) S2G_GS(2) S2G_GS(3) S2G_GS(4) S2G_GS(5) S2G_GS(6) S2G_GS(7) S2G_GS(8)
+    S2G_GS(9) S2G_GS(10) S2G_GS(11) S2G_GS(12) S2G_GS(13) S2G_GS(14) S2G_GS(15) S2G_GS(16)
+#undef S2G_GS
+    default: break;
+  }
   S2G_LAUNCHED();
 }
 
 void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int ng, int bl, int nb,
                     bool real, double c, cudaStream_t st) {
-  S2G_REQUIRE(nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
+  S2G_REQUIRE(nn >= 1 && nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
   const int64_t total = (int64_t)nb * bl * (2 * bl - 1);
   if (total <= 0) return;
-  KTimer kt(KC_GAMMA, st, 0.0, 0.0);
-  k_gamma_anal<<<ceil_div(total, 256), 256, 0, st>>>(spec, G, ns, nn, ng, bl, nb, real, c);
+  const int sw = real ? bl : 2 * bl - 1;
+  KTimer kt(KC_GAMMA, st, 0.0, (double)nb * bl * ((double)ng * sw + (double)nn * (2 * bl - 1)) * 16.0);
+  const unsigned grid = (unsigned)ceil_div(total, 256);
+  switch (nn) {
+#define S2G_GA(N) \
+  case N: k_gamma_anal<N><<<grid, 256, 0, st>>>(spec, G, ns, ng, bl, nb, real, c); break;
+    S2G_GA(1) S2G_GA(2) S2G_GA(3) S2G_GA(4) S2G_GA(5) S2G_GA(6) S2G_GA(7) S2G_GA(8)
+    S2G_GA(9) S2G_GA(10) S2G_GA(11) S2G_GA(12) S2G_GA(13) S2G_GA(14) S2G_GA(15) S2G_GA(16)
+#undef S2G_GA
+    default: break;
+  }
   S2G_LAUNCHED();
 }
 

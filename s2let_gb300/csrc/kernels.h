@@ -49,6 +49,9 @@ struct L2T {
   int nb;
 };
 void contract_l2t(const L2T &a, cudaStream_t st);
+// n problems on the same table (same band-limit, n, m range and batch): one
+// table pass on the split-precision path when n <= 2, else one call each.
+void contract_l2t_group(const L2T *a, int n, cudaStream_t st);
 
 // Contraction over t producing harmonic coefficients ("t -> l"):
 //   y[b*ys + l^2+l+m] = w(l) sum_t A_m[l][t] in[b][t][m - imlo]
@@ -72,6 +75,7 @@ struct T2L {
   int nb;
 };
 void contract_t2l(const T2L &a, cudaStream_t st);
+void contract_t2l_group(const T2L *a, int n, cudaStream_t st);
 
 // gamma synthesis: spec[b][g][t][m - (real?0:-(bl-1))] from coefficients
 // G[b][k][t][m + bl - 1] of directions ns[k]; real: Hermitian in (m, n).

@@ -43,20 +43,24 @@ constexpr int kS = 7;                  // digit slices per operand
 constexpr int kB0 = 6;                 // bits of the first digit (later digits: 7)
 constexpr int kPK = 64;                // K per panel
 constexpr int kPM = 128;               // rows per panel
-constexpr int kNC = 16;                // real coefficient columns per CTA
 constexpr int kPanelA = kPM * kPK;     // 8192 elements, 16 KB
-constexpr int kPanelX = kS * kNC * kPK;  // 7168 elements, 14 KB
+constexpr int kMaxParts = 2;           // scales sharing one table pass
 constexpr int kAST = 10, kXST = 2;     // pipeline depths
-constexpr int kAccCols = kS * kNC;     // 112 TMEM columns per accumulator
-constexpr int kTmemCols = 256;
 constexpr int kThreads = 192;
 constexpr int kMinBl = 128;            // below this the FP64 kernel is used
 constexpr long long kWaitCycles = 4000000000LL;
-
 constexpr size_t kSmemA = (size_t)kAST * kPanelA * 2;
-constexpr size_t kSmemX = (size_t)kXST * kPanelX * 2;
 constexpr int kNumBars = 2 * kAST + 2 * kXST + 4 + 1;
-constexpr size_t kSmemBytes = 1024 + kSmemA + kSmemX + kNumBars * 8 + 16;
+
+// NC real coefficient columns per CTA: 16 per part (8 complex maps)
+template <int NC>
+struct Cfg {
+  static constexpr int kPanelX = kS * NC * kPK;       // 7168 or 14336 elements
+  static constexpr int kAccCols = kS * NC;            // TMEM columns per accumulator
+  static constexpr int kTmemCols = NC == 16 ? 256 : 512;
+  static constexpr size_t kSmemX = (size_t)kXST * kPanelX * 2;
+  static constexpr size_t kSmemBytes = 1024 + kSmemA + kSmemX + kNumBars * 8 + 16;
+};
 
 struct Geom {
   int l0, nl, rows, K, nkc, nrt;
@@ -161,15 +165,25 @@ __global__ void __launch_bounds__(128) k_slice_table(const double *__restrict__ 
 // coefficient slicing (per call)
 // ---------------------------------------------------------------------------
 
-struct XArgs {
-  int q;  // 0: l -> t (K = l - l0), 1: t -> l (K = t)
-  int bl, an, mlo, lmin;
-  const double2 *src;
+// One scale's coefficients and outputs inside a fused table pass.
+struct Part {
+  const double2 *src;  // l -> t: flm-like (l^2 + l + m); t -> l: spectra [t][m - s_mlo]
   int64_t ss;
   int sw, s_mlo, x_half;
-  const double2 *w;
+  const double2 *w;  // per-l weight (l -> t: on the input; t -> l: on the output)
   double wscale;
   int wconj;
+  int lmin;
+  double2 *dst;  // l -> t: spectra [t][m - d_mlo] (row width dw); t -> l: l^2 + l + m
+  int64_t ds;
+  int dw, d_mlo;
+};
+
+struct XArgs {
+  int q;  // 0: l -> t (K = l - l0), 1: t -> l (K = t)
+  int bl, an, mlo, lmin;  // lmin: smallest lmin over the parts
+  int nparts;
+  Part part[kMaxParts];
   int nb, b0;
   const int64_t *xoff;
   uint16_t *xpan;
@@ -182,55 +196,59 @@ __device__ __forceinline__ double2 weight_of(const double2 *w, double wscale, in
   return make_double2(v.x * wscale, v.y * wscale);
 }
 
-__device__ __forceinline__ double x_value(const XArgs &a, int m, int am, const Geom &g, int lst, int k,
-                                          int c) {
-  const int b = a.b0 + (c >> 1);
-  if (b >= a.nb) return 0.0;
+// column c: part c / 16, map b0 + (c % 16) / 2, real (c even) or imaginary part
+__device__ __forceinline__ double x_value(const XArgs &a, int m, int am, const Geom &g, int k, int c) {
+  const int pi = c >> 4;
+  const int b = a.b0 + ((c & 15) >> 1);
+  if (pi >= a.nparts || b >= a.nb) return 0.0;
+  const Part &P = a.part[pi];
   double2 v;
   if (!a.q) {
     const int l = g.l0 + k;
-    if (l < lst || l >= a.bl) return 0.0;
-    const int64_t base = (int64_t)b * a.ss + (int64_t)l * l + l;
-    if (a.x_half && m < 0) {
-      v = a.src[base - m];
+    if (l < P.lmin || l >= a.bl) return 0.0;
+    const int64_t base = (int64_t)b * P.ss + (int64_t)l * l + l;
+    if (P.x_half && m < 0) {
+      v = P.src[base - m];
       v.y = -v.y;
       if (am & 1) v = make_double2(-v.x, -v.y);
     } else {
-      v = a.src[base + m];
+      v = P.src[base + m];
     }
-    const double2 wt = weight_of(a.w, a.wscale, a.wconj, l);
+    const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
     v = make_double2(v.x * wt.x - v.y * wt.y, v.x * wt.y + v.y * wt.x);
   } else {
     if (k >= a.bl) return 0.0;
-    v = a.src[(int64_t)b * a.ss + (int64_t)k * a.sw + (m - a.s_mlo)];
+    v = P.src[(int64_t)b * P.ss + (int64_t)k * P.sw + (m - P.s_mlo)];
   }
   return (c & 1) ? v.y : v.x;
 }
 
-__global__ void __launch_bounds__(256) k_slice_x(XArgs a) {
+template <int NC>
+__global__ void __launch_bounds__(16 * NC) k_slice_x(XArgs a) {
+  constexpr int PX = Cfg<NC>::kPanelX;
   const int pm = blockIdx.x, m = a.mlo + pm, am = m < 0 ? -m : m;
   const Geom g = geom(a.bl, a.an, m, a.q != 0);
   const int c = threadIdx.x >> 4, sub = threadIdx.x & 15;
   if (g.nkc == 0) {
-    if (sub == 0) a.eX[pm * kNC + c] = 0;
+    if (sub == 0) a.eX[pm * NC + c] = 0;
     return;
   }
   const int lst = g.l0 > a.lmin ? g.l0 : a.lmin;
   int kc0 = 0;
   if (!a.q) kc0 = lst >= a.bl ? g.nkc : (lst - g.l0) / kPK;
   double mx = 0.0;
-  for (int k = kc0 * kPK + sub; k < g.nkc * kPK; k += 16) mx = fmax(mx, fabs(x_value(a, m, am, g, lst, k, c)));
+  for (int k = kc0 * kPK + sub; k < g.nkc * kPK; k += 16) mx = fmax(mx, fabs(x_value(a, m, am, g, k, c)));
 #pragma unroll
   for (int o = 8; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   const int e = exponent_of(mx);
-  if (sub == 0) a.eX[pm * kNC + c] = e;
-  uint16_t *base = a.xpan + a.xoff[pm];
+  if (sub == 0) a.eX[pm * NC + c] = e;
+  uint16_t *base = a.xpan + a.xoff[pm] * (NC / 16);
   for (int k = kc0 * kPK + sub; k < g.nkc * kPK; k += 16) {
     uint16_t dg[kS];
-    split_digits(ldexp(x_value(a, m, am, g, lst, k, c), -e), dg);
-    uint16_t *p = base + (int64_t)(k / kPK) * kPanelX;
+    split_digits(ldexp(x_value(a, m, am, g, k, c), -e), dg);
+    uint16_t *p = base + (int64_t)(k / kPK) * PX;
 #pragma unroll
-    for (int j = 0; j < kS; ++j) p[swz(j * kNC + c, k % kPK)] = dg[j];
+    for (int j = 0; j < kS; ++j) p[swz(j * NC + c, k % kPK)] = dg[j];
   }
 }
 
@@ -345,24 +363,20 @@ struct MxArgs {
   const int64_t *pan_off;
   const int8_t *eA;
   const int64_t *e_off;
-  int bl, an, tmlo, n, mlo, lmin;
+  int bl, an, tmlo, n, mlo, lmin;  // lmin: smallest over the parts
   const uint16_t *xpan;
   const int64_t *xoff;
   const int *eX;
   const int2 *tiles;
   int ntiles;
-  double2 *dst;
-  int64_t ds;
-  int dw, d_mlo;
-  const double2 *w;
-  double wscale;
-  int wconj;
+  int nparts;
+  Part part[kMaxParts];
   int nb, b0;
   int *err;
 };
 
 struct TileInfo {
-  int pm, m, mi, rt, kc0, nkc, l0, lst;
+  int pm, m, mi, rt, kc0, nkc, l0;
   double sign;
 };
 __device__ __forceinline__ TileInfo tile_info(const MxArgs &a, int t) {
@@ -377,18 +391,38 @@ __device__ __forceinline__ TileInfo tile_info(const MxArgs &a, int t) {
   const Geom g = geom(a.bl, a.an, ti.m, a.q != 0);
   ti.l0 = g.l0;
   ti.nkc = g.nkc;
-  ti.lst = g.l0 > a.lmin ? g.l0 : a.lmin;
+  const int lst = g.l0 > a.lmin ? g.l0 : a.lmin;
   ti.kc0 = 0;
-  if (!a.q) ti.kc0 = ti.lst >= a.bl ? g.nkc : (ti.lst - g.l0) / kPK;
+  if (!a.q) ti.kc0 = lst >= a.bl ? g.nkc : (lst - g.l0) / kPK;
   return ti;
 }
 
+// combine the 7 class accumulators of 16 columns [col0, col0 + 16) for this thread's row
+__device__ __forceinline__ void combine16(uint32_t taddr, int ncols_per_class, int ea, const int *eX, double sign,
+                                          double *y) {
+  float acc[kS][16];
+#pragma unroll
+  for (int c = 0; c < kS; ++c) tmem_ld16(taddr + (uint32_t)(c * ncols_per_class), acc[c]);
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int col = 0; col < 16; ++col) {
+    double s = 0.0;
+#pragma unroll
+    for (int c = kS - 1; c >= 0; --c) s = s * (1.0 / 128.0) + (double)acc[c][col];
+    y[col] = ldexp(s, ea + eX[col] - 2 * kB0) * sign;
+  }
+}
+
+template <int NC>
 __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
+  constexpr int PX = Cfg<NC>::kPanelX;
+  constexpr int ACC = Cfg<NC>::kAccCols;
+  constexpr int TMC = Cfg<NC>::kTmemCols;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint16_t *sA = (uint16_t *)smem;
   uint16_t *sX = (uint16_t *)(smem + kSmemA);
-  uint64_t *bars = (uint64_t *)(smem + kSmemA + kSmemX);
+  uint64_t *bars = (uint64_t *)(smem + kSmemA + Cfg<NC>::kSmemX);
   uint64_t *fullA = bars, *emptyA = bars + kAST, *fullX = bars + 2 * kAST, *emptyX = bars + 2 * kAST + kXST;
   uint64_t *tfull = bars + 2 * kAST + 2 * kXST, *tempty = tfull + 2, *mma_done = tfull + 4;
   volatile int *abort_flag = (volatile int *)(bars + kNumBars);
@@ -417,7 +451,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(tmem_slot)),
-                 "r"(kTmemCols)
+                 "r"(TMC)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -433,12 +467,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
     for (int t = blockIdx.x; ok && t < a.ntiles; t += gridDim.x) {
       const TileInfo ti = tile_info(a, t);
       const uint16_t *pan = a.panels + a.pan_off[ti.mi] + (int64_t)ti.rt * ti.nkc * kS * kPanelA;
-      const uint16_t *xp = a.xpan + a.xoff[ti.pm];
+      const uint16_t *xp = a.xpan + a.xoff[ti.pm] * (NC / 16);
       for (int kc = ti.kc0; ok && kc < ti.nkc; ++kc) {
         const int xs = issuedX % kXST;
         if (!(ok = bar_wait(&emptyX[xs], ((issuedX / kXST) & 1) ^ 1, abort_flag, a.err))) break;
-        bar_expect_tx(&fullX[xs], kPanelX * 2);
-        bulk_g2s(sX + (size_t)xs * kPanelX, xp + (int64_t)kc * kPanelX, kPanelX * 2, &fullX[xs]);
+        bar_expect_tx(&fullX[xs], PX * 2);
+        bulk_g2s(sX + (size_t)xs * PX, xp + (int64_t)kc * PX, PX * 2, &fullX[xs]);
         ++issuedX;
         for (int j = 0; j < kS; ++j) {
           const int as = issuedA % kAST;
@@ -458,7 +492,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
       const int ab = ti_n & 1;
       if (!(ok = bar_wait(&tempty[ab], ((ti_n >> 1) & 1) ^ 1, abort_flag, a.err))) break;
       tc_fence_after();
-      const uint32_t d0 = tmem + (uint32_t)(ab * kAccCols);
+      const uint32_t d0 = tmem + (uint32_t)(ab * ACC);
       if (ti.kc0 >= ti.nkc) {
         bar_arrive(&tfull[ab]);  // nothing to accumulate: the epilogue writes zeros
         continue;
@@ -467,17 +501,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
         const int xs = cx % kXST;
         if (!(ok = bar_wait(&fullX[xs], (cx / kXST) & 1, abort_flag, a.err))) break;
         tc_fence_after();
-        const uint64_t bdesc = sw128_desc(sX + (size_t)xs * kPanelX);
+        const uint64_t bdesc = sw128_desc(sX + (size_t)xs * PX);
         for (int j = 0; j < kS; ++j) {
           const int as = ca % kAST;
           if (!(ok = bar_wait(&fullA[as], (ca / kAST) & 1, abort_flag, a.err))) break;
           tc_fence_after();
           const uint64_t adesc = sw128_desc(sA + (size_t)as * kPanelA);
-          const uint32_t idesc = idesc_bf16(kPM, kNC * (kS - j));
+          const uint32_t idesc = idesc_bf16(kPM, NC * (kS - j));
 #pragma unroll
           for (int k = 0; k < kPK / 16; ++k) {
             // K advance of 16 bf16 = 32 bytes inside the swizzle atom
-            mma_bf16(d0 + (uint32_t)(kNC * j), adesc + (uint64_t)(2 * k), bdesc + (uint64_t)(2 * k), idesc,
+            mma_bf16(d0 + (uint32_t)(NC * j), adesc + (uint64_t)(2 * k), bdesc + (uint64_t)(2 * k), idesc,
                      (kc == ti.kc0 && j == 0 && k == 0) ? 0u : 1u);
           }
           any = true;
@@ -508,52 +542,47 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
       // warp-uniform outcome: tcgen05.ld below is .sync.aligned
       if (!__all_sync(0xffffffffu, bar_wait(&tfull[ab], (ti_n >> 1) & 1, abort_flag, a.err))) break;
       tc_fence_after();
-      double y[kNC];
-      if (ti.kc0 < ti.nkc) {
-        float acc[kS][kNC];
-        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * kAccCols);
+      const bool live = ti.kc0 < ti.nkc;
+      const int ea = live ? (int)a.eA[a.e_off[ti.mi] + ti.rt * kPM + rr] : 0;
+      const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * ACC);
+      for (int pi = 0; pi < NC / 16; ++pi) {
+        double y[16];
+        if (live) {
+          combine16(taddr + (uint32_t)(pi * 16), NC, ea, a.eX + ti.pm * NC + pi * 16, ti.sign, y);
+        } else {
 #pragma unroll
-        for (int c = 0; c < kS; ++c) tmem_ld16(taddr + (uint32_t)(c * kNC), acc[c]);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        tc_fence_before();
-        bar_arrive(&tempty[ab]);
-        const int rowg = ti.rt * kPM + rr;
-        const int ea = a.eA[a.e_off[ti.mi] + rowg];
-#pragma unroll
-        for (int col = 0; col < kNC; ++col) {
-          double s = 0.0;
-#pragma unroll
-          for (int c = kS - 1; c >= 0; --c) s = s * (1.0 / 128.0) + (double)acc[c][col];
-          y[col] = ldexp(s, ea + a.eX[ti.pm * kNC + col] - 2 * kB0) * ti.sign;
+          for (int col = 0; col < 16; ++col) y[col] = 0.0;
         }
-      } else {
-        tc_fence_before();
-        bar_arrive(&tempty[ab]);
+        if (pi == NC / 16 - 1) {  // all columns read: hand the accumulator back
+          tc_fence_before();
+          bar_arrive(&tempty[ab]);
+        }
+        if (pi >= a.nparts) continue;
+        const Part &P = a.part[pi];
+        if (!a.q) {
+          const int t_row = ti.rt * kPM + rr;
+          if (t_row < a.bl) {
 #pragma unroll
-        for (int col = 0; col < kNC; ++col) y[col] = 0.0;
-      }
-      if (!a.q) {
-        const int t_row = ti.rt * kPM + rr;
-        if (t_row < a.bl) {
-#pragma unroll
-          for (int bb = 0; bb < kNC / 2; ++bb) {
-            const int b = a.b0 + bb;
-            if (b < a.nb)
-              a.dst[(int64_t)b * a.ds + (int64_t)t_row * a.dw + (ti.m - a.d_mlo)] =
-                  make_double2(y[2 * bb], y[2 * bb + 1]);
+            for (int bb = 0; bb < 8; ++bb) {
+              const int b = a.b0 + bb;
+              if (b < a.nb)
+                P.dst[(int64_t)b * P.ds + (int64_t)t_row * P.dw + (ti.m - P.d_mlo)] =
+                    make_double2(y[2 * bb], y[2 * bb + 1]);
+            }
           }
-        }
-      } else {
-        const int l = ti.l0 + ti.rt * kPM + rr;
-        if (l >= ti.lst && l < a.bl) {
-          const double2 wt = weight_of(a.w, a.wscale, a.wconj, l);
+        } else {
+          const int l = ti.l0 + ti.rt * kPM + rr;
+          const int lst = ti.l0 > P.lmin ? ti.l0 : P.lmin;
+          if (l >= lst && l < a.bl) {
+            const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
 #pragma unroll
-          for (int bb = 0; bb < kNC / 2; ++bb) {
-            const int b = a.b0 + bb;
-            if (b < a.nb) {
-              const double yr = y[2 * bb], yi = y[2 * bb + 1];
-              a.dst[(int64_t)b * a.ds + (int64_t)l * l + l + ti.m] =
-                  make_double2(yr * wt.x - yi * wt.y, yr * wt.y + yi * wt.x);
+            for (int bb = 0; bb < 8; ++bb) {
+              const int b = a.b0 + bb;
+              if (b < a.nb) {
+                const double yr = y[2 * bb], yi = y[2 * bb + 1];
+                P.dst[(int64_t)b * P.ds + (int64_t)l * l + l + ti.m] =
+                    make_double2(yr * wt.x - yi * wt.y, yr * wt.y + yi * wt.x);
+              }
             }
           }
         }
@@ -571,13 +600,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
     for (int i = cons[1]; i < issuedX; ++i)
       while (!bar_try(&fullX[i % kXST], (i / kXST) & 1) && clock64() - t0 < kWaitCycles) {
       }
-    (void)t0;
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   if (warp == 1)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMC) : "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -665,7 +693,7 @@ const TileList &tile_list(SlicedTable &s, int n, int mlo, int mhi, int lmin, cud
   for (int m = mlo; m <= mhi; ++m) {
     const Geom g = geom(s.bl, s.an, m, s.q);
     xoff[m - mlo] = xe;
-    xe += (int64_t)g.nkc * kPanelX;
+    xe += (int64_t)g.nkc * Cfg<16>::kPanelX;
     if (g.nl <= 0) continue;
     const int lst = g.l0 > lmin ? g.l0 : lmin;
     int rt0 = 0, kc0 = 0;
@@ -716,50 +744,49 @@ int *error_flag() {
 struct Problem {
   bool q;
   const WignerTable *tb;
-  int n, mlo, mhi, lmin;
-  const double2 *src;
-  int64_t ss;
-  int sw, s_mlo, x_half;
-  const double2 *w;
-  double wscale;
-  int wconj;
-  double2 *dst;
-  int64_t ds;
-  int dw, d_mlo;
+  int n, mlo, mhi;
+  int nparts;
+  Part part[kMaxParts];
   int nb;
 };
 
+template <int NC>
 void run_mixed(const Problem &p, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
-    S2G_CUDA(cudaFuncSetAttribute(k_contract_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
+    S2G_CUDA(cudaFuncSetAttribute(k_contract_mx<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)Cfg<NC>::kSmemBytes));
     attr = true;
   }
+  int lmin = p.part[0].lmin;
+  for (int i = 1; i < p.nparts; ++i) lmin = std::min(lmin, p.part[i].lmin);
   SlicedTable *s;
   const TileList *L;
   int *err;
   {
     std::lock_guard<std::mutex> lk(g_mx_mu);
     s = &sliced(*p.tb, p.q, st);
-    L = &tile_list(*s, p.n, p.mlo, p.mhi, p.lmin, st);
+    L = &tile_list(*s, p.n, p.mlo, p.mhi, lmin, st);
     err = error_flag();
   }
   const int nmp = p.mhi - p.mlo + 1;
-  const int ngroups = (p.nb + kNC / 2 - 1) / (kNC / 2);
+  const int ngroups = (p.nb + 7) / 8;
+  // coefficient panels: the tile list's offsets count 16-column panels; an
+  // NC-column panel is NC/16 times larger, so offsets scale by NC/16
+  const int64_t x_elems = L->x_elems * (NC / 16);
   uint16_t *xpan = nullptr;
   int *eX = nullptr;
-  S2G_CUDA(cudaMallocAsync((void **)&xpan, sizeof(uint16_t) * (size_t)(L->x_elems ? L->x_elems : 1), st));
-  S2G_CUDA(cudaMallocAsync((void **)&eX, sizeof(int) * (size_t)nmp * kNC, st));
-  // algorithmic work: 4 flop per (entry, complex map); bytes: 14 B per table
-  // entry streamed + coefficient panels + FP64 outputs
+  const int64_t *xoff = L->d_xoff;
+  S2G_CUDA(cudaMallocAsync((void **)&xpan, sizeof(uint16_t) * (size_t)(x_elems ? x_elems : 1), st));
+  S2G_CUDA(cudaMallocAsync((void **)&eX, sizeof(int) * (size_t)nmp * NC, st));
   const double entries = (double)L->work_entries;
   for (int g = 0; g < ngroups; ++g) {
-    const int b0 = g * (kNC / 2);
-    const int nbg = p.nb - b0 < kNC / 2 ? p.nb - b0 : kNC / 2;
+    const int b0 = g * 8;
+    const int nbg = p.nb - b0 < 8 ? p.nb - b0 : 8;
     double fl = 0, by = 0;
     if (timing_enabled()) {
-      fl = 4.0 * entries * nbg;
-      by = entries * 2.0 * kS + (double)L->x_elems * 2.0 + 16.0 * nbg * (double)p.tb->bl * nmp;
+      fl = 4.0 * entries * nbg * p.nparts;
+      by = entries * 2.0 * kS + (double)x_elems * 2.0 + 16.0 * nbg * p.nparts * (double)p.tb->bl * nmp;
     }
     KTimer kt(KC_MIXED, st, fl, by);
     XArgs xa{};
@@ -767,21 +794,15 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     xa.bl = p.tb->bl;
     xa.an = p.tb->an;
     xa.mlo = p.mlo;
-    xa.lmin = p.lmin;
-    xa.src = p.src;
-    xa.ss = p.ss;
-    xa.sw = p.sw;
-    xa.s_mlo = p.s_mlo;
-    xa.x_half = p.x_half;
-    xa.w = p.w;
-    xa.wscale = p.wscale;
-    xa.wconj = p.wconj;
+    xa.lmin = lmin;
+    xa.nparts = p.nparts;
+    for (int i = 0; i < p.nparts; ++i) xa.part[i] = p.part[i];
     xa.nb = p.nb;
     xa.b0 = b0;
-    xa.xoff = L->d_xoff;
+    xa.xoff = xoff;
     xa.xpan = xpan;
     xa.eX = eX;
-    k_slice_x<<<nmp, 256, 0, st>>>(xa);
+    k_slice_x<NC><<<nmp, 16 * NC, 0, st>>>(xa);
     S2G_LAUNCHED();
     if (L->ntiles == 0) continue;
     MxArgs ma{};
@@ -795,76 +816,103 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     ma.tmlo = p.tb->mlo;
     ma.n = p.n;
     ma.mlo = p.mlo;
-    ma.lmin = p.lmin;
+    ma.lmin = lmin;
     ma.xpan = xpan;
-    ma.xoff = L->d_xoff;
+    ma.xoff = xoff;
     ma.eX = eX;
     ma.tiles = L->d_tiles;
     ma.ntiles = L->ntiles;
-    ma.dst = p.dst;
-    ma.ds = p.ds;
-    ma.dw = p.dw;
-    ma.d_mlo = p.d_mlo;
-    ma.w = p.w;
-    ma.wscale = p.wscale;
-    ma.wconj = p.wconj;
+    ma.nparts = p.nparts;
+    for (int i = 0; i < p.nparts; ++i) ma.part[i] = p.part[i];
     ma.nb = p.nb;
     ma.b0 = b0;
     ma.err = err;
     const int grid = L->ntiles < num_sms() ? L->ntiles : num_sms();
-    k_contract_mx<<<grid, kThreads, kSmemBytes, st>>>(ma);
+    k_contract_mx<NC><<<grid, kThreads, Cfg<NC>::kSmemBytes, st>>>(ma);
     S2G_LAUNCHED();
   }
   cudaFreeAsync(xpan, st);
   cudaFreeAsync(eX, st);
 }
 
+void run_problem(const Problem &p, cudaStream_t st) {
+  if (p.nparts == 1)
+    run_mixed<16>(p, st);
+  else
+    run_mixed<32>(p, st);
+}
+
+Part part_of(const L2T &a) {
+  Part P{};
+  P.src = a.x;
+  P.ss = a.xs;
+  P.x_half = a.x_half ? 1 : 0;
+  P.w = a.w;
+  P.wscale = a.wscale;
+  P.wconj = a.wconj ? 1 : 0;
+  P.lmin = a.lmin;
+  P.dst = a.out;
+  P.ds = a.os;
+  P.dw = a.ow;
+  P.d_mlo = a.omlo;
+  return P;
+}
+
+Part part_of(const T2L &a) {
+  Part P{};
+  P.src = a.in;
+  P.ss = a.is;
+  P.sw = a.iw;
+  P.s_mlo = a.imlo;
+  P.w = a.w;
+  P.wscale = a.wscale;
+  P.wconj = a.wconj ? 1 : 0;
+  P.lmin = a.lmin;
+  P.dst = a.y;
+  P.ds = a.ys;
+  return P;
+}
+
+template <class A>
+bool same_problem(const A &x, const A &y) {
+  return x.tb == y.tb && x.n == y.n && x.use_q == y.use_q && x.mlo == y.mlo && x.mhi == y.mhi && x.nb == y.nb;
+}
+
 }  // namespace
 
-bool contract_l2t_mixed(const L2T &a, cudaStream_t st) {
-  if (a.use_q || a.tb->bl < kMinBl || a.nb <= 0 || a.mhi < a.mlo) return false;
+bool contract_l2t_mixed(const L2T *a, int nparts, cudaStream_t st) {
+  if (nparts < 1 || nparts > kMaxParts) return false;
+  if (a[0].use_q || a[0].tb->bl < kMinBl || a[0].nb <= 0 || a[0].mhi < a[0].mlo) return false;
+  for (int i = 1; i < nparts; ++i)
+    if (!same_problem(a[0], a[i])) return false;
   Problem p{};
   p.q = false;
-  p.tb = a.tb;
-  p.n = a.n;
-  p.mlo = a.mlo;
-  p.mhi = a.mhi;
-  p.lmin = a.lmin;
-  p.src = a.x;
-  p.ss = a.xs;
-  p.x_half = a.x_half ? 1 : 0;
-  p.w = a.w;
-  p.wscale = a.wscale;
-  p.wconj = a.wconj ? 1 : 0;
-  p.dst = a.out;
-  p.ds = a.os;
-  p.dw = a.ow;
-  p.d_mlo = a.omlo;
-  p.nb = a.nb;
-  run_mixed(p, st);
+  p.tb = a[0].tb;
+  p.n = a[0].n;
+  p.mlo = a[0].mlo;
+  p.mhi = a[0].mhi;
+  p.nb = a[0].nb;
+  p.nparts = nparts;
+  for (int i = 0; i < nparts; ++i) p.part[i] = part_of(a[i]);
+  run_problem(p, st);
   return true;
 }
 
-bool contract_t2l_mixed(const T2L &a, cudaStream_t st) {
-  if (!a.use_q || a.tb->bl < kMinBl || a.nb <= 0 || a.mhi < a.mlo) return false;
+bool contract_t2l_mixed(const T2L *a, int nparts, cudaStream_t st) {
+  if (nparts < 1 || nparts > kMaxParts) return false;
+  if (!a[0].use_q || a[0].tb->bl < kMinBl || a[0].nb <= 0 || a[0].mhi < a[0].mlo) return false;
+  for (int i = 1; i < nparts; ++i)
+    if (!same_problem(a[0], a[i])) return false;
   Problem p{};
   p.q = true;
-  p.tb = a.tb;
-  p.n = a.n;
-  p.mlo = a.mlo;
-  p.mhi = a.mhi;
-  p.lmin = a.lmin;
-  p.src = a.in;
-  p.ss = a.is;
-  p.sw = a.iw;
-  p.s_mlo = a.imlo;
-  p.w = a.w;
-  p.wscale = a.wscale;
-  p.wconj = a.wconj ? 1 : 0;
-  p.dst = a.y;
-  p.ds = a.ys;
-  p.nb = a.nb;
-  run_mixed(p, st);
+  p.tb = a[0].tb;
+  p.n = a[0].n;
+  p.mlo = a[0].mlo;
+  p.mhi = a[0].mhi;
+  p.nb = a[0].nb;
+  p.nparts = nparts;
+  for (int i = 0; i < nparts; ++i) p.part[i] = part_of(a[i]);
+  run_problem(p, st);
   return true;
 }
 

@@ -20,8 +20,11 @@ namespace s2g {
 // True when the contraction ran on the tensor cores; false when the problem is
 // outside the split-precision kernel's domain (small band-limit, adjoint table
 // orientation) and the caller must run the FP64 kernel.
-bool contract_l2t_mixed(const L2T &a, cudaStream_t st);
-bool contract_t2l_mixed(const T2L &a, cudaStream_t st);
+// nparts (1 or 2) problems that differ only in their coefficients, weights,
+// lmin and outputs (scales sharing one band-limit and n) share one pass over
+// the table.
+bool contract_l2t_mixed(const L2T *a, int nparts, cudaStream_t st);
+bool contract_t2l_mixed(const T2L *a, int nparts, cudaStream_t st);
 
 void release_sliced_tables();
 size_t sliced_table_bytes();
