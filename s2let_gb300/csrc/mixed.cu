@@ -84,22 +84,30 @@ __host__ __device__ inline int swz(int row, int col) {
   return (row >> 3) * 512 + (row & 7) * 64 + chunk * 8 + (col & 7);
 }
 
-__device__ __forceinline__ uint16_t digit_bf16(double d) {
-  // |d| <= 64 is an integer: exact in bf16 (top half of the fp32 pattern)
+
+// Balanced digits of q = round(v 2^(48-e)), |v| < 2^e: q = sum_j d_j 2^(42-7j)
+// with d_1..d_6 in [-64, 63] (base-128 digits taken from the low end) and
+// d_0 in [-64, 64].  Integer arithmetic only, so the split costs no FP64 work.
+__device__ __forceinline__ void int_digits(long long q, int *d) {
+#pragma unroll
+  for (int j = kS - 1; j >= 1; --j) {
+    int r = (int)(q & 127);
+    if (r >= 64) r -= 128;
+    d[j] = r;
+    q = (q - r) >> 7;
+  }
+  d[0] = (int)q;
+}
+__device__ __forceinline__ uint16_t bf16_of_int(int d) {
+  // |d| <= 64: exact in bf16 (top half of the fp32 pattern)
   return (uint16_t)(__float_as_uint((float)d) >> 16);
 }
-
-// digits of r = v 2^-e, |r| <= 1
-__device__ __forceinline__ void split_digits(double r, uint16_t *out) {
-  double d = rint(r * 64.0);
-  out[0] = digit_bf16(d);
-  r = r * 64.0 - d;
+// digits of v 2^-e as bf16 bit patterns
+__device__ __forceinline__ void split_digits(double v, int e, uint16_t *out) {
+  int d[kS];
+  int_digits(__double2ll_rn(ldexp(v, 48 - e)), d);
 #pragma unroll
-  for (int j = 1; j < kS; ++j) {
-    d = rint(r * 128.0);
-    out[j] = digit_bf16(d);
-    r = r * 128.0 - d;
-  }
+  for (int j = 0; j < kS; ++j) out[j] = bf16_of_int(d[j]);
 }
 
 __device__ __forceinline__ int exponent_of(double mx) { return mx > 0.0 ? ilogb(mx) + 1 : 0; }
@@ -151,7 +159,7 @@ __global__ void __launch_bounds__(128) k_slice_table(const double *__restrict__ 
     for (int k = lane; k < kpad; k += 32) {
       const double v = (live && k < g.K) ? Tm[(int64_t)row * g.K + k] : 0.0;
       uint16_t dg[kS];
-      split_digits(ldexp(v, -e), dg);
+      split_digits(v, e, dg);
       const int kc = k / kPK;
       uint16_t *p = panels + pan_off[mi] + (int64_t)(rt * g.nkc + kc) * kS * kPanelA;
       const int idx = swz(rr, k % kPK);
@@ -196,17 +204,18 @@ __device__ __forceinline__ double2 weight_of(const double2 *w, double wscale, in
   return make_double2(v.x * wscale, v.y * wscale);
 }
 
-// column c: part c / 16, map b0 + (c % 16) / 2, real (c even) or imaginary part
-__device__ __forceinline__ double x_value(const XArgs &a, int m, int am, const Geom &g, int k, int c) {
-  const int pi = c >> 4;
-  const int b = a.b0 + ((c & 15) >> 1);
-  if (pi >= a.nparts || b >= a.nb) return 0.0;
+// Complex coefficient of column pair cp (part cp / 8, map b0 + cp % 8) at K index k.
+__device__ __forceinline__ double2 x_value(const XArgs &a, int m, int am, const Geom &g, int k, int cp) {
+  const int pi = cp >> 3;
+  const int b = a.b0 + (cp & 7);
+  const double2 zero = make_double2(0.0, 0.0);
+  if (pi >= a.nparts || b >= a.nb) return zero;
   const Part &P = a.part[pi];
-  double2 v;
   if (!a.q) {
     const int l = g.l0 + k;
-    if (l < P.lmin || l >= a.bl) return 0.0;
+    if (l < P.lmin || l >= a.bl) return zero;
     const int64_t base = (int64_t)b * P.ss + (int64_t)l * l + l;
+    double2 v;
     if (P.x_half && m < 0) {
       v = P.src[base - m];
       v.y = -v.y;
@@ -215,40 +224,75 @@ __device__ __forceinline__ double x_value(const XArgs &a, int m, int am, const G
       v = P.src[base + m];
     }
     const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
-    v = make_double2(v.x * wt.x - v.y * wt.y, v.x * wt.y + v.y * wt.x);
-  } else {
-    if (k >= a.bl) return 0.0;
-    v = P.src[(int64_t)b * P.ss + (int64_t)k * P.sw + (m - P.s_mlo)];
+    return make_double2(v.x * wt.x - v.y * wt.y, v.x * wt.y + v.y * wt.x);
   }
-  return (c & 1) ? v.y : v.x;
+  if (k >= a.bl) return zero;
+  return P.src[(int64_t)b * P.ss + (int64_t)k * P.sw + (m - P.s_mlo)];
 }
 
+// One block per problem m; thread (cp, h): column pair cp (real part in column
+// 2cp, imaginary part in 2cp + 1) and the 8-wide K chunk h of every panel, so
+// that each slice row of a panel is written by 8 consecutive lanes as eight
+// 16-byte (8 x bf16) stores = one full 128-byte row.
 template <int NC>
-__global__ void __launch_bounds__(16 * NC) k_slice_x(XArgs a) {
+__global__ void __launch_bounds__(NC * 4) k_slice_x(XArgs a) {
   constexpr int PX = Cfg<NC>::kPanelX;
   const int pm = blockIdx.x, m = a.mlo + pm, am = m < 0 ? -m : m;
   const Geom g = geom(a.bl, a.an, m, a.q != 0);
-  const int c = threadIdx.x >> 4, sub = threadIdx.x & 15;
+  const int cp = threadIdx.x >> 3, h = threadIdx.x & 7;
+  const int c0 = 2 * cp;
   if (g.nkc == 0) {
-    if (sub == 0) a.eX[pm * NC + c] = 0;
+    if (h == 0) a.eX[pm * NC + c0] = a.eX[pm * NC + c0 + 1] = 0;
     return;
   }
   const int lst = g.l0 > a.lmin ? g.l0 : a.lmin;
   int kc0 = 0;
   if (!a.q) kc0 = lst >= a.bl ? g.nkc : (lst - g.l0) / kPK;
-  double mx = 0.0;
-  for (int k = kc0 * kPK + sub; k < g.nkc * kPK; k += 16) mx = fmax(mx, fabs(x_value(a, m, am, g, k, c)));
+  double mr = 0.0, mi = 0.0;
+  for (int kc = kc0; kc < g.nkc; ++kc)
+#pragma unroll 4
+    for (int e = 0; e < 8; ++e) {
+      const double2 v = x_value(a, m, am, g, kc * kPK + h * 8 + e, cp);
+      mr = fmax(mr, fabs(v.x));
+      mi = fmax(mi, fabs(v.y));
+    }
 #pragma unroll
-  for (int o = 8; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  const int e = exponent_of(mx);
-  if (sub == 0) a.eX[pm * NC + c] = e;
+  for (int o = 4; o > 0; o >>= 1) {
+    mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+    mi = fmax(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+  }
+  const int er = exponent_of(mr), ei = exponent_of(mi);
+  if (h == 0) {
+    a.eX[pm * NC + c0] = er;
+    a.eX[pm * NC + c0 + 1] = ei;
+  }
   uint16_t *base = a.xpan + a.xoff[pm] * (NC / 16);
-  for (int k = kc0 * kPK + sub; k < g.nkc * kPK; k += 16) {
-    uint16_t dg[kS];
-    split_digits(ldexp(x_value(a, m, am, g, k, c), -e), dg);
-    uint16_t *p = base + (int64_t)(k / kPK) * PX;
+  for (int kc = kc0; kc < g.nkc; ++kc) {
+    uint32_t pr[kS][4], pi[kS][4];
 #pragma unroll
-    for (int j = 0; j < kS; ++j) p[swz(j * NC + c, k % kPK)] = dg[j];
+    for (int e = 0; e < 8; ++e) {
+      const double2 v = x_value(a, m, am, g, kc * kPK + h * 8 + e, cp);
+      int dr[kS], di[kS];
+      int_digits(__double2ll_rn(ldexp(v.x, 48 - er)), dr);
+      int_digits(__double2ll_rn(ldexp(v.y, 48 - ei)), di);
+#pragma unroll
+      for (int j = 0; j < kS; ++j) {
+        const uint32_t br = bf16_of_int(dr[j]), bi = bf16_of_int(di[j]);
+        if (e & 1) {
+          pr[j][e >> 1] |= br << 16;
+          pi[j][e >> 1] |= bi << 16;
+        } else {
+          pr[j][e >> 1] = br;
+          pi[j][e >> 1] = bi;
+        }
+      }
+    }
+    uint16_t *p = base + (int64_t)kc * PX;
+#pragma unroll
+    for (int j = 0; j < kS; ++j) {
+      *(uint4 *)(p + swz(j * NC + c0, h * 8)) = make_uint4(pr[j][0], pr[j][1], pr[j][2], pr[j][3]);
+      *(uint4 *)(p + swz(j * NC + c0 + 1, h * 8)) = make_uint4(pi[j][0], pi[j][1], pi[j][2], pi[j][3]);
+    }
   }
 }
 
@@ -397,7 +441,17 @@ __device__ __forceinline__ TileInfo tile_info(const MxArgs &a, int t) {
   return ti;
 }
 
-// combine the 7 class accumulators of 16 columns [col0, col0 + 16) for this thread's row
+// Combine the 7 class accumulators of 16 columns for this thread's row:
+// S = sum_c acc_c 2^(-7c) by Horner in double-float on the FP32 pipe (the class
+// values and 2^-7 scalings are exact floats), then one conversion to FP64 and
+// one multiplication by the power of two 2^(ea + eX - 12), built from its bits.
+__device__ __forceinline__ double pow2_signed(int k, double sign) {
+  if (k >= -1022 && k <= 1023) {
+    const unsigned long long bits = (unsigned long long)(k + 1023) << 52;
+    return __longlong_as_double((long long)(sign < 0.0 ? (bits | (1ull << 63)) : bits));
+  }
+  return ldexp(sign, k);
+}
 __device__ __forceinline__ void combine16(uint32_t taddr, int ncols_per_class, int ea, const int *eX, double sign,
                                           double *y) {
   float acc[kS][16];
@@ -406,10 +460,19 @@ __device__ __forceinline__ void combine16(uint32_t taddr, int ncols_per_class, i
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
   for (int col = 0; col < 16; ++col) {
-    double s = 0.0;
+    float hi = acc[kS - 1][col], lo = 0.0f;
 #pragma unroll
-    for (int c = kS - 1; c >= 0; --c) s = s * (1.0 / 128.0) + (double)acc[c][col];
-    y[col] = ldexp(s, ea + eX[col] - 2 * kB0) * sign;
+    for (int c = kS - 2; c >= 0; --c) {
+      hi = __fmul_rn(hi, 0.0078125f);
+      lo = __fmul_rn(lo, 0.0078125f);
+      const float s = __fadd_rn(acc[c][col], hi);
+      const float v = __fsub_rn(s, acc[c][col]);
+      float e = __fadd_rn(__fsub_rn(acc[c][col], __fsub_rn(s, v)), __fsub_rn(hi, v));
+      e = __fadd_rn(e, lo);
+      hi = __fadd_rn(s, e);
+      lo = __fsub_rn(e, __fsub_rn(hi, s));
+    }
+    y[col] = ((double)hi + (double)lo) * pow2_signed(ea + eX[col] - 2 * kB0, sign);
   }
 }
 
@@ -802,7 +865,7 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     xa.xoff = xoff;
     xa.xpan = xpan;
     xa.eX = eX;
-    k_slice_x<NC><<<nmp, 16 * NC, 0, st>>>(xa);
+    k_slice_x<NC><<<nmp, NC * 4, 0, st>>>(xa);
     S2G_LAUNCHED();
     if (L->ntiles == 0) continue;
     MxArgs ma{};
