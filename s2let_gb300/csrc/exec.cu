@@ -369,6 +369,15 @@ enum MergeMode { MERGE_SYNTHESIS, MERGE_ANALYSIS_ADJ };
 const double kSqrt2Pi = 2.5066282746310005024;
 
 // flm -> (f_wav, f_scal).  SPLIT_ANALYSIS: lm2wav.  SPLIT_SYNTH_ADJ: adjoint of wav2lm.
+// Ring DFTs per theta ring on the nn n-components (one complex DFT each) when
+// that is fewer than on the ng gamma slices (real slices pair up, two per
+// complex DFT); the gamma DFT then runs on pixels.
+bool rings_on_n(const WavPlan &P, const Scale &sd) {
+  const double on_n = (double)sd.ns.size();
+  const double on_g = P.real ? 0.5 * sd.ng : (double)sd.ng;
+  return on_n < on_g;
+}
+
 void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_half, void *f_wav,
                int64_t wstride, void *f_scal, int64_t sstride, int nb, Scratch &S) {
   const bool real = P.real;
@@ -446,11 +455,23 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
     for (int q = 0; q < ngrp; ++q) {
       const Scale &sd = P.sc[k0 + q];
       const int ng = sd.ng;
-      const int sw = real ? bl : W, mlo = real ? 0 : -(bl - 1);
-      gamma_synthesis(Gbuf + q * gsz, spec, sd.d_ns, nn, ng, bl, nb, real, adj && !P.axisym ? 1.0 / ng : 1.0,
-                      S.st);
+      const double c = adj && !P.axisym ? 1.0 / ng : 1.0;
       char *out = (char *)f_wav + (size_t)sd.woff * esz;
-      ring_inverse(spec, sw, sw, mlo, out, W, wstride, ng * bl, nb * ng * bl, bl, real, S.st);
+      const double2 *Gq = Gbuf + q * gsz;
+      if (rings_on_n(P, sd)) {
+        // F_n(t, p) = sum_m G_n(t, m) e^{i m phi_p}; spec holds F[b][i][t][p]
+        for (int i = 0; i < nn; ++i) {
+          const bool herm = real && sd.ns[i] == 0;  // real signal, n = 0: only m >= 0 computed
+          ring_inverse_c(Gq + (int64_t)i * bl * W + (herm ? bl - 1 : 0), W, (int64_t)nn * bl * W, bl,
+                         herm ? bl : W, herm ? 0 : -(bl - 1), herm, spec + (int64_t)i * bl * W, W,
+                         (int64_t)nn * bl * W, bl, nb * bl, bl, S.st);
+        }
+        gamma_px_synthesis(spec, out, wstride, sd.d_ns, nn, ng, bl, nb, real, c, S.st);
+      } else {
+        const int sw = real ? bl : W, mlo = real ? 0 : -(bl - 1);
+        gamma_synthesis(Gq, spec, sd.d_ns, nn, ng, bl, nb, real, c, S.st);
+        ring_inverse(spec, sw, sw, mlo, out, W, wstride, ng * bl, nb * ng * bl, bl, real, S.st);
+      }
     }
     k0 = k1;
   }
@@ -503,10 +524,19 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
     for (int q = 0; q < ngrp; ++q) {
       const Scale &sd = P.sc[k0 + q];
       const int ng = sd.ng;
+      const double c = (adj || P.axisym) ? 1.0 : 1.0 / ng;
       const char *in = (const char *)f_wav + (size_t)sd.woff * esz;
-      ring_forward(in, W, wstride, ng * bl, spec, sw, sw, mlo, nb * ng * bl, bl, real, S.st);
-      gamma_analysis(spec, Gbuf + q * gsz, sd.d_ns, nn, ng, bl, nb, real, (adj || P.axisym) ? 1.0 : 1.0 / ng,
-                     S.st);
+      double2 *Gq = Gbuf + q * gsz;
+      if (rings_on_n(P, sd)) {
+        // F_n(t, p) = c sum_g e^{-i n gamma_g} f_g(t, p), then one DFT per (n, t)
+        gamma_px_analysis(in, wstride, spec, sd.d_ns, nn, ng, bl, nb, real, c, S.st);
+        for (int i = 0; i < nn; ++i)
+          ring_forward_c(spec + (int64_t)i * bl * W, W, (int64_t)nn * bl * W, bl, Gq + (int64_t)i * bl * W, W,
+                         (int64_t)nn * bl * W, bl, W, -(bl - 1), nb * bl, bl, S.st);
+      } else {
+        ring_forward(in, W, wstride, ng * bl, spec, sw, sw, mlo, nb * ng * bl, bl, real, S.st);
+        gamma_analysis(spec, Gq, sd.d_ns, nn, ng, bl, nb, real, c, S.st);
+      }
     }
     for (int i = 0; i < nn; ++i) {
       T2L grp[2];

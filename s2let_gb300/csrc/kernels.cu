@@ -44,7 +44,10 @@ struct RingArgs {
   int rpm;              // rings per map
   const double2 *spec_in;
   double2 *spec_out;
-  int64_t spec_stride;
+  int64_t spec_stride;      // between spectra of one map
+  int64_t spec_map_stride;  // between maps (spectra of ring r at spec_base(r))
+  int spec_rpm;             // spectra per map
+  int herm;                 // complex inverse: m < 0 taken as conj of m > 0 (real-valued ring)
   int sw, mlo;
   int nrings, bl, K, P, logP;
   const double2 *chirp, *bhat, *tw;
@@ -54,6 +57,9 @@ struct RingArgs {
 // element offset of ring r (rings of a map are ring_stride apart, maps map_stride)
 __device__ __forceinline__ int64_t ring_base(const RingArgs &a, int r) {
   return (int64_t)(r / a.rpm) * a.map_stride + (int64_t)(r % a.rpm) * a.ring_stride;
+}
+__device__ __forceinline__ int64_t spec_base(const RingArgs &a, int r) {
+  return (int64_t)(r / a.spec_rpm) * a.spec_map_stride + (int64_t)(r % a.spec_rpm) * a.spec_stride;
 }
 
 // In-place transforms on the shared buffer.
@@ -118,14 +124,14 @@ __global__ void __launch_bounds__(512) k_ring_forward(RingArgs a) {
   bluestein_core(buf, a);
   const double inv = 1.0 / (double)P;
   if (!REAL) {
-    double2 *out = a.spec_out + (int64_t)r0 * a.spec_stride;
+    double2 *out = a.spec_out + spec_base(a, r0);
     for (int c = threadIdx.x; c < a.sw; c += blockDim.x) {
       const int m = a.mlo + c;
       const int k = ((m % K) + K) % K;
       out[c] = scl2(cmulc(buf[brev(k, logP)], __ldg(&a.chirp[k])), inv);
     }
   } else {
-    double2 *out0 = a.spec_out + (int64_t)r0 * a.spec_stride;
+    double2 *out0 = a.spec_out + spec_base(a, r0);
     for (int m = threadIdx.x; m < a.sw; m += blockDim.x) {
       const int km = (K - m) % K;
       const double2 zm = scl2(cmulc(buf[brev(m, logP)], __ldg(&a.chirp[m])), inv);
@@ -147,7 +153,7 @@ __global__ void __launch_bounds__(512) k_ring_inverse(RingArgs a) {
   const int K = a.K, P = a.P, logP = a.logP, bl = a.bl;
   const int r0 = REAL ? 2 * blockIdx.x : blockIdx.x;
   const bool has1 = REAL && (r0 + 1 < a.nrings);
-  const double2 *s0 = a.spec_in + (int64_t)r0 * a.spec_stride;
+  const double2 *s0 = a.spec_in + spec_base(a, r0);
   for (int j = threadIdx.x; j < P; j += blockDim.x) {
     double2 z = make_double2(0.0, 0.0);
     if (j < K) {
@@ -165,7 +171,10 @@ __global__ void __launch_bounds__(512) k_ring_inverse(RingArgs a) {
         }
       } else {
         const int c = m - a.mlo;
-        if (c >= 0 && c < a.sw) z = s0[c];
+        if (c >= 0 && c < a.sw)
+          z = s0[c];
+        else if (a.herm && m < 0 && -m - a.mlo < a.sw)
+          z = conj2(s0[-m - a.mlo]);
       }
       // inverse DFT = conj(forward(conj z)):  a_j = conj(z_j) conj(c_j)
       z = conj2(cmul(z, __ldg(&a.chirp[j])));
@@ -336,14 +345,14 @@ __global__ void __launch_bounds__(512) k_ring_forward_df(RingArgs a) {
   ifft_dif_df(bufd, a.tw_df, P, logP);
   const int eo = e - logP;  // undo the ring scaling and the 1/P of the unnormalised transforms
   if (!REAL) {
-    double2 *out = a.spec_out + (int64_t)r0 * a.spec_stride;
+    double2 *out = a.spec_out + spec_base(a, r0);
     for (int c = threadIdx.x; c < a.sw; c += blockDim.x) {
       const int m = a.mlo + c;
       const int k = ((m % K) + K) % K;
       out[c] = dc_to(dc_mulc(bufd[brev(k, logP)], __ldg(&a.chirp_df[k])), eo);
     }
   } else {
-    double2 *out0 = a.spec_out + (int64_t)r0 * a.spec_stride;
+    double2 *out0 = a.spec_out + spec_base(a, r0);
     for (int m = threadIdx.x; m < a.sw; m += blockDim.x) {
       const int km = (K - m) % K;
       const float4 zm = dc_mulc(bufd[brev(m, logP)], __ldg(&a.chirp_df[m]));
@@ -365,7 +374,7 @@ __global__ void __launch_bounds__(512) k_ring_inverse_df(RingArgs a) {
   const int K = a.K, P = a.P, logP = a.logP, bl = a.bl;
   const int r0 = REAL ? 2 * blockIdx.x : blockIdx.x;
   const bool has1 = REAL && (r0 + 1 < a.nrings);
-  const double2 *s0 = a.spec_in + (int64_t)r0 * a.spec_stride;
+  const double2 *s0 = a.spec_in + spec_base(a, r0);
   double mx = 0.0;
   for (int c = threadIdx.x; c < a.sw; c += blockDim.x) {
     const double2 A = s0[c];
@@ -398,6 +407,9 @@ __global__ void __launch_bounds__(512) k_ring_inverse_df(RingArgs a) {
         if (c >= 0 && c < a.sw) {
           z = s0[c];
           live = true;
+        } else if (a.herm && m < 0 && -m - a.mlo < a.sw) {
+          z = conj2(s0[-m - a.mlo]);
+          live = true;
         }
       }
     }
@@ -429,6 +441,8 @@ __global__ void __launch_bounds__(512) k_ring_inverse_df(RingArgs a) {
 
 RingArgs ring_args(const RingFFT &rf, int bl, int nrings) {
   RingArgs a{};
+  a.spec_rpm = 1 << 30;  // single-level spectrum addressing unless set
+  a.spec_map_stride = 0;
   a.K = rf.K;
   a.P = rf.P;
   a.logP = rf.logP;
@@ -732,6 +746,86 @@ __global__ void k_gamma_anal(const double2 *__restrict__ spec, double2 *__restri
   for (int k = 0; k < NN; ++k) G[((int64_t)b * NN + k) * bl * W + (int64_t)t * W + col] = scl2(acc[k], c);
 }
 
+// gamma DFT on pixels: between the n-components F_n(t, p) (complex, one ring
+// per (n, t)) and the gamma slices f_g(t, p) of the f_wav layout.  The phi DFT
+// commutes with it, so the ring DFTs can run on the nn n-components instead of
+// the ng = 2N-1 gamma slices.
+//   synthesis: f_g = c sum_n e^{i n gamma_g} F_n  (real signals: n > 0 stand for
+//              the +-n pair, 2 Re(e^{i n gamma_g} F_n); n = 0 adds Re F_0)
+//   analysis:  F_n = c sum_g e^{-i n gamma_g} f_g
+template <int NN>
+__global__ void k_gamma_px_synth(const double2 *__restrict__ F, void *__restrict__ out, int64_t out_ms,
+                                 const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+  __shared__ double2 tw[kMaxGammaTw];  // tw[g * NN + k] = e^{i n_k gamma_g} (x2 for n_k > 0, real)
+  for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
+    const int g = i / NN, k = i % NN;
+    double sn, cs;
+    sincospi(2.0 * (double)((ns[k] * g) % ng) / (double)ng, &sn, &cs);
+    const double f = (real && ns[k] != 0) ? 2.0 : 1.0;
+    tw[i] = make_double2(f * cs, f * sn);
+  }
+  __syncthreads();
+  const int K = 2 * bl - 1;
+  const int64_t npx = (int64_t)bl * K;
+  const int64_t total = (int64_t)nb * npx;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const int b = (int)(gid / npx);
+  const int64_t px = gid - (int64_t)b * npx;
+  double2 v[NN];
+#pragma unroll
+  for (int k = 0; k < NN; ++k) v[k] = F[((int64_t)b * NN + k) * npx + px];
+  for (int g = 0; g < ng; ++g) {
+    double re = 0.0, im = 0.0;
+#pragma unroll
+    for (int k = 0; k < NN; ++k) {
+      const double2 e = tw[g * NN + k];
+      re = fma(e.x, v[k].x, fma(-e.y, v[k].y, re));
+      if (!real) im = fma(e.x, v[k].y, fma(e.y, v[k].x, im));
+    }
+    const int64_t o = (int64_t)b * out_ms + (int64_t)g * npx + px;
+    if (real)
+      ((double *)out)[o] = re * c;
+    else
+      ((double2 *)out)[o] = make_double2(re * c, im * c);
+  }
+}
+
+template <int NN>
+__global__ void k_gamma_px_anal(const void *__restrict__ in, int64_t in_ms, double2 *__restrict__ F,
+                                const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+  __shared__ double2 tw[kMaxGammaTw];  // tw[g * NN + k] = e^{-i n_k gamma_g}
+  for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
+    const int g = i / NN, k = i % NN;
+    double sn, cs;
+    sincospi(2.0 * (double)((ns[k] * g) % ng) / (double)ng, &sn, &cs);
+    tw[i] = make_double2(cs, -sn);
+  }
+  __syncthreads();
+  const int K = 2 * bl - 1;
+  const int64_t npx = (int64_t)bl * K;
+  const int64_t total = (int64_t)nb * npx;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const int b = (int)(gid / npx);
+  const int64_t px = gid - (int64_t)b * npx;
+  double2 acc[NN];
+#pragma unroll
+  for (int k = 0; k < NN; ++k) acc[k] = make_double2(0.0, 0.0);
+  for (int g = 0; g < ng; ++g) {
+    const int64_t o = (int64_t)b * in_ms + (int64_t)g * npx + px;
+    const double2 f = real ? make_double2(((const double *)in)[o], 0.0) : ((const double2 *)in)[o];
+#pragma unroll
+    for (int k = 0; k < NN; ++k) {
+      const double2 e = tw[g * NN + k];
+      acc[k].x = fma(e.x, f.x, fma(-e.y, f.y, acc[k].x));
+      acc[k].y = fma(e.x, f.y, fma(e.y, f.x, acc[k].y));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NN; ++k) F[((int64_t)b * NN + k) * npx + px] = scl2(acc[k], c);
+}
+
 // ---------------------------------------------------------------------------
 // lmn -> lm merge
 // ---------------------------------------------------------------------------
@@ -797,6 +891,48 @@ __global__ void k_scale_copy(const double *x, double *y, int64_t n, double s) {
 // wrappers
 // ===========================================================================
 
+namespace {
+
+template <class KF>
+void launch_ring(KF kernel, const RingArgs &a, int nblk, int P, cudaStream_t st) {
+  const size_t smem = sizeof(double2) * P;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kernel<<<nblk, ring_threads(P), smem, st>>>(a);
+  S2G_LAUNCHED();
+}
+
+void run_ring_forward(const RingArgs &a, int nrings, bool real, cudaStream_t st) {
+  const int nblk = real ? (nrings + 1) / 2 : nrings;
+  KTimer kt(KC_RING, st, 0.0, (double)nrings * a.K * (real ? 8.0 : 16.0) + (double)nrings * a.sw * 16.0);
+  if (t_precision == 1) {
+    if (real)
+      launch_ring(k_ring_forward_df<true>, a, nblk, a.P, st);
+    else
+      launch_ring(k_ring_forward_df<false>, a, nblk, a.P, st);
+  } else if (real) {
+    launch_ring(k_ring_forward<true>, a, nblk, a.P, st);
+  } else {
+    launch_ring(k_ring_forward<false>, a, nblk, a.P, st);
+  }
+}
+
+void run_ring_inverse(const RingArgs &a, int nrings, bool real, cudaStream_t st) {
+  const int nblk = real ? (nrings + 1) / 2 : nrings;
+  KTimer kt(KC_RING, st, 0.0, (double)nrings * a.K * (real ? 8.0 : 16.0) + (double)nrings * a.sw * 16.0);
+  if (t_precision == 1) {
+    if (real)
+      launch_ring(k_ring_inverse_df<true>, a, nblk, a.P, st);
+    else
+      launch_ring(k_ring_inverse_df<false>, a, nblk, a.P, st);
+  } else if (real) {
+    launch_ring(k_ring_inverse<true>, a, nblk, a.P, st);
+  } else {
+    launch_ring(k_ring_inverse<false>, a, nblk, a.P, st);
+  }
+}
+
+}  // namespace
+
 void ring_forward(const void *rings, int64_t ring_stride, int64_t map_stride, int rpm, double2 *spec,
                   int64_t spec_stride, int sw, int mlo, int nrings, int bl, bool real, cudaStream_t st) {
   if (nrings <= 0) return;
@@ -810,25 +946,7 @@ void ring_forward(const void *rings, int64_t ring_stride, int64_t map_stride, in
   a.spec_stride = spec_stride;
   a.sw = sw;
   a.mlo = mlo;
-  const int nblk = real ? (nrings + 1) / 2 : nrings;
-  const size_t smem = sizeof(double2) * rf.P;
-  KTimer kt(KC_RING, st, 0.0, (double)nrings * (2 * bl - 1) * (real ? 8.0 : 16.0) + (double)nrings * sw * 16.0);
-  if (t_precision == 1) {
-    if (real) {
-      if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_forward_df<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_ring_forward_df<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
-    } else {
-      if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_forward_df<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_ring_forward_df<false><<<nblk, ring_threads(rf.P), smem, st>>>(a);
-    }
-  } else if (real) {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_ring_forward<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
-  } else {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_ring_forward<false><<<nblk, ring_threads(rf.P), smem, st>>>(a);
-  }
-  S2G_LAUNCHED();
+  run_ring_forward(a, nrings, real, st);
 }
 
 void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, void *rings,
@@ -845,25 +963,46 @@ void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, voi
   a.ring_stride = ring_stride;
   a.map_stride = map_stride;
   a.rpm = rpm;
-  const int nblk = real ? (nrings + 1) / 2 : nrings;
-  const size_t smem = sizeof(double2) * rf.P;
-  KTimer kt(KC_RING, st, 0.0, (double)nrings * (2 * bl - 1) * (real ? 8.0 : 16.0) + (double)nrings * sw * 16.0);
-  if (t_precision == 1) {
-    if (real) {
-      if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_inverse_df<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_ring_inverse_df<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
-    } else {
-      if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_inverse_df<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_ring_inverse_df<false><<<nblk, ring_threads(rf.P), smem, st>>>(a);
-    }
-  } else if (real) {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_inverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_ring_inverse<true><<<nblk, ring_threads(rf.P), smem, st>>>(a);
-  } else {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_ring_inverse<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_ring_inverse<false><<<nblk, ring_threads(rf.P), smem, st>>>(a);
-  }
-  S2G_LAUNCHED();
+  run_ring_inverse(a, nrings, real, st);
+}
+
+void ring_forward_c(const double2 *rings, int64_t ring_stride, int64_t map_stride, int rpm, double2 *spec,
+                    int64_t spec_stride, int64_t spec_map_stride, int spec_rpm, int sw, int mlo, int nrings, int bl,
+                    cudaStream_t st) {
+  if (nrings <= 0) return;
+  const RingFFT &rf = ring_fft(2 * bl - 1);
+  RingArgs a = ring_args(rf, bl, nrings);
+  a.rings = rings;
+  a.ring_stride = ring_stride;
+  a.map_stride = map_stride;
+  a.rpm = rpm;
+  a.spec_out = spec;
+  a.spec_stride = spec_stride;
+  a.spec_map_stride = spec_map_stride;
+  a.spec_rpm = spec_rpm;
+  a.sw = sw;
+  a.mlo = mlo;
+  run_ring_forward(a, nrings, false, st);
+}
+
+void ring_inverse_c(const double2 *spec, int64_t spec_stride, int64_t spec_map_stride, int spec_rpm, int sw,
+                    int mlo, bool herm, double2 *rings, int64_t ring_stride, int64_t map_stride, int rpm, int nrings,
+                    int bl, cudaStream_t st) {
+  if (nrings <= 0) return;
+  const RingFFT &rf = ring_fft(2 * bl - 1);
+  RingArgs a = ring_args(rf, bl, nrings);
+  a.spec_in = spec;
+  a.spec_stride = spec_stride;
+  a.spec_map_stride = spec_map_stride;
+  a.spec_rpm = spec_rpm;
+  a.herm = herm ? 1 : 0;
+  a.sw = sw;
+  a.mlo = mlo;
+  a.rings_out = rings;
+  a.ring_stride = ring_stride;
+  a.map_stride = map_stride;
+  a.rpm = rpm;
+  run_ring_inverse(a, nrings, false, st);
 }
 
 void contract_l2t(const L2T &p, cudaStream_t st) {
@@ -975,6 +1114,45 @@ void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int 
   }
   S2G_LAUNCHED();
 }
+
+void gamma_px_synthesis(const double2 *F, void *out, int64_t out_ms, const int *ns, int nn, int ng, int bl,
+                        int nb, bool real, double c, cudaStream_t st) {
+  S2G_REQUIRE(nn >= 1 && nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
+  const int64_t npx = (int64_t)bl * (2 * bl - 1);
+  const int64_t total = (int64_t)nb * npx;
+  if (total <= 0) return;
+  KTimer kt(KC_GAMMA, st, 0.0, (double)total * (16.0 * nn + (real ? 8.0 : 16.0) * ng));
+  const unsigned grid = (unsigned)ceil_div(total, 256);
+  switch (nn) {
+#define S2G_GPS(N) \
+  case N: k_gamma_px_synth<N><<<grid, 256, 0, st>>>(F, out, out_ms, ns, ng, bl, nb, real, c); break;
+    S2G_GPS(1) S2G_GPS(2) S2G_GPS(3) S2G_GPS(4) S2G_GPS(5) S2G_GPS(6) S2G_GPS(7) S2G_GPS(8)
+    S2G_GPS(9) S2G_GPS(10) S2G_GPS(11) S2G_GPS(12) S2G_GPS(13) S2G_GPS(14) S2G_GPS(15) S2G_GPS(16)
+#undef S2G_GPS
+    default: break;
+  }
+  S2G_LAUNCHED();
+}
+
+void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns, int nn, int ng, int bl, int nb,
+                       bool real, double c, cudaStream_t st) {
+  S2G_REQUIRE(nn >= 1 && nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
+  const int64_t npx = (int64_t)bl * (2 * bl - 1);
+  const int64_t total = (int64_t)nb * npx;
+  if (total <= 0) return;
+  KTimer kt(KC_GAMMA, st, 0.0, (double)total * (16.0 * nn + (real ? 8.0 : 16.0) * ng));
+  const unsigned grid = (unsigned)ceil_div(total, 256);
+  switch (nn) {
+#define S2G_GPA(N) \
+  case N: k_gamma_px_anal<N><<<grid, 256, 0, st>>>(in, in_ms, F, ns, ng, bl, nb, real, c); break;
+    S2G_GPA(1) S2G_GPA(2) S2G_GPA(3) S2G_GPA(4) S2G_GPA(5) S2G_GPA(6) S2G_GPA(7) S2G_GPA(8)
+    S2G_GPA(9) S2G_GPA(10) S2G_GPA(11) S2G_GPA(12) S2G_GPA(13) S2G_GPA(14) S2G_GPA(15) S2G_GPA(16)
+#undef S2G_GPA
+    default: break;
+  }
+  S2G_LAUNCHED();
+}
+
 
 void merge_lmn(double2 *flm, int L, int64_t fs, const double2 *z, int64_t zs, const MergePair *pairs,
                int npairs, const double2 *wts, const double2 *zscal, int64_t zss, int bl_scal,

@@ -29,6 +29,16 @@ void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, voi
 // (band-limit xL >= bl); when x_half, x holds m >= 0 only and
 // x(l,-m) = (-1)^m conj(x(l,m)).  w(l) = wre/wim arrays (nullable => 1) times
 // wscale, conjugated when wconj.  Rows l < lmin contribute nothing.
+// Complex rings with two-level spectrum addressing: spectrum of ring r at
+// spec + (r / spec_rpm) * spec_map_stride + (r % spec_rpm) * spec_stride.
+// herm (inverse): columns m < 0 are conj of m > 0 (a real-valued ring held as complex).
+void ring_forward_c(const double2 *rings, int64_t ring_stride, int64_t map_stride, int rpm, double2 *spec,
+                    int64_t spec_stride, int64_t spec_map_stride, int spec_rpm, int sw, int mlo, int nrings, int bl,
+                    cudaStream_t st);
+void ring_inverse_c(const double2 *spec, int64_t spec_stride, int64_t spec_map_stride, int spec_rpm, int sw,
+                    int mlo, bool herm, double2 *rings, int64_t ring_stride, int64_t map_stride, int rpm, int nrings,
+                    int bl, cudaStream_t st);
+
 struct L2T {
   const WignerTable *tb;
   int n;
@@ -85,6 +95,12 @@ void gamma_synthesis(const double2 *G, double2 *spec, const int *ns, int nn, int
 // gamma analysis: G[b][k][t][m + bl - 1] = c sum_g e^{-i n_k gamma_g} spec_g(m), all m.
 void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int ng, int bl, int nb,
                     bool real, double c, cudaStream_t st);
+// gamma DFT on pixels between F[b][k][t][p] (complex, k < nn) and the gamma slices
+// out[b * ms + g * bl * K + t * K + p] (double for real signals, else double2)
+void gamma_px_synthesis(const double2 *F, void *out, int64_t out_ms, const int *ns, int nn, int ng, int bl,
+                        int nb, bool real, double c, cudaStream_t st);
+void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns, int nn, int ng, int bl, int nb,
+                       bool real, double c, cudaStream_t st);
 
 // Merge of per-(scale, direction) Wigner coefficients into flm (lmn2lm):
 //   flm(l,m) = sum_pairs [ psi_p(l) z_p(l,m) + real&&n>0 : (-1)^{m+n} conj(z_p(l,-m)) psin_p(l) ]
