@@ -812,14 +812,25 @@ __global__ void k_gamma_px_anal(const void *__restrict__ in, int64_t in_ms, doub
   double2 acc[NN];
 #pragma unroll
   for (int k = 0; k < NN; ++k) acc[k] = make_double2(0.0, 0.0);
-  for (int g = 0; g < ng; ++g) {
-    const int64_t o = (int64_t)b * in_ms + (int64_t)g * npx + px;
-    const double2 f = real ? make_double2(((const double *)in)[o], 0.0) : ((const double2 *)in)[o];
+  if (real) {
+    for (int g = 0; g < ng; ++g) {
+      const double f = ((const double *)in)[(int64_t)b * in_ms + (int64_t)g * npx + px];
 #pragma unroll
-    for (int k = 0; k < NN; ++k) {
-      const double2 e = tw[g * NN + k];
-      acc[k].x = fma(e.x, f.x, fma(-e.y, f.y, acc[k].x));
-      acc[k].y = fma(e.x, f.y, fma(e.y, f.x, acc[k].y));
+      for (int k = 0; k < NN; ++k) {
+        const double2 e = tw[g * NN + k];
+        acc[k].x = fma(e.x, f, acc[k].x);
+        acc[k].y = fma(e.y, f, acc[k].y);
+      }
+    }
+  } else {
+    for (int g = 0; g < ng; ++g) {
+      const double2 f = ((const double2 *)in)[(int64_t)b * in_ms + (int64_t)g * npx + px];
+#pragma unroll
+      for (int k = 0; k < NN; ++k) {
+        const double2 e = tw[g * NN + k];
+        acc[k].x = fma(e.x, f.x, fma(-e.y, f.y, acc[k].x));
+        acc[k].y = fma(e.x, f.y, fma(e.y, f.x, acc[k].y));
+      }
     }
   }
 #pragma unroll
