@@ -10,6 +10,7 @@
 //  k_gamma_*   DFT over the 2N-1 gamma samples of the rotation group.
 //  k_merge     harmonic tiling merge (lmn -> lm) fused over scales/directions.
 #include "common.h"
+#include "dfconv.h"
 #include "kernels.h"
 #include "mixed.h"
 #include "timing.h"
@@ -254,13 +255,16 @@ __device__ __forceinline__ float4 dc_sub(float4 a, float4 b) {
   return dmk(df_add(dre(a), df_neg(dre(b))), df_add(dim_(a), df_neg(dim_(b))));
 }
 __device__ __forceinline__ float4 dc_conj(float4 a) { return make_float4(a.x, a.y, -a.z, -a.w); }
-__device__ __forceinline__ float2 df_from(double v) {
-  const float h = __double2float_rn(v);
-  return make_float2(h, __double2float_rn(v - (double)h));
+// FP64 <-> double-float with a power-of-two block scale, by bit construction
+// (dfconv.h): no FP64 instructions but one add per value joined
+__device__ __forceinline__ float2 df_split(double v, int e) {
+  float h, l;
+  split_scaled(v, e, h, l);
+  return make_float2(h, l);
 }
-__device__ __forceinline__ float4 dc_from(double2 v) { return dmk(df_from(v.x), df_from(v.y)); }
+__device__ __forceinline__ float4 dc_split(double2 v, int e) { return dmk(df_split(v.x, e), df_split(v.y, e)); }
 __device__ __forceinline__ double2 dc_to(float4 z, int e) {
-  return make_double2(ldexp((double)z.x + (double)z.y, e), ldexp((double)z.z + (double)z.w, e));
+  return make_double2(join_scaled(z.x, z.y, e), join_scaled(z.z, z.w, e));
 }
 
 __device__ void fft_dit_df(float4 *buf, const float4 *__restrict__ tw, int P, int logP) {
@@ -292,20 +296,20 @@ __device__ void ifft_dif_df(float4 *buf, const float4 *__restrict__ tw, int P, i
   }
 }
 
-// block-wide max of v over all threads (blockDim.x <= 1024)
-__device__ double block_max(double v) {
-  __shared__ double red[32];
+
+// block-wide max of an int (blockDim.x <= 1024)
+__device__ int block_max_int(int v) {
+  __shared__ int redi[32];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
   __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  if ((threadIdx.x & 31) == 0) redi[threadIdx.x >> 5] = v;
   __syncthreads();
-  double m = 0.0;
-  for (int i = 0; i < (int)((blockDim.x + 31) >> 5); ++i) m = fmax(m, red[i]);
+  int m = 0;
+  for (int i = 0; i < (int)((blockDim.x + 31) >> 5); ++i) m = max(m, redi[i]);
   return m;
 }
-
-__device__ __forceinline__ int pow2_exponent(double mx) { return mx > 0.0 ? ilogb(mx) + 1 : 0; }
+__device__ __forceinline__ int emax2(int m, double2 z) { return max(m, max(exp_field(z.x), exp_field(z.y))); }
 
 template <bool REAL>
 __global__ void __launch_bounds__(512) k_ring_forward_df(RingArgs a) {
@@ -313,17 +317,16 @@ __global__ void __launch_bounds__(512) k_ring_forward_df(RingArgs a) {
   const int K = a.K, P = a.P, logP = a.logP;
   const int r0 = REAL ? 2 * blockIdx.x : blockIdx.x;
   const bool has1 = REAL && (r0 + 1 < a.nrings);
-  double mx = 0.0;
+  int em = 0;
   for (int j = threadIdx.x; j < K; j += blockDim.x) {
     if (REAL) {
-      mx = fmax(mx, fabs(((const double *)a.rings)[ring_base(a, r0) + j]));
-      if (has1) mx = fmax(mx, fabs(((const double *)a.rings)[ring_base(a, r0 + 1) + j]));
+      em = max(em, exp_field(((const double *)a.rings)[ring_base(a, r0) + j]));
+      if (has1) em = max(em, exp_field(((const double *)a.rings)[ring_base(a, r0 + 1) + j]));
     } else {
-      const double2 z = ((const double2 *)a.rings)[ring_base(a, r0) + j];
-      mx = fmax(mx, fmax(fabs(z.x), fabs(z.y)));
+      em = emax2(em, ((const double2 *)a.rings)[ring_base(a, r0) + j]);
     }
   }
-  const int e = pow2_exponent(block_max(mx));
+  const int e = block_scale(block_max_int(em));
   for (int j = threadIdx.x; j < P; j += blockDim.x) {
     float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     if (j < K) {
@@ -334,7 +337,7 @@ __global__ void __launch_bounds__(512) k_ring_forward_df(RingArgs a) {
       } else {
         v = ((const double2 *)a.rings)[ring_base(a, r0) + j];
       }
-      z = dc_mulc(dc_from(make_double2(ldexp(v.x, -e), ldexp(v.y, -e))), __ldg(&a.chirp_df[j]));
+      z = dc_mulc(dc_split(v, e), __ldg(&a.chirp_df[j]));
     }
     bufd[brev(j, logP)] = z;
   }
@@ -375,50 +378,39 @@ __global__ void __launch_bounds__(512) k_ring_inverse_df(RingArgs a) {
   const int r0 = REAL ? 2 * blockIdx.x : blockIdx.x;
   const bool has1 = REAL && (r0 + 1 < a.nrings);
   const double2 *s0 = a.spec_in + spec_base(a, r0);
-  double mx = 0.0;
+  int em = 0;
   for (int c = threadIdx.x; c < a.sw; c += blockDim.x) {
-    const double2 A = s0[c];
-    mx = fmax(mx, fmax(fabs(A.x), fabs(A.y)));
-    if (has1) {
-      const double2 B = s0[a.spec_stride + c];
-      mx = fmax(mx, fmax(fabs(B.x), fabs(B.y)));
-    }
+    em = emax2(em, s0[c]);
+    if (has1) em = emax2(em, s0[a.spec_stride + c]);
   }
-  const int e = pow2_exponent(block_max(mx));
+  const int e = block_scale(block_max_int(em));
   for (int j = threadIdx.x; j < P; j += blockDim.x) {
-    double2 z = make_double2(0.0, 0.0);
-    bool live = false;
+    float4 zz = make_float4(0.f, 0.f, 0.f, 0.f);
     if (j < K) {
       const int m = (j < bl) ? j : j - K;
       if (REAL) {
         const int am = m < 0 ? -m : m;
         if (am < a.sw) {
-          double2 A = s0[am];
-          double2 B = has1 ? s0[a.spec_stride + am] : make_double2(0.0, 0.0);
+          float4 A = dc_split(s0[am], e);
+          float4 B = has1 ? dc_split(s0[a.spec_stride + am], e) : make_float4(0.f, 0.f, 0.f, 0.f);
           if (m < 0) {
-            A = conj2(A);
-            B = conj2(B);
+            A = dc_conj(A);
+            B = dc_conj(B);
           }
-          z = make_double2(A.x - B.y, A.y + B.x);  // A + i B, exact up to one rounding per part
-          live = true;
+          // A + i B
+          zz = dmk(df_add(dre(A), df_neg(dim_(B))), df_add(dim_(A), dre(B)));
         }
       } else {
         const int c = m - a.mlo;
-        if (c >= 0 && c < a.sw) {
-          z = s0[c];
-          live = true;
-        } else if (a.herm && m < 0 && -m - a.mlo < a.sw) {
-          z = conj2(s0[-m - a.mlo]);
-          live = true;
-        }
+        if (c >= 0 && c < a.sw)
+          zz = dc_split(s0[c], e);
+        else if (a.herm && m < 0 && -m - a.mlo < a.sw)
+          zz = dc_conj(dc_split(s0[-m - a.mlo], e));
       }
     }
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (j < K) {
-      // inverse DFT = conj(forward(conj z)):  a_j = conj(z_j) conj(c_j)
-      const float4 zz = live ? dc_from(make_double2(ldexp(z.x, -e), ldexp(z.y, -e))) : v;
-      v = dc_conj(dc_mul(zz, __ldg(&a.chirp_df[j])));
-    }
+    // inverse DFT = conj(forward(conj z)):  a_j = conj(z_j) conj(c_j)
+    if (j < K) v = dc_conj(dc_mul(zz, __ldg(&a.chirp_df[j])));
     bufd[brev(j, logP)] = v;
   }
   __syncthreads();

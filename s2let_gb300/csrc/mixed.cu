@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "common.h"
+#include "dfconv.h"
 #include "kernels.h"
 #include "mixed.h"
 #include "plan.h"
@@ -102,15 +103,31 @@ __device__ __forceinline__ uint16_t bf16_of_int(int d) {
   // |d| <= 64: exact in bf16 (top half of the fp32 pattern)
   return (uint16_t)(__float_as_uint((float)d) >> 16);
 }
+// round(v 2^(48-e)) for |v| < 2^e, from the significand bits (no FP64 work)
+__device__ __forceinline__ long long fixed48(double v, int e) {
+  const uint64_t u = bits_of(v);
+  const int E = (int)((u >> 52) & 0x7FF);
+  if (E == 0) return 0;
+  const long long M = (long long)((u & 0xFFFFFFFFFFFFFull) | (1ull << 52));
+  const int sh = E - 1075 + 48 - e;  // v 2^(48-e) = M 2^sh
+  long long q;
+  if (sh >= 0)
+    q = M << sh;  // |v| < 2^e keeps this below 2^48
+  else if (sh > -64)
+    q = (M + (1ll << (-sh - 1))) >> (-sh);
+  else
+    q = 0;
+  return (u >> 63) ? -q : q;
+}
+
 // digits of v 2^-e as bf16 bit patterns
 __device__ __forceinline__ void split_digits(double v, int e, uint16_t *out) {
   int d[kS];
-  int_digits(__double2ll_rn(ldexp(v, 48 - e)), d);
+  int_digits(fixed48(v, e), d);
 #pragma unroll
   for (int j = 0; j < kS; ++j) out[j] = bf16_of_int(d[j]);
 }
 
-__device__ __forceinline__ int exponent_of(double mx) { return mx > 0.0 ? ilogb(mx) + 1 : 0; }
 
 struct TableRefM {
   int mi;
@@ -148,12 +165,12 @@ __global__ void __launch_bounds__(128) k_slice_table(const double *__restrict__ 
   for (int rr = warp; rr < kPM; rr += 4) {
     const int row = rt * kPM + rr;
     const bool live = row < g.rows;
-    double mx = 0.0;
+    int mx = 0;
     if (live)
-      for (int k = lane; k < g.K; k += 32) mx = fmax(mx, fabs(Tm[(int64_t)row * g.K + k]));
+      for (int k = lane; k < g.K; k += 32) mx = max(mx, exp_field(Tm[(int64_t)row * g.K + k]));
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    int e = exponent_of(mx);
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = block_scale(mx);
     e = e < -126 ? -126 : (e > 126 ? 126 : e);
     if (lane == 0) eA[e_off[mi] + row] = (int8_t)e;
     for (int k = lane; k < kpad; k += 32) {
@@ -248,20 +265,21 @@ __global__ void __launch_bounds__(NC * 4) k_slice_x(XArgs a) {
   const int lst = g.l0 > a.lmin ? g.l0 : a.lmin;
   int kc0 = 0;
   if (!a.q) kc0 = lst >= a.bl ? g.nkc : (lst - g.l0) / kPK;
-  double mr = 0.0, mi = 0.0;
+  int mr = 0, mi = 0;  // largest exponent fields
   for (int kc = kc0; kc < g.nkc; ++kc)
 #pragma unroll 4
     for (int e = 0; e < 8; ++e) {
       const double2 v = x_value(a, m, am, g, kc * kPK + h * 8 + e, cp);
-      mr = fmax(mr, fabs(v.x));
-      mi = fmax(mi, fabs(v.y));
+      mr = max(mr, exp_field(v.x));
+      mi = max(mi, exp_field(v.y));
     }
 #pragma unroll
   for (int o = 4; o > 0; o >>= 1) {
-    mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
-    mi = fmax(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+    mr = max(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+    mi = max(mi, __shfl_xor_sync(0xffffffffu, mi, o));
   }
-  const int er = exponent_of(mr), ei = exponent_of(mi);
+  // |v| < 2^e for every value of the column (e = largest unbiased exponent + 1)
+  const int er = block_scale(mr), ei = block_scale(mi);
   if (h == 0) {
     a.eX[pm * NC + c0] = er;
     a.eX[pm * NC + c0 + 1] = ei;
@@ -273,8 +291,8 @@ __global__ void __launch_bounds__(NC * 4) k_slice_x(XArgs a) {
     for (int e = 0; e < 8; ++e) {
       const double2 v = x_value(a, m, am, g, kc * kPK + h * 8 + e, cp);
       int dr[kS], di[kS];
-      int_digits(__double2ll_rn(ldexp(v.x, 48 - er)), dr);
-      int_digits(__double2ll_rn(ldexp(v.y, 48 - ei)), di);
+      int_digits(fixed48(v.x, er), dr);
+      int_digits(fixed48(v.y, ei), di);
 #pragma unroll
       for (int j = 0; j < kS; ++j) {
         const uint32_t br = bf16_of_int(dr[j]), bi = bf16_of_int(di[j]);
@@ -444,14 +462,7 @@ __device__ __forceinline__ TileInfo tile_info(const MxArgs &a, int t) {
 // Combine the 7 class accumulators of 16 columns for this thread's row:
 // S = sum_c acc_c 2^(-7c) by Horner in double-float on the FP32 pipe (the class
 // values and 2^-7 scalings are exact floats), then one conversion to FP64 and
-// one multiplication by the power of two 2^(ea + eX - 12), built from its bits.
-__device__ __forceinline__ double pow2_signed(int k, double sign) {
-  if (k >= -1022 && k <= 1023) {
-    const unsigned long long bits = (unsigned long long)(k + 1023) << 52;
-    return __longlong_as_double((long long)(sign < 0.0 ? (bits | (1ull << 63)) : bits));
-  }
-  return ldexp(sign, k);
-}
+// the power of two 2^(ea + eX - 12) applied while widening (dfconv.h).
 __device__ __forceinline__ void combine16(uint32_t taddr, int ncols_per_class, int ea, const int *eX, double sign,
                                           double *y) {
   float acc[kS][16];
@@ -472,7 +483,11 @@ __device__ __forceinline__ void combine16(uint32_t taddr, int ncols_per_class, i
       hi = __fadd_rn(s, e);
       lo = __fsub_rn(e, __fsub_rn(hi, s));
     }
-    y[col] = ((double)hi + (double)lo) * pow2_signed(ea + eX[col] - 2 * kB0, sign);
+    if (sign < 0.0) {
+      hi = -hi;
+      lo = -lo;
+    }
+    y[col] = join_scaled(hi, lo, ea + eX[col] - 2 * kB0);
   }
 }
 
