@@ -829,6 +829,121 @@ __global__ void k_gamma_px_anal(const void *__restrict__ in, int64_t in_ms, doub
   for (int k = 0; k < NN; ++k) F[((int64_t)b * NN + k) * npx + px] = scl2(acc[k], c);
 }
 
+// The same gamma DFTs in double-float arithmetic on the FP32 pipe (split-
+// precision path): each pixel's inputs are rescaled by a power of two taken
+// from their largest exponent field, the twiddles (times the normalisation c,
+// times 2 for the real +-n pairs) are double-float constants, and each output
+// costs one FP64 add to widen.
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = __fmaf_rn(a.x, b.x, -p);
+  e = __fmaf_rn(a.x, b.y, e);
+  e = __fmaf_rn(a.y, b.x, e);
+  return df_fast(p, e);
+}
+
+template <int NN>
+__global__ void k_gamma_px_synth_df(const double2 *__restrict__ F, void *__restrict__ out, int64_t out_ms,
+                                    const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+  __shared__ float4 tw[kMaxGammaTw];  // c e^{i n_k gamma_g} (x2 for n_k > 0, real)
+  for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
+    const int g = i / NN, k = i % NN;
+    double sn, cs;
+    sincospi(2.0 * (double)((ns[k] * g) % ng) / (double)ng, &sn, &cs);
+    const double f = ((real && ns[k] != 0) ? 2.0 : 1.0) * c;
+    float2 re, im;
+    split_scaled(f * cs, 0, re.x, re.y);
+    split_scaled(f * sn, 0, im.x, im.y);
+    tw[i] = dmk(re, im);
+  }
+  __syncthreads();
+  const int K = 2 * bl - 1;
+  const int64_t npx = (int64_t)bl * K;
+  const int64_t total = (int64_t)nb * npx;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const int b = (int)(gid / npx);
+  const int64_t px = gid - (int64_t)b * npx;
+  double2 v[NN];
+  int em = 0;
+#pragma unroll
+  for (int k = 0; k < NN; ++k) {
+    v[k] = F[((int64_t)b * NN + k) * npx + px];
+    em = max(em, max(exp_field(v[k].x), exp_field(v[k].y)));
+  }
+  const int e = block_scale(em);
+  float4 z[NN];
+#pragma unroll
+  for (int k = 0; k < NN; ++k) z[k] = dc_split(v[k], e);
+  for (int g = 0; g < ng; ++g) {
+    float2 re = make_float2(0.f, 0.f), im = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < NN; ++k) {
+      const float4 w = tw[g * NN + k];
+      re = df_add(re, df_dot2(dre(w), dre(z[k]), df_neg(dim_(w)), dim_(z[k])));
+      if (!real) im = df_add(im, df_dot2(dre(w), dim_(z[k]), dim_(w), dre(z[k])));
+    }
+    const int64_t o = (int64_t)b * out_ms + (int64_t)g * npx + px;
+    if (real)
+      ((double *)out)[o] = join_scaled(re.x, re.y, e);
+    else
+      ((double2 *)out)[o] = make_double2(join_scaled(re.x, re.y, e), join_scaled(im.x, im.y, e));
+  }
+}
+
+template <int NN>
+__global__ void k_gamma_px_anal_df(const void *__restrict__ in, int64_t in_ms, double2 *__restrict__ F,
+                                   const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+  __shared__ float4 tw[kMaxGammaTw];  // c e^{-i n_k gamma_g}
+  for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
+    const int g = i / NN, k = i % NN;
+    double sn, cs;
+    sincospi(2.0 * (double)((ns[k] * g) % ng) / (double)ng, &sn, &cs);
+    float2 re, im;
+    split_scaled(c * cs, 0, re.x, re.y);
+    split_scaled(-c * sn, 0, im.x, im.y);
+    tw[i] = dmk(re, im);
+  }
+  __syncthreads();
+  const int K = 2 * bl - 1;
+  const int64_t npx = (int64_t)bl * K;
+  const int64_t total = (int64_t)nb * npx;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const int b = (int)(gid / npx);
+  const int64_t px = gid - (int64_t)b * npx;
+  float4 acc[NN];
+#pragma unroll
+  for (int k = 0; k < NN; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int64_t base = (int64_t)b * in_ms + px;
+  int em = 0;
+  for (int g = 0; g < ng; ++g) {
+    if (real) {
+      em = max(em, exp_field(((const double *)in)[base + (int64_t)g * npx]));
+    } else {
+      const double2 f = ((const double2 *)in)[base + (int64_t)g * npx];
+      em = max(em, max(exp_field(f.x), exp_field(f.y)));
+    }
+  }
+  const int e = block_scale(em);
+  for (int g = 0; g < ng; ++g) {
+    if (real) {
+      const float2 f = df_split(((const double *)in)[base + (int64_t)g * npx], e);
+#pragma unroll
+      for (int k = 0; k < NN; ++k) {
+        const float4 w = tw[g * NN + k];
+        acc[k] = dmk(df_add(dre(acc[k]), df_mul(dre(w), f)), df_add(dim_(acc[k]), df_mul(dim_(w), f)));
+      }
+    } else {
+      const float4 f = dc_split(((const double2 *)in)[base + (int64_t)g * npx], e);
+#pragma unroll
+      for (int k = 0; k < NN; ++k) acc[k] = dc_add(acc[k], dc_mul(tw[g * NN + k], f));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NN; ++k) F[((int64_t)b * NN + k) * npx + px] = dc_to(acc[k], e);
+}
+
 // ---------------------------------------------------------------------------
 // lmn -> lm merge
 // ---------------------------------------------------------------------------
@@ -1127,8 +1242,13 @@ void gamma_px_synthesis(const double2 *F, void *out, int64_t out_ms, const int *
   KTimer kt(KC_GAMMA, st, 0.0, (double)total * (16.0 * nn + (real ? 8.0 : 16.0) * ng));
   const unsigned grid = (unsigned)ceil_div(total, 256);
   switch (nn) {
-#define S2G_GPS(N) \
-  case N: k_gamma_px_synth<N><<<grid, 256, 0, st>>>(F, out, out_ms, ns, ng, bl, nb, real, c); break;
+#define S2G_GPS(N)                                                                       \
+  case N:                                                                                \
+    if (t_precision == 1)                                                                \
+      k_gamma_px_synth_df<N><<<grid, 256, 0, st>>>(F, out, out_ms, ns, ng, bl, nb, real, c); \
+    else                                                                                 \
+      k_gamma_px_synth<N><<<grid, 256, 0, st>>>(F, out, out_ms, ns, ng, bl, nb, real, c);    \
+    break;
     S2G_GPS(1) S2G_GPS(2) S2G_GPS(3) S2G_GPS(4) S2G_GPS(5) S2G_GPS(6) S2G_GPS(7) S2G_GPS(8)
     S2G_GPS(9) S2G_GPS(10) S2G_GPS(11) S2G_GPS(12) S2G_GPS(13) S2G_GPS(14) S2G_GPS(15) S2G_GPS(16)
 #undef S2G_GPS
@@ -1146,8 +1266,13 @@ void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns,
   KTimer kt(KC_GAMMA, st, 0.0, (double)total * (16.0 * nn + (real ? 8.0 : 16.0) * ng));
   const unsigned grid = (unsigned)ceil_div(total, 256);
   switch (nn) {
-#define S2G_GPA(N) \
-  case N: k_gamma_px_anal<N><<<grid, 256, 0, st>>>(in, in_ms, F, ns, ng, bl, nb, real, c); break;
+#define S2G_GPA(N)                                                                      \
+  case N:                                                                               \
+    if (t_precision == 1)                                                               \
+      k_gamma_px_anal_df<N><<<grid, 256, 0, st>>>(in, in_ms, F, ns, ng, bl, nb, real, c); \
+    else                                                                                \
+      k_gamma_px_anal<N><<<grid, 256, 0, st>>>(in, in_ms, F, ns, ng, bl, nb, real, c);    \
+    break;
     S2G_GPA(1) S2G_GPA(2) S2G_GPA(3) S2G_GPA(4) S2G_GPA(5) S2G_GPA(6) S2G_GPA(7) S2G_GPA(8)
     S2G_GPA(9) S2G_GPA(10) S2G_GPA(11) S2G_GPA(12) S2G_GPA(13) S2G_GPA(14) S2G_GPA(15) S2G_GPA(16)
 #undef S2G_GPA
