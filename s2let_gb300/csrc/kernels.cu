@@ -267,8 +267,33 @@ __device__ __forceinline__ double2 dc_to(float4 z, int e) {
   return make_double2(join_scaled(z.x, z.y, e), join_scaled(z.z, z.w, e));
 }
 
+// Stages are paired (radix 2^2): one pass over shared memory and one barrier
+// per two radix-2 stages; a leftover single stage when log2 P is odd.
+__device__ __forceinline__ float4 dc_mul_mi(float4 a) { return make_float4(a.z, a.w, -a.x, -a.y); }  // a * (-i)
+__device__ __forceinline__ float4 dc_mul_pi(float4 a) { return make_float4(-a.z, -a.w, a.x, a.y); }  // a * (+i)
+
+// bit-reversed input, natural output, forward transform (w = e^{-2 pi i k / P})
 __device__ void fft_dit_df(float4 *buf, const float4 *__restrict__ tw, int P, int logP) {
-  for (int s = 1; s <= logP; ++s) {
+  int s = 1;
+  for (; s + 1 <= logP; s += 2) {
+    const int h = 1 << (s - 1);
+    for (int i = threadIdx.x; i < P / 4; i += blockDim.x) {
+      const int jp = i & (h - 1);
+      const int p0 = ((i >> (s - 1)) << (s + 1)) + jp;
+      const float4 w1 = __ldg(&tw[jp << (logP - s)]);
+      const float4 w2 = __ldg(&tw[jp << (logP - s - 1)]);
+      const float4 a0 = buf[p0], a1 = buf[p0 + h], a2 = buf[p0 + 2 * h], a3 = buf[p0 + 3 * h];
+      const float4 t1 = dc_mul(a1, w1), t3 = dc_mul(a3, w1);
+      const float4 b0 = dc_add(a0, t1), b1 = dc_sub(a0, t1), b2 = dc_add(a2, t3), b3 = dc_sub(a2, t3);
+      const float4 u2 = dc_mul(b2, w2), u3 = dc_mul_mi(dc_mul(b3, w2));
+      buf[p0] = dc_add(b0, u2);
+      buf[p0 + 2 * h] = dc_sub(b0, u2);
+      buf[p0 + h] = dc_add(b1, u3);
+      buf[p0 + 3 * h] = dc_sub(b1, u3);
+    }
+    __syncthreads();
+  }
+  if (s == logP) {
     const int half = 1 << (s - 1);
     for (int i = threadIdx.x; i < P / 2; i += blockDim.x) {
       const int j = i & (half - 1);
@@ -281,21 +306,35 @@ __device__ void fft_dit_df(float4 *buf, const float4 *__restrict__ tw, int P, in
     __syncthreads();
   }
 }
+// natural input, bit-reversed output, unnormalised inverse transform
 __device__ void ifft_dif_df(float4 *buf, const float4 *__restrict__ tw, int P, int logP) {
-  for (int s = logP; s >= 1; --s) {
-    const int half = 1 << (s - 1);
+  int s = logP;
+  for (; s - 1 >= 1; s -= 2) {
+    const int h = 1 << (s - 2);
+    for (int i = threadIdx.x; i < P / 4; i += blockDim.x) {
+      const int jp = i & (h - 1);
+      const int p0 = ((i >> (s - 2)) << s) + jp;
+      const float4 c2 = __ldg(&tw[jp << (logP - s)]);
+      const float4 c1 = __ldg(&tw[jp << (logP - s + 1)]);
+      const float4 a0 = buf[p0], a1 = buf[p0 + h], a2 = buf[p0 + 2 * h], a3 = buf[p0 + 3 * h];
+      const float4 b0 = dc_add(a0, a2), b1 = dc_add(a1, a3);
+      const float4 b2 = dc_mulc(dc_sub(a0, a2), c2), b3 = dc_mul_pi(dc_mulc(dc_sub(a1, a3), c2));
+      buf[p0] = dc_add(b0, b1);
+      buf[p0 + h] = dc_mulc(dc_sub(b0, b1), c1);
+      buf[p0 + 2 * h] = dc_add(b2, b3);
+      buf[p0 + 3 * h] = dc_mulc(dc_sub(b2, b3), c1);
+    }
+    __syncthreads();
+  }
+  if (s == 1) {
     for (int i = threadIdx.x; i < P / 2; i += blockDim.x) {
-      const int j = i & (half - 1);
-      const int i0 = ((i >> (s - 1)) << s) + j, i1 = i0 + half;
-      const float4 w = __ldg(&tw[j << (logP - s)]);
-      const float4 u = buf[i0], v = buf[i1];
-      buf[i0] = dc_add(u, v);
-      buf[i1] = dc_mulc(dc_sub(u, v), w);
+      const float4 u = buf[2 * i], v = buf[2 * i + 1];
+      buf[2 * i] = dc_add(u, v);
+      buf[2 * i + 1] = dc_sub(u, v);
     }
     __syncthreads();
   }
 }
-
 
 // block-wide max of an int (blockDim.x <= 1024)
 __device__ int block_max_int(int v) {
@@ -312,7 +351,7 @@ __device__ int block_max_int(int v) {
 __device__ __forceinline__ int emax2(int m, double2 z) { return max(m, max(exp_field(z.x), exp_field(z.y))); }
 
 template <bool REAL>
-__global__ void __launch_bounds__(512) k_ring_forward_df(RingArgs a) {
+__global__ void __launch_bounds__(512, 3) k_ring_forward_df(RingArgs a) {
   extern __shared__ float4 bufd[];
   const int K = a.K, P = a.P, logP = a.logP;
   const int r0 = REAL ? 2 * blockIdx.x : blockIdx.x;
@@ -372,7 +411,7 @@ __global__ void __launch_bounds__(512) k_ring_forward_df(RingArgs a) {
 }
 
 template <bool REAL>
-__global__ void __launch_bounds__(512) k_ring_inverse_df(RingArgs a) {
+__global__ void __launch_bounds__(512, 3) k_ring_inverse_df(RingArgs a) {
   extern __shared__ float4 bufd[];
   const int K = a.K, P = a.P, logP = a.logP, bl = a.bl;
   const int r0 = REAL ? 2 * blockIdx.x : blockIdx.x;
