@@ -46,22 +46,31 @@ constexpr int kPK = 64;                // K per panel
 constexpr int kPM = 128;               // rows per panel
 constexpr int kPanelA = kPM * kPK;     // 8192 elements, 16 KB
 constexpr int kMaxParts = 2;           // scales sharing one table pass
-constexpr int kAST = 10, kXST = 2;     // pipeline depths
+constexpr int kXST = 2;                // coefficient pipeline depth
 constexpr int kThreads = 192;
 constexpr int kMinBl = 128;            // below this the FP64 kernel is used
 constexpr long long kWaitCycles = 4000000000LL;
-constexpr size_t kSmemA = (size_t)kAST * kPanelA * 2;
-constexpr int kNumBars = 2 * kAST + 2 * kXST + 4 + 1;
 
-// NC real coefficient columns per CTA: 16 per part (8 complex maps)
+// NC real coefficient columns per CTA (16, 32 or 64): parts x maps x {re, im}.
+// NC <= 32: two TMEM accumulators alternate between tiles; NC = 64: one
+// accumulator of 448 columns, and a shallower table ring to fit shared memory.
 template <int NC>
 struct Cfg {
-  static constexpr int kPanelX = kS * NC * kPK;       // 7168 or 14336 elements
-  static constexpr int kAccCols = kS * NC;            // TMEM columns per accumulator
+  static constexpr int kAST = NC == 64 ? 6 : 10;       // table pipeline depth
+  static constexpr int kNBuf = NC == 64 ? 1 : 2;       // TMEM accumulators
+  static constexpr int kPanelX = kS * NC * kPK;        // elements
+  static constexpr int kAccCols = kS * NC;             // TMEM columns per accumulator
   static constexpr int kTmemCols = NC == 16 ? 256 : 512;
+  static constexpr size_t kSmemA = (size_t)kAST * kPanelA * 2;
   static constexpr size_t kSmemX = (size_t)kXST * kPanelX * 2;
+  static constexpr int kNumBars = 2 * kAST + 2 * kXST + 4 + 1;
   static constexpr size_t kSmemBytes = 1024 + kSmemA + kSmemX + kNumBars * 8 + 16;
 };
+static_assert(Cfg<64>::kSmemBytes <= 232448, "shared memory");
+static_assert(Cfg<32>::kSmemBytes <= 232448, "shared memory");
+static_assert(Cfg<64>::kNBuf * Cfg<64>::kAccCols <= Cfg<64>::kTmemCols, "TMEM");
+static_assert(Cfg<32>::kNBuf * Cfg<32>::kAccCols <= Cfg<32>::kTmemCols, "TMEM");
+static_assert(Cfg<16>::kNBuf * Cfg<16>::kAccCols <= Cfg<16>::kTmemCols, "TMEM");
 
 struct Geom {
   int l0, nl, rows, K, nkc, nrt;
@@ -209,7 +218,7 @@ struct XArgs {
   int bl, an, mlo, lmin;  // lmin: smallest lmin over the parts
   int nparts;
   Part part[kMaxParts];
-  int nb, b0;
+  int nb, b0, mpp;  // maps per part in this launch: column pair cp -> part cp / mpp, map b0 + cp % mpp
   const int64_t *xoff;
   uint16_t *xpan;
   int *eX;
@@ -221,10 +230,10 @@ __device__ __forceinline__ double2 weight_of(const double2 *w, double wscale, in
   return make_double2(v.x * wscale, v.y * wscale);
 }
 
-// Complex coefficient of column pair cp (part cp / 8, map b0 + cp % 8) at K index k.
+// Complex coefficient of column pair cp (part cp / mpp, map b0 + cp % mpp) at K index k.
 __device__ __forceinline__ double2 x_value(const XArgs &a, int m, int am, const Geom &g, int k, int cp) {
-  const int pi = cp >> 3;
-  const int b = a.b0 + (cp & 7);
+  const int pi = cp / a.mpp;
+  const int b = a.b0 + cp % a.mpp;
   const double2 zero = make_double2(0.0, 0.0);
   if (pi >= a.nparts || b >= a.nb) return zero;
   const Part &P = a.part[pi];
@@ -403,17 +412,7 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
+
 
 // ---------------------------------------------------------------------------
 // the contraction
@@ -433,7 +432,7 @@ struct MxArgs {
   int ntiles;
   int nparts;
   Part part[kMaxParts];
-  int nb, b0;
+  int nb, b0, mpp;
   int *err;
 };
 
@@ -461,8 +460,19 @@ __device__ __forceinline__ TileInfo tile_info(const MxArgs &a, int t) {
 
 // Combine the 7 class accumulators of 16 columns for this thread's row:
 // S = sum_c acc_c 2^(-7c) by Horner in double-float on the FP32 pipe (the class
-// values and 2^-7 scalings are exact floats), then one conversion to FP64 and
+// values and 2^-7 scalings are exact floats), then one widening to FP64 with
 // the power of two 2^(ea + eX - 12) applied while widening (dfconv.h).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
 __device__ __forceinline__ void combine16(uint32_t taddr, int ncols_per_class, int ea, const int *eX, double sign,
                                           double *y) {
   float acc[kS][16];
@@ -496,11 +506,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
   constexpr int PX = Cfg<NC>::kPanelX;
   constexpr int ACC = Cfg<NC>::kAccCols;
   constexpr int TMC = Cfg<NC>::kTmemCols;
+  constexpr int kAST = Cfg<NC>::kAST;
+  constexpr int NBUF = Cfg<NC>::kNBuf;
+  constexpr int kNumBars = Cfg<NC>::kNumBars;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint16_t *sA = (uint16_t *)smem;
-  uint16_t *sX = (uint16_t *)(smem + kSmemA);
-  uint64_t *bars = (uint64_t *)(smem + kSmemA + Cfg<NC>::kSmemX);
+  uint16_t *sX = (uint16_t *)(smem + Cfg<NC>::kSmemA);
+  uint64_t *bars = (uint64_t *)(smem + Cfg<NC>::kSmemA + Cfg<NC>::kSmemX);
   uint64_t *fullA = bars, *emptyA = bars + kAST, *fullX = bars + 2 * kAST, *emptyX = bars + 2 * kAST + kXST;
   uint64_t *tfull = bars + 2 * kAST + 2 * kXST, *tempty = tfull + 2, *mma_done = tfull + 4;
   volatile int *abort_flag = (volatile int *)(bars + kNumBars);
@@ -567,8 +580,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
     bool ok = true, any = false;
     for (int t = blockIdx.x; ok && t < a.ntiles; t += gridDim.x, ++ti_n) {
       const TileInfo ti = tile_info(a, t);
-      const int ab = ti_n & 1;
-      if (!(ok = bar_wait(&tempty[ab], ((ti_n >> 1) & 1) ^ 1, abort_flag, a.err))) break;
+      const int ab = ti_n % NBUF;
+      if (!(ok = bar_wait(&tempty[ab], ((ti_n / NBUF) & 1) ^ 1, abort_flag, a.err))) break;
       tc_fence_after();
       const uint32_t d0 = tmem + (uint32_t)(ab * ACC);
       if (ti.kc0 >= ti.nkc) {
@@ -585,12 +598,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
           if (!(ok = bar_wait(&fullA[as], (ca / kAST) & 1, abort_flag, a.err))) break;
           tc_fence_after();
           const uint64_t adesc = sw128_desc(sA + (size_t)as * kPanelA);
-          const uint32_t idesc = idesc_bf16(kPM, NC * (kS - j));
+          // B rows [0, NC (7 - j)) -> accumulator columns NC j + row, in MMAs of N <= 256
+          const int ntot = NC * (kS - j);
+          for (int off = 0; off < ntot; off += 256) {
+            const int n = ntot - off < 256 ? ntot - off : 256;
+            const uint32_t idesc = idesc_bf16(kPM, n);
+            // 8-row atoms of 128 B: a row offset of `off` moves the start by off * 128 B
+            const uint64_t bd = bdesc + (uint64_t)(off * 8);
 #pragma unroll
-          for (int k = 0; k < kPK / 16; ++k) {
-            // K advance of 16 bf16 = 32 bytes inside the swizzle atom
-            mma_bf16(d0 + (uint32_t)(NC * j), adesc + (uint64_t)(2 * k), bdesc + (uint64_t)(2 * k), idesc,
-                     (kc == ti.kc0 && j == 0 && k == 0) ? 0u : 1u);
+            for (int k = 0; k < kPK / 16; ++k) {
+              // K advance of 16 bf16 = 32 bytes inside the swizzle atom
+              mma_bf16(d0 + (uint32_t)(NC * j + off), adesc + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc,
+                       (kc == ti.kc0 && j == 0 && k == 0) ? 0u : 1u);
+            }
           }
           any = true;
           mma_commit(&emptyA[as]);
@@ -616,13 +636,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
     int ti_n = 0;
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++ti_n) {
       const TileInfo ti = tile_info(a, t);
-      const int ab = ti_n & 1;
+      const int ab = ti_n % NBUF;
       // warp-uniform outcome: tcgen05.ld below is .sync.aligned
-      if (!__all_sync(0xffffffffu, bar_wait(&tfull[ab], (ti_n >> 1) & 1, abort_flag, a.err))) break;
+      if (!__all_sync(0xffffffffu, bar_wait(&tfull[ab], (ti_n / NBUF) & 1, abort_flag, a.err))) break;
       tc_fence_after();
       const bool live = ti.kc0 < ti.nkc;
       const int ea = live ? (int)a.eA[a.e_off[ti.mi] + ti.rt * kPM + rr] : 0;
       const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * ACC);
+      const int t_row = ti.rt * kPM + rr;
+      const int l = ti.l0 + ti.rt * kPM + rr;
       for (int pi = 0; pi < NC / 16; ++pi) {
         double y[16];
         if (live) {
@@ -635,32 +657,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
           tc_fence_before();
           bar_arrive(&tempty[ab]);
         }
-        if (pi >= a.nparts) continue;
-        const Part &P = a.part[pi];
-        if (!a.q) {
-          const int t_row = ti.rt * kPM + rr;
-          if (t_row < a.bl) {
+        // column pair cp = 8 pi + bb: part cp / mpp, map b0 + cp % mpp
 #pragma unroll
-            for (int bb = 0; bb < 8; ++bb) {
-              const int b = a.b0 + bb;
-              if (b < a.nb)
-                P.dst[(int64_t)b * P.ds + (int64_t)t_row * P.dw + (ti.m - P.d_mlo)] =
-                    make_double2(y[2 * bb], y[2 * bb + 1]);
-            }
-          }
-        } else {
-          const int l = ti.l0 + ti.rt * kPM + rr;
-          const int lst = ti.l0 > P.lmin ? ti.l0 : P.lmin;
-          if (l >= lst && l < a.bl) {
-            const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
-#pragma unroll
-            for (int bb = 0; bb < 8; ++bb) {
-              const int b = a.b0 + bb;
-              if (b < a.nb) {
-                const double yr = y[2 * bb], yi = y[2 * bb + 1];
-                P.dst[(int64_t)b * P.ds + (int64_t)l * l + l + ti.m] =
-                    make_double2(yr * wt.x - yi * wt.y, yr * wt.y + yi * wt.x);
-              }
+        for (int bb = 0; bb < 8; ++bb) {
+          const int cp = pi * 8 + bb;
+          const int part = cp / a.mpp;
+          const int b = a.b0 + cp % a.mpp;
+          if (part >= a.nparts || b >= a.nb) continue;
+          const Part &P = a.part[part];
+          if (!a.q) {
+            if (t_row < a.bl)
+              P.dst[(int64_t)b * P.ds + (int64_t)t_row * P.dw + (ti.m - P.d_mlo)] =
+                  make_double2(y[2 * bb], y[2 * bb + 1]);
+          } else {
+            const int lst = ti.l0 > P.lmin ? ti.l0 : P.lmin;
+            if (l >= lst && l < a.bl) {
+              const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
+              const double yr = y[2 * bb], yi = y[2 * bb + 1];
+              P.dst[(int64_t)b * P.ds + (int64_t)l * l + l + ti.m] =
+                  make_double2(yr * wt.x - yi * wt.y, yr * wt.y + yi * wt.x);
             }
           }
         }
@@ -848,7 +863,8 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     err = error_flag();
   }
   const int nmp = p.mhi - p.mlo + 1;
-  const int ngroups = (p.nb + 7) / 8;
+  const int mpp = NC / (2 * p.nparts);  // maps per part per launch
+  const int ngroups = (p.nb + mpp - 1) / mpp;
   // coefficient panels: the tile list's offsets count 16-column panels; an
   // NC-column panel is NC/16 times larger, so offsets scale by NC/16
   const int64_t x_elems = L->x_elems * (NC / 16);
@@ -859,8 +875,8 @@ void run_mixed(const Problem &p, cudaStream_t st) {
   S2G_CUDA(cudaMallocAsync((void **)&eX, sizeof(int) * (size_t)nmp * NC, st));
   const double entries = (double)L->work_entries;
   for (int g = 0; g < ngroups; ++g) {
-    const int b0 = g * 8;
-    const int nbg = p.nb - b0 < 8 ? p.nb - b0 : 8;
+    const int b0 = g * mpp;
+    const int nbg = p.nb - b0 < mpp ? p.nb - b0 : mpp;
     double fl = 0, by = 0;
     if (timing_enabled()) {
       fl = 4.0 * entries * nbg * p.nparts;
@@ -877,6 +893,7 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     for (int i = 0; i < p.nparts; ++i) xa.part[i] = p.part[i];
     xa.nb = p.nb;
     xa.b0 = b0;
+    xa.mpp = mpp;
     xa.xoff = xoff;
     xa.xpan = xpan;
     xa.eX = eX;
@@ -904,6 +921,7 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     for (int i = 0; i < p.nparts; ++i) ma.part[i] = p.part[i];
     ma.nb = p.nb;
     ma.b0 = b0;
+    ma.mpp = mpp;
     ma.err = err;
     const int grid = L->ntiles < num_sms() ? L->ntiles : num_sms();
     k_contract_mx<NC><<<grid, kThreads, Cfg<NC>::kSmemBytes, st>>>(ma);
@@ -913,11 +931,16 @@ void run_mixed(const Problem &p, cudaStream_t st) {
   cudaFreeAsync(eX, st);
 }
 
+// columns per table pass: 2 (re, im) x maps x parts, in the smallest of 16 /
+// 32 / 64 that holds the whole batch (larger batches loop over map groups)
 void run_problem(const Problem &p, cudaStream_t st) {
-  if (p.nparts == 1)
+  const int cols = 2 * p.nb * p.nparts;
+  if (cols <= 16)
     run_mixed<16>(p, st);
-  else
+  else if (cols <= 32)
     run_mixed<32>(p, st);
+  else
+    run_mixed<64>(p, st);
 }
 
 Part part_of(const L2T &a) {

@@ -68,3 +68,25 @@ def test_mixed_sht(gpu):
     assert rel_err(f, f0) < TOL_MIXED
     a, a0 = _both(gpu, lambda: gpu.map2alm(f0, L, 0))
     assert rel_err(a, a0) < TOL_MIXED
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,N,nb", [(256, 4, 12), (160, 3, 20)])
+def test_mixed_large_batches(gpu, L, N, nb):
+    """Batches that need 48-64 coefficient columns per table pass (one 448-column
+    TMEM accumulator, MMAs split at N = 256) against the FP64 path."""
+    torch = pytest.importorskip("torch")
+    from s2let_gb300 import torch_ops as T
+
+    p = make_parameters(L, 2.0, 2, N, 0, 0)
+    s = T.sizes(p)
+    g = torch.Generator().manual_seed(nb)
+    f = (torch.rand((nb, s["n_px"]), generator=g, dtype=torch.float64) * 2 - 1).cuda()
+    w0, s0 = T.px2wav(f, p, precision="fp64")
+    w1, s1 = T.px2wav(f, p, precision="mixed")
+    assert gpu.lib.s2let_gpu_device_fault() == 0
+    rel = lambda a, b: float((a - b).abs().max() / b.abs().max())
+    assert rel(w1, w0) < TOL_MIXED and rel(s1, s0) < TOL_MIXED
+    r0 = T.wav2px(w0, s0, p, precision="fp64")
+    r1 = T.wav2px(w0, s0, p, precision="mixed")
+    assert rel(r1, r0) < TOL_MIXED
