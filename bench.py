@@ -45,7 +45,7 @@ def args_():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=8, help="maps per step per GPU")
+    ap.add_argument("--batch", type=int, default=16, help="maps per step per GPU")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="mixed: split-precision tensor-core contraction (headline; the FP64 path is timed "
                          "beside it on the same inputs); fp64: the FP64 path alone")

@@ -47,7 +47,8 @@ constexpr int kPM = 128;               // rows per panel
 constexpr int kPanelA = kPM * kPK;     // 8192 elements, 16 KB
 constexpr int kMaxParts = 2;           // scales sharing one table pass
 constexpr int kXST = 2;                // coefficient pipeline depth
-constexpr int kThreads = 192;
+constexpr int kEpiWarps = 8;           // two warps per TMEM lane quarter, alternating 16-column chunks
+constexpr int kThreads = 64 + 32 * kEpiWarps;
 constexpr int kMinBl = 128;            // below this the FP64 kernel is used
 constexpr long long kWaitCycles = 4000000000LL;
 
@@ -532,7 +533,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
     }
     for (int i = 0; i < 2; ++i) {
       bar_init(&tfull[i], 1);
-      bar_init(&tempty[i], 128);
+      bar_init(&tempty[i], 32 * kEpiWarps);
     }
     bar_init(mma_done, 1);
     *abort_flag = 0;
@@ -632,6 +633,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
   } else if (warp >= 2) {
     // ---------------- epilogue ----------------
     const int quarter = warp & 3;
+    const int half = (warp - 2) / 4;  // which alternate 16-column chunks this warp combines
     const int rr = quarter * 32 + lane;
     int ti_n = 0;
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++ti_n) {
@@ -645,7 +647,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
       const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * ACC);
       const int t_row = ti.rt * kPM + rr;
       const int l = ti.l0 + ti.rt * kPM + rr;
-      for (int pi = 0; pi < NC / 16; ++pi) {
+      // chunks pi = half, half + 2, ...; a warp with no chunk left still arrives
+      const int last = ((NC / 16 - 1 - half) / 2) * 2 + half;
+      if (half >= NC / 16) {
+        tc_fence_before();
+        bar_arrive(&tempty[ab]);
+      }
+      for (int pi = half; pi < NC / 16; pi += 2) {
         double y[16];
         if (live) {
           combine16(taddr + (uint32_t)(pi * 16), NC, ea, a.eX + ti.pm * NC + pi * 16, ti.sign, y);
@@ -653,7 +661,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
 #pragma unroll
           for (int col = 0; col < 16; ++col) y[col] = 0.0;
         }
-        if (pi == NC / 16 - 1) {  // all columns read: hand the accumulator back
+        if (pi == last) {  // this warp's columns read: hand the accumulator back
           tc_fence_before();
           bar_arrive(&tempty[ab]);
         }
