@@ -341,6 +341,17 @@ def main():
         t64 = kd["flops"] / (kd["ms"] * 1e-3) / 1e12
         roof["fp64"] = {"achieved_tflops": t64, "nominal_peak_tflops": NOMINAL_FP64_TFLOPS,
                         "frac_of_nominal": t64 / NOMINAL_FP64_TFLOPS}
+    if dom == "ring_dft" and kd["ms"]:
+        # double-float ring DFTs: bound by the FP32 pipe, not HBM.  Work = model
+        # count of FP32 instructions (s2let_gb300/csrc/kernels.cu ring_work);
+        # peak = SMs x 128 FP32 lanes x the SM clock sampled during the run.
+        props = torch.cuda.get_device_properties(dev)
+        mhz = (clk or {}).get("sm_mhz") or 2070.0
+        peak_ti = props.multi_processor_count * 128 * mhz * 1e6 / 1e12
+        if a.precision == "mixed":
+            ti = kd["flops"] / (kd["ms"] * 1e-3) / 1e12
+            roof["fp32_pipe"] = {"achieved_tinst_per_s": ti, "peak_tinst_per_s": peak_ti, "frac": ti / peak_ti,
+                                 "work": "double-float FP32 instructions (model)"}
     km = kernels["tensor_contraction"]
     if km["launches"] and km["ms"]:
         g = km["bytes"] / (km["ms"] * 1e-3) / 1e9

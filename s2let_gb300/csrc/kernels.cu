@@ -269,6 +269,9 @@ __device__ __forceinline__ double2 dc_to(float4 z, int e) {
 
 // Stages are paired (radix 2^2): one pass over shared memory and one barrier
 // per two radix-2 stages; a leftover single stage when log2 P is odd.
+// Shared-memory index i is stored at i + i/8 (one float4 of padding per 8),
+// which spreads the small-span strided accesses of the early stages over the banks.
+__device__ __forceinline__ int pd(int i) { return i + (i >> 3); }
 __device__ __forceinline__ float4 dc_mul_mi(float4 a) { return make_float4(a.z, a.w, -a.x, -a.y); }  // a * (-i)
 __device__ __forceinline__ float4 dc_mul_pi(float4 a) { return make_float4(-a.z, -a.w, a.x, a.y); }  // a * (+i)
 
@@ -282,14 +285,14 @@ __device__ void fft_dit_df(float4 *buf, const float4 *__restrict__ tw, int P, in
       const int p0 = ((i >> (s - 1)) << (s + 1)) + jp;
       const float4 w1 = __ldg(&tw[jp << (logP - s)]);
       const float4 w2 = __ldg(&tw[jp << (logP - s - 1)]);
-      const float4 a0 = buf[p0], a1 = buf[p0 + h], a2 = buf[p0 + 2 * h], a3 = buf[p0 + 3 * h];
+      const float4 a0 = buf[pd(p0)], a1 = buf[pd(p0 + h)], a2 = buf[pd(p0 + 2 * h)], a3 = buf[pd(p0 + 3 * h)];
       const float4 t1 = dc_mul(a1, w1), t3 = dc_mul(a3, w1);
       const float4 b0 = dc_add(a0, t1), b1 = dc_sub(a0, t1), b2 = dc_add(a2, t3), b3 = dc_sub(a2, t3);
       const float4 u2 = dc_mul(b2, w2), u3 = dc_mul_mi(dc_mul(b3, w2));
-      buf[p0] = dc_add(b0, u2);
-      buf[p0 + 2 * h] = dc_sub(b0, u2);
-      buf[p0 + h] = dc_add(b1, u3);
-      buf[p0 + 3 * h] = dc_sub(b1, u3);
+      buf[pd(p0)] = dc_add(b0, u2);
+      buf[pd(p0 + 2 * h)] = dc_sub(b0, u2);
+      buf[pd(p0 + h)] = dc_add(b1, u3);
+      buf[pd(p0 + 3 * h)] = dc_sub(b1, u3);
     }
     __syncthreads();
   }
@@ -299,9 +302,9 @@ __device__ void fft_dit_df(float4 *buf, const float4 *__restrict__ tw, int P, in
       const int j = i & (half - 1);
       const int i0 = ((i >> (s - 1)) << s) + j, i1 = i0 + half;
       const float4 w = __ldg(&tw[j << (logP - s)]);
-      const float4 u = buf[i0], v = dc_mul(buf[i1], w);
-      buf[i0] = dc_add(u, v);
-      buf[i1] = dc_sub(u, v);
+      const float4 u = buf[pd(i0)], v = dc_mul(buf[pd(i1)], w);
+      buf[pd(i0)] = dc_add(u, v);
+      buf[pd(i1)] = dc_sub(u, v);
     }
     __syncthreads();
   }
@@ -316,21 +319,21 @@ __device__ void ifft_dif_df(float4 *buf, const float4 *__restrict__ tw, int P, i
       const int p0 = ((i >> (s - 2)) << s) + jp;
       const float4 c2 = __ldg(&tw[jp << (logP - s)]);
       const float4 c1 = __ldg(&tw[jp << (logP - s + 1)]);
-      const float4 a0 = buf[p0], a1 = buf[p0 + h], a2 = buf[p0 + 2 * h], a3 = buf[p0 + 3 * h];
+      const float4 a0 = buf[pd(p0)], a1 = buf[pd(p0 + h)], a2 = buf[pd(p0 + 2 * h)], a3 = buf[pd(p0 + 3 * h)];
       const float4 b0 = dc_add(a0, a2), b1 = dc_add(a1, a3);
       const float4 b2 = dc_mulc(dc_sub(a0, a2), c2), b3 = dc_mul_pi(dc_mulc(dc_sub(a1, a3), c2));
-      buf[p0] = dc_add(b0, b1);
-      buf[p0 + h] = dc_mulc(dc_sub(b0, b1), c1);
-      buf[p0 + 2 * h] = dc_add(b2, b3);
-      buf[p0 + 3 * h] = dc_mulc(dc_sub(b2, b3), c1);
+      buf[pd(p0)] = dc_add(b0, b1);
+      buf[pd(p0 + h)] = dc_mulc(dc_sub(b0, b1), c1);
+      buf[pd(p0 + 2 * h)] = dc_add(b2, b3);
+      buf[pd(p0 + 3 * h)] = dc_mulc(dc_sub(b2, b3), c1);
     }
     __syncthreads();
   }
   if (s == 1) {
     for (int i = threadIdx.x; i < P / 2; i += blockDim.x) {
-      const float4 u = buf[2 * i], v = buf[2 * i + 1];
-      buf[2 * i] = dc_add(u, v);
-      buf[2 * i + 1] = dc_sub(u, v);
+      const float4 u = buf[pd(2 * i)], v = buf[pd(2 * i + 1)];
+      buf[pd(2 * i)] = dc_add(u, v);
+      buf[pd(2 * i + 1)] = dc_sub(u, v);
     }
     __syncthreads();
   }
@@ -378,11 +381,11 @@ __global__ void __launch_bounds__(512, 3) k_ring_forward_df(RingArgs a) {
       }
       z = dc_mulc(dc_split(v, e), __ldg(&a.chirp_df[j]));
     }
-    bufd[brev(j, logP)] = z;
+    bufd[pd(brev(j, logP))] = z;
   }
   __syncthreads();
   fft_dit_df(bufd, a.tw_df, P, logP);
-  for (int k = threadIdx.x; k < P; k += blockDim.x) bufd[k] = dc_mul(bufd[k], __ldg(&a.bhat_df[k]));
+  for (int k = threadIdx.x; k < P; k += blockDim.x) bufd[pd(k)] = dc_mul(bufd[pd(k)], __ldg(&a.bhat_df[k]));
   __syncthreads();
   ifft_dif_df(bufd, a.tw_df, P, logP);
   const int eo = e - logP;  // undo the ring scaling and the 1/P of the unnormalised transforms
@@ -391,14 +394,14 @@ __global__ void __launch_bounds__(512, 3) k_ring_forward_df(RingArgs a) {
     for (int c = threadIdx.x; c < a.sw; c += blockDim.x) {
       const int m = a.mlo + c;
       const int k = ((m % K) + K) % K;
-      out[c] = dc_to(dc_mulc(bufd[brev(k, logP)], __ldg(&a.chirp_df[k])), eo);
+      out[c] = dc_to(dc_mulc(bufd[pd(brev(k, logP))], __ldg(&a.chirp_df[k])), eo);
     }
   } else {
     double2 *out0 = a.spec_out + spec_base(a, r0);
     for (int m = threadIdx.x; m < a.sw; m += blockDim.x) {
       const int km = (K - m) % K;
-      const float4 zm = dc_mulc(bufd[brev(m, logP)], __ldg(&a.chirp_df[m]));
-      const float4 zc = dc_conj(dc_mulc(bufd[brev(km, logP)], __ldg(&a.chirp_df[km])));
+      const float4 zm = dc_mulc(bufd[pd(brev(m, logP))], __ldg(&a.chirp_df[m]));
+      const float4 zc = dc_conj(dc_mulc(bufd[pd(brev(km, logP))], __ldg(&a.chirp_df[km])));
       // A = (Z_m + conj Z_{-m})/2,  B = (Z_m - conj Z_{-m})/(2i)
       const double2 s = dc_to(dc_add(zm, zc), eo - 1);
       out0[m] = s;
@@ -450,17 +453,17 @@ __global__ void __launch_bounds__(512, 3) k_ring_inverse_df(RingArgs a) {
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
     // inverse DFT = conj(forward(conj z)):  a_j = conj(z_j) conj(c_j)
     if (j < K) v = dc_conj(dc_mul(zz, __ldg(&a.chirp_df[j])));
-    bufd[brev(j, logP)] = v;
+    bufd[pd(brev(j, logP))] = v;
   }
   __syncthreads();
   fft_dit_df(bufd, a.tw_df, P, logP);
-  for (int k = threadIdx.x; k < P; k += blockDim.x) bufd[k] = dc_mul(bufd[k], __ldg(&a.bhat_df[k]));
+  for (int k = threadIdx.x; k < P; k += blockDim.x) bufd[pd(k)] = dc_mul(bufd[pd(k)], __ldg(&a.bhat_df[k]));
   __syncthreads();
   ifft_dif_df(bufd, a.tw_df, P, logP);
   const int eo = e - logP;
   for (int p = threadIdx.x; p < K; p += blockDim.x) {
     // f_p = c_p conj(y_p)
-    const double2 f = dc_to(dc_mul(__ldg(&a.chirp_df[p]), dc_conj(bufd[brev(p, logP)])), eo);
+    const double2 f = dc_to(dc_mul(__ldg(&a.chirp_df[p]), dc_conj(bufd[pd(brev(p, logP))])), eo);
     if (REAL) {
       ((double *)a.rings_out)[ring_base(a, r0) + p] = f.x;
       if (has1) ((double *)a.rings_out)[ring_base(a, r0 + 1) + p] = f.y;
@@ -1051,21 +1054,32 @@ __global__ void k_scale_copy(const double *x, double *y, int64_t n, double s) {
 namespace {
 
 template <class KF>
-void launch_ring(KF kernel, const RingArgs &a, int nblk, int P, cudaStream_t st) {
-  const size_t smem = sizeof(double2) * P;
+void launch_ring(KF kernel, const RingArgs &a, int nblk, int P, cudaStream_t st, bool padded = false) {
+  const size_t smem = sizeof(double2) * (padded ? P + P / 8 : P);
   if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   kernel<<<nblk, ring_threads(P), smem, st>>>(a);
   S2G_LAUNCHED();
 }
 
+// Work model of one Bluestein transform of padded length P (for the timing
+// report): the split path counts double-float FP32 instructions (41 per
+// element per radix-2 stage and FFT, a complex multiply of 38 for the kernel
+// spectrum and each chirp); the FP64 path counts 5 P log2 P flop per FFT.
+double ring_work(const RingArgs &a, int nblk) {
+  const double P = a.P, lg = a.logP;
+  if (t_precision == 1) return (double)nblk * P * (82.0 * lg + 38.0 + 76.0 * a.K / P);
+  return (double)nblk * (10.0 * P * lg + 6.0 * P + 12.0 * a.K);
+}
+
 void run_ring_forward(const RingArgs &a, int nrings, bool real, cudaStream_t st) {
   const int nblk = real ? (nrings + 1) / 2 : nrings;
-  KTimer kt(KC_RING, st, 0.0, (double)nrings * a.K * (real ? 8.0 : 16.0) + (double)nrings * a.sw * 16.0);
+  KTimer kt(KC_RING, st, timing_enabled() ? ring_work(a, nblk) : 0.0,
+            (double)nrings * a.K * (real ? 8.0 : 16.0) + (double)nrings * a.sw * 16.0);
   if (t_precision == 1) {
     if (real)
-      launch_ring(k_ring_forward_df<true>, a, nblk, a.P, st);
+      launch_ring(k_ring_forward_df<true>, a, nblk, a.P, st, true);
     else
-      launch_ring(k_ring_forward_df<false>, a, nblk, a.P, st);
+      launch_ring(k_ring_forward_df<false>, a, nblk, a.P, st, true);
   } else if (real) {
     launch_ring(k_ring_forward<true>, a, nblk, a.P, st);
   } else {
@@ -1075,12 +1089,13 @@ void run_ring_forward(const RingArgs &a, int nrings, bool real, cudaStream_t st)
 
 void run_ring_inverse(const RingArgs &a, int nrings, bool real, cudaStream_t st) {
   const int nblk = real ? (nrings + 1) / 2 : nrings;
-  KTimer kt(KC_RING, st, 0.0, (double)nrings * a.K * (real ? 8.0 : 16.0) + (double)nrings * a.sw * 16.0);
+  KTimer kt(KC_RING, st, timing_enabled() ? ring_work(a, nblk) : 0.0,
+            (double)nrings * a.K * (real ? 8.0 : 16.0) + (double)nrings * a.sw * 16.0);
   if (t_precision == 1) {
     if (real)
-      launch_ring(k_ring_inverse_df<true>, a, nblk, a.P, st);
+      launch_ring(k_ring_inverse_df<true>, a, nblk, a.P, st, true);
     else
-      launch_ring(k_ring_inverse_df<false>, a, nblk, a.P, st);
+      launch_ring(k_ring_inverse_df<false>, a, nblk, a.P, st, true);
   } else if (real) {
     launch_ring(k_ring_inverse<true>, a, nblk, a.P, st);
   } else {
