@@ -39,6 +39,28 @@ METRIC = "px2wav+wav2px maps/s at L=1024,N=4: mixed vs FP64 GPU at stated max er
 NOMINAL_FP64_TFLOPS = 1.25  # GB300 FP64 (vendor nominal; no measured FP64 peak is available)
 
 
+def max_over_ranks(x, dist=None, device="cpu"):
+    """Largest x over all ranks of the process group (x itself without one):
+    the time of a replica step is the slowest replica's."""
+    if not dist:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(rank):
+    """Each rank synthesises its own maps (weak scaling: distinct inputs per replica)."""
+    return 1000 + rank
+
+
+def whole_job_rate(units_per_rank, world, seconds):
+    """Units per second over all ranks, from the slowest rank's time."""
+    return world * units_per_rank / seconds
+
+
 def args_():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -230,7 +252,7 @@ def main():
     npx, nw, ns = sz["n_px"], sz["n_wav"], sz["n_scal"]
 
     # seeded band-limited inputs, synthesised on the GPU from power-law flm
-    rng = np.random.default_rng(1000 + rank)
+    rng = np.random.default_rng(replica_seed(rank))
     f_host = np.stack([api.alm2map(power_law_real_flm(rng, a.L), a.L, real=True) for _ in range(nb)])
     s2let_gb300.check(lib, "alm2map_real")
     f = torch.tensor(f_host, device=dev)
@@ -270,12 +292,7 @@ def main():
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-        ms = e0.elapsed_time(e1) / nsteps
-        if dist:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(e0.elapsed_time(e1) / nsteps, dist, dev)
 
     # ---- timed region (device-resident inputs) ----
     clocks = ClockSampler(local)
@@ -284,7 +301,7 @@ def main():
     ms_max = timed(a.steps)
     launches = lib.s2let_gpu_launch_count() - launches0
     clk = clocks.stop()
-    value = world * nb * 1000.0 / ms_max
+    value = whole_job_rate(nb, world, ms_max * 1e-3)
     fault = lib.s2let_gpu_device_fault()
     if fault:
         raise RuntimeError(f"device fault flag {fault} raised by the split-precision contraction")
@@ -301,7 +318,7 @@ def main():
             step()
         ms64 = timed(a.steps)
         rel = lambda x, y: float(((x - y).abs().max() / y.abs().max()).item())
-        fp64 = {"value": world * nb * 1000.0 / ms64, "unit": "maps/s", "ms_per_step": ms64,
+        fp64 = {"value": whole_job_rate(nb, world, ms64 * 1e-3), "unit": "maps/s", "ms_per_step": ms64,
                 "speedup_mixed_over_fp64": ms64 / ms_max,
                 "max_rel_err_mixed_vs_fp64": {"f_wav": rel(w_mx, w), "f_scal": rel(sc_mx, sc),
                                               "wav2px": rel(fr_mx, fr)}}
@@ -379,12 +396,8 @@ def main():
         t0 = time.perf_counter()
         for _ in range(a.steps):
             e2e_step()
-        e2e_s = (time.perf_counter() - t0) / a.steps
-        if dist:
-            t = torch.tensor([e2e_s], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": world * nb / e2e_s, "unit": "maps/s",
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / a.steps, dist, dev)
+        e2e = {"value": whole_job_rate(nb, world, e2e_s), "unit": "maps/s",
                "h2d_bytes_per_step": nb * (npx + nw + ns) * 8, "d2h_bytes_per_step": nb * (nw + ns + npx) * 8,
                "api": "s2let_analysis_px2wav_real + s2let_synthesis_wav2px_real, pinned host buffers"}
 
