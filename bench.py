@@ -75,6 +75,10 @@ def args_():
     ap.add_argument("--N", type=int, default=4)
     ap.add_argument("--B", type=float, default=2.0)
     ap.add_argument("--J_min", type=int, default=2)
+    ap.add_argument("--workload", default="metric", choices=["metric", "spin2", "sparsity"],
+                    help="metric: the headline (real maps, L=1024, N=4); spin2: complex spin-2 maps, "
+                         "L=1024, N=5, J_min=3, error per scale; sparsity: differentiable wavelet-sparsity "
+                         "loss, 32 real maps at L=256, forward + backward")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -221,6 +225,127 @@ def run_reference(a, rank):
     }), flush=True)
 
 
+def spin2_flm(rng, L, s=2):
+    """Spin-s Gaussian flm with C_l ∝ l^-2 for l >= |s|, zero below (no reality symmetry)."""
+    l = np.repeat(np.arange(L), 2 * np.arange(L) + 1)
+    amp = np.where(l >= abs(s), 1.0 / np.maximum(l, 1.0), 0.0)
+    return (rng.normal(size=L * L) + 1j * rng.normal(size=L * L)) * amp / np.sqrt(2.0)
+
+
+def run_workload(a, world, rank, local):
+    """Secondary workloads (one JSON line each): the split-precision path against
+    the FP64 path on the same inputs, CUDA-event timing after warm-up."""
+    import torch
+
+    import s2let_gb300
+    from s2let_gb300 import torch_ops as T
+    from s2let_gb300.capi import make_parameters
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    api = s2let_gb300.api()
+    lib = api.lib
+    stream = torch.cuda.current_stream(dev)
+
+    def event_ms(fn, steps):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    rel = lambda x, y: float(((x - y).abs().max() / y.abs().max()).item())
+    clocks = ClockSampler(local)
+    out = {"n_gpus": world, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "data": "synthetic"}
+    if a.workload == "spin2":
+        L, N, J_min, nb = 1024, 5, 3, min(a.batch, 8)
+        p = make_parameters(L, 2.0, J_min, N, 2, 0)
+        rng = np.random.default_rng(replica_seed(rank))
+        lib.s2let_gpu_set_precision(0)
+        f = torch.tensor(np.stack([api.alm2map(spin2_flm(rng, L), L, 2) for _ in range(nb)]), device=dev)
+        w0, s0 = T.px2wav(f, p, precision="fp64")
+        res = {}
+        for prec in ("mixed", "fp64"):
+            def step():
+                w, sc = T.px2wav(f, p, precision=prec)
+                T.wav2px(w, sc, p, precision=prec)
+            for _ in range(a.warmup):
+                step()
+            if prec == "mixed":
+                clocks.start()
+            ms = max_over_ranks(event_ms(step, a.steps), None)
+            if prec == "mixed":
+                clk = clocks.stop()
+            res[prec] = ms
+        w1, s1 = T.px2wav(f, p, precision="mixed")
+        r1 = T.wav2px(w1, s1, p, precision="mixed")
+        J = lib.s2let_j_max(C.byref(p))
+        per_scale, off = {}, 0
+        for j in range(J_min, J + 1):
+            n = lib.s2let_n_wav_j(j, C.byref(p))
+            per_scale[str(j)] = rel(w1[:, off:off + n], w0[:, off:off + n])
+            off += n
+        out.update({
+            "metric": "spin-2 complex px2wav+wav2px maps/s at L=1024,N=5,J_min=3 (split precision)",
+            "value": whole_job_rate(nb, world, res["mixed"] * 1e-3), "unit": "maps/s",
+            "ms_per_step": res["mixed"], "dtype": "bf16-split/f32-acc/f64 (complex128 I/O)",
+            "config": {"workload": "complex spin-2 maps, C_l ∝ l^-2 (l >= 2), L=1024, N=5, B=2, J_min=3, "
+                                   "upsample=0, MW", "batch_per_gpu": nb},
+            "fp64_path": {"value": whole_job_rate(nb, world, res["fp64"] * 1e-3), "unit": "maps/s",
+                          "ms_per_step": res["fp64"], "speedup_mixed_over_fp64": res["fp64"] / res["mixed"]},
+            "max_rel_err_vs_fp64": {"f_wav_per_scale": per_scale, "f_scal": rel(s1, s0),
+                                    "wav2px_round_trip": rel(r1, f)},
+            "clocks": clk,
+        })
+    else:
+        L, nb = 256, 32
+        p = make_parameters(L, 2.0, 2, 4, 0, 0)
+        sz = T.sizes(p)
+        g = torch.Generator().manual_seed(replica_seed(rank))
+        lib.s2let_gpu_set_precision(0)
+        smooth = torch.tensor(np.stack([api.alm2map(power_law_real_flm(np.random.default_rng(replica_seed(rank) + b),
+                                                                         L), L, real=True) for b in range(nb)]))
+        y = (smooth + 0.1 * torch.randn((nb, sz["n_px"]), generator=g, dtype=torch.float64)).to(dev)
+        x0 = y.to(torch.float32)  # FP32 storage of the iterate; the transforms run on its FP64 copy
+        lam, thr = 1e-3, 0.05
+        grads, res = {}, {}
+        for prec in ("mixed", "fp64"):
+            def step():
+                x = x0.to(torch.float64).requires_grad_(True)
+                w, sc = T.px2wav(x, p, precision=prec)
+                ws = torch.sign(w) * torch.clamp(w.abs() - thr, min=0.0)
+                r = T.wav2px(ws, sc, p, precision=prec) - y
+                loss = 0.5 * torch.sum(r * r) + lam * torch.sum(w.abs())
+                (gx,) = torch.autograd.grad(loss, x)
+                return gx
+            for _ in range(a.warmup):
+                grads[prec] = step()
+            if prec == "mixed":
+                clocks.start()
+            res[prec] = event_ms(step, a.steps)
+            if prec == "mixed":
+                clk = clocks.stop()
+        out.update({
+            "metric": "wavelet-sparsity loss forward+backward maps/s, 32 real maps at L=256, N=4 (split precision)",
+            "value": whole_job_rate(nb, world, res["mixed"] * 1e-3), "unit": "maps/s",
+            "ms_per_step": res["mixed"], "dtype": "f32 storage, bf16-split/f32-acc/f64 transforms",
+            "config": {"workload": "loss = 0.5||wav2px(soft(px2wav(x))) - y||^2 + 1e-3 ||px2wav(x)||_1, "
+                                   "y = smooth Gaussian field + N(0, 0.1^2)", "L": L, "N": 4, "B": 2.0,
+                       "J_min": 2, "batch_per_gpu": nb},
+            "fp64_path": {"value": whole_job_rate(nb, world, res["fp64"] * 1e-3), "unit": "maps/s",
+                          "ms_per_step": res["fp64"], "speedup_mixed_over_fp64": res["fp64"] / res["mixed"]},
+            "max_rel_err_grad_vs_fp64": rel(grads["mixed"], grads["fp64"]),
+            "clocks": clk,
+        })
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def main():
     a = args_()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -228,6 +353,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if a.impl == "reference":
         run_reference(a, rank)
+        return
+    if a.workload != "metric":
+        run_workload(a, world, rank, local)
         return
 
     import torch
