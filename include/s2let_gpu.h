@@ -1,6 +1,7 @@
 /*
  * s2let_gpu.h — C ABI of libs2let_gpu.so, a GB300 (sm_103a) implementation of
- * S2LET's scale-discretised wavelet transforms on McEwen–Wiaux (MW) sampling.
+ * S2LET's scale-discretised wavelet transforms on McEwen–Wiaux sampling (MW
+ * and its symmetric variant MWSS).
  *
  * Drop-in boundary.  Every s2let_* function below has the name, argument list,
  * argument meaning and coefficient layout of the reference C API
@@ -19,8 +20,14 @@
  * environment variable S2LET_GPU_ABORT_ON_ERROR=1 restores the reference's
  * exit(1) behaviour.
  *
- * Sampling.  Only S2LET_SAMPLING_MW is implemented on the GPU; MW_SS returns
- * S2LET_GPU_ERR_UNSUPPORTED.
+ * Sampling.  The directional transforms (px2wav / wav2px, lm2wav / wav2lm and
+ * their adjoints) follow parameters->sampling_scheme as the reference does:
+ * S2LET_SAMPLING_MW (L rings of 2L-1 samples) or S2LET_SAMPLING_MW_SS (L+1
+ * rings of 2L samples, both poles), for the signal, the scaling map and the
+ * SO3 wavelet maps alike.  Any other value is S2LET_GPU_ERR_UNSUPPORTED (the
+ * reference's "Sampling scheme not supported.").  The axisymmetric pixel-space
+ * transforms, the manual-tiling entry points and s2let_mw_* use MW whatever the
+ * parameters say, as in the reference.
  *
  * Extensions (no reference counterpart) are prefixed s2let_gpu_: precision
  * selection, device-pointer batched entry points on a caller stream, and the
@@ -369,7 +376,7 @@ double s2let_lm_power(S2LET_COMPLEX(double) *flm, int L);                       
 enum {
   S2LET_GPU_OK = 0,
   S2LET_GPU_ERR_INVALID = 1,     /* bad parameter (L<1, N<1, B<=1, |spin|>=L, ...) */
-  S2LET_GPU_ERR_UNSUPPORTED = 2, /* e.g. MW_SS sampling, spline/needlet kernels on GPU paths */
+  S2LET_GPU_ERR_UNSUPPORTED = 2, /* e.g. an unknown sampling scheme, more than 16 directions per scale */
   S2LET_GPU_ERR_CUDA = 3,        /* a CUDA runtime call failed */
   S2LET_GPU_ERR_NOMEM = 4,       /* device or host allocation failed */
   S2LET_GPU_ERR_NO_DEVICE = 5    /* no usable CUDA device */
@@ -395,6 +402,15 @@ void s2let_gpu_mw_adjoint_map2alm(S2LET_COMPLEX(double) *f, const S2LET_COMPLEX(
                                   int spin);
 void s2let_gpu_mw_adjoint_alm2map(S2LET_COMPLEX(double) *flm, const S2LET_COMPLEX(double) *f, int L,
                                   int spin);
+
+/* The SSHT transforms the wavelet transforms call, on either sampling (host
+ * buffers; f is double* when real != 0, then spin must be 0):
+ *   dir 0  forward, pixels -> flm    ssht_core_mw_forward_sov_conv_sym[_ss][_real]  (src/c/s2let_analysis.c:471-474)
+ *   dir 1  inverse, flm -> pixels    ssht_core_mw_inverse_sov_sym[_ss][_real]       (src/c/s2let_synthesis.c:489-492)
+ *   dir 2  adjoint of the forward    ssht_adjoint_mw_forward_sov_sym[_ss][_real]    (src/c/s2let_analysis_adjoint.c:505-509)
+ *   dir 3  adjoint of the inverse    ssht_adjoint_mw_inverse_sov_sym[_ss][_real]    (src/c/s2let_synthesis_adjoint.c:479-483)
+ * sampling_scheme: S2LET_SAMPLING_MW or S2LET_SAMPLING_MW_SS.  Returns the status. */
+int s2let_gpu_sht(int dir, int sampling_scheme, int L, int spin, int real, void *f, void *flm);
 
 /* Drops cached plans (Wigner tables, FFT chirps) and frees their device memory. */
 void s2let_gpu_release_plans(void);

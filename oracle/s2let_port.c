@@ -554,12 +554,18 @@ void s2let_analysis_adjoint_lmn2lm_real(complex double *flm, const complex doubl
 /* Orchestration: harmonic <-> wavelet space                                 */
 /* ======================================================================== */
 
+/* src/c/s2let_analysis.c:231-246: MW and MWSS are supported, anything else is an error */
 static void check_mw(const s2let_parameters_t *p) {
-  if (p->sampling_scheme != S2LET_SAMPLING_MW) {
-    printf("ERROR: oracle restates MW sampling only.\n");
+  if (p->sampling_scheme != S2LET_SAMPLING_MW && p->sampling_scheme != S2LET_SAMPLING_MW_SS) {
+    printf("ERROR: Sampling scheme not supported.\n");
     exit(1);
   }
 }
+
+/* the SSHT entry point of the parameters' sampling scheme (the switch at e.g.
+ * src/c/s2let_analysis.c:322-333): base##suffix for MW, base##_ss##suffix for MWSS */
+#define SS_PICK(p, base, suffix) \
+  ((p)->sampling_scheme == S2LET_SAMPLING_MW_SS ? base##_ss##suffix : base##suffix)
 
 typedef enum { DIR_ANALYSIS, DIR_SYNTHESIS, DIR_ANALYSIS_ADJ, DIR_SYNTHESIS_ADJ } direction;
 
@@ -593,20 +599,20 @@ static void wavelet_driver(direction dir, complex double *flm, void *wav, void *
   /* scaling part: always a spin-0 transform (src/c/s2let_analysis.c:321) */
   switch (dir) {
   case DIR_ANALYSIS:
-    if (real) ssht_core_mw_inverse_sov_sym_real(scal, fscal, bs, 0, 0);
-    else ssht_core_mw_inverse_sov_sym(scal, fscal, bs, 0, 0, 0);
+    if (real) SS_PICK(p, ssht_core_mw_inverse_sov_sym, _real)(scal, fscal, bs, 0, 0);
+    else SS_PICK(p, ssht_core_mw_inverse_sov_sym, )(scal, fscal, bs, 0, 0, 0);
     break;
   case DIR_SYNTHESIS:
-    if (real) ssht_core_mw_forward_sov_conv_sym_real(fscal, scal, bs, 0, 0);
-    else ssht_core_mw_forward_sov_conv_sym(fscal, scal, bs, 0, 0, 0);
+    if (real) SS_PICK(p, ssht_core_mw_forward_sov_conv_sym, _real)(fscal, scal, bs, 0, 0);
+    else SS_PICK(p, ssht_core_mw_forward_sov_conv_sym, )(fscal, scal, bs, 0, 0, 0);
     break;
   case DIR_ANALYSIS_ADJ:
-    if (real) ssht_adjoint_mw_inverse_sov_sym_real(fscal, scal, bs, 0, 0);
-    else ssht_adjoint_mw_inverse_sov_sym(fscal, scal, bs, 0, 0, 0);
+    if (real) SS_PICK(p, ssht_adjoint_mw_inverse_sov_sym, _real)(fscal, scal, bs, 0, 0);
+    else SS_PICK(p, ssht_adjoint_mw_inverse_sov_sym, )(fscal, scal, bs, 0, 0, 0);
     break;
   case DIR_SYNTHESIS_ADJ:
-    if (real) ssht_adjoint_mw_forward_sov_sym_real(scal, fscal, bs, 0, 0);
-    else ssht_adjoint_mw_forward_sov_sym(scal, fscal, bs, 0, 0, 0);
+    if (real) SS_PICK(p, ssht_adjoint_mw_forward_sov_sym, _real)(scal, fscal, bs, 0, 0);
+    else SS_PICK(p, ssht_adjoint_mw_forward_sov_sym, )(scal, fscal, bs, 0, 0, 0);
     break;
   }
 
@@ -676,14 +682,14 @@ void s2let_analysis_px2wav(complex double *w, complex double *s, const complex d
                            const s2let_parameters_t *p) {
   check_mw(p);
   complex double *flm = calloc((size_t)p->L * p->L, sizeof *flm);
-  ssht_core_mw_forward_sov_conv_sym(flm, f, p->L, p->spin, 0, 0);
+  SS_PICK(p, ssht_core_mw_forward_sov_conv_sym, )(flm, f, p->L, p->spin, 0, 0);
   s2let_analysis_lm2wav(w, s, flm, p);
   free(flm);
 }
 void s2let_analysis_px2wav_real(double *w, double *s, const double *f, const s2let_parameters_t *p) {
   check_mw(p);
   complex double *flm = calloc((size_t)p->L * p->L, sizeof *flm);
-  ssht_core_mw_forward_sov_conv_sym_real(flm, f, p->L, 0, 0);
+  SS_PICK(p, ssht_core_mw_forward_sov_conv_sym, _real)(flm, f, p->L, 0, 0);
   s2let_analysis_lm2wav_real(w, s, flm, p);
   free(flm);
 }
@@ -692,14 +698,14 @@ void s2let_synthesis_wav2px(complex double *f, const complex double *w, const co
   check_mw(p);
   complex double *flm = calloc((size_t)p->L * p->L, sizeof *flm);
   s2let_synthesis_wav2lm(flm, w, s, p);
-  ssht_core_mw_inverse_sov_sym(f, flm, p->L, p->spin, 0, 0);
+  SS_PICK(p, ssht_core_mw_inverse_sov_sym, )(f, flm, p->L, p->spin, 0, 0);
   free(flm);
 }
 void s2let_synthesis_wav2px_real(double *f, const double *w, const double *s, const s2let_parameters_t *p) {
   check_mw(p);
   complex double *flm = calloc((size_t)p->L * p->L, sizeof *flm);
   s2let_synthesis_wav2lm_real(flm, w, s, p);
-  ssht_core_mw_inverse_sov_sym_real(f, flm, p->L, 0, 0);
+  SS_PICK(p, ssht_core_mw_inverse_sov_sym, _real)(f, flm, p->L, 0, 0);
   free(flm);
 }
 void s2let_analysis_adjoint_wav2px(complex double *f, const complex double *w, const complex double *s,
@@ -707,7 +713,7 @@ void s2let_analysis_adjoint_wav2px(complex double *f, const complex double *w, c
   check_mw(p);
   complex double *flm = calloc((size_t)p->L * p->L, sizeof *flm);
   s2let_analysis_adjoint_wav2lm(flm, w, s, p);
-  ssht_adjoint_mw_forward_sov_sym(f, flm, p->L, p->spin, 0, 0);
+  SS_PICK(p, ssht_adjoint_mw_forward_sov_sym, )(f, flm, p->L, p->spin, 0, 0);
   free(flm);
 }
 void s2let_analysis_adjoint_wav2px_real(double *f, const double *w, const double *s,
@@ -715,21 +721,21 @@ void s2let_analysis_adjoint_wav2px_real(double *f, const double *w, const double
   check_mw(p);
   complex double *flm = calloc((size_t)p->L * p->L, sizeof *flm);
   s2let_analysis_adjoint_wav2lm_real(flm, w, s, p);
-  ssht_adjoint_mw_forward_sov_sym_real(f, flm, p->L, 0, 0);
+  SS_PICK(p, ssht_adjoint_mw_forward_sov_sym, _real)(f, flm, p->L, 0, 0);
   free(flm);
 }
 void s2let_synthesis_adjoint_px2wav(complex double *w, complex double *s, const complex double *f,
                                     const s2let_parameters_t *p) {
   check_mw(p);
   complex double *flm = calloc((size_t)p->L * p->L, sizeof *flm);
-  ssht_adjoint_mw_inverse_sov_sym(flm, f, p->L, p->spin, 0, 0);
+  SS_PICK(p, ssht_adjoint_mw_inverse_sov_sym, )(flm, f, p->L, p->spin, 0, 0);
   s2let_synthesis_adjoint_lm2wav(w, s, flm, p);
   free(flm);
 }
 void s2let_synthesis_adjoint_px2wav_real(double *w, double *s, const double *f, const s2let_parameters_t *p) {
   check_mw(p);
   complex double *flm = calloc((size_t)p->L * p->L, sizeof *flm);
-  ssht_adjoint_mw_inverse_sov_sym_real(flm, f, p->L, 0, 0);
+  SS_PICK(p, ssht_adjoint_mw_inverse_sov_sym, _real)(flm, f, p->L, 0, 0);
   s2let_synthesis_adjoint_lm2wav_real(w, s, flm, p);
   free(flm);
 }

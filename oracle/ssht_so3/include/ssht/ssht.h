@@ -13,7 +13,7 @@
  * Conventions:
  *   sY_lm(theta,phi) = (-1)^s sqrt((2l+1)/4pi) e^{i m phi} d^l_{m,-s}(theta)
  *   (Condon-Shortley phase), theta_t = pi(2t+1)/(2L-1), phi_p = 2 pi p/(2L-1),
- *   map index t*(2L-1)+p, harmonic index l^2+l+m.
+ *   map index t*(2L-1)+p, harmonic index l^2+l+m (MW; MWSS further below).
  */
 #ifndef ORACLE_SSHT_H
 #define ORACLE_SSHT_H
@@ -60,7 +60,8 @@ void ssht_adjoint_mw_forward_sov_sym(complex double *f, const complex double *fl
 void ssht_adjoint_mw_forward_sov_sym_real(double *f, const complex double *flm, int L,
                                           ssht_dl_method_t dl_method, int verbosity);
 
-/* MW symmetric sampling (MWSS) is not restated; these abort with a message. */
+/* MW symmetric sampling (MWSS): theta_t = pi t/L, t = 0..L (both poles),
+ * phi_p = 2 pi p/(2L), map index t*2L+p. */
 void ssht_core_mw_forward_sov_conv_sym_ss(complex double *flm, const complex double *f, int L,
                                           int spin, ssht_dl_method_t dl_method, int verbosity);
 void ssht_core_mw_forward_sov_conv_sym_ss_real(complex double *flm, const double *f, int L,

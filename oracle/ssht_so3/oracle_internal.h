@@ -4,13 +4,14 @@
 #define ORACLE_INTERNAL_H
 #include <complex.h>
 
-/* f[j] is double* when real[j] != 0 (spin must be 0), else complex double*. */
+/* f[j] is double* when real[j] != 0 (spin must be 0), else complex double*.
+ * ss = 0: MW sampling, ss = 1: MWSS sampling. */
 void oracle_ssht_inverse_multi(void **f, const complex double **flm, const int *spin,
-                               const int *real, int njob, int L);
+                               const int *real, int njob, int L, int ss);
 void oracle_ssht_forward_multi(complex double **flm, const void **f, const int *spin,
-                               const int *real, int njob, int L);
+                               const int *real, int njob, int L, int ss);
 void oracle_ssht_adjoint_inverse_multi(complex double **flm, const void **f, const int *spin,
-                                       const int *real, int njob, int L);
+                                       const int *real, int njob, int L, int ss);
 void oracle_ssht_adjoint_forward_multi(void **f, const complex double **flm, const int *spin,
-                                       const int *real, int njob, int L);
+                                       const int *real, int njob, int L, int ss);
 #endif

@@ -7,7 +7,9 @@
  * spin-(-n) spherical-harmonic transform (relation
  *   e^{i m a} d^l_{mn}(b) = (-1)^n sY_lm(b,a) / sqrt((2l+1)/4pi),  s = -n)
  * followed by a DFT over the 2N-1 gamma samples; the spherical-harmonic parts
- * reuse the SSHT restatement, with Delta shared across directions.
+ * reuse the SSHT restatement, with Delta shared across directions.  Both
+ * SO3_SAMPLING_MW and SO3_SAMPLING_MW_SS take the (alpha, beta) grid of the
+ * matching SSHT sampling; gamma has 2N-1 samples in both.
  *
  * "direct" and "via_ssht" variants compute the same linear map and share one
  * implementation here.  L0 (a lower band-limit hint in SO3) only skips work in
@@ -103,8 +105,8 @@ static int n_list(int *ns, const so3_parameters_t *p, int real_only) {
 }
 
 static void check_params(const so3_parameters_t *p) {
-  if (p->sampling_scheme != SO3_SAMPLING_MW) {
-    fprintf(stderr, "oracle: only SO3_SAMPLING_MW is restated\n");
+  if (p->sampling_scheme != SO3_SAMPLING_MW && p->sampling_scheme != SO3_SAMPLING_MW_SS) {
+    fprintf(stderr, "oracle: unknown SO3 sampling scheme\n");
     exit(1);
   }
   if (p->steerable) {
@@ -128,8 +130,9 @@ static int flmn_index(int l, int m, int n, const so3_parameters_t *p, int real) 
 static void inverse_any(void *fout, const complex double *flmn, const so3_parameters_t *p,
                         int real) {
   check_params(p);
-  const int L = p->L, N = p->N, ng = so3_sampling_ngamma(p), K = 2 * L - 1;
-  const size_t npx = (size_t)L * K;
+  const int L = p->L, N = p->N, ng = so3_sampling_ngamma(p);
+  const size_t npx = (size_t)so3_sampling_nalpha(p) * so3_sampling_nbeta(p);
+  const int ss = p->sampling_scheme == SO3_SAMPLING_MW_SS;
   int ns[256];
   int nn = n_list(ns, p, real);
   complex double **x = (complex double **)xcalloc(nn, sizeof(void *));
@@ -147,7 +150,7 @@ static void inverse_any(void *fout, const complex double *flmn, const so3_parame
     rl[k] = real && n == 0;
     maps[k] = rl[k] ? xcalloc(npx, sizeof(double)) : xcalloc(npx, sizeof(complex double));
   }
-  oracle_ssht_inverse_multi(maps, (const complex double **)x, spin, rl, nn, L);
+  oracle_ssht_inverse_multi(maps, (const complex double **)x, spin, rl, nn, L, ss);
   for (int g = 0; g < ng; ++g) {
     double gam = 2.0 * SPI * g / ng;
 #pragma omp parallel for schedule(static) if (npx >= 4096)
@@ -196,8 +199,9 @@ void so3_core_inverse_via_ssht_real(double *f, const complex double *flmn, const
 
 static void forward_any(complex double *flmn, const void *fin, const so3_parameters_t *p, int real) {
   check_params(p);
-  const int L = p->L, ng = so3_sampling_ngamma(p), K = 2 * L - 1;
-  const size_t npx = (size_t)L * K;
+  const int L = p->L, ng = so3_sampling_ngamma(p);
+  const size_t npx = (size_t)so3_sampling_nalpha(p) * so3_sampling_nbeta(p);
+  const int ss = p->sampling_scheme == SO3_SAMPLING_MW_SS;
   int ns[256];
   int nn = n_list(ns, p, real);
   memset(flmn, 0, sizeof(complex double) * so3_sampling_flmn_size(p));
@@ -227,7 +231,7 @@ static void forward_any(complex double *flmn, const void *fin, const so3_paramet
         ((complex double *)maps[k])[i] = acc;
     }
   }
-  oracle_ssht_forward_multi(y, (const void **)maps, spin, rl, nn, L);
+  oracle_ssht_forward_multi(y, (const void **)maps, spin, rl, nn, L, ss);
   for (int k = 0; k < nn; ++k) {
     int n = ns[k];
     for (int l = abs(n); l < L; ++l) {
@@ -261,8 +265,9 @@ void so3_core_forward_via_ssht_real(complex double *flmn, const double *f, const
 static void adjoint_inverse_any(complex double *flmn, const void *fin, const so3_parameters_t *p,
                                 int real) {
   check_params(p);
-  const int L = p->L, ng = so3_sampling_ngamma(p), K = 2 * L - 1;
-  const size_t npx = (size_t)L * K;
+  const int L = p->L, ng = so3_sampling_ngamma(p);
+  const size_t npx = (size_t)so3_sampling_nalpha(p) * so3_sampling_nbeta(p);
+  const int ss = p->sampling_scheme == SO3_SAMPLING_MW_SS;
   int ns[256];
   int nn = n_list(ns, p, real);
   memset(flmn, 0, sizeof(complex double) * so3_sampling_flmn_size(p));
@@ -291,7 +296,7 @@ static void adjoint_inverse_any(complex double *flmn, const void *fin, const so3
         ((complex double *)maps[k])[i] = acc;
     }
   }
-  oracle_ssht_adjoint_inverse_multi(y, (const void **)maps, spin, rl, nn, L);
+  oracle_ssht_adjoint_inverse_multi(y, (const void **)maps, spin, rl, nn, L, ss);
   for (int k = 0; k < nn; ++k) {
     int n = ns[k];
     for (int l = abs(n); l < L; ++l) {
@@ -319,8 +324,9 @@ void so3_adjoint_inverse_direct_real(complex double *flmn, const double *f, cons
 static void adjoint_forward_any(void *fout, const complex double *flmn, const so3_parameters_t *p,
                                 int real) {
   check_params(p);
-  const int L = p->L, ng = so3_sampling_ngamma(p), K = 2 * L - 1;
-  const size_t npx = (size_t)L * K;
+  const int L = p->L, ng = so3_sampling_ngamma(p);
+  const size_t npx = (size_t)so3_sampling_nalpha(p) * so3_sampling_nbeta(p);
+  const int ss = p->sampling_scheme == SO3_SAMPLING_MW_SS;
   int ns[256];
   int nn = n_list(ns, p, 0); /* all directions; the real case is Re of the complex adjoint */
   complex double **x = (complex double **)xcalloc(nn, sizeof(void *));
@@ -347,7 +353,7 @@ static void adjoint_forward_any(void *fout, const complex double *flmn, const so
       }
     }
   }
-  oracle_ssht_adjoint_forward_multi(maps, (const complex double **)x, spin, rl, nn, L);
+  oracle_ssht_adjoint_forward_multi(maps, (const complex double **)x, spin, rl, nn, L, ss);
   for (int g = 0; g < ng; ++g) {
     double gam = 2.0 * SPI * g / ng;
 #pragma omp parallel for schedule(static) if (npx >= 4096)

@@ -15,6 +15,10 @@
  *             convolution with w(p) = int_0^pi e^{ipt} sin t dt, then the Delta
  *             contraction.  Exact for band-limited signals.
  *   adjoints: each of the steps above transposed (true adjoints, not inverses).
+ *   MWSS:     the same operators on the symmetric grid (theta_t = pi t/L with
+ *             both poles, 2L samples per ring): the extension to the full
+ *             circle mirrors ring t to 2L - t and carries no half-step phase,
+ *             both DFTs have length 2L and their Nyquist bins are dropped.
  *
  * Delta^l is generated per l by a three-term recursion in its second index,
  * started from the closed form Delta^l_{m',l} = sqrt(C(2l, l+m'))/2^l and kept
@@ -192,6 +196,56 @@ static void delta_column(double *P, const double *D, int l, int n) {
  *   m <  0:  Delta_{mp,m} = (-1)^{l+|m|} D[|m|][mp]
  * Returned as (row pointer, constant factor, alternate flag).
  */
+/* ------------------------------------------------------------------------ */
+/* Sampling grids                                                           */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * MW   (McEwen & Wiaux 2011): theta_t = pi (2t+1)/(2L-1), t < L;  phi_p = 2 pi p/(2L-1).
+ * MWSS (the symmetric variant): theta_t = pi t / L, t <= L (both poles);
+ *      phi_p = 2 pi p/(2L).
+ * The rings and their mirror images theta -> 2 pi - theta are kt equispaced
+ * samples of the full theta circle: kt = 2L-1 starting half a step in (MW) or
+ * kt = 2L starting at theta = 0 (MWSS).  A band-limited m-signal extends to the
+ * circle with parity (-1)^{m+s}, and the kt samples give its Fourier
+ * coefficients m' in [-(L-1), L-1] exactly.  With an even number of samples
+ * (MWSS) the Nyquist bins (m' = L on the circle, m = L on a ring) are not
+ * harmonic content of a band-limited signal and are dropped.
+ */
+typedef struct {
+  int L, ss;
+  int nt; /* rings */
+  int np; /* samples per ring = phi-DFT length */
+  int kt; /* samples on the full theta circle = theta-DFT length */
+} grid_t;
+
+static grid_t grid_of(int L, int ss) {
+  grid_t g;
+  g.L = L;
+  g.ss = ss;
+  g.nt = ss ? L + 1 : L;
+  g.np = ss ? 2 * L : 2 * L - 1;
+  g.kt = ss ? 2 * L : 2 * L - 1;
+  return g;
+}
+
+/* e^{i m' theta_0}: the MW rings start half a step into the circle */
+static complex double theta_phase(const grid_t *g, int mp) {
+  if (g->ss) return 1.0;
+  double a = SPI * mp / g->kt;
+  return cos(a) + I * sin(a);
+}
+
+/* position on the full circle of the mirror image of ring t, or -1 for the
+ * rings that are their own mirror image (theta = 0 or pi) */
+static int mirror_of(const grid_t *g, int t) {
+  if (g->ss) return (t >= 1 && t <= g->L - 1) ? 2 * g->L - t : -1;
+  return (t < g->L - 1) ? g->kt - 1 - t : -1;
+}
+
+/* quadrature scale of the forward transform: 2 pi (phi integral) over the two
+ * unnormalised DFT lengths */
+static double fwd_scale(const grid_t *g) { return 2.0 * SPI / ((double)g->np * g->kt); }
 
 /* ------------------------------------------------------------------------ */
 /* Fourier-space weight for the exact forward transform                     */
@@ -260,8 +314,8 @@ static void wconv(complex double *out, const complex double *in, int L, int conj
  * times the forward-adjoint scale (adjoint forward).  mode 0: inverse, 1: adjoint-forward.
  */
 static void harm_to_mm(complex double **F, const complex double **flm, const int *spin,
-                       int njob, int L, int mlo, int mode) {
-  const int K = 2 * L - 1;
+                       int njob, const grid_t *g, int mlo, int mode) {
+  const int L = g->L, K = 2 * L - 1;
   double *D = (double *)xcalloc((size_t)L * L, sizeof(double));
   double *Pn = (double *)xcalloc((size_t)L, sizeof(double));
   double *Pa = (double *)xcalloc((size_t)L, sizeof(double));
@@ -283,7 +337,7 @@ static void harm_to_mm(complex double **F, const complex double **flm, const int
         complex double a = flm[j][l * l + l + m];
         if (a == 0) continue;
         complex double ph = neg1(s) * cl * ipow(n - m);
-        if (mode == 1) ph = conj(ph) * (2.0 * SPI / ((double)K * K));
+        if (mode == 1) ph = conj(ph) * fwd_scale(g);
         a *= ph;
         complex double *row = F[j] + (size_t)(m + L - 1) * L;
         const double *drow = D + (size_t)abs(m) * w;
@@ -305,12 +359,12 @@ static void harm_to_mm(complex double **F, const complex double **flm, const int
 /*
  * (m, m') coefficients -> harmonic, for several spins at once.
  * flm_j(l,m) = scale_l sum_{mp>=0} Delta_{mp,m} Delta_{mp,n} G_j[mi*L+mp]
- * mode 0: forward (scale (-1)^s c_l 2pi/K^2 i^{n-m}); mode 1: adjoint-inverse
- * (scale (-1)^s c_l i^{n-m}).
+ * mode 0: forward (scale (-1)^s c_l i^{n-m} times the quadrature scale); mode 1:
+ * adjoint-inverse (scale (-1)^s c_l i^{n-m}).
  */
 static void mm_to_harm(complex double **flm, complex double **G, const int *spin, int njob,
-                       int L, int mlo, int mode) {
-  const int K = 2 * L - 1;
+                       const grid_t *g, int mlo, int mode) {
+  const int L = g->L;
   double *D = (double *)xcalloc((size_t)L * L, sizeof(double));
   double *Pn = (double *)xcalloc((size_t)L, sizeof(double));
   double *Pa = (double *)xcalloc((size_t)L, sizeof(double));
@@ -340,7 +394,7 @@ static void mm_to_harm(complex double **flm, complex double **G, const int *spin
           acc *= neg1(l - m);
         }
         complex double ph = neg1(s) * cl * ipow(n - m);
-        if (mode == 0) ph *= 2.0 * SPI / ((double)K * K);
+        if (mode == 0) ph *= fwd_scale(g);
         flm[j][l * l + l + m] = acc * ph;
       }
     }
@@ -355,128 +409,112 @@ static void mm_to_harm(complex double **flm, complex double **G, const int *spin
 /* ------------------------------------------------------------------------ */
 
 /* F (m,mp>=0) -> map; real != 0 writes Re into fr, else complex into fc. */
-static void mm_to_map(complex double *fc, double *fr, const complex double *F, int L, int s,
-                      int mlo) {
-  const int K = 2 * L - 1, n = -s;
-  complex double *ring = (complex double *)xcalloc((size_t)L * K, sizeof(complex double));
+static void mm_to_map(complex double *fc, double *fr, const complex double *F, const grid_t *g,
+                      int s, int mlo) {
+  const int L = g->L, n = -s, nt = g->nt, np = g->np, kt = g->kt;
+  complex double *ring = (complex double *)xcalloc((size_t)nt * np, sizeof(complex double));
 #pragma omp parallel if (L >= 64)
   {
-  complex double *x = (complex double *)xcalloc(K, sizeof(complex double));
+  complex double *x = (complex double *)xcalloc(kt, sizeof(complex double));
 #pragma omp for schedule(static)
   for (int m = mlo; m <= L - 1; ++m) {
     const complex double *row = F + (size_t)(m + L - 1) * L;
-    memset(x, 0, sizeof(complex double) * K);
+    memset(x, 0, sizeof(complex double) * kt);
     double sym = neg1(m + n);
     for (int mp = -(L - 1); mp <= L - 1; ++mp) {
       complex double v = (mp >= 0) ? row[mp] : sym * row[-mp];
-      double a = SPI * mp / K;
-      x[modk(mp, K)] += v * (cos(a) + I * sin(a));
+      x[modk(mp, kt)] += v * theta_phase(g, mp);
     }
-    offt_dft(x, K, +1);
-    for (int t = 0; t < L; ++t) ring[(size_t)t * K + modk(m, K)] = x[t];
+    offt_dft(x, kt, +1);
+    for (int t = 0; t < nt; ++t) ring[(size_t)t * np + modk(m, np)] = x[t];
   }
   free(x);
   }
 #pragma omp parallel for schedule(static) if (L >= 64)
-  for (int t = 0; t < L; ++t) {
-    complex double *r = ring + (size_t)t * K;
+  for (int t = 0; t < nt; ++t) {
+    complex double *r = ring + (size_t)t * np;
     if (mlo == 0) /* Hermitian completion for a real signal */
-      for (int m = 1; m <= L - 1; ++m) r[modk(-m, K)] = conj(r[m]);
-    offt_dft(r, K, +1);
-    for (int p = 0; p < K; ++p) {
+      for (int m = 1; m <= L - 1; ++m) r[modk(-m, np)] = conj(r[m]);
+    offt_dft(r, np, +1);
+    for (int p = 0; p < np; ++p) {
       if (fr)
-        fr[(size_t)t * K + p] = creal(r[p]);
+        fr[(size_t)t * np + p] = creal(r[p]);
       else
-        fc[(size_t)t * K + p] = r[p];
+        fc[(size_t)t * np + p] = r[p];
     }
   }
   free(ring);
 }
 
 void oracle_ssht_inverse_multi(void **f, const complex double **flm, const int *spin,
-                               const int *real, int njob, int L) {
+                               const int *real, int njob, int L, int ss) {
+  const grid_t g = grid_of(L, ss);
   const int K = 2 * L - 1;
   complex double **F = (complex double **)xcalloc(njob, sizeof(void *));
   for (int j = 0; j < njob; ++j) F[j] = (complex double *)xcalloc((size_t)K * L, sizeof(complex double));
   int allreal = 1;
   for (int j = 0; j < njob; ++j) allreal &= real[j] != 0;
-  harm_to_mm(F, flm, spin, njob, L, allreal ? 0 : -(L - 1), 0);
+  harm_to_mm(F, flm, spin, njob, &g, allreal ? 0 : -(L - 1), 0);
   for (int j = 0; j < njob; ++j) {
     if (real[j])
-      mm_to_map(NULL, (double *)f[j], F[j], L, spin[j], 0);
+      mm_to_map(NULL, (double *)f[j], F[j], &g, spin[j], 0);
     else
-      mm_to_map((complex double *)f[j], NULL, F[j], L, spin[j], -(L - 1));
+      mm_to_map((complex double *)f[j], NULL, F[j], &g, spin[j], -(L - 1));
     free(F[j]);
   }
   free(F);
-}
-
-void ssht_core_mw_inverse_sov_sym(complex double *f, const complex double *flm, int L, int spin,
-                                  ssht_dl_method_t dl_method, int verbosity) {
-  (void)dl_method;
-  (void)verbosity;
-  void *fo[1] = {f};
-  const complex double *fi[1] = {flm};
-  int sp[1] = {spin}, re[1] = {0};
-  oracle_ssht_inverse_multi(fo, fi, sp, re, 1, L);
-}
-
-void ssht_core_mw_inverse_sov_sym_real(double *f, const complex double *flm, int L,
-                                       ssht_dl_method_t dl_method, int verbosity) {
-  (void)dl_method;
-  (void)verbosity;
-  void *fo[1] = {f};
-  const complex double *fi[1] = {flm};
-  int sp[1] = {0}, re[1] = {1};
-  oracle_ssht_inverse_multi(fo, fi, sp, re, 1, L);
 }
 
 /* ------------------------------------------------------------------------ */
 /* Forward                                                                  */
 /* ------------------------------------------------------------------------ */
 
-/* map -> per-m ring spectra Fm[mi*L + t] (unnormalised phi-DFT). */
-static void map_to_rings(complex double *Fm, const complex double *fc, const double *fr, int L) {
-  const int K = 2 * L - 1;
+/* map -> per-m ring spectra Fm[mi*nt + t] (unnormalised phi-DFT). */
+static void map_to_rings(complex double *Fm, const complex double *fc, const double *fr,
+                         const grid_t *g) {
+  const int L = g->L, nt = g->nt, np = g->np;
 #pragma omp parallel if (L >= 64)
   {
-    complex double *x = (complex double *)xcalloc(K, sizeof(complex double));
+    complex double *x = (complex double *)xcalloc(np, sizeof(complex double));
 #pragma omp for schedule(static)
-    for (int t = 0; t < L; ++t) {
-      for (int p = 0; p < K; ++p) x[p] = fr ? fr[(size_t)t * K + p] : fc[(size_t)t * K + p];
-      offt_dft(x, K, -1);
-      for (int m = -(L - 1); m <= L - 1; ++m) Fm[(size_t)(m + L - 1) * L + t] = x[modk(m, K)];
+    for (int t = 0; t < nt; ++t) {
+      for (int p = 0; p < np; ++p) x[p] = fr ? fr[(size_t)t * np + p] : fc[(size_t)t * np + p];
+      offt_dft(x, np, -1);
+      for (int m = -(L - 1); m <= L - 1; ++m) Fm[(size_t)(m + L - 1) * nt + t] = x[modk(m, np)];
     }
     free(x);
   }
 }
 
 /* per-m ring spectra -> G (mp >= 0, symmetrised) for the forward contraction */
-static void rings_to_G(complex double *G, const complex double *Fm, int L, int s, int mlo) {
-  const int K = 2 * L - 1, n = -s;
+static void rings_to_G(complex double *G, const complex double *Fm, const grid_t *g, int s, int mlo) {
+  const int L = g->L, K = 2 * L - 1, n = -s, nt = g->nt, kt = g->kt;
   memset(G, 0, sizeof(complex double) * (size_t)K * L);
 #pragma omp parallel if (L >= 64)
   {
   conv_plan *cp = get_conv(L);
-  complex double *ext = (complex double *)xcalloc(K, sizeof(complex double));
+  complex double *ext = (complex double *)xcalloc(kt, sizeof(complex double));
   complex double *Fh = (complex double *)xcalloc(K, sizeof(complex double));
   complex double *Gf = (complex double *)xcalloc(K, sizeof(complex double));
   complex double *scr = (complex double *)xcalloc(cp->P, sizeof(complex double));
 #pragma omp for schedule(static)
   for (int m = mlo; m <= L - 1; ++m) {
-    const complex double *Fr = Fm + (size_t)(m + L - 1) * L;
+    const complex double *Fr = Fm + (size_t)(m + L - 1) * nt;
     double eps = neg1(m + s);
-    for (int k = 0; k < K; ++k) ext[k] = (k < L) ? Fr[k] : eps * Fr[K - 1 - k];
-    offt_dft(ext, K, -1);
-    for (int mp = -(L - 1); mp <= L - 1; ++mp) {
-      double a = -SPI * mp / K;
-      Fh[mp + L - 1] = ext[modk(mp, K)] * (cos(a) + I * sin(a));
+    /* extension to the full circle with parity eps */
+    memset(ext, 0, sizeof(complex double) * kt);
+    for (int t = 0; t < nt; ++t) {
+      ext[t] = Fr[t];
+      const int mt = mirror_of(g, t);
+      if (mt >= 0) ext[mt] = eps * Fr[t];
     }
+    offt_dft(ext, kt, -1);
+    for (int mp = -(L - 1); mp <= L - 1; ++mp) Fh[mp + L - 1] = ext[modk(mp, kt)] * conj(theta_phase(g, mp));
     wconv(Gf, Fh, L, 0, scr);
-    complex double *g = G + (size_t)(m + L - 1) * L;
+    complex double *gr = G + (size_t)(m + L - 1) * L;
     double sym = neg1(m + n);
-    g[0] = Gf[L - 1];
-    for (int mp = 1; mp <= L - 1; ++mp) g[mp] = Gf[mp + L - 1] + sym * Gf[-mp + L - 1];
+    gr[0] = Gf[L - 1];
+    for (int mp = 1; mp <= L - 1; ++mp) gr[mp] = Gf[mp + L - 1] + sym * Gf[-mp + L - 1];
   }
   free(ext);
   free(Fh);
@@ -486,21 +524,22 @@ static void rings_to_G(complex double *G, const complex double *Fm, int L, int s
 }
 
 void oracle_ssht_forward_multi(complex double **flm, const void **f, const int *spin,
-                               const int *real, int njob, int L) {
+                               const int *real, int njob, int L, int ss) {
+  const grid_t g = grid_of(L, ss);
   const int K = 2 * L - 1;
-  complex double *Fm = (complex double *)xcalloc((size_t)K * L, sizeof(complex double));
+  complex double *Fm = (complex double *)xcalloc((size_t)K * g.nt, sizeof(complex double));
   complex double **G = (complex double **)xcalloc(njob, sizeof(void *));
   int allreal = 1;
   for (int j = 0; j < njob; ++j) allreal &= real[j] != 0;
   for (int j = 0; j < njob; ++j) {
     G[j] = (complex double *)xcalloc((size_t)K * L, sizeof(complex double));
     if (real[j])
-      map_to_rings(Fm, NULL, (const double *)f[j], L);
+      map_to_rings(Fm, NULL, (const double *)f[j], &g);
     else
-      map_to_rings(Fm, (const complex double *)f[j], NULL, L);
-    rings_to_G(G[j], Fm, L, spin[j], real[j] ? 0 : -(L - 1));
+      map_to_rings(Fm, (const complex double *)f[j], NULL, &g);
+    rings_to_G(G[j], Fm, &g, spin[j], real[j] ? 0 : -(L - 1));
   }
-  mm_to_harm(flm, G, spin, njob, L, allreal ? 0 : -(L - 1), 0);
+  mm_to_harm(flm, G, spin, njob, &g, allreal ? 0 : -(L - 1), 0);
   for (int j = 0; j < njob; ++j) {
     if (real[j])
       for (int l = 0; l < L; ++l)
@@ -511,52 +550,27 @@ void oracle_ssht_forward_multi(complex double **flm, const void **f, const int *
   free(Fm);
 }
 
-void ssht_core_mw_forward_sov_conv_sym(complex double *flm, const complex double *f, int L,
-                                       int spin, ssht_dl_method_t dl_method, int verbosity) {
-  (void)dl_method;
-  (void)verbosity;
-  complex double *fo[1] = {flm};
-  const void *fi[1] = {f};
-  int sp[1] = {spin}, re[1] = {0};
-  oracle_ssht_forward_multi(fo, fi, sp, re, 1, L);
-}
-
-void ssht_core_mw_forward_sov_conv_sym_real(complex double *flm, const double *f, int L,
-                                            ssht_dl_method_t dl_method, int verbosity) {
-  (void)dl_method;
-  (void)verbosity;
-  complex double *fo[1] = {flm};
-  const void *fi[1] = {f};
-  int sp[1] = {0}, re[1] = {1};
-  oracle_ssht_forward_multi(fo, fi, sp, re, 1, L);
-}
-
 /* ------------------------------------------------------------------------ */
 /* Adjoint of the inverse: a_lm = sum_{t,p} f(t,p) conj(sY_lm(t,p))         */
 /* ------------------------------------------------------------------------ */
 
-static void rings_to_H(complex double *H, const complex double *Fm, int L, int s, int mlo) {
-  const int K = 2 * L - 1, n = -s;
+static void rings_to_H(complex double *H, const complex double *Fm, const grid_t *g, int s, int mlo) {
+  const int L = g->L, K = 2 * L - 1, n = -s, nt = g->nt, kt = g->kt;
   memset(H, 0, sizeof(complex double) * (size_t)K * L);
 #pragma omp parallel if (L >= 64)
   {
-  complex double *x = (complex double *)xcalloc(K, sizeof(complex double));
+  complex double *x = (complex double *)xcalloc(kt, sizeof(complex double));
 #pragma omp for schedule(static)
   for (int m = mlo; m <= L - 1; ++m) {
-    const complex double *Fr = Fm + (size_t)(m + L - 1) * L;
-    memset(x, 0, sizeof(complex double) * K);
-    for (int t = 0; t < L; ++t) x[t] = Fr[t];
-    offt_dft(x, K, +1);
+    const complex double *Fr = Fm + (size_t)(m + L - 1) * nt;
+    memset(x, 0, sizeof(complex double) * kt);
+    for (int t = 0; t < nt; ++t) x[t] = Fr[t];
+    offt_dft(x, kt, +1);
     complex double *h = H + (size_t)(m + L - 1) * L;
     double sym = neg1(m + n);
     for (int mp = 0; mp <= L - 1; ++mp) {
-      double a = SPI * mp / K;
-      complex double hp = x[modk(mp, K)] * (cos(a) + I * sin(a));
-      h[mp] = hp;
-      if (mp > 0) {
-        complex double hm = x[modk(-mp, K)] * (cos(-a) + I * sin(-a));
-        h[mp] += sym * hm;
-      }
+      h[mp] = x[modk(mp, kt)] * theta_phase(g, mp);
+      if (mp > 0) h[mp] += sym * x[modk(-mp, kt)] * theta_phase(g, -mp);
     }
   }
   free(x);
@@ -564,21 +578,22 @@ static void rings_to_H(complex double *H, const complex double *Fm, int L, int s
 }
 
 void oracle_ssht_adjoint_inverse_multi(complex double **flm, const void **f, const int *spin,
-                                       const int *real, int njob, int L) {
+                                       const int *real, int njob, int L, int ss) {
+  const grid_t g = grid_of(L, ss);
   const int K = 2 * L - 1;
-  complex double *Fm = (complex double *)xcalloc((size_t)K * L, sizeof(complex double));
+  complex double *Fm = (complex double *)xcalloc((size_t)K * g.nt, sizeof(complex double));
   complex double **H = (complex double **)xcalloc(njob, sizeof(void *));
   int allreal = 1;
   for (int j = 0; j < njob; ++j) allreal &= real[j] != 0;
   for (int j = 0; j < njob; ++j) {
     H[j] = (complex double *)xcalloc((size_t)K * L, sizeof(complex double));
     if (real[j])
-      map_to_rings(Fm, NULL, (const double *)f[j], L);
+      map_to_rings(Fm, NULL, (const double *)f[j], &g);
     else
-      map_to_rings(Fm, (const complex double *)f[j], NULL, L);
-    rings_to_H(H[j], Fm, L, spin[j], real[j] ? 0 : -(L - 1));
+      map_to_rings(Fm, (const complex double *)f[j], NULL, &g);
+    rings_to_H(H[j], Fm, &g, spin[j], real[j] ? 0 : -(L - 1));
   }
-  mm_to_harm(flm, H, spin, njob, L, allreal ? 0 : -(L - 1), 1);
+  mm_to_harm(flm, H, spin, njob, &g, allreal ? 0 : -(L - 1), 1);
   for (int j = 0; j < njob; ++j) {
     if (real[j])
       for (int l = 0; l < L; ++l)
@@ -589,61 +604,39 @@ void oracle_ssht_adjoint_inverse_multi(complex double **flm, const void **f, con
   free(Fm);
 }
 
-void ssht_adjoint_mw_inverse_sov_sym(complex double *flm, const complex double *f, int L,
-                                     int spin, ssht_dl_method_t dl_method, int verbosity) {
-  (void)dl_method;
-  (void)verbosity;
-  complex double *fo[1] = {flm};
-  const void *fi[1] = {f};
-  int sp[1] = {spin}, re[1] = {0};
-  oracle_ssht_adjoint_inverse_multi(fo, fi, sp, re, 1, L);
-}
-
-void ssht_adjoint_mw_inverse_sov_sym_real(complex double *flm, const double *f, int L,
-                                          ssht_dl_method_t dl_method, int verbosity) {
-  (void)dl_method;
-  (void)verbosity;
-  complex double *fo[1] = {flm};
-  const void *fi[1] = {f};
-  int sp[1] = {0}, re[1] = {1};
-  oracle_ssht_adjoint_inverse_multi(fo, fi, sp, re, 1, L);
-}
-
 /* ------------------------------------------------------------------------ */
 /* Adjoint of the forward                                                   */
 /* ------------------------------------------------------------------------ */
 
-static void G_to_map_adj(complex double *fc, double *fr, const complex double *Gs, int L, int s,
-                         int mlo) {
-  const int K = 2 * L - 1, n = -s;
-  complex double *ring = (complex double *)xcalloc((size_t)L * K, sizeof(complex double));
+static void G_to_map_adj(complex double *fc, double *fr, const complex double *Gs, const grid_t *g,
+                         int s, int mlo) {
+  const int L = g->L, K = 2 * L - 1, n = -s, nt = g->nt, np = g->np, kt = g->kt;
+  complex double *ring = (complex double *)xcalloc((size_t)nt * np, sizeof(complex double));
 #pragma omp parallel if (L >= 64)
   {
   conv_plan *cp = get_conv(L);
   complex double *Gf = (complex double *)xcalloc(K, sizeof(complex double));
   complex double *Fh = (complex double *)xcalloc(K, sizeof(complex double));
-  complex double *x = (complex double *)xcalloc(K, sizeof(complex double));
+  complex double *x = (complex double *)xcalloc(kt, sizeof(complex double));
   complex double *scr = (complex double *)xcalloc(cp->P, sizeof(complex double));
 #pragma omp for schedule(static)
   for (int m = mlo; m <= L - 1; ++m) {
-    const complex double *g = Gs + (size_t)(m + L - 1) * L;
+    const complex double *gr = Gs + (size_t)(m + L - 1) * L;
     double sym = neg1(m + n);
     for (int mp = 0; mp <= L - 1; ++mp) {
-      Gf[mp + L - 1] = g[mp];
-      if (mp > 0) Gf[-mp + L - 1] = sym * g[mp];
+      Gf[mp + L - 1] = gr[mp];
+      if (mp > 0) Gf[-mp + L - 1] = sym * gr[mp];
     }
     wconv(Fh, Gf, L, 1, scr);
-    memset(x, 0, sizeof(complex double) * K);
-    for (int mp = -(L - 1); mp <= L - 1; ++mp) {
-      double a = SPI * mp / K;
-      x[modk(mp, K)] += Fh[mp + L - 1] * (cos(a) + I * sin(a));
-    }
-    offt_dft(x, K, +1); /* x[k] = F_ext*(k) */
+    memset(x, 0, sizeof(complex double) * kt);
+    for (int mp = -(L - 1); mp <= L - 1; ++mp) x[modk(mp, kt)] += Fh[mp + L - 1] * theta_phase(g, mp);
+    offt_dft(x, kt, +1); /* x[k] = adjoint of the theta DFT at circle position k */
     double eps = neg1(m + s);
-    for (int t = 0; t < L; ++t) {
+    for (int t = 0; t < nt; ++t) {
       complex double v = x[t];
-      if (t < L - 1) v += eps * x[K - 1 - t];
-      ring[(size_t)t * K + modk(m, K)] = v;
+      const int mt = mirror_of(g, t);
+      if (mt >= 0) v += eps * x[mt];
+      ring[(size_t)t * np + modk(m, np)] = v;
     }
   }
   free(Gf);
@@ -652,79 +645,147 @@ static void G_to_map_adj(complex double *fc, double *fr, const complex double *G
   free(scr);
   }
 #pragma omp parallel for schedule(static) if (L >= 64)
-  for (int t = 0; t < L; ++t) {
-    complex double *r = ring + (size_t)t * K;
-    offt_dft(r, K, +1);
-    for (int p = 0; p < K; ++p) {
+  for (int t = 0; t < nt; ++t) {
+    complex double *r = ring + (size_t)t * np;
+    offt_dft(r, np, +1);
+    for (int p = 0; p < np; ++p) {
       if (fr)
-        fr[(size_t)t * K + p] = creal(r[p]);
+        fr[(size_t)t * np + p] = creal(r[p]);
       else
-        fc[(size_t)t * K + p] = r[p];
+        fc[(size_t)t * np + p] = r[p];
     }
   }
   free(ring);
 }
 
 void oracle_ssht_adjoint_forward_multi(void **f, const complex double **flm, const int *spin,
-                                       const int *real, int njob, int L) {
+                                       const int *real, int njob, int L, int ss) {
+  const grid_t g = grid_of(L, ss);
   const int K = 2 * L - 1;
   complex double **G = (complex double **)xcalloc(njob, sizeof(void *));
   for (int j = 0; j < njob; ++j) G[j] = (complex double *)xcalloc((size_t)K * L, sizeof(complex double));
   /* the real adjoint is Re of the complex adjoint: all m are needed */
-  harm_to_mm(G, flm, spin, njob, L, -(L - 1), 1);
+  harm_to_mm(G, flm, spin, njob, &g, -(L - 1), 1);
   for (int j = 0; j < njob; ++j) {
     if (real[j])
-      G_to_map_adj(NULL, (double *)f[j], G[j], L, spin[j], -(L - 1));
+      G_to_map_adj(NULL, (double *)f[j], G[j], &g, spin[j], -(L - 1));
     else
-      G_to_map_adj((complex double *)f[j], NULL, G[j], L, spin[j], -(L - 1));
+      G_to_map_adj((complex double *)f[j], NULL, G[j], &g, spin[j], -(L - 1));
     free(G[j]);
   }
   free(G);
 }
 
+/* ------------------------------------------------------------------------ */
+/* Public single-transform entry points (MW and MWSS)                       */
+/* ------------------------------------------------------------------------ */
+
+static void one_inverse(void *f, const complex double *flm, int L, int spin, int real, int ss) {
+  void *fo[1] = {f};
+  const complex double *fi[1] = {flm};
+  int sp[1] = {spin}, re[1] = {real};
+  oracle_ssht_inverse_multi(fo, fi, sp, re, 1, L, ss);
+}
+static void one_forward(complex double *flm, const void *f, int L, int spin, int real, int ss) {
+  complex double *fo[1] = {flm};
+  const void *fi[1] = {f};
+  int sp[1] = {spin}, re[1] = {real};
+  oracle_ssht_forward_multi(fo, fi, sp, re, 1, L, ss);
+}
+static void one_adjoint_inverse(complex double *flm, const void *f, int L, int spin, int real, int ss) {
+  complex double *fo[1] = {flm};
+  const void *fi[1] = {f};
+  int sp[1] = {spin}, re[1] = {real};
+  oracle_ssht_adjoint_inverse_multi(fo, fi, sp, re, 1, L, ss);
+}
+static void one_adjoint_forward(void *f, const complex double *flm, int L, int spin, int real, int ss) {
+  void *fo[1] = {f};
+  const complex double *fi[1] = {flm};
+  int sp[1] = {spin}, re[1] = {real};
+  oracle_ssht_adjoint_forward_multi(fo, fi, sp, re, 1, L, ss);
+}
+
+#define UNUSED_DL (void)dl_method, (void)verbosity
+
+void ssht_core_mw_inverse_sov_sym(complex double *f, const complex double *flm, int L, int spin,
+                                  ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_inverse(f, flm, L, spin, 0, 0);
+}
+void ssht_core_mw_inverse_sov_sym_real(double *f, const complex double *flm, int L,
+                                       ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_inverse(f, flm, L, 0, 1, 0);
+}
+void ssht_core_mw_forward_sov_conv_sym(complex double *flm, const complex double *f, int L,
+                                       int spin, ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_forward(flm, f, L, spin, 0, 0);
+}
+void ssht_core_mw_forward_sov_conv_sym_real(complex double *flm, const double *f, int L,
+                                            ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_forward(flm, f, L, 0, 1, 0);
+}
+void ssht_adjoint_mw_inverse_sov_sym(complex double *flm, const complex double *f, int L,
+                                     int spin, ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_adjoint_inverse(flm, f, L, spin, 0, 0);
+}
+void ssht_adjoint_mw_inverse_sov_sym_real(complex double *flm, const double *f, int L,
+                                          ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_adjoint_inverse(flm, f, L, 0, 1, 0);
+}
 void ssht_adjoint_mw_forward_sov_sym(complex double *f, const complex double *flm, int L,
                                      int spin, ssht_dl_method_t dl_method, int verbosity) {
-  (void)dl_method;
-  (void)verbosity;
-  void *fo[1] = {f};
-  const complex double *fi[1] = {flm};
-  int sp[1] = {spin}, re[1] = {0};
-  oracle_ssht_adjoint_forward_multi(fo, fi, sp, re, 1, L);
+  UNUSED_DL;
+  one_adjoint_forward(f, flm, L, spin, 0, 0);
 }
-
 void ssht_adjoint_mw_forward_sov_sym_real(double *f, const complex double *flm, int L,
                                           ssht_dl_method_t dl_method, int verbosity) {
-  (void)dl_method;
-  (void)verbosity;
-  void *fo[1] = {f};
-  const complex double *fi[1] = {flm};
-  int sp[1] = {0}, re[1] = {1};
-  oracle_ssht_adjoint_forward_multi(fo, fi, sp, re, 1, L);
+  UNUSED_DL;
+  one_adjoint_forward(f, flm, L, 0, 1, 0);
 }
 
-/* ------------------------------------------------------------------------ */
-/* MWSS: not restated                                                       */
-/* ------------------------------------------------------------------------ */
-
-static void mwss_unsupported(const char *fn) {
-  fprintf(stderr, "oracle: %s: MW_SS sampling is not restated in the oracle\n", fn);
-  exit(1);
+/* MWSS: the same operators on the symmetric grid */
+void ssht_core_mw_inverse_sov_sym_ss(complex double *f, const complex double *flm, int L, int spin,
+                                     ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_inverse(f, flm, L, spin, 0, 1);
 }
-#define MWSS_STUB(name, ...)                                                                     \
-  void name(__VA_ARGS__) { mwss_unsupported(#name); }
-MWSS_STUB(ssht_core_mw_forward_sov_conv_sym_ss, complex double *a, const complex double *b, int L,
-          int s, ssht_dl_method_t d, int v)
-MWSS_STUB(ssht_core_mw_forward_sov_conv_sym_ss_real, complex double *a, const double *b, int L,
-          ssht_dl_method_t d, int v)
-MWSS_STUB(ssht_core_mw_inverse_sov_sym_ss, complex double *a, const complex double *b, int L,
-          int s, ssht_dl_method_t d, int v)
-MWSS_STUB(ssht_core_mw_inverse_sov_sym_ss_real, double *a, const complex double *b, int L,
-          ssht_dl_method_t d, int v)
-MWSS_STUB(ssht_adjoint_mw_inverse_sov_sym_ss, complex double *a, const complex double *b, int L,
-          int s, ssht_dl_method_t d, int v)
-MWSS_STUB(ssht_adjoint_mw_inverse_sov_sym_ss_real, complex double *a, const double *b, int L,
-          ssht_dl_method_t d, int v)
-MWSS_STUB(ssht_adjoint_mw_forward_sov_sym_ss, complex double *a, const complex double *b, int L,
-          int s, ssht_dl_method_t d, int v)
-MWSS_STUB(ssht_adjoint_mw_forward_sov_sym_ss_real, double *a, const complex double *b, int L,
-          ssht_dl_method_t d, int v)
+void ssht_core_mw_inverse_sov_sym_ss_real(double *f, const complex double *flm, int L,
+                                          ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_inverse(f, flm, L, 0, 1, 1);
+}
+void ssht_core_mw_forward_sov_conv_sym_ss(complex double *flm, const complex double *f, int L,
+                                          int spin, ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_forward(flm, f, L, spin, 0, 1);
+}
+void ssht_core_mw_forward_sov_conv_sym_ss_real(complex double *flm, const double *f, int L,
+                                               ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_forward(flm, f, L, 0, 1, 1);
+}
+void ssht_adjoint_mw_inverse_sov_sym_ss(complex double *flm, const complex double *f, int L,
+                                        int spin, ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_adjoint_inverse(flm, f, L, spin, 0, 1);
+}
+void ssht_adjoint_mw_inverse_sov_sym_ss_real(complex double *flm, const double *f, int L,
+                                             ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_adjoint_inverse(flm, f, L, 0, 1, 1);
+}
+void ssht_adjoint_mw_forward_sov_sym_ss(complex double *f, const complex double *flm, int L,
+                                        int spin, ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_adjoint_forward(f, flm, L, spin, 0, 1);
+}
+void ssht_adjoint_mw_forward_sov_sym_ss_real(double *f, const complex double *flm, int L,
+                                             ssht_dl_method_t dl_method, int verbosity) {
+  UNUSED_DL;
+  one_adjoint_forward(f, flm, L, 0, 1, 1);
+}

@@ -128,6 +128,7 @@ GPU_SIGNATURES = {
     "s2let_gpu_axisym_wav_hardthreshold_real_noalloc": (I, [V, V, P, I]),
     "s2let_gpu_mw_adjoint_map2alm": (None, [V, V, I, I]),
     "s2let_gpu_mw_adjoint_alm2map": (None, [V, V, I, I]),
+    "s2let_gpu_sht": (I, [I, I, I, I, I, V, V]),
     "s2let_gpu_analysis_px2wav_real_batch": (I, [V, V, V, I, P, V]),
     "s2let_gpu_synthesis_wav2px_real_batch": (I, [V, V, V, I, P, V]),
     "s2let_gpu_analysis_px2wav_batch": (I, [V, V, V, I, P, V]),
@@ -309,6 +310,23 @@ class S2let:
             f = np.ascontiguousarray(f, dtype=np.complex128)
             self.lib.s2let_mw_map2alm(ptr(flm), ptr(f), L, spin)
         return flm
+
+    def sht(self, direction, x, L, spin=0, real=False, sampling=SAMPLING_MW):
+        """s2let_gpu_sht: direction 0 forward (map -> flm), 1 inverse, 2 adjoint
+        of the forward (flm -> map), 3 adjoint of the inverse (map -> flm), on
+        MW or MWSS sampling."""
+        npx = (L + 1) * 2 * L if sampling == SAMPLING_MW_SS else L * (2 * L - 1)
+        fdt = np.float64 if real else np.complex128
+        if direction in (0, 3):
+            f = np.ascontiguousarray(x, dtype=fdt)
+            flm = np.zeros(L * L, np.complex128)
+        else:
+            flm = np.ascontiguousarray(x, dtype=np.complex128)
+            f = np.zeros(npx, fdt)
+        st = self.lib.s2let_gpu_sht(direction, sampling, L, spin, int(real), ptr(f), ptr(flm))
+        if st != 0:
+            raise RuntimeError(f"s2let_gpu_sht failed with status {st}")
+        return flm if direction in (0, 3) else f
 
     # axisymmetric -------------------------------------------------------------
     def axisym_sizes(self, p, multires):

@@ -64,6 +64,7 @@ struct Scale {
 
 struct WavPlan {
   int L = 0, s = 0;
+  int ss = 0;  // sampling: 0 MW, 1 MWSS (rings and ring length per band-limit below)
   bool real = false, axisym = false;
   int bl_scal = 1, scal_lmin = 0;
   std::vector<Scale> sc;
@@ -73,6 +74,8 @@ struct WavPlan {
   int npairs = 0;
   int64_t z_per_map = 0;
   int max_bl = 1, max_nn = 1, max_ng = 1;
+  int nt(int bl) const { return grid_rings(bl, ss); }
+  int K(int bl) const { return grid_ring_len(bl, ss); }
   void release() {
     cudaFree(d_w);
     cudaFree(d_pairs);
@@ -84,7 +87,7 @@ struct WavPlan {
 
 // Inputs of plan construction.
 struct PlanSpec {
-  int L = 0, spin = 0;
+  int L = 0, spin = 0, ss = 0;
   bool real = false, axisym = false;
   int bl_scal = 1, scal_lmin = 0;
   std::vector<int> jrow, bl, Nj;  // per scale: psi row (or axisym kernel row), band-limits
@@ -100,6 +103,7 @@ std::unique_ptr<WavPlan> build_plan(const PlanSpec &ps) {
   auto P = std::make_unique<WavPlan>();
   P->L = ps.L;
   P->s = ps.real ? 0 : ps.spin;
+  P->ss = ps.ss;
   P->real = ps.real;
   P->axisym = ps.axisym;
   P->bl_scal = ps.bl_scal;
@@ -190,19 +194,19 @@ std::unique_ptr<WavPlan> build_plan(const PlanSpec &ps) {
   P->d_pairs = upload(pairs);
   for (auto &sd : P->sc) sd.d_ns = upload(sd.ns);
   // build the Wigner tables and FFT data now, outside the transforms' timing
-  wigner_table(L, std::abs(P->s));
-  wigner_table(ps.bl_scal, 0);
+  wigner_table(L, std::abs(P->s), P->ss);
+  wigner_table(ps.bl_scal, 0, P->ss);
   for (auto &sd : P->sc)
-    for (int n : sd.ns) wigner_table(sd.bl, std::abs(n));
-  ring_fft(2 * L - 1);
-  ring_fft(2 * ps.bl_scal - 1);
-  for (auto &sd : P->sc) ring_fft(2 * sd.bl - 1);
+    for (int n : sd.ns) wigner_table(sd.bl, std::abs(n), P->ss);
+  ring_fft(P->K(L));
+  ring_fft(P->K(ps.bl_scal));
+  for (auto &sd : P->sc) ring_fft(P->K(sd.bl));
   return P;
 }
 
 // standard (tiling from the parameters), cached per parameter set ------------
 struct PlanKey {
-  int L, J_min, N, spin, original_spin, upsample, reality, real, axisym, multires, kernel;
+  int L, J_min, N, spin, original_spin, upsample, reality, real, axisym, multires, kernel, sampling;
   double B;
   bool operator<(const PlanKey &o) const { return std::memcmp(this, &o, sizeof(PlanKey)) < 0; }
 };
@@ -221,6 +225,7 @@ const WavPlan &directional_plan(const s2let_parameters_t &p, bool real) {
   key.reality = p.reality;
   key.real = real;
   key.kernel = current_kernel_type();
+  key.sampling = p.sampling_scheme;
   key.B = p.B;
   std::lock_guard<std::mutex> lk(g_plan_mu);
   auto it = g_plans.find(key);
@@ -238,6 +243,7 @@ const WavPlan &directional_plan(const s2let_parameters_t &p, bool real) {
   PlanSpec ps;
   ps.L = L;
   ps.spin = q.spin;
+  ps.ss = p.sampling_scheme == S2LET_SAMPLING_MW_SS ? 1 : 0;
   ps.real = real;
   ps.bl_scal = g.bl_scal;
   ps.jrow = g.j;
@@ -292,34 +298,34 @@ const WavPlan &axisym_plan(const s2let_parameters_t &p, bool real, bool multires
 }
 
 // ---------------------------------------------------------------------------
-// full-band spin-s spherical-harmonic transforms (MW)
+// full-band spin-s spherical-harmonic transforms (MW or MWSS)
 // ---------------------------------------------------------------------------
 
 struct Sht {
-  int L, s;
+  int L, s, ss;
   bool real;
   const double2 *cl;  // (-1)^s sqrt((2l+1)/4pi), l < L (device)
 };
-Sht sht_of(const WavPlan &P) { return Sht{P.L, P.s, P.real, P.d_w + P.w_cl}; }
+Sht sht_of(const WavPlan &P) { return Sht{P.L, P.s, P.ss, P.real, P.d_w + P.w_cl}; }
 
 // flm (nb x L^2, zero outside the computed range) <- forward transform of maps
 // (or the adjoint of the inverse)
 void sht_forward(const Sht &H, const void *f, int64_t fstride, double2 *flm, int nb, Scratch &S,
                  bool adjoint_of_inverse) {
-  const int L = H.L, s = H.s, K = 2 * L - 1;
+  const int L = H.L, s = H.s, K = grid_ring_len(L, H.ss), nt = grid_rings(L, H.ss);
   const bool real = H.real;
-  const int sw = real ? L : K, mlo = real ? 0 : -(L - 1);
-  double2 *spec = S.get<double2>((int64_t)nb * L * sw);
-  ring_forward(f, K, fstride, L, spec, sw, sw, mlo, nb * L, L, real, S.st);
+  const int sw = real ? L : 2 * L - 1, mlo = real ? 0 : -(L - 1);
+  double2 *spec = S.get<double2>((int64_t)nb * nt * sw);
+  ring_forward(f, K, fstride, nt, spec, sw, sw, mlo, nb * nt, L, H.ss, real, S.st);
   S2G_CUDA(cudaMemsetAsync(flm, 0, sizeof(double2) * nb * L * L, S.st));
   T2L a{};
-  a.tb = &wigner_table(L, std::abs(s));
+  a.tb = &wigner_table(L, std::abs(s), H.ss);
   a.n = -s;
   a.use_q = !adjoint_of_inverse;
   a.mlo = mlo;
   a.mhi = L - 1;
   a.in = spec;
-  a.is = (int64_t)L * sw;
+  a.is = (int64_t)nt * sw;
   a.iw = sw;
   a.imlo = mlo;
   a.w = H.cl;
@@ -334,12 +340,12 @@ void sht_forward(const Sht &H, const void *f, int64_t fstride, double2 *flm, int
 // maps <- inverse transform (or adjoint of the forward) of flm
 void sht_inverse(const Sht &H, const double2 *flm, bool flm_half, void *f, int64_t fstride, int nb,
                  Scratch &S, bool adjoint_of_forward) {
-  const int L = H.L, s = H.s, K = 2 * L - 1;
+  const int L = H.L, s = H.s, K = grid_ring_len(L, H.ss), nt = grid_rings(L, H.ss);
   const bool real = H.real;
-  const int sw = real ? L : K, mlo = real ? 0 : -(L - 1);
-  double2 *spec = S.get<double2>((int64_t)nb * L * sw);
+  const int sw = real ? L : 2 * L - 1, mlo = real ? 0 : -(L - 1);
+  double2 *spec = S.get<double2>((int64_t)nb * nt * sw);
   L2T a{};
-  a.tb = &wigner_table(L, std::abs(s));
+  a.tb = &wigner_table(L, std::abs(s), H.ss);
   a.n = -s;
   a.use_q = adjoint_of_forward;
   a.mlo = mlo;
@@ -352,12 +358,12 @@ void sht_inverse(const Sht &H, const double2 *flm, bool flm_half, void *f, int64
   a.wscale = adjoint_of_forward ? 2.0 * kPi / K : 1.0;
   a.lmin = std::abs(s);
   a.out = spec;
-  a.os = (int64_t)L * sw;
+  a.os = (int64_t)nt * sw;
   a.ow = sw;
   a.omlo = mlo;
   a.nb = nb;
   contract_l2t(a, S.st);
-  ring_inverse(spec, sw, sw, mlo, f, K, fstride, L, nb * L, L, real, S.st);
+  ring_inverse(spec, sw, sw, mlo, f, K, fstride, nt, nb * nt, L, H.ss, real, S.st);
 }
 
 // ---------------------------------------------------------------------------
@@ -386,11 +392,11 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
   const bool adj = (mode == SPLIT_SYNTH_ADJ);
   // scaling function: spin-0 transform at bl_scal
   {
-    const int bs = P.bl_scal, Ks = 2 * bs - 1;
-    const int sw = real ? bs : Ks, mlo = real ? 0 : -(bs - 1);
-    double2 *spec = S.get<double2>((int64_t)nb * bs * sw);
+    const int bs = P.bl_scal, Ks = P.K(bs), nts = P.nt(bs);
+    const int sw = real ? bs : 2 * bs - 1, mlo = real ? 0 : -(bs - 1);
+    double2 *spec = S.get<double2>((int64_t)nb * nts * sw);
     L2T a{};
-    a.tb = &wigner_table(bs, 0);
+    a.tb = &wigner_table(bs, 0, P.ss);
     a.n = 0;
     a.use_q = adj;
     a.mlo = mlo;
@@ -403,23 +409,25 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
     a.wscale = adj ? 2.0 * kPi / Ks : 1.0;
     a.lmin = P.scal_lmin;
     a.out = spec;
-    a.os = (int64_t)bs * sw;
+    a.os = (int64_t)nts * sw;
     a.ow = sw;
     a.omlo = mlo;
     a.nb = nb;
     contract_l2t(a, S.st);
-    ring_inverse(spec, sw, sw, mlo, f_scal, Ks, sstride, bs, nb * bs, bs, real, S.st);
+    ring_inverse(spec, sw, sw, mlo, f_scal, Ks, sstride, nts, nb * nts, bs, P.ss, real, S.st);
   }
-  const int64_t Wmax = 2 * P.max_bl - 1;
-  const int64_t gsz = (int64_t)nb * P.max_nn * P.max_bl * Wmax;
+  // G buffers [b][n][t][m] (spectral width W = 2bl-1), ring buffers [b][n or g][t][p]
+  const int64_t Wmax = 2 * P.max_bl - 1, Kmax = 2 * P.max_bl, ntmax = P.nt(P.max_bl);
+  const int64_t gsz = (int64_t)nb * P.max_nn * ntmax * Wmax;
   double2 *Gbuf = S.get<double2>(2 * gsz);
-  double2 *spec = S.get<double2>((int64_t)nb * P.max_ng * P.max_bl * Wmax);
+  double2 *spec = S.get<double2>((int64_t)nb * std::max(P.max_ng, P.max_nn) * ntmax * Kmax);
   for (size_t k0 = 0; k0 < P.sc.size();) {
     // scales sharing band-limit and directions share each table pass
     size_t k1 = k0 + 1;
     if (k1 < P.sc.size() && P.sc[k1].bl == P.sc[k0].bl && P.sc[k1].ns == P.sc[k0].ns) ++k1;
     const int ngrp = (int)(k1 - k0);
     const int bl = P.sc[k0].bl, W = 2 * bl - 1, nn = (int)P.sc[k0].ns.size();
+    const int nt = P.nt(bl), K = P.K(bl);
     for (int i = 0; i < nn; ++i) {
       L2T grp[2];
       for (int q = 0; q < ngrp; ++q) {
@@ -427,7 +435,7 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
         const int n = sd.ns[i];
         L2T &a = grp[q];
         a = L2T{};
-        a.tb = &wigner_table(bl, std::abs(n));
+        a.tb = &wigner_table(bl, std::abs(n), P.ss);
         a.n = n;
         a.use_q = adj;
         a.mlo = (real && n == 0) ? 0 : -(bl - 1);
@@ -438,14 +446,14 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
         a.x_half = flm_half;
         if (P.axisym) {
           a.w = P.d_w + sd.w_axi;
-          a.wscale = adj ? 2.0 * kPi / W * kSqrt2Pi : 1.0 / kSqrt2Pi;
+          a.wscale = adj ? 2.0 * kPi / K * kSqrt2Pi : 1.0 / kSqrt2Pi;
         } else {
           a.w = P.d_w + sd.w_split[i];
-          a.wscale = adj ? 4.0 * kPi * kPi / W : 1.0;
+          a.wscale = adj ? 4.0 * kPi * kPi / K : 1.0;
         }
         a.lmin = std::max((real || P.axisym) ? 0 : std::abs(P.s), sd.lsup_split[i]);
-        a.out = Gbuf + q * gsz + (int64_t)i * bl * W;
-        a.os = (int64_t)nn * bl * W;
+        a.out = Gbuf + q * gsz + (int64_t)i * nt * W;
+        a.os = (int64_t)nn * nt * W;
         a.ow = W;
         a.omlo = -(bl - 1);
         a.nb = nb;
@@ -462,15 +470,15 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
         // F_n(t, p) = sum_m G_n(t, m) e^{i m phi_p}; spec holds F[b][i][t][p]
         for (int i = 0; i < nn; ++i) {
           const bool herm = real && sd.ns[i] == 0;  // real signal, n = 0: only m >= 0 computed
-          ring_inverse_c(Gq + (int64_t)i * bl * W + (herm ? bl - 1 : 0), W, (int64_t)nn * bl * W, bl,
-                         herm ? bl : W, herm ? 0 : -(bl - 1), herm, spec + (int64_t)i * bl * W, W,
-                         (int64_t)nn * bl * W, bl, nb * bl, bl, S.st);
+          ring_inverse_c(Gq + (int64_t)i * nt * W + (herm ? bl - 1 : 0), W, (int64_t)nn * nt * W, nt,
+                         herm ? bl : W, herm ? 0 : -(bl - 1), herm, spec + (int64_t)i * nt * K, K,
+                         (int64_t)nn * nt * K, nt, nb * nt, bl, P.ss, S.st);
         }
-        gamma_px_synthesis(spec, out, wstride, sd.d_ns, nn, ng, bl, nb, real, c, S.st);
+        gamma_px_synthesis(spec, out, wstride, sd.d_ns, nn, ng, bl, P.ss, nb, real, c, S.st);
       } else {
         const int sw = real ? bl : W, mlo = real ? 0 : -(bl - 1);
-        gamma_synthesis(Gq, spec, sd.d_ns, nn, ng, bl, nb, real, c, S.st);
-        ring_inverse(spec, sw, sw, mlo, out, W, wstride, ng * bl, nb * ng * bl, bl, real, S.st);
+        gamma_synthesis(Gq, spec, sd.d_ns, nn, ng, bl, P.ss, nb, real, c, S.st);
+        ring_inverse(spec, sw, sw, mlo, out, K, wstride, ng * nt, nb * ng * nt, bl, P.ss, real, S.st);
       }
     }
     k0 = k1;
@@ -486,21 +494,21 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
   const size_t esz = real ? sizeof(double) : sizeof(double2);
   const bool adj = (mode == MERGE_ANALYSIS_ADJ);
   double2 *z = S.get<double2>((int64_t)nb * std::max<int64_t>(1, P.z_per_map));
-  const int bs = P.bl_scal, Ks = 2 * bs - 1;
+  const int bs = P.bl_scal, Ks = P.K(bs), nts = P.nt(bs);
   double2 *zs = S.get<double2>((int64_t)nb * bs * bs);
   {
-    const int sw = real ? bs : Ks, mlo = real ? 0 : -(bs - 1);
-    double2 *spec = S.get<double2>((int64_t)nb * bs * sw);
-    ring_forward(f_scal, Ks, sstride, bs, spec, sw, sw, mlo, nb * bs, bs, real, S.st);
+    const int sw = real ? bs : 2 * bs - 1, mlo = real ? 0 : -(bs - 1);
+    double2 *spec = S.get<double2>((int64_t)nb * nts * sw);
+    ring_forward(f_scal, Ks, sstride, nts, spec, sw, sw, mlo, nb * nts, bs, P.ss, real, S.st);
     if (P.scal_lmin > 0) S2G_CUDA(cudaMemsetAsync(zs, 0, sizeof(double2) * nb * bs * bs, S.st));
     T2L a{};
-    a.tb = &wigner_table(bs, 0);
+    a.tb = &wigner_table(bs, 0, P.ss);
     a.n = 0;
     a.use_q = !adj;
     a.mlo = mlo;
     a.mhi = bs - 1;
     a.in = spec;
-    a.is = (int64_t)bs * sw;
+    a.is = (int64_t)nts * sw;
     a.iw = sw;
     a.imlo = mlo;
     a.w = P.d_w + P.w_phi;
@@ -511,15 +519,16 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
     a.nb = nb;
     contract_t2l(a, S.st);
   }
-  const int64_t Wmax = 2 * P.max_bl - 1;
-  const int64_t gsz = (int64_t)nb * P.max_nn * P.max_bl * Wmax;
+  const int64_t Wmax = 2 * P.max_bl - 1, Kmax = 2 * P.max_bl, ntmax = P.nt(P.max_bl);
+  const int64_t gsz = (int64_t)nb * P.max_nn * ntmax * Wmax;
   double2 *Gbuf = S.get<double2>(2 * gsz);
-  double2 *spec = S.get<double2>((int64_t)nb * P.max_ng * P.max_bl * Wmax);
+  double2 *spec = S.get<double2>((int64_t)nb * std::max(P.max_ng, P.max_nn) * ntmax * Kmax);
   for (size_t k0 = 0; k0 < P.sc.size();) {
     size_t k1 = k0 + 1;
     if (k1 < P.sc.size() && P.sc[k1].bl == P.sc[k0].bl && P.sc[k1].ns == P.sc[k0].ns) ++k1;
     const int ngrp = (int)(k1 - k0);
     const int bl = P.sc[k0].bl, W = 2 * bl - 1, nn = (int)P.sc[k0].ns.size();
+    const int nt = P.nt(bl), K = P.K(bl);
     const int sw = real ? bl : W, mlo = real ? 0 : -(bl - 1);
     for (int q = 0; q < ngrp; ++q) {
       const Scale &sd = P.sc[k0 + q];
@@ -529,13 +538,13 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
       double2 *Gq = Gbuf + q * gsz;
       if (rings_on_n(P, sd)) {
         // F_n(t, p) = c sum_g e^{-i n gamma_g} f_g(t, p), then one DFT per (n, t)
-        gamma_px_analysis(in, wstride, spec, sd.d_ns, nn, ng, bl, nb, real, c, S.st);
+        gamma_px_analysis(in, wstride, spec, sd.d_ns, nn, ng, bl, P.ss, nb, real, c, S.st);
         for (int i = 0; i < nn; ++i)
-          ring_forward_c(spec + (int64_t)i * bl * W, W, (int64_t)nn * bl * W, bl, Gq + (int64_t)i * bl * W, W,
-                         (int64_t)nn * bl * W, bl, W, -(bl - 1), nb * bl, bl, S.st);
+          ring_forward_c(spec + (int64_t)i * nt * K, K, (int64_t)nn * nt * K, nt, Gq + (int64_t)i * nt * W, W,
+                         (int64_t)nn * nt * W, nt, W, -(bl - 1), nb * nt, bl, P.ss, S.st);
       } else {
-        ring_forward(in, W, wstride, ng * bl, spec, sw, sw, mlo, nb * ng * bl, bl, real, S.st);
-        gamma_analysis(spec, Gq, sd.d_ns, nn, ng, bl, nb, real, c, S.st);
+        ring_forward(in, K, wstride, ng * nt, spec, sw, sw, mlo, nb * ng * nt, bl, P.ss, real, S.st);
+        gamma_analysis(spec, Gq, sd.d_ns, nn, ng, bl, P.ss, nb, real, c, S.st);
       }
     }
     for (int i = 0; i < nn; ++i) {
@@ -545,22 +554,22 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
         const int n = sd.ns[i];
         T2L &a = grp[q];
         a = T2L{};
-        a.tb = &wigner_table(bl, std::abs(n));
+        a.tb = &wigner_table(bl, std::abs(n), P.ss);
         a.n = n;
         a.use_q = !adj;
         a.mlo = (real && n == 0) ? 0 : -(bl - 1);
         a.mhi = bl - 1;
-        a.in = Gbuf + q * gsz + (int64_t)i * bl * W;
-        a.is = (int64_t)nn * bl * W;
+        a.in = Gbuf + q * gsz + (int64_t)i * nt * W;
+        a.is = (int64_t)nn * nt * W;
         a.iw = W;
         a.imlo = -(bl - 1);
         if (P.axisym) {
           a.w = P.d_w + sd.w_axi;
-          a.wscale = adj ? 1.0 / kSqrt2Pi : 2.0 * kPi / W * kSqrt2Pi;
+          a.wscale = adj ? 1.0 / kSqrt2Pi : 2.0 * kPi / K * kSqrt2Pi;
           a.lmin = sd.lsup_merge[i];
         } else {
           a.w = nullptr;
-          a.wscale = adj ? 1.0 : 4.0 * kPi * kPi / W;
+          a.wscale = adj ? 1.0 : 4.0 * kPi * kPi / K;
           a.lmin = std::max(real ? 0 : std::abs(P.s), sd.lsup_merge[i]);
         }
         a.y = z + sd.z_off[i];
@@ -647,7 +656,7 @@ void run_plan(Op op, const WavPlan &P, void *px, void *lm, void *wav, int64_t nw
   Scratch S(st);
   const int L = P.L;
   const bool real = P.real;
-  const int64_t npx = (int64_t)L * (2 * L - 1);
+  const int64_t npx = (int64_t)P.nt(L) * P.K(L);
   const bool lm_api = (op == OP_LM2WAV || op == OP_WAV2LM || op == OP_ADJ_WAV2LM || op == OP_ADJ_LM2WAV);
   double2 *flm = lm_api ? (double2 *)lm : S.get<double2>((int64_t)nb * L * L);
   switch (op) {
@@ -691,17 +700,18 @@ void run_directional(Op op, const s2let_parameters_t &p, bool real, void *px, vo
   run_plan(op, P, px, lm, wav, s2let_n_wav(&p), scal, s2let_n_scal(&p), nb, st);
 }
 
-// Plain MW spherical-harmonic transform on device buffers.
-// dir: 0 forward (map -> flm), 1 inverse, 2 adjoint of forward (flm -> map),
-// 3 adjoint of inverse (map -> flm).  Real signals: flm returned complete.
-void run_sht(int dir, int L, int spin, bool real, void *f, double2 *flm, int nb, cudaStream_t st) {
+// Plain spherical-harmonic transform on device buffers, MW (ss = 0) or MWSS
+// (ss = 1) sampling.  dir: 0 forward (map -> flm), 1 inverse, 2 adjoint of
+// forward (flm -> map), 3 adjoint of inverse (map -> flm).  Real signals: flm
+// returned complete.
+void run_sht(int dir, int L, int spin, bool real, int ss, void *f, double2 *flm, int nb, cudaStream_t st) {
   S2G_REQUIRE(L >= 1 && L <= 8192, ERR_INVALID, "L must lie in [1, 8192]");
   S2G_REQUIRE(std::abs(spin) < L, ERR_INVALID, "|spin| must be < L");
   if (real) S2G_REQUIRE(spin == 0, ERR_INVALID, "real signals are spin 0");
   Scratch S(st);
-  const Sht H{L, real ? 0 : spin, real, cl_weights(L, real ? 0 : spin)};
-  wigner_table(L, std::abs(H.s));
-  const int64_t npx = (int64_t)L * (2 * L - 1);
+  const Sht H{L, real ? 0 : spin, ss, real, cl_weights(L, real ? 0 : spin)};
+  wigner_table(L, std::abs(H.s), ss);
+  const int64_t npx = (int64_t)grid_rings(L, ss) * grid_ring_len(L, ss);
   if (dir == 0 || dir == 3) {
     sht_forward(H, f, npx, flm, nb, S, dir == 3);
     if (real) symmetrize_flm(flm, L, (int64_t)L * L, nb, st);
@@ -729,7 +739,7 @@ int host_directional(const char *fn, s2g::Op op, const s2let_parameters_t *p, bo
     s2g::Scratch S(st);
     s2g::Staged io(S);
     const int L = p->L;
-    const int64_t npx = (int64_t)L * (2 * L - 1), ns = s2let_n_scal(p);
+    const int64_t npx = s2let_n_px(p), ns = s2let_n_scal(p);
     // the transforms advance scale offsets with N_j; when some N_j < N the end of
     // the s2let_n_wav-sized buffer is never touched (src/c/s2let_analysis.c:340-350),
     // so only the used prefix crosses the bus
@@ -763,13 +773,13 @@ int host_directional(const char *fn, s2g::Op op, const s2let_parameters_t *p, bo
   });
 }
 
-void host_sht(const char *fn, int dir, int L, int spin, bool real, void *f, void *flm) {
+void host_sht(const char *fn, int dir, int L, int spin, bool real, void *f, void *flm, int ss = 0) {
   s2g::guarded(fn, [&] {
     s2g::ensure_device();
     cudaStream_t st = s2g::host_stream();
     s2g::Scratch S(st);
     s2g::Staged io(S);
-    const int64_t npx = (int64_t)L * (2 * L - 1) * (real ? 1 : 2);
+    const int64_t npx = (int64_t)s2g::grid_rings(L, ss) * s2g::grid_ring_len(L, ss) * (real ? 1 : 2);
     void *df;
     double2 *dlm;
     if (dir == 0 || dir == 3) {
@@ -779,7 +789,7 @@ void host_sht(const char *fn, int dir, int L, int spin, bool real, void *f, void
       dlm = io.in<double2>(flm, (int64_t)L * L);
       df = io.out<double>(f, npx);
     }
-    s2g::run_sht(dir, L, spin, real, df, dlm, 1, st);
+    s2g::run_sht(dir, L, spin, real, ss, df, dlm, 1, st);
     io.finish();
   });
 }
@@ -1066,6 +1076,22 @@ void s2let_gpu_mw_adjoint_map2alm(cplx *f, const cplx *flm, int L, int spin) {
 }
 void s2let_gpu_mw_adjoint_alm2map(cplx *flm, const cplx *f, int L, int spin) {
   host_sht(__func__, 3, L, spin, false, (void *)f, flm);
+}
+// Plain transforms on either sampling (the SSHT entry points that the wavelet
+// transforms call, MW or MWSS), host buffers.
+int s2let_gpu_sht(int dir, int sampling_scheme, int L, int spin, int real, void *f, void *flm) {
+  if (sampling_scheme != S2LET_SAMPLING_MW && sampling_scheme != S2LET_SAMPLING_MW_SS) {
+    s2g::set_status(s2g::ERR_UNSUPPORTED, "s2let_gpu_sht: unknown sampling scheme");
+    s2g::report_failure();
+    return s2g::ERR_UNSUPPORTED;
+  }
+  if (dir < 0 || dir > 3 || f == nullptr || flm == nullptr) {
+    s2g::set_status(s2g::ERR_INVALID, "s2let_gpu_sht: bad direction or NULL buffer");
+    s2g::report_failure();
+    return s2g::ERR_INVALID;
+  }
+  host_sht(__func__, dir, L, spin, real != 0, f, flm, sampling_scheme == S2LET_SAMPLING_MW_SS);
+  return s2g::last_status();
 }
 
 // ---- batched device-pointer extensions

@@ -204,6 +204,7 @@ Layout make_layout(const s2let_parameters_t &p, bool real) {
     s.N = Nj;
     s.reality = real ? 1 : p.reality;
     s.n_mode_odd = (p.N % 2) ? 0 : 1;
+    s.mwss = p.sampling_scheme == S2LET_SAMPLING_MW_SS ? 1 : 0;
     g.j.push_back(j);
     g.bl.push_back(bl);
     g.Nj.push_back(Nj);
@@ -243,7 +244,7 @@ void axisym_kernels(double *wav_lm, double *scal_lm, const s2let_parameters_t &p
   for (int l = 0; l < L; l++) scal_lm[l] = sqrt((2 * l + 1) / (4.0 * kPi)) * kappa0[l];
 }
 
-void validate(const s2let_parameters_t *p, bool need_mw) {
+void validate(const s2let_parameters_t *p, bool check_sampling) {
   S2G_REQUIRE(p != nullptr, ERR_INVALID, "parameters is NULL");
   S2G_REQUIRE(p->L >= 1, ERR_INVALID, "L must be >= 1");
   S2G_REQUIRE(p->L <= 8192, ERR_INVALID, "L must be <= 8192");
@@ -251,9 +252,10 @@ void validate(const s2let_parameters_t *p, bool need_mw) {
   S2G_REQUIRE(p->B > 1.0, ERR_INVALID, "B must be > 1");
   S2G_REQUIRE(std::abs(p->spin) < p->L, ERR_INVALID, "|spin| must be < L");
   S2G_REQUIRE(p->J_min >= 0 && p->J_min <= j_max(*p), ERR_INVALID, "J_min must lie in [0, J]");
-  if (need_mw)
-    S2G_REQUIRE(p->sampling_scheme == S2LET_SAMPLING_MW, ERR_UNSUPPORTED,
-                "only S2LET_SAMPLING_MW is implemented on the GPU");
+  // src/c/s2let_analysis.c:231-246: MW and MWSS, anything else is an error
+  if (check_sampling)
+    S2G_REQUIRE(p->sampling_scheme == S2LET_SAMPLING_MW || p->sampling_scheme == S2LET_SAMPLING_MW_SS,
+                ERR_UNSUPPORTED, "Sampling scheme not supported.");
 }
 
 }  // namespace s2g

@@ -16,9 +16,10 @@ using cplx = std::complex<double>;
 // Wigner-space storage of one scale: the SO3 "compact, n negative first" layout
 // (n >= 0 only for real signals) that s2let_analysis_lm2lmn writes.
 struct SO3Shape {
-  int L = 0, N = 0, reality = 0, n_mode_odd = 0;
+  int L = 0, N = 0, reality = 0, n_mode_odd = 0, mwss = 0;
   int64_t flmn_size() const;
-  int64_t f_size() const { return (int64_t)(2 * N - 1) * L * (2 * L - 1); }
+  // (2N-1) gamma samples times the (alpha, beta) grid of the MW / MWSS sampling
+  int64_t f_size() const { return (int64_t)(2 * N - 1) * (mwss ? (int64_t)2 * L * (L + 1) : (int64_t)L * (2 * L - 1)); }
   int64_t index(int l, int m, int n) const;       // complex storage
   int64_t index_real(int l, int m, int n) const;  // n >= 0 storage
 };
@@ -46,7 +47,9 @@ void axisym_kernels(double *wav_lm, double *scal_lm, const s2let_parameters_t &p
 int j_max(const s2let_parameters_t &p);
 int bandlimit(int j, const s2let_parameters_t &p);
 
-// Validation shared by every entry point; throws s2g::Error.
-void validate(const s2let_parameters_t *p, bool need_mw = true);
+// Validation shared by every entry point; throws s2g::Error.  check_sampling:
+// the sampling scheme must be MW or MWSS (the entry points whose reference
+// counterpart reads it).
+void validate(const s2let_parameters_t *p, bool check_sampling = true);
 
 }  // namespace s2g

@@ -1,7 +1,7 @@
 // Transform kernels, FP64 path.
 //
-//  k_ring      batched Bluestein DFT of MW rings (length 2bl-1, odd) in shared
-//              memory: chirp premultiply, radix-2 DIT FFT of the padded length,
+//  k_ring      batched Bluestein DFT of rings (length 2bl-1 on MW, 2bl on MWSS
+//              sampling) in shared memory: chirp premultiply, radix-2 DIT FFT of the padded length,
 //              pointwise multiply by the chirp-kernel spectrum, DIF inverse FFT,
 //              chirp postmultiply.  Two real rings share one complex FFT.
 //  k_contract  per-m Legendre/Wigner contraction against the cached d-tables,
@@ -520,7 +520,7 @@ __device__ __forceinline__ TableRef table_ref(int mlo_table, int n, int m) {
 struct ContractArgs {
   const double *table;
   const int64_t *off;
-  int bl, an, tmlo, n, mlo, lmin;
+  int bl, nt, an, tmlo, n, mlo, lmin;  // nt: theta samples of the table
   const double2 *w;
   double wscale;
   int wconj;
@@ -563,9 +563,10 @@ __global__ void __launch_bounds__(CT_M) k_contract(ContractArgs a) {
   const int r = threadIdx.x;
   // rows of this CTA
   const int row0 = blockIdx.y * CT_M;
-  const int rows_total = L2T ? bl : (bl - lst);
+  const int nt = a.nt;
+  const int rows_total = L2T ? nt : (bl - lst);
   if (row0 >= rows_total) return;
-  const int kbeg = L2T ? lst : 0, kend = bl;  // reduction range (l for L2T, t for T2L)
+  const int kbeg = L2T ? lst : 0, kend = L2T ? bl : nt;  // reduction range (l for L2T, t for T2L)
 
   double2 acc[NBT];
 #pragma unroll
@@ -603,7 +604,7 @@ __global__ void __launch_bounds__(CT_M) k_contract(ContractArgs a) {
           if (MODE == 0)
             v = T[(int64_t)row * nl + (k - l0)];
           else
-            v = T[(int64_t)(lst + row - l0) * bl + k];
+            v = T[(int64_t)(lst + row - l0) * nt + k];
         }
         sA[rr][kk] = v;
       }
@@ -616,7 +617,7 @@ __global__ void __launch_bounds__(CT_M) k_contract(ContractArgs a) {
         double v = 0.0;
         if (row < rows_total && k < kend) {
           if (MODE == 1)
-            v = T[(int64_t)(k - l0) * bl + row];
+            v = T[(int64_t)(k - l0) * nt + row];
           else
             v = T[(int64_t)k * nl + (lst + row - l0)];
         }
@@ -661,9 +662,9 @@ void contract_work(const ContractArgs &a, int nm, double *flops, double *bytes) 
     const int l0 = am > a.an ? am : a.an, lst = l0 > a.lmin ? l0 : a.lmin;
     const int nl = a.bl - lst;
     if (nl <= 0) continue;
-    macs += (double)nl * a.bl;
-    tab += (double)nl * a.bl;
-    io += (double)nl + a.bl;
+    macs += (double)nl * a.nt;
+    tab += (double)nl * a.nt;
+    io += (double)nl + a.nt;
   }
   *flops = 4.0 * macs * a.nb;
   *bytes = 8.0 * tab + 16.0 * io * a.nb;
@@ -695,7 +696,7 @@ constexpr int kMaxGammaTw = 512;
 // NN = number of n values (compile time, so that the per-n values live in registers)
 template <int NN>
 __global__ void k_gamma_synth(const double2 *__restrict__ G, double2 *__restrict__ spec,
-                              const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+                              const int *__restrict__ ns, int ng, int bl, int nt, int nb, int real, double c) {
   __shared__ double2 tw[kMaxGammaTw];  // tw[g * NN + k]
   for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
     const int g = i / NN, k = i % NN;
@@ -706,26 +707,26 @@ __global__ void k_gamma_synth(const double2 *__restrict__ G, double2 *__restrict
   __syncthreads();
   const int W = 2 * bl - 1;
   const int sw = real ? bl : W, smlo = real ? 0 : -(bl - 1);
-  const int64_t total = (int64_t)nb * bl * sw;
+  const int64_t total = (int64_t)nb * nt * sw;
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const int col = (int)(gid % sw);
-  const int t = (int)((gid / sw) % bl);
-  const int b = (int)(gid / ((int64_t)sw * bl));
+  const int t = (int)((gid / sw) % nt);
+  const int b = (int)(gid / ((int64_t)sw * nt));
   const int m = smlo + col;
-  const int64_t gb = (int64_t)b * NN * bl * W;
+  const int64_t gb = (int64_t)b * NN * nt * W;
   // real signals: the -n term is conj of G_n at -m, folded in as
   // e G_n(m) + conj(e) conj(G_n(-m)) = e.re (G + H) + i e.im (G - H),  H = conj(G_n(-m))
   double2 S[NN], D[NN];
 #pragma unroll
   for (int k = 0; k < NN; ++k) {
-    const double2 *Gk = G + gb + (int64_t)k * bl * W + (int64_t)t * W;
+    const double2 *Gk = G + gb + (int64_t)k * nt * W + (int64_t)t * W;
     const double2 gv = Gk[m + bl - 1];
     const double2 gm = (real && ns[k] > 0) ? conj2(Gk[-m + bl - 1]) : make_double2(0.0, 0.0);
     S[k] = add2(gv, gm);
     D[k] = sub2(gv, gm);
   }
-  double2 *out = spec + (int64_t)b * ng * bl * sw + (int64_t)t * sw + col;
+  double2 *out = spec + (int64_t)b * ng * nt * sw + (int64_t)t * sw + col;
   for (int g = 0; g < ng; ++g) {
     double2 acc = make_double2(0.0, 0.0);
 #pragma unroll
@@ -735,13 +736,13 @@ __global__ void k_gamma_synth(const double2 *__restrict__ G, double2 *__restrict
       acc.x = fma(e.x, S[k].x, fma(-e.y, D[k].y, acc.x));
       acc.y = fma(e.x, S[k].y, fma(e.y, D[k].x, acc.y));
     }
-    out[(int64_t)g * bl * sw] = scl2(acc, c);
+    out[(int64_t)g * nt * sw] = scl2(acc, c);
   }
 }
 
 template <int NN>
 __global__ void k_gamma_anal(const double2 *__restrict__ spec, double2 *__restrict__ G,
-                             const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+                             const int *__restrict__ ns, int ng, int bl, int nt, int nb, int real, double c) {
   __shared__ double2 tw[kMaxGammaTw];  // tw[g * NN + k] = e^{-i n_k gamma_g}
   for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
     const int g = i / NN, k = i % NN;
@@ -752,18 +753,18 @@ __global__ void k_gamma_anal(const double2 *__restrict__ spec, double2 *__restri
   __syncthreads();
   const int W = 2 * bl - 1;
   const int sw = real ? bl : W, smlo = real ? 0 : -(bl - 1);
-  const int64_t total = (int64_t)nb * bl * W;
+  const int64_t total = (int64_t)nb * nt * W;
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const int col = (int)(gid % W);
-  const int t = (int)((gid / W) % bl);
-  const int b = (int)(gid / ((int64_t)W * bl));
+  const int t = (int)((gid / W) % nt);
+  const int b = (int)(gid / ((int64_t)W * nt));
   const int m = col - (bl - 1);
   double2 acc[NN];
 #pragma unroll
   for (int k = 0; k < NN; ++k) acc[k] = make_double2(0.0, 0.0);
-  const double2 *sg = spec + (int64_t)b * ng * bl * sw + (int64_t)t * sw;
-  for (int g = 0; g < ng; ++g, sg += (int64_t)bl * sw) {
+  const double2 *sg = spec + (int64_t)b * ng * nt * sw + (int64_t)t * sw;
+  for (int g = 0; g < ng; ++g, sg += (int64_t)nt * sw) {
     double2 s;
     if (real)
       s = m >= 0 ? sg[m] : conj2(sg[-m]);
@@ -777,7 +778,7 @@ __global__ void k_gamma_anal(const double2 *__restrict__ spec, double2 *__restri
     }
   }
 #pragma unroll
-  for (int k = 0; k < NN; ++k) G[((int64_t)b * NN + k) * bl * W + (int64_t)t * W + col] = scl2(acc[k], c);
+  for (int k = 0; k < NN; ++k) G[((int64_t)b * NN + k) * nt * W + (int64_t)t * W + col] = scl2(acc[k], c);
 }
 
 // gamma DFT on pixels: between the n-components F_n(t, p) (complex, one ring
@@ -789,7 +790,7 @@ __global__ void k_gamma_anal(const double2 *__restrict__ spec, double2 *__restri
 //   analysis:  F_n = c sum_g e^{-i n gamma_g} f_g
 template <int NN>
 __global__ void k_gamma_px_synth(const double2 *__restrict__ F, void *__restrict__ out, int64_t out_ms,
-                                 const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+                                 const int *__restrict__ ns, int ng, int64_t npx, int nb, int real, double c) {
   __shared__ double2 tw[kMaxGammaTw];  // tw[g * NN + k] = e^{i n_k gamma_g} (x2 for n_k > 0, real)
   for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
     const int g = i / NN, k = i % NN;
@@ -799,8 +800,6 @@ __global__ void k_gamma_px_synth(const double2 *__restrict__ F, void *__restrict
     tw[i] = make_double2(f * cs, f * sn);
   }
   __syncthreads();
-  const int K = 2 * bl - 1;
-  const int64_t npx = (int64_t)bl * K;
   const int64_t total = (int64_t)nb * npx;
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
@@ -827,7 +826,7 @@ __global__ void k_gamma_px_synth(const double2 *__restrict__ F, void *__restrict
 
 template <int NN>
 __global__ void k_gamma_px_anal(const void *__restrict__ in, int64_t in_ms, double2 *__restrict__ F,
-                                const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+                                const int *__restrict__ ns, int ng, int64_t npx, int nb, int real, double c) {
   __shared__ double2 tw[kMaxGammaTw];  // tw[g * NN + k] = e^{-i n_k gamma_g}
   for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
     const int g = i / NN, k = i % NN;
@@ -836,8 +835,6 @@ __global__ void k_gamma_px_anal(const void *__restrict__ in, int64_t in_ms, doub
     tw[i] = make_double2(cs, -sn);
   }
   __syncthreads();
-  const int K = 2 * bl - 1;
-  const int64_t npx = (int64_t)bl * K;
   const int64_t total = (int64_t)nb * npx;
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
@@ -886,7 +883,7 @@ __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
 
 template <int NN>
 __global__ void k_gamma_px_synth_df(const double2 *__restrict__ F, void *__restrict__ out, int64_t out_ms,
-                                    const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+                                    const int *__restrict__ ns, int ng, int64_t npx, int nb, int real, double c) {
   __shared__ float4 tw[kMaxGammaTw];  // c e^{i n_k gamma_g} (x2 for n_k > 0, real)
   for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
     const int g = i / NN, k = i % NN;
@@ -899,8 +896,6 @@ __global__ void k_gamma_px_synth_df(const double2 *__restrict__ F, void *__restr
     tw[i] = dmk(re, im);
   }
   __syncthreads();
-  const int K = 2 * bl - 1;
-  const int64_t npx = (int64_t)bl * K;
   const int64_t total = (int64_t)nb * npx;
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
@@ -935,7 +930,7 @@ __global__ void k_gamma_px_synth_df(const double2 *__restrict__ F, void *__restr
 
 template <int NN>
 __global__ void k_gamma_px_anal_df(const void *__restrict__ in, int64_t in_ms, double2 *__restrict__ F,
-                                   const int *__restrict__ ns, int ng, int bl, int nb, int real, double c) {
+                                   const int *__restrict__ ns, int ng, int64_t npx, int nb, int real, double c) {
   __shared__ float4 tw[kMaxGammaTw];  // c e^{-i n_k gamma_g}
   for (int i = threadIdx.x; i < ng * NN; i += blockDim.x) {
     const int g = i / NN, k = i % NN;
@@ -947,8 +942,6 @@ __global__ void k_gamma_px_anal_df(const void *__restrict__ in, int64_t in_ms, d
     tw[i] = dmk(re, im);
   }
   __syncthreads();
-  const int K = 2 * bl - 1;
-  const int64_t npx = (int64_t)bl * K;
   const int64_t total = (int64_t)nb * npx;
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
@@ -1106,9 +1099,9 @@ void run_ring_inverse(const RingArgs &a, int nrings, bool real, cudaStream_t st)
 }  // namespace
 
 void ring_forward(const void *rings, int64_t ring_stride, int64_t map_stride, int rpm, double2 *spec,
-                  int64_t spec_stride, int sw, int mlo, int nrings, int bl, bool real, cudaStream_t st) {
+                  int64_t spec_stride, int sw, int mlo, int nrings, int bl, int ss, bool real, cudaStream_t st) {
   if (nrings <= 0) return;
-  const RingFFT &rf = ring_fft(2 * bl - 1);
+  const RingFFT &rf = ring_fft(grid_ring_len(bl, ss));
   RingArgs a = ring_args(rf, bl, nrings);
   a.rings = rings;
   a.ring_stride = ring_stride;
@@ -1122,10 +1115,10 @@ void ring_forward(const void *rings, int64_t ring_stride, int64_t map_stride, in
 }
 
 void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, void *rings,
-                  int64_t ring_stride, int64_t map_stride, int rpm, int nrings, int bl, bool real,
+                  int64_t ring_stride, int64_t map_stride, int rpm, int nrings, int bl, int ss, bool real,
                   cudaStream_t st) {
   if (nrings <= 0) return;
-  const RingFFT &rf = ring_fft(2 * bl - 1);
+  const RingFFT &rf = ring_fft(grid_ring_len(bl, ss));
   RingArgs a = ring_args(rf, bl, nrings);
   a.spec_in = spec;
   a.spec_stride = spec_stride;
@@ -1140,9 +1133,9 @@ void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, voi
 
 void ring_forward_c(const double2 *rings, int64_t ring_stride, int64_t map_stride, int rpm, double2 *spec,
                     int64_t spec_stride, int64_t spec_map_stride, int spec_rpm, int sw, int mlo, int nrings, int bl,
-                    cudaStream_t st) {
+                    int ss, cudaStream_t st) {
   if (nrings <= 0) return;
-  const RingFFT &rf = ring_fft(2 * bl - 1);
+  const RingFFT &rf = ring_fft(grid_ring_len(bl, ss));
   RingArgs a = ring_args(rf, bl, nrings);
   a.rings = rings;
   a.ring_stride = ring_stride;
@@ -1159,9 +1152,9 @@ void ring_forward_c(const double2 *rings, int64_t ring_stride, int64_t map_strid
 
 void ring_inverse_c(const double2 *spec, int64_t spec_stride, int64_t spec_map_stride, int spec_rpm, int sw,
                     int mlo, bool herm, double2 *rings, int64_t ring_stride, int64_t map_stride, int rpm, int nrings,
-                    int bl, cudaStream_t st) {
+                    int bl, int ss, cudaStream_t st) {
   if (nrings <= 0) return;
-  const RingFFT &rf = ring_fft(2 * bl - 1);
+  const RingFFT &rf = ring_fft(grid_ring_len(bl, ss));
   RingArgs a = ring_args(rf, bl, nrings);
   a.spec_in = spec;
   a.spec_stride = spec_stride;
@@ -1184,6 +1177,7 @@ void contract_l2t(const L2T &p, cudaStream_t st) {
   a.table = p.use_q ? p.tb->Q : p.tb->D;
   a.off = p.tb->d_off;
   a.bl = p.tb->bl;
+  a.nt = p.tb->nt;
   a.an = p.tb->an;
   a.tmlo = p.tb->mlo;
   a.n = p.n;
@@ -1203,9 +1197,9 @@ void contract_l2t(const L2T &p, cudaStream_t st) {
   a.nb = p.nb;
   const int nm = p.mhi - p.mlo + 1;
   if (p.use_q)
-    launch_contract<1>(a, nm, a.bl, st);
+    launch_contract<1>(a, nm, a.nt, st);
   else
-    launch_contract<0>(a, nm, a.bl, st);
+    launch_contract<0>(a, nm, a.nt, st);
 }
 
 void contract_t2l(const T2L &p, cudaStream_t st) {
@@ -1215,6 +1209,7 @@ void contract_t2l(const T2L &p, cudaStream_t st) {
   a.table = p.use_q ? p.tb->Q : p.tb->D;
   a.off = p.tb->d_off;
   a.bl = p.tb->bl;
+  a.nt = p.tb->nt;
   a.an = p.tb->an;
   a.tmlo = p.tb->mlo;
   a.n = p.n;
@@ -1249,17 +1244,17 @@ void contract_t2l_group(const T2L *a, int n, cudaStream_t st) {
   for (int i = 0; i < n; ++i) contract_t2l(a[i], st);
 }
 
-void gamma_synthesis(const double2 *G, double2 *spec, const int *ns, int nn, int ng, int bl, int nb,
+void gamma_synthesis(const double2 *G, double2 *spec, const int *ns, int nn, int ng, int bl, int ss, int nb,
                      bool real, double c, cudaStream_t st) {
   S2G_REQUIRE(nn >= 1 && nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
-  const int sw = real ? bl : 2 * bl - 1;
-  const int64_t total = (int64_t)nb * bl * sw;
+  const int sw = real ? bl : 2 * bl - 1, nt = grid_rings(bl, ss);
+  const int64_t total = (int64_t)nb * nt * sw;
   if (total <= 0) return;
-  KTimer kt(KC_GAMMA, st, 0.0, (double)nb * bl * ((real ? 2.0 : 1.0) * nn + ng) * sw * 16.0);
+  KTimer kt(KC_GAMMA, st, 0.0, (double)nb * nt * ((real ? 2.0 : 1.0) * nn + ng) * sw * 16.0);
   const unsigned grid = (unsigned)ceil_div(total, 256);
   switch (nn) {
 #define S2G_GS(N) \
-  case N: k_gamma_synth<N><<<grid, 256, 0, st>>>(G, spec, ns, ng, bl, nb, real, c); break;
+  case N: k_gamma_synth<N><<<grid, 256, 0, st>>>(G, spec, ns, ng, bl, nt, nb, real, c); break;
     S2G_GS(1) S2G_GS(2) S2G_GS(3) S2G_GS(4) S2G_GS(5) S2G_GS(6) S2G_GS(7) S2G_GS(8)
     S2G_GS(9) S2G_GS(10) S2G_GS(11) S2G_GS(12) S2G_GS(13) S2G_GS(14) S2G_GS(15) S2G_GS(16)
 #undef S2G_GS
@@ -1268,17 +1263,18 @@ void gamma_synthesis(const double2 *G, double2 *spec, const int *ns, int nn, int
   S2G_LAUNCHED();
 }
 
-void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int ng, int bl, int nb,
+void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int ng, int bl, int ss, int nb,
                     bool real, double c, cudaStream_t st) {
   S2G_REQUIRE(nn >= 1 && nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
-  const int64_t total = (int64_t)nb * bl * (2 * bl - 1);
+  const int nt = grid_rings(bl, ss);
+  const int64_t total = (int64_t)nb * nt * (2 * bl - 1);
   if (total <= 0) return;
   const int sw = real ? bl : 2 * bl - 1;
-  KTimer kt(KC_GAMMA, st, 0.0, (double)nb * bl * ((double)ng * sw + (double)nn * (2 * bl - 1)) * 16.0);
+  KTimer kt(KC_GAMMA, st, 0.0, (double)nb * nt * ((double)ng * sw + (double)nn * (2 * bl - 1)) * 16.0);
   const unsigned grid = (unsigned)ceil_div(total, 256);
   switch (nn) {
 #define S2G_GA(N) \
-  case N: k_gamma_anal<N><<<grid, 256, 0, st>>>(spec, G, ns, ng, bl, nb, real, c); break;
+  case N: k_gamma_anal<N><<<grid, 256, 0, st>>>(spec, G, ns, ng, bl, nt, nb, real, c); break;
     S2G_GA(1) S2G_GA(2) S2G_GA(3) S2G_GA(4) S2G_GA(5) S2G_GA(6) S2G_GA(7) S2G_GA(8)
     S2G_GA(9) S2G_GA(10) S2G_GA(11) S2G_GA(12) S2G_GA(13) S2G_GA(14) S2G_GA(15) S2G_GA(16)
 #undef S2G_GA
@@ -1288,9 +1284,9 @@ void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int 
 }
 
 void gamma_px_synthesis(const double2 *F, void *out, int64_t out_ms, const int *ns, int nn, int ng, int bl,
-                        int nb, bool real, double c, cudaStream_t st) {
+                        int ss, int nb, bool real, double c, cudaStream_t st) {
   S2G_REQUIRE(nn >= 1 && nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
-  const int64_t npx = (int64_t)bl * (2 * bl - 1);
+  const int64_t npx = (int64_t)grid_rings(bl, ss) * grid_ring_len(bl, ss);
   const int64_t total = (int64_t)nb * npx;
   if (total <= 0) return;
   KTimer kt(KC_GAMMA, st, 0.0, (double)total * (16.0 * nn + (real ? 8.0 : 16.0) * ng));
@@ -1299,9 +1295,9 @@ void gamma_px_synthesis(const double2 *F, void *out, int64_t out_ms, const int *
 #define S2G_GPS(N)                                                                       \
   case N:                                                                                \
     if (t_precision == 1)                                                                \
-      k_gamma_px_synth_df<N><<<grid, 256, 0, st>>>(F, out, out_ms, ns, ng, bl, nb, real, c); \
+      k_gamma_px_synth_df<N><<<grid, 256, 0, st>>>(F, out, out_ms, ns, ng, npx, nb, real, c); \
     else                                                                                 \
-      k_gamma_px_synth<N><<<grid, 256, 0, st>>>(F, out, out_ms, ns, ng, bl, nb, real, c);    \
+      k_gamma_px_synth<N><<<grid, 256, 0, st>>>(F, out, out_ms, ns, ng, npx, nb, real, c);    \
     break;
     S2G_GPS(1) S2G_GPS(2) S2G_GPS(3) S2G_GPS(4) S2G_GPS(5) S2G_GPS(6) S2G_GPS(7) S2G_GPS(8)
     S2G_GPS(9) S2G_GPS(10) S2G_GPS(11) S2G_GPS(12) S2G_GPS(13) S2G_GPS(14) S2G_GPS(15) S2G_GPS(16)
@@ -1311,10 +1307,10 @@ void gamma_px_synthesis(const double2 *F, void *out, int64_t out_ms, const int *
   S2G_LAUNCHED();
 }
 
-void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns, int nn, int ng, int bl, int nb,
-                       bool real, double c, cudaStream_t st) {
+void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns, int nn, int ng, int bl, int ss,
+                       int nb, bool real, double c, cudaStream_t st) {
   S2G_REQUIRE(nn >= 1 && nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
-  const int64_t npx = (int64_t)bl * (2 * bl - 1);
+  const int64_t npx = (int64_t)grid_rings(bl, ss) * grid_ring_len(bl, ss);
   const int64_t total = (int64_t)nb * npx;
   if (total <= 0) return;
   KTimer kt(KC_GAMMA, st, 0.0, (double)total * (16.0 * nn + (real ? 8.0 : 16.0) * ng));
@@ -1323,9 +1319,9 @@ void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns,
 #define S2G_GPA(N)                                                                      \
   case N:                                                                               \
     if (t_precision == 1)                                                               \
-      k_gamma_px_anal_df<N><<<grid, 256, 0, st>>>(in, in_ms, F, ns, ng, bl, nb, real, c); \
+      k_gamma_px_anal_df<N><<<grid, 256, 0, st>>>(in, in_ms, F, ns, ng, npx, nb, real, c); \
     else                                                                                \
-      k_gamma_px_anal<N><<<grid, 256, 0, st>>>(in, in_ms, F, ns, ng, bl, nb, real, c);    \
+      k_gamma_px_anal<N><<<grid, 256, 0, st>>>(in, in_ms, F, ns, ng, npx, nb, real, c);    \
     break;
     S2G_GPA(1) S2G_GPA(2) S2G_GPA(3) S2G_GPA(4) S2G_GPA(5) S2G_GPA(6) S2G_GPA(7) S2G_GPA(8)
     S2G_GPA(9) S2G_GPA(10) S2G_GPA(11) S2G_GPA(12) S2G_GPA(13) S2G_GPA(14) S2G_GPA(15) S2G_GPA(16)

@@ -10,19 +10,20 @@
 
 namespace s2g {
 
-// Ring DFTs over a batch of rings of length K = 2 bl - 1.
+// Ring DFTs over a batch of rings of length K = grid_ring_len(bl, ss)
+// (2bl-1 on MW, 2bl on MWSS sampling).
 //   forward:  spec[r][m - mlo] = sum_p ring_r[p] e^{-2 pi i m p / K},  m in [mlo, bl-1]
-//   inverse:  ring_r[p] = sum_m spec[r][m - mlo] e^{+2 pi i m p / K}
+//   inverse:  ring_r[p] = sum_m spec[r][m - mlo] e^{+2 pi i m p / K}   (MWSS: no m = bl term)
 // real != 0: rings are real; spectra hold m >= 0 only (mlo = 0) and are
 // Hermitian-completed on the inverse.  Spectrum rows have width `sw`.
 // Ring r lives at (r / rpm) * map_stride + (r % rpm) * ring_stride elements.
 void ring_forward(const void *rings, int64_t ring_stride, int64_t map_stride, int rpm, double2 *spec,
-                  int64_t spec_stride, int sw, int mlo, int nrings, int bl, bool real, cudaStream_t st);
+                  int64_t spec_stride, int sw, int mlo, int nrings, int bl, int ss, bool real, cudaStream_t st);
 void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, void *rings,
-                  int64_t ring_stride, int64_t map_stride, int rpm, int nrings, int bl, bool real,
+                  int64_t ring_stride, int64_t map_stride, int rpm, int nrings, int bl, int ss, bool real,
                   cudaStream_t st);
 
-// Contraction over l producing ring spectra ("l -> t"):
+// Contraction over l producing ring spectra ("l -> t", t < tb->nt):
 //   out[b][t][m - omlo] = sum_l A_m[t][l] x_b(l, m) w(l)
 // A = D (use_q = false) or Q^T (use_q = true) of the |n| table at band-limit bl,
 // read at direction n (sign/mirror for n < 0).  x_b(l,m) = x[b*xs + l^2+l+m]
@@ -34,10 +35,10 @@ void ring_inverse(const double2 *spec, int64_t spec_stride, int sw, int mlo, voi
 // herm (inverse): columns m < 0 are conj of m > 0 (a real-valued ring held as complex).
 void ring_forward_c(const double2 *rings, int64_t ring_stride, int64_t map_stride, int rpm, double2 *spec,
                     int64_t spec_stride, int64_t spec_map_stride, int spec_rpm, int sw, int mlo, int nrings, int bl,
-                    cudaStream_t st);
+                    int ss, cudaStream_t st);
 void ring_inverse_c(const double2 *spec, int64_t spec_stride, int64_t spec_map_stride, int spec_rpm, int sw,
                     int mlo, bool herm, double2 *rings, int64_t ring_stride, int64_t map_stride, int rpm, int nrings,
-                    int bl, cudaStream_t st);
+                    int bl, int ss, cudaStream_t st);
 
 struct L2T {
   const WignerTable *tb;
@@ -88,19 +89,21 @@ void contract_t2l(const T2L &a, cudaStream_t st);
 void contract_t2l_group(const T2L *a, int n, cudaStream_t st);
 
 // gamma synthesis: spec[b][g][t][m - (real?0:-(bl-1))] from coefficients
-// G[b][k][t][m + bl - 1] of directions ns[k]; real: Hermitian in (m, n).
+// G[b][k][t][m + bl - 1] of directions ns[k], t < grid_rings(bl, ss); real:
+// Hermitian in (m, n).
 //   spec_g(m) = c sum_k e^{i n_k gamma_g} G_k(m)  (+ conj mirror for real n > 0)
-void gamma_synthesis(const double2 *G, double2 *spec, const int *ns, int nn, int ng, int bl, int nb,
+void gamma_synthesis(const double2 *G, double2 *spec, const int *ns, int nn, int ng, int bl, int ss, int nb,
                      bool real, double c, cudaStream_t st);
 // gamma analysis: G[b][k][t][m + bl - 1] = c sum_g e^{-i n_k gamma_g} spec_g(m), all m.
-void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int ng, int bl, int nb,
+void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int ng, int bl, int ss, int nb,
                     bool real, double c, cudaStream_t st);
 // gamma DFT on pixels between F[b][k][t][p] (complex, k < nn) and the gamma slices
-// out[b * ms + g * bl * K + t * K + p] (double for real signals, else double2)
+// out[b * ms + g * npx + t * K + p] (double for real signals, else double2),
+// npx = nt * K the pixels of one slice on the sampling's grid
 void gamma_px_synthesis(const double2 *F, void *out, int64_t out_ms, const int *ns, int nn, int ng, int bl,
-                        int nb, bool real, double c, cudaStream_t st);
-void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns, int nn, int ng, int bl, int nb,
-                       bool real, double c, cudaStream_t st);
+                        int ss, int nb, bool real, double c, cudaStream_t st);
+void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns, int nn, int ng, int bl, int ss,
+                       int nb, bool real, double c, cudaStream_t st);
 
 // Merge of per-(scale, direction) Wigner coefficients into flm (lmn2lm):
 //   flm(l,m) = sum_pairs [ psi_p(l) z_p(l,m) + real&&n>0 : (-1)^{m+n} conj(z_p(l,-m)) psin_p(l) ]

@@ -76,13 +76,15 @@ static_assert(Cfg<16>::kNBuf * Cfg<16>::kAccCols <= Cfg<16>::kTmemCols, "TMEM");
 struct Geom {
   int l0, nl, rows, K, nkc, nrt;
 };
-__host__ __device__ inline Geom geom(int bl, int an, int m, bool q) {
+// Tile geometry of one m block of a table with nt theta samples: l -> t has
+// rows t < nt and reduction K = l - l0; t -> l has rows l - l0 and K = t.
+__host__ __device__ inline Geom geom(int bl, int nt, int an, int m, bool q) {
   Geom g;
   const int am = m < 0 ? -m : m;
   g.l0 = am > an ? am : an;
   g.nl = bl - g.l0 > 0 ? bl - g.l0 : 0;
-  g.rows = q ? g.nl : bl;
-  g.K = q ? bl : g.nl;
+  g.rows = q ? g.nl : nt;
+  g.K = q ? nt : g.nl;
   g.nkc = g.nl > 0 ? (g.K + kPK - 1) / kPK : 0;
   g.nrt = (g.rows + kPM - 1) / kPM;  // l -> t keeps its rows (written as zeros) when nl = 0
   return g;
@@ -161,13 +163,13 @@ __device__ __forceinline__ TableRefM table_ref_m(int tmlo, int n, int m) {
 // ---------------------------------------------------------------------------
 
 __global__ void __launch_bounds__(128) k_slice_table(const double *__restrict__ T,
-                                                     const int64_t *__restrict__ off, int bl, int an,
-                                                     int tmlo, int q, uint16_t *__restrict__ panels,
+                                                     const int64_t *__restrict__ off, int bl, int nt,
+                                                     int an, int tmlo, int q, uint16_t *__restrict__ panels,
                                                      const int64_t *__restrict__ pan_off,
                                                      int8_t *__restrict__ eA,
                                                      const int64_t *__restrict__ e_off) {
   const int mi = blockIdx.x, rt = blockIdx.y;
-  const Geom g = geom(bl, an, tmlo + mi, q != 0);
+  const Geom g = geom(bl, nt, an, tmlo + mi, q != 0);
   if (rt >= g.nrt) return;
   const double *Tm = T + off[mi];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -216,7 +218,7 @@ struct Part {
 
 struct XArgs {
   int q;  // 0: l -> t (K = l - l0), 1: t -> l (K = t)
-  int bl, an, mlo, lmin;  // lmin: smallest lmin over the parts
+  int bl, nt, an, mlo, lmin;  // lmin: smallest lmin over the parts
   int nparts;
   Part part[kMaxParts];
   int nb, b0, mpp;  // maps per part in this launch: column pair cp -> part cp / mpp, map b0 + cp % mpp
@@ -253,7 +255,7 @@ __device__ __forceinline__ double2 x_value(const XArgs &a, int m, int am, const 
     const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
     return make_double2(v.x * wt.x - v.y * wt.y, v.x * wt.y + v.y * wt.x);
   }
-  if (k >= a.bl) return zero;
+  if (k >= a.nt) return zero;
   return P.src[(int64_t)b * P.ss + (int64_t)k * P.sw + (m - P.s_mlo)];
 }
 
@@ -265,7 +267,7 @@ template <int NC>
 __global__ void __launch_bounds__(NC * 4) k_slice_x(XArgs a) {
   constexpr int PX = Cfg<NC>::kPanelX;
   const int pm = blockIdx.x, m = a.mlo + pm, am = m < 0 ? -m : m;
-  const Geom g = geom(a.bl, a.an, m, a.q != 0);
+  const Geom g = geom(a.bl, a.nt, a.an, m, a.q != 0);
   const int cp = threadIdx.x >> 3, h = threadIdx.x & 7;
   const int c0 = 2 * cp;
   if (g.nkc == 0) {
@@ -425,7 +427,7 @@ struct MxArgs {
   const int64_t *pan_off;
   const int8_t *eA;
   const int64_t *e_off;
-  int bl, an, tmlo, n, mlo, lmin;  // lmin: smallest over the parts
+  int bl, nt, an, tmlo, n, mlo, lmin;  // lmin: smallest over the parts
   const uint16_t *xpan;
   const int64_t *xoff;
   const int *eX;
@@ -450,7 +452,7 @@ __device__ __forceinline__ TileInfo tile_info(const MxArgs &a, int t) {
   const TableRefM r = table_ref_m(a.tmlo, a.n, ti.m);
   ti.mi = r.mi;
   ti.sign = r.sign;
-  const Geom g = geom(a.bl, a.an, ti.m, a.q != 0);
+  const Geom g = geom(a.bl, a.nt, a.an, ti.m, a.q != 0);
   ti.l0 = g.l0;
   ti.nkc = g.nkc;
   const int lst = g.l0 > a.lmin ? g.l0 : a.lmin;
@@ -674,7 +676,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
           if (part >= a.nparts || b >= a.nb) continue;
           const Part &P = a.part[part];
           if (!a.q) {
-            if (t_row < a.bl)
+            if (t_row < a.nt)
               P.dst[(int64_t)b * P.ds + (int64_t)t_row * P.dw + (ti.m - P.d_mlo)] =
                   make_double2(y[2 * bb], y[2 * bb + 1]);
           } else {
@@ -722,7 +724,7 @@ struct TileList {
 };
 
 struct SlicedTable {
-  int bl = 0, an = 0, mlo = 0, nm = 0;
+  int bl = 0, nt = 0, an = 0, mlo = 0, nm = 0;
   bool q = false;
   uint16_t *panels = nullptr;
   int8_t *eA = nullptr;
@@ -732,7 +734,7 @@ struct SlicedTable {
 };
 
 std::mutex g_mx_mu;
-std::map<std::tuple<int, int, int>, std::unique_ptr<SlicedTable>> g_sliced;
+std::map<std::tuple<int, int, int, int>, std::unique_ptr<SlicedTable>> g_sliced;  // (bl, an, ss, q)
 size_t g_mx_bytes = 0;
 int *g_err = nullptr;
 
@@ -745,11 +747,12 @@ T *dev_alloc(size_t n, size_t *acc) {
 }
 
 SlicedTable &sliced(const WignerTable &tb, bool q, cudaStream_t st) {
-  auto key = std::make_tuple(tb.bl, tb.an, q ? 1 : 0);
+  auto key = std::make_tuple(tb.bl, tb.an, tb.ss, q ? 1 : 0);
   auto it = g_sliced.find(key);
   if (it != g_sliced.end()) return *it->second;
   auto s = std::make_unique<SlicedTable>();
   s->bl = tb.bl;
+  s->nt = tb.nt;
   s->an = tb.an;
   s->mlo = tb.mlo;
   s->nm = tb.nm;
@@ -757,7 +760,7 @@ SlicedTable &sliced(const WignerTable &tb, bool q, cudaStream_t st) {
   std::vector<int64_t> po(tb.nm), eo(tb.nm);
   int64_t ptot = 0, etot = 0;
   for (int mi = 0; mi < tb.nm; ++mi) {
-    const Geom g = geom(tb.bl, tb.an, tb.mlo + mi, q);
+    const Geom g = geom(tb.bl, tb.nt, tb.an, tb.mlo + mi, q);
     po[mi] = ptot;
     eo[mi] = etot;
     ptot += (int64_t)g.nrt * g.nkc * kS * kPanelA;
@@ -770,10 +773,10 @@ SlicedTable &sliced(const WignerTable &tb, bool q, cudaStream_t st) {
   s->d_e_off = dev_alloc<int64_t>(tb.nm, &by);
   S2G_CUDA(cudaMemcpyAsync(s->d_pan_off, po.data(), sizeof(int64_t) * tb.nm, cudaMemcpyHostToDevice, st));
   S2G_CUDA(cudaMemcpyAsync(s->d_e_off, eo.data(), sizeof(int64_t) * tb.nm, cudaMemcpyHostToDevice, st));
-  int nrt_max = (tb.bl + kPM - 1) / kPM;
+  int nrt_max = (std::max(tb.bl, tb.nt) + kPM - 1) / kPM;
   dim3 grid(tb.nm, nrt_max);
-  k_slice_table<<<grid, 128, 0, st>>>(q ? tb.Q : tb.D, tb.d_off, tb.bl, tb.an, tb.mlo, q ? 1 : 0, s->panels,
-                                      s->d_pan_off, s->eA, s->d_e_off);
+  k_slice_table<<<grid, 128, 0, st>>>(q ? tb.Q : tb.D, tb.d_off, tb.bl, tb.nt, tb.an, tb.mlo, q ? 1 : 0,
+                                      s->panels, s->d_pan_off, s->eA, s->d_e_off);
   S2G_LAUNCHED();
   S2G_CUDA(cudaStreamSynchronize(st));
   s->bytes = by;
@@ -792,7 +795,7 @@ const TileList &tile_list(SlicedTable &s, int n, int mlo, int mhi, int lmin, cud
   std::vector<int64_t> xoff(mhi - mlo + 1);
   int64_t xe = 0, work = 0;
   for (int m = mlo; m <= mhi; ++m) {
-    const Geom g = geom(s.bl, s.an, m, s.q);
+    const Geom g = geom(s.bl, s.nt, s.an, m, s.q);
     xoff[m - mlo] = xe;
     xe += (int64_t)g.nkc * Cfg<16>::kPanelX;
     if (g.nl <= 0) continue;
@@ -888,12 +891,13 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     double fl = 0, by = 0;
     if (timing_enabled()) {
       fl = 4.0 * entries * nbg * p.nparts;
-      by = entries * 2.0 * kS + (double)x_elems * 2.0 + 16.0 * nbg * p.nparts * (double)p.tb->bl * nmp;
+      by = entries * 2.0 * kS + (double)x_elems * 2.0 + 16.0 * nbg * p.nparts * (double)p.tb->nt * nmp;
     }
     KTimer kt(KC_MIXED, st, fl, by);
     XArgs xa{};
     xa.q = p.q ? 1 : 0;
     xa.bl = p.tb->bl;
+    xa.nt = p.tb->nt;
     xa.an = p.tb->an;
     xa.mlo = p.mlo;
     xa.lmin = lmin;
@@ -915,6 +919,7 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     ma.eA = s->eA;
     ma.e_off = s->d_e_off;
     ma.bl = p.tb->bl;
+    ma.nt = p.tb->nt;
     ma.an = p.tb->an;
     ma.tmlo = p.tb->mlo;
     ma.n = p.n;

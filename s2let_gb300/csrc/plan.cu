@@ -1,10 +1,12 @@
-// Plan construction: Wigner-d tables (FP64 scaled three-term recursion on the
-// GPU), the exact MW forward-quadrature operator W_eps, the forward tables
-// Q = D^T W / K^2 (FP64 GEMM on the GPU), and Bluestein FFT data.
+// Plan construction: Wigner-d tables (double-double three-term recursion on
+// the GPU), the exact forward-quadrature operator W_eps of the MW or MWSS
+// sampling, the forward tables Q = D^T W (FP64 GEMM on the GPU), and Bluestein
+// FFT data.
 #include <cmath>
 #include <complex>
 #include <map>
 #include <mutex>
+#include <tuple>
 
 #include "common.h"
 #include "plan.h"
@@ -87,14 +89,15 @@ __device__ dd dd_pow(dd x, int k, int &E) {
 }
 
 // ---------------------------------------------------------------------------
-// d^l_{m,an}(theta_t), l = l0..bl-1, for one (m, t) per thread, in double-double.
+// d^l_{m,an}(theta_t), l = l0..bl-1, for one (m, t) per thread (t < nt), in double-double.
 //
 // Start value at l0 = max(|m|, an) (closed forms of d^{l0}):
 //   l0 = m  >= an : (-1)^{l0-an} sqrt(C(2l0, l0+an)) c^{l0+an} s^{l0-an}
 //   l0 = -m >= an : sqrt(C(2l0, l0-an)) c^{l0-an} s^{l0+an}
 //   l0 = an > |m| : sqrt(C(2l0, l0+m)) c^{l0+m} s^{l0-m}
 // c = cos(theta/2), s = sin(theta/2), both supplied by the host in double-double
-// from the exact rational theta_t = pi (2t+1)/(2bl-1); sqrt(C) arrives as
+// from the exact rational theta_t (pi (2t+1)/(2bl-1) for MW, pi t/bl for MWSS,
+// where the poles give s = 0 or c = 0 exactly); sqrt(C) arrives as
 // double-double mantissa * 2^e.  Three-term recursion in l:
 //   d^{l+1} = [(2l+1)(l(l+1) x - m an) d^l - (l+1) sqrt((l^2-m^2)(l^2-an^2)) d^{l-1}]
 //             / [l sqrt(((l+1)^2-m^2)((l+1)^2-an^2))],     x = cos(theta).
@@ -106,24 +109,24 @@ __device__ dd dd_pow(dd x, int k, int &E) {
 // ---------------------------------------------------------------------------
 struct AngleDD {
   double s_hi, s_lo, c_hi, c_lo, u_hi, u_lo;  // u = 2 s^2 (north) or 2 c^2 (south)
+  int north, pad;                             // theta <= pi/2
 };
 
-__global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ off, int bl, int an,
+__global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ off, int bl, int nt, int an,
                            int mlo, int nm, const double *__restrict__ start_hi,
                            const double *__restrict__ start_lo, const int *__restrict__ start_exp,
                            const AngleDD *__restrict__ ang) {
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= (int64_t)nm * bl) return;
-  const int mi = (int)(gid / bl), t = (int)(gid % bl);
+  if (gid >= (int64_t)nm * nt) return;
+  const int mi = (int)(gid / nt), t = (int)(gid % nt);
   const int m = mlo + mi;
   const int am = m < 0 ? -m : m;
   const int l0 = am > an ? am : an;
   const int nl = bl - l0;
   if (nl <= 0) return;
-  const int K = 2 * bl - 1;
   const AngleDD A = ang[t];
   const dd s{A.s_hi, A.s_lo}, c{A.c_hi, A.c_lo}, u{A.u_hi, A.u_lo};
-  const bool north = (2 * (2 * t + 1) <= K);
+  const bool north = A.north != 0;
   int ka, kb;
   double sign = 1.0;
   if (m >= 0 && m >= an) {
@@ -135,7 +138,7 @@ __global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ o
   }
   double *row = D + off[mi] + (int64_t)t * nl;
   if ((ka > 0 && c.hi == 0.0) || (kb > 0 && s.hi == 0.0)) {
-    // the closed form vanishes (theta = pi); so does the whole recursion
+    // the closed form vanishes (a pole); so does the whole recursion
     for (int i = 0; i < nl; ++i) row[i] = 0.0;
     return;
   }
@@ -192,51 +195,64 @@ __device__ inline double2 wsin(int p) {
   return make_double2(2.0 / (1.0 - (double)p * (double)p), 0.0);
 }
 
-// A[m'][t] = e^{-i m' theta_t} + [t < bl-1] eps e^{i m' theta_t}   (m' in [-(bl-1), bl-1])
-__device__ inline double2 fold_basis(int mp, int t, int bl, int eps) {
-  const int K = 2 * bl - 1;
+// A[m'][t] = e^{-i m' theta_t} + [ring t has a distinct mirror] eps e^{i m' theta_t}
+// (m' in [-(bl-1), bl-1]): the Fourier basis on the full theta circle folded
+// onto the rings.  Mirrors: MW rings t < bl-1 (theta = pi is its own);
+// MWSS rings 1 <= t <= bl-1 (the poles are their own).
+__device__ inline double2 fold_basis(int mp, int t, int bl, int ss, int eps) {
   double sn, cs;
-  // angle m' * pi (2t+1)/K reduced modulo 2K for accuracy
-  long q = ((long)mp * (2 * t + 1)) % (2L * K);
-  sincospi((double)q / (double)K, &sn, &cs);
+  bool mirrored;
+  if (!ss) {
+    const int K = 2 * bl - 1;
+    // angle m' pi (2t+1)/K reduced modulo 2K for accuracy
+    const long q = ((long)mp * (2 * t + 1)) % (2L * K);
+    sincospi((double)q / (double)K, &sn, &cs);
+    mirrored = t < bl - 1;
+  } else {
+    // angle m' pi t / bl reduced modulo 2 bl
+    const long q = ((long)mp * t) % (2L * bl);
+    sincospi((double)q / (double)bl, &sn, &cs);
+    mirrored = t >= 1 && t <= bl - 1;
+  }
   double2 r = make_double2(cs, -sn);
-  if (t < bl - 1) {
+  if (mirrored) {
     r.x += eps * cs;
     r.y += eps * sn;
   }
   return r;
 }
 
-// TA[m''][t'] = sum_{m'} w(m' + m'') A[m'][t']
-__global__ void k_wmat_ta(double2 *__restrict__ TA, int bl, int eps) {
+// TA[m''][t'] = sum_{m'} w(m' + m'') A[m'][t']   (t' < nt)
+__global__ void k_wmat_ta(double2 *__restrict__ TA, int bl, int nt, int ss, int eps) {
   const int K = 2 * bl - 1;
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= (int64_t)K * bl) return;
-  const int mpp = (int)(gid / bl) - (bl - 1), tp = (int)(gid % bl);
+  if (gid >= (int64_t)K * nt) return;
+  const int mpp = (int)(gid / nt) - (bl - 1), tp = (int)(gid % nt);
   double2 acc = make_double2(0.0, 0.0);
   for (int mp = -(bl - 1); mp <= bl - 1; ++mp) {
     const int p = mp + mpp;
     if ((p & 1) && p != 1 && p != -1) continue;
-    const double2 w = wsin(p), a = fold_basis(mp, tp, bl, eps);
+    const double2 w = wsin(p), a = fold_basis(mp, tp, bl, ss, eps);
     acc.x += w.x * a.x - w.y * a.y;
     acc.y += w.x * a.y + w.y * a.x;
   }
   TA[gid] = acc;
 }
 
-// W[t][t'] = Re sum_{m''} A[m''][t] TA[m''][t'] / K^2
-__global__ void k_wmat_w(double *__restrict__ W, const double2 *__restrict__ TA, int bl, int eps) {
-  const int K = 2 * bl - 1;
+// W[t][t'] = Re sum_{m''} A[m''][t] TA[m''][t'] / kt^2,  kt = samples on the full circle
+__global__ void k_wmat_w(double *__restrict__ W, const double2 *__restrict__ TA, int bl, int nt, int ss,
+                         int eps) {
+  const int kt = ss ? 2 * bl : 2 * bl - 1;
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= (int64_t)bl * bl) return;
-  const int t = (int)(gid / bl), tp = (int)(gid % bl);
+  if (gid >= (int64_t)nt * nt) return;
+  const int t = (int)(gid / nt), tp = (int)(gid % nt);
   double acc = 0.0;
   for (int mpp = -(bl - 1); mpp <= bl - 1; ++mpp) {
-    const double2 a = fold_basis(mpp, t, bl, eps);
-    const double2 b = TA[(int64_t)(mpp + bl - 1) * bl + tp];
+    const double2 a = fold_basis(mpp, t, bl, ss, eps);
+    const double2 b = TA[(int64_t)(mpp + bl - 1) * nt + tp];
     acc += a.x * b.x - a.y * b.y;
   }
-  W[gid] = acc / ((double)K * (double)K);
+  W[gid] = acc / ((double)kt * (double)kt);
 }
 
 // Q_m[l][t'] = sum_t D_m[t][l] W_eps(m)[t][t'], tiled FP64 GEMM per m (grid.z = m).
@@ -244,8 +260,8 @@ constexpr int QG_T = 64, QG_K = 16;
 __global__ void __launch_bounds__(256) k_qgemm(double *__restrict__ Q, const double *__restrict__ D,
                                                const int64_t *__restrict__ off,
                                                const double *__restrict__ Wp,
-                                               const double *__restrict__ Wm, int bl, int an,
-                                               int mlo) {
+                                               const double *__restrict__ Wm, int bl, int nt,
+                                               int an, int mlo) {
   const int mi = blockIdx.z, m = mlo + mi;
   const int am = m < 0 ? -m : m;
   const int l0 = am > an ? am : an, nl = bl - l0;
@@ -258,12 +274,12 @@ __global__ void __launch_bounds__(256) k_qgemm(double *__restrict__ Q, const dou
   __shared__ double sB[QG_K][QG_T + 1];  // [t][t']
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   double acc[4][4] = {};
-  for (int k0 = 0; k0 < bl; k0 += QG_K) {
+  for (int k0 = 0; k0 < nt; k0 += QG_K) {
     for (int i = threadIdx.x; i < QG_K * QG_T; i += 256) {
       const int kk = i / QG_T, c = i % QG_T;
       const int t = k0 + kk;
-      sA[kk][c] = (t < bl && row0 + c < nl) ? Dm[(int64_t)t * nl + row0 + c] : 0.0;
-      sB[kk][c] = (t < bl && col0 + c < bl) ? W[(int64_t)t * bl + col0 + c] : 0.0;
+      sA[kk][c] = (t < nt && row0 + c < nl) ? Dm[(int64_t)t * nl + row0 + c] : 0.0;
+      sB[kk][c] = (t < nt && col0 + c < nt) ? W[(int64_t)t * nt + col0 + c] : 0.0;
     }
     __syncthreads();
 #pragma unroll
@@ -287,7 +303,7 @@ __global__ void __launch_bounds__(256) k_qgemm(double *__restrict__ Q, const dou
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int c = col0 + tx * 4 + j;
-      if (c < bl) Qm[(int64_t)r * bl + c] = acc[i][j];
+      if (c < nt) Qm[(int64_t)r * nt + c] = acc[i][j];
     }
   }
 }
@@ -314,7 +330,7 @@ void host_fft(std::vector<std::complex<double>> &x) {
 }
 
 std::mutex g_plan_mu;
-std::map<std::pair<int, int>, std::unique_ptr<WignerTable>> g_tables;
+std::map<std::tuple<int, int, int>, std::unique_ptr<WignerTable>> g_tables;
 std::map<int, std::unique_ptr<RingFFT>> g_rings;
 size_t g_bytes = 0;
 
@@ -326,10 +342,13 @@ T *dev_alloc(size_t n) {
   return p;
 }
 
-std::unique_ptr<WignerTable> build_table(int bl, int an) {
+std::unique_ptr<WignerTable> build_table(int bl, int an, int ss) {
   auto tb = std::make_unique<WignerTable>();
   tb->bl = bl;
   tb->an = an;
+  tb->ss = ss;
+  tb->nt = grid_rings(bl, ss);
+  const int nt = tb->nt;
   tb->mlo = an == 0 ? 0 : -(bl - 1);
   tb->nm = bl - tb->mlo;
   tb->off.assign(tb->nm + 1, 0);
@@ -340,7 +359,7 @@ std::unique_ptr<WignerTable> build_table(int bl, int an) {
     const int m = tb->mlo + mi;
     const int l0 = tb->l0(m);
     const int64_t nl = std::max(0, bl - l0);
-    tb->off[mi + 1] = tb->off[mi] + nl * bl;
+    tb->off[mi + 1] = tb->off[mi] + nl * nt;
     // sqrt(C(2 l0, ka)) in extended precision, split into (hi + lo) * 2^e
     int ka;
     const int am = std::abs(m);
@@ -357,30 +376,38 @@ std::unique_ptr<WignerTable> build_table(int bl, int an) {
     st_lo[mi] = (double)(mant - (long double)st_hi[mi]);
     ex[mi] = e;
   }
-  // half-angles of the MW rings, theta_t / 2 = pi (2t+1) / (2(2bl-1)), in extended precision
-  std::vector<AngleDD> ang(bl);
+  // half-angles of the rings in extended precision:
+  //   MW:   theta_t / 2 = pi (2t+1) / (2(2bl-1)),   MWSS: theta_t / 2 = pi t / (2 bl)
+  // written as pi a / b with integers a / b <= 1/2 (north) or >= 1/2 (south)
+  std::vector<AngleDD> ang(nt);
   {
     const long double pi_l = 3.141592653589793238462643383279502884197L;
-    const int K = 2 * bl - 1;
     auto split = [](long double x, double &hi, double &lo) {
       hi = (double)x;
       lo = (double)(x - (long double)hi);
     };
-    for (int t = 0; t < bl; ++t) {
+    for (int t = 0; t < nt; ++t) {
+      const long a = ss ? t : 2 * t + 1;            // theta_t / pi = a / b
+      const long b = ss ? bl : 2 * bl - 1;
       long double sl, cl;
-      if (2 * t + 1 == K) {
-        sl = 1.0L;
-        cl = 0.0L;  // theta = pi exactly
+      if (a == 0) {
+        sl = 0.0L;  // theta = 0 exactly
+        cl = 1.0L;
+      } else if (a == b) {
+        sl = 1.0L;  // theta = pi exactly
+        cl = 0.0L;
       } else {
-        const long double h = pi_l * (long double)(2 * t + 1) / (long double)(2 * K);
+        const long double h = pi_l * (long double)a / (long double)(2 * b);
         sl = sinl(h);
         cl = cosl(h);
       }
-      const bool north = (2 * (2 * t + 1) <= K);
+      const bool north = 2 * a <= b;
       const long double u = north ? 2.0L * sl * sl : 2.0L * cl * cl;
       split(sl, ang[t].s_hi, ang[t].s_lo);
       split(cl, ang[t].c_hi, ang[t].c_lo);
       split(u, ang[t].u_hi, ang[t].u_lo);
+      ang[t].north = north ? 1 : 0;
+      ang[t].pad = 0;
     }
   }
   const int64_t n = tb->elems();
@@ -394,32 +421,33 @@ std::unique_ptr<WignerTable> build_table(int bl, int an) {
   S2G_CUDA(cudaMalloc(&d_hi, sizeof(double) * tb->nm));
   S2G_CUDA(cudaMalloc(&d_lo, sizeof(double) * tb->nm));
   S2G_CUDA(cudaMalloc(&d_ex, sizeof(int) * tb->nm));
-  S2G_CUDA(cudaMalloc(&d_ang, sizeof(AngleDD) * bl));
+  S2G_CUDA(cudaMalloc(&d_ang, sizeof(AngleDD) * nt));
   S2G_CUDA(cudaMemcpy(d_hi, st_hi.data(), sizeof(double) * tb->nm, cudaMemcpyHostToDevice));
   S2G_CUDA(cudaMemcpy(d_lo, st_lo.data(), sizeof(double) * tb->nm, cudaMemcpyHostToDevice));
   S2G_CUDA(cudaMemcpy(d_ex, ex.data(), sizeof(int) * tb->nm, cudaMemcpyHostToDevice));
-  S2G_CUDA(cudaMemcpy(d_ang, ang.data(), sizeof(AngleDD) * bl, cudaMemcpyHostToDevice));
+  S2G_CUDA(cudaMemcpy(d_ang, ang.data(), sizeof(AngleDD) * nt, cudaMemcpyHostToDevice));
   {
-    const int64_t nthr = (int64_t)tb->nm * bl;
-    k_wigner_d<<<ceil_div(nthr, 128), 128>>>(tb->D, tb->d_off, bl, an, tb->mlo, tb->nm, d_hi, d_lo, d_ex, d_ang);
+    const int64_t nthr = (int64_t)tb->nm * nt;
+    k_wigner_d<<<ceil_div(nthr, 128), 128>>>(tb->D, tb->d_off, bl, nt, an, tb->mlo, tb->nm, d_hi, d_lo, d_ex,
+                                             d_ang);
     S2G_LAUNCHED();
   }
   // W_+ and W_- (exact forward quadrature operators), then Q = D^T W per m
   const int K = 2 * bl - 1;
   double2 *TA = nullptr;
   double *W[2] = {nullptr, nullptr};
-  S2G_CUDA(cudaMalloc(&TA, sizeof(double2) * (size_t)K * bl));
+  S2G_CUDA(cudaMalloc(&TA, sizeof(double2) * (size_t)K * nt));
   for (int e = 0; e < 2; ++e) {
-    S2G_CUDA(cudaMalloc(&W[e], sizeof(double) * (size_t)bl * bl));
+    S2G_CUDA(cudaMalloc(&W[e], sizeof(double) * (size_t)nt * nt));
     const int eps = e == 0 ? 1 : -1;
-    k_wmat_ta<<<ceil_div((int64_t)K * bl, 128), 128>>>(TA, bl, eps);
+    k_wmat_ta<<<ceil_div((int64_t)K * nt, 128), 128>>>(TA, bl, nt, ss, eps);
     S2G_LAUNCHED();
-    k_wmat_w<<<ceil_div((int64_t)bl * bl, 128), 128>>>(W[e], TA, bl, eps);
+    k_wmat_w<<<ceil_div((int64_t)nt * nt, 128), 128>>>(W[e], TA, bl, nt, ss, eps);
     S2G_LAUNCHED();
   }
   {
-    dim3 grid(ceil_div(bl, QG_T), ceil_div(bl, QG_T), tb->nm);
-    k_qgemm<<<grid, 256>>>(tb->Q, tb->D, tb->d_off, W[0], W[1], bl, an, tb->mlo);
+    dim3 grid(ceil_div(nt, QG_T), ceil_div(bl, QG_T), tb->nm);
+    k_qgemm<<<grid, 256>>>(tb->Q, tb->D, tb->d_off, W[0], W[1], bl, nt, an, tb->mlo);
     S2G_LAUNCHED();
   }
   S2G_CUDA(cudaDeviceSynchronize());
@@ -482,12 +510,12 @@ std::unique_ptr<RingFFT> build_ring(int K) {
 
 }  // namespace
 
-const WignerTable &wigner_table(int bl, int an) {
+const WignerTable &wigner_table(int bl, int an, int ss) {
   std::lock_guard<std::mutex> lk(g_plan_mu);
-  auto key = std::make_pair(bl, an);
+  auto key = std::make_tuple(bl, an, ss);
   auto it = g_tables.find(key);
   if (it != g_tables.end()) return *it->second;
-  auto tb = build_table(bl, an);
+  auto tb = build_table(bl, an, ss);
   const WignerTable &ref = *tb;
   g_tables.emplace(key, std::move(tb));
   return ref;

@@ -10,18 +10,20 @@
 
 namespace s2g {
 
-// Wigner-d table of one band-limit bl and direction an = |n| >= 0 on the MW
-// theta grid theta_t = pi (2t+1)/(2bl-1), t < bl, for m in [mlo, bl-1]
-// (mlo = 0 when an = 0, else -(bl-1)); per m the l-range is
-// [l0(m), bl), l0 = max(|m|, an), nl = bl - l0.
+// Wigner-d table of one band-limit bl and direction an = |n| >= 0 on the theta
+// grid of one sampling scheme, for m in [mlo, bl-1] (mlo = 0 when an = 0, else
+// -(bl-1)); per m the l-range is [l0(m), bl), l0 = max(|m|, an), nl = bl - l0.
+//   MW   (ss = 0): nt = bl rings,     theta_t = pi (2t+1)/(2bl-1)
+//   MWSS (ss = 1): nt = bl + 1 rings, theta_t = pi t / bl (both poles)
 //   D (inverse)  block m: row-major [t][l - l0]      value d^l_{m,an}(theta_t)
-//   Q (forward)  block m: row-major [l - l0][t']     value sum_t d^l_{m,an}(theta_t) W_eps[t][t'] / (2bl-1)^2
-// where W_eps (eps = (-1)^{m+an}) is the exact MW quadrature operator: extension
-// of a ring signal to the full circle with parity eps, Fourier transform,
-// convolution with w(p) = int_0^pi e^{ipt} sin t dt, and folding back.
+//   Q (forward)  block m: row-major [l - l0][t']     value sum_t d^l_{m,an}(theta_t) W_eps[t][t']
+// where W_eps (eps = (-1)^{m+an}) is the exact quadrature operator of the
+// sampling: extension of a ring signal to the full theta circle with parity
+// eps (kt = 2bl-1 or 2bl samples), Fourier transform, convolution with
+// w(p) = int_0^pi e^{ipt} sin t dt, and folding back, divided by kt^2.
 // Entries for n < 0 are read from the |n| table at -m with sign (-1)^{m+|n|}.
 struct WignerTable {
-  int bl = 0, an = 0, mlo = 0, nm = 0;
+  int bl = 0, an = 0, ss = 0, nt = 0, mlo = 0, nm = 0;
   std::vector<int64_t> off;  // host copy, nm+1 entries (elements)
   int64_t *d_off = nullptr;
   double *D = nullptr;
@@ -29,6 +31,12 @@ struct WignerTable {
   int64_t elems() const { return off.empty() ? 0 : off.back(); }
   int l0(int m) const { return (m < 0 ? -m : m) > an ? (m < 0 ? -m : m) : an; }
 };
+
+// Ring geometry of a sampling scheme at band-limit bl: rings per map and
+// samples per ring (= phi-DFT length).  The spectra of both keep m in
+// [-(bl-1), bl-1]; the MWSS Nyquist bin m = bl is dropped / zero.
+inline int grid_rings(int bl, int ss) { return ss ? bl + 1 : bl; }
+inline int grid_ring_len(int bl, int ss) { return ss ? 2 * bl : 2 * bl - 1; }
 
 // Bluestein data for ring length K (odd or even), padded FFT size P = 2^logP >= 2K-1.
 struct RingFFT {
@@ -41,7 +49,7 @@ struct RingFFT {
   float4 *chirp_df = nullptr, *bhat_df = nullptr, *tw_df = nullptr;
 };
 
-const WignerTable &wigner_table(int bl, int an);
+const WignerTable &wigner_table(int bl, int an, int ss = 0);
 const RingFFT &ring_fft(int K);
 void release_plans();
 size_t plan_bytes();

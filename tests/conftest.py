@@ -53,3 +53,47 @@ def random_flm(rng, L, spin=0, real=False, power=None):
         elif l >= abs(spin):
             flm[l * l:(l + 1) * (l + 1)] = (rng.normal(size=2 * l + 1) + 1j * rng.normal(size=2 * l + 1)) * amp
     return flm
+
+
+def params_of(g):
+    """make_parameters from a golden fixture's params (a seventh entry, when
+    present, is the sampling scheme)."""
+    from s2let_gb300.capi import make_parameters
+
+    v = g["params"]
+    ss = int(v[6]) if len(v) > 6 else 0
+    return make_parameters(int(v[0]), float(v[2]), int(v[3]), int(v[1]), int(v[4]), int(v[5]), sampling_scheme=ss)
+
+
+_SSHT_NAMES = {
+    # direction -> SSHT entry point of the oracle's restatement
+    0: "ssht_core_mw_forward_sov_conv_sym",
+    1: "ssht_core_mw_inverse_sov_sym",
+    2: "ssht_adjoint_mw_forward_sov_sym",
+    3: "ssht_adjoint_mw_inverse_sov_sym",
+}
+
+
+def oracle_sht(O, direction, x, L, spin=0, real=False, ss=0):
+    """The oracle's SSHT restatement on MW (ss=0) or MWSS (ss=1) sampling;
+    directions as s2let_gpu_sht (0 forward, 1 inverse, 2 adjoint of the
+    forward, 3 adjoint of the inverse)."""
+    import ctypes as C
+
+    name = _SSHT_NAMES[direction] + ("_ss" if ss else "") + ("_real" if real else "")
+    fn = getattr(O.lib, name)
+    fn.restype = None
+    npx = (L + 1) * 2 * L if ss else L * (2 * L - 1)
+    fdt = np.float64 if real else np.complex128
+    if direction in (0, 3):
+        f = np.ascontiguousarray(x, dtype=fdt)
+        flm = np.zeros(L * L, np.complex128)
+    else:
+        flm = np.ascontiguousarray(x, dtype=np.complex128)
+        f = np.zeros(npx, fdt)
+    first, second = (flm, f) if direction in (0, 3) else (f, flm)
+    args = [C.c_void_p(first.ctypes.data), C.c_void_p(second.ctypes.data), C.c_int(L)]
+    if not real:
+        args.append(C.c_int(spin))
+    fn(*args, C.c_int(0), C.c_int(0))
+    return flm if direction in (0, 3) else f

@@ -3,7 +3,9 @@ in place (oracle/_ref/libs2let_ref.so, see oracle/Makefile) over the project's
 SSHT/SO3 restatement.  Inputs are seeded numpy draws stored with the outputs, so
 the fixtures pin the oracle port (oracle/s2let_port.c) without the reference.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [name-prefix ...]
+(with prefixes, only the fixtures whose names start with one of them are written).
+MWSS fixtures (mwss_*) store the sampling scheme as a seventh parameter.
 """
 import os
 import sys
@@ -28,18 +30,30 @@ CASES = {
     "dir_L24_N5_s2_Jmin3": (24, 5, 2.0, 3, 2, 0),
 }
 AXI = {"axi_L16_J0": (16, 2.0, 0), "axi_L32_B3_J1": (32, 3.0, 1)}
+# McEwen-Wiaux symmetric sampling (theta_t = pi t / L, both poles, 2L phi samples)
+MWSS = {
+    "mwss_L16_N4_s0_multires": (16, 4, 2.0, 2, 0, 0),
+    "mwss_L16_N3_s2_fullres": (16, 3, 2.0, 2, 2, 1),
+    "mwss_L13_N5_s1_Jmin1": (13, 5, 2.0, 1, 1, 0),
+}
 
 
-def main():
+def main(prefixes=()):
     oracle.build(ref=True)
     R = oracle.ref()
     rng = np.random.default_rng(20261203)
-    for name, (L, N, B, J_min, spin, up) in CASES.items():
-        p = make_parameters(L, B, J_min, N, spin, up)
-        npx = L * (2 * L - 1)
-        out = {"params": np.array([L, N, B, J_min, spin, up], dtype=np.float64)}
-        f = rng.normal(size=npx) + 1j * rng.normal(size=npx)
-        flm = rng.normal(size=L * L) + 1j * rng.normal(size=L * L)
+    rng_ss = np.random.default_rng(20261204)  # MWSS inputs: a stream of their own
+    want = lambda name: not prefixes or any(name.startswith(x) for x in prefixes)
+    todo = [(k, v, 0) for k, v in CASES.items()] + [(k, v, 1) for k, v in MWSS.items()]
+    written = 0
+    for name, (L, N, B, J_min, spin, up), ss in todo:
+        p = make_parameters(L, B, J_min, N, spin, up, sampling_scheme=ss)
+        npx = (L + 1) * 2 * L if ss else L * (2 * L - 1)
+        par = [L, N, B, J_min, spin, up] + ([ss] if ss else [])
+        out = {"params": np.array(par, dtype=np.float64)}
+        rng_case = rng_ss if ss else rng
+        f = rng_case.normal(size=npx) + 1j * rng_case.normal(size=npx)
+        flm = rng_case.normal(size=L * L) + 1j * rng_case.normal(size=L * L)
         out["f"] = f
         out["flm"] = flm
         out["px2wav_wav"], out["px2wav_scal"] = R.px2wav(f, p)
@@ -53,13 +67,15 @@ def main():
         psi, phi = R.tiling(p)
         out["psi"], out["phi"] = psi, phi
         if spin == 0:
-            fr = rng.normal(size=npx)
+            fr = rng_case.normal(size=npx)
             out["f_real"] = fr
             out["px2wav_real_wav"], out["px2wav_real_scal"] = R.px2wav(fr, p, real=True)
             out["wav2px_real"] = R.wav2px(out["px2wav_real_wav"], out["px2wav_real_scal"], p, real=True)
             out["adj_wav2px_real"] = R.analysis_adjoint_wav2px(out["px2wav_real_wav"], out["px2wav_real_scal"], p,
                                                                real=True)
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        if want(name):
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+            written += 1
     for name, (L, B, J_min) in AXI.items():
         p = make_parameters(L, B, J_min, 1, 0, 0)
         npx = L * (2 * L - 1)
@@ -69,9 +85,11 @@ def main():
             w, s = R.axisym("analysis", [f], p, bool(mr), True)
             out[f"ana_mr{mr}_wav"], out[f"ana_mr{mr}_scal"] = w, s
             out[f"syn_mr{mr}"] = R.axisym("synthesis", [w, s], p, bool(mr), True)
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
-    print("wrote", len(CASES) + len(AXI), "fixtures")
+        if want(name):
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+            written += 1
+    print("wrote", written, "fixtures")
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

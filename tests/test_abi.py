@@ -121,8 +121,10 @@ def test_invalid_parameters_report_status(lib):
                 make_parameters(16, 2.0, 9, 1), make_parameters(16, 2.0, 0, 1, spin=16)):
         lib.s2let_analysis_px2wav_real(ptr(w), ptr(s), ptr(f), C.byref(bad))
         assert lib.s2let_gpu_last_error() == 1, lib.s2let_gpu_last_error_string()
-    ss = make_parameters(16, 2.0, 0, 1, sampling_scheme=1)
-    lib.s2let_analysis_px2wav_real(ptr(w), ptr(s), ptr(f), C.byref(ss))
+    # MW and MWSS are the two schemes; anything else is "not supported"
+    # (src/c/s2let_analysis.c:244-245)
+    unknown = make_parameters(16, 2.0, 0, 1, sampling_scheme=2)
+    lib.s2let_analysis_px2wav_real(ptr(w), ptr(s), ptr(f), C.byref(unknown))
     assert lib.s2let_gpu_last_error() == 2
     assert np.all(w == 0) and np.all(s == 0)
 

@@ -10,19 +10,18 @@ from math import comb, factorial, pi, sqrt
 import numpy as np
 import pytest
 
-from conftest import random_flm, rel_err
+from conftest import params_of, random_flm, rel_err
 from oracle import oracle
 from s2let_gb300.capi import make_parameters, ptr
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
 
 
-@pytest.mark.parametrize("path", [p for p in GOLDEN if "dir_" in os.path.basename(p)],
+@pytest.mark.parametrize("path", [p for p in GOLDEN if os.path.basename(p).startswith(("dir_", "mwss_"))],
                          ids=lambda p: os.path.basename(p)[:-4])
 def test_port_matches_reference_golden_directional(oracle_port, path):
     g = np.load(path)
-    L, N, B, J_min, spin, up = g["params"]
-    p = make_parameters(int(L), B, int(J_min), int(N), int(spin), int(up))
+    p = params_of(g)
     O = oracle_port
     tol = 1e-14
     w, s = O.px2wav(g["f"], p)
