@@ -393,6 +393,19 @@ const char *s2let_gpu_last_error_string(void);
 int s2let_gpu_set_precision(int mode);
 int s2let_gpu_get_precision(void);
 
+/* Wigner tables used by plans built afterwards on this thread.
+ *   0 = auto (default): stored D and Q tables while a plan's tables fit 60 % of
+ *       the free device memory (S2LET_GPU_TABLE_BUDGET_GB overrides), else the
+ *       largest band-limits recomputed;
+ *   1 = stored tables always;
+ *   2 = recomputed always: the kernels regenerate the Wigner d values from
+ *       double-double checkpoints every 64 degrees (≈ 1/50 of the memory) and
+ *       apply the forward quadrature as a separate FP64 operator.  FP64
+ *       contraction (the split-precision setting applies to stored tables only).
+ * Returns the status. */
+int s2let_gpu_set_table_mode(int mode);
+int s2let_gpu_get_table_mode(void);
+
 /* Adjoints of the plain MW transforms (host buffers): the adjoint of
  * s2let_mw_map2alm maps flm to pixels, the adjoint of s2let_mw_alm2map maps
  * pixels to flm.  These are the SSHT adjoints the reference calls internally

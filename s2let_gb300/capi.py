@@ -119,6 +119,8 @@ GPU_SIGNATURES = {
     "s2let_gpu_last_error_string": (C.c_char_p, []),
     "s2let_gpu_set_precision": (I, [I]),
     "s2let_gpu_get_precision": (I, []),
+    "s2let_gpu_set_table_mode": (I, [I]),
+    "s2let_gpu_get_table_mode": (I, []),
     "s2let_gpu_release_plans": (None, []),
     "s2let_gpu_plan_bytes": (C.c_size_t, []),
     "s2let_gpu_launch_count": (C.c_uint64, []),

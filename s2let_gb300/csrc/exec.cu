@@ -12,8 +12,10 @@
 // mirror image with the forward tables Q_n and merges all (j, n) in one kernel.
 // The axisymmetric transforms are the same machinery with one direction (n = 0)
 // per scale and the axisymmetric kernels as weights.
+#include <algorithm>
 #include <cstring>
 #include <map>
+#include <set>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -31,11 +33,14 @@ namespace s2g {
 std::atomic<uint64_t> g_launches{0};
 int current_kernel_type();  // host_layer.cpp
 thread_local int t_precision = 0;
+thread_local int t_table_mode = 0;  // 0 auto, 1 stored tables, 2 recomputed tables
 
 namespace {
 
 thread_local int t_status = 0;
 thread_local std::string t_message;
+
+int64_t table_budget_bytes();
 
 template <class T>
 T *upload(const std::vector<T> &v) {
@@ -74,6 +79,9 @@ struct WavPlan {
   int npairs = 0;
   int64_t z_per_map = 0;
   int max_bl = 1, max_nn = 1, max_ng = 1;
+  std::vector<int> rc_bl;  // band-limits whose tables are recomputed (not stored)
+  bool rc(int bl) const { return std::find(rc_bl.begin(), rc_bl.end(), bl) != rc_bl.end(); }
+  const WignerTable &table(int bl, int an) const { return wigner_table(bl, an, ss, rc(bl)); }
   int nt(int bl) const { return grid_rings(bl, ss); }
   int K(int bl) const { return grid_ring_len(bl, ss); }
   void release() {
@@ -193,11 +201,37 @@ std::unique_ptr<WavPlan> build_plan(const PlanSpec &ps) {
   P->d_w = upload(w);
   P->d_pairs = upload(pairs);
   for (auto &sd : P->sc) sd.d_ns = upload(sd.ns);
+  // stored or recomputed tables: stored while the plan's tables fit the budget,
+  // else the largest band-limits are recomputed first
+  {
+    std::map<int, std::set<int>> need;  // bl -> |n|
+    need[L].insert(std::abs(P->s));
+    need[ps.bl_scal].insert(0);
+    for (auto &sd : P->sc)
+      for (int n : sd.ns) need[sd.bl].insert(std::abs(n));
+    std::map<int, int64_t> bytes;
+    int64_t total = 0;
+    for (auto &kv : need)
+      for (int an : kv.second) {
+        const int64_t b = stored_table_bytes(kv.first, an, P->ss);
+        bytes[kv.first] += b;
+        total += b;
+      }
+    if (t_table_mode == 2) {
+      for (auto &kv : need) P->rc_bl.push_back(kv.first);
+    } else if (t_table_mode == 0) {
+      const int64_t budget = table_budget_bytes();
+      for (auto it = need.rbegin(); it != need.rend() && total > budget; ++it) {
+        P->rc_bl.push_back(it->first);
+        total -= bytes[it->first];
+      }
+    }
+  }
   // build the Wigner tables and FFT data now, outside the transforms' timing
-  wigner_table(L, std::abs(P->s), P->ss);
-  wigner_table(ps.bl_scal, 0, P->ss);
+  P->table(L, std::abs(P->s));
+  P->table(ps.bl_scal, 0);
   for (auto &sd : P->sc)
-    for (int n : sd.ns) wigner_table(sd.bl, std::abs(n), P->ss);
+    for (int n : sd.ns) P->table(sd.bl, std::abs(n));
   ring_fft(P->K(L));
   ring_fft(P->K(ps.bl_scal));
   for (auto &sd : P->sc) ring_fft(P->K(sd.bl));
@@ -206,7 +240,7 @@ std::unique_ptr<WavPlan> build_plan(const PlanSpec &ps) {
 
 // standard (tiling from the parameters), cached per parameter set ------------
 struct PlanKey {
-  int L, J_min, N, spin, original_spin, upsample, reality, real, axisym, multires, kernel, sampling;
+  int L, J_min, N, spin, original_spin, upsample, reality, real, axisym, multires, kernel, sampling, table_mode;
   double B;
   bool operator<(const PlanKey &o) const { return std::memcmp(this, &o, sizeof(PlanKey)) < 0; }
 };
@@ -226,6 +260,7 @@ const WavPlan &directional_plan(const s2let_parameters_t &p, bool real) {
   key.real = real;
   key.kernel = current_kernel_type();
   key.sampling = p.sampling_scheme;
+  key.table_mode = t_table_mode;
   key.B = p.B;
   std::lock_guard<std::mutex> lk(g_plan_mu);
   auto it = g_plans.find(key);
@@ -267,6 +302,7 @@ const WavPlan &axisym_plan(const s2let_parameters_t &p, bool real, bool multires
   key.axisym = 1;
   key.multires = multires;
   key.kernel = current_kernel_type();
+  key.table_mode = t_table_mode;
   key.B = p.B;
   std::lock_guard<std::mutex> lk(g_plan_mu);
   auto it = g_plans.find(key);
@@ -305,8 +341,9 @@ struct Sht {
   int L, s, ss;
   bool real;
   const double2 *cl;  // (-1)^s sqrt((2l+1)/4pi), l < L (device)
+  bool rc;            // recomputed table
 };
-Sht sht_of(const WavPlan &P) { return Sht{P.L, P.s, P.ss, P.real, P.d_w + P.w_cl}; }
+Sht sht_of(const WavPlan &P) { return Sht{P.L, P.s, P.ss, P.real, P.d_w + P.w_cl, P.rc(P.L)}; }
 
 // flm (nb x L^2, zero outside the computed range) <- forward transform of maps
 // (or the adjoint of the inverse)
@@ -319,7 +356,7 @@ void sht_forward(const Sht &H, const void *f, int64_t fstride, double2 *flm, int
   ring_forward(f, K, fstride, nt, spec, sw, sw, mlo, nb * nt, L, H.ss, real, S.st);
   S2G_CUDA(cudaMemsetAsync(flm, 0, sizeof(double2) * nb * L * L, S.st));
   T2L a{};
-  a.tb = &wigner_table(L, std::abs(s), H.ss);
+  a.tb = &wigner_table(L, std::abs(s), H.ss, H.rc);
   a.n = -s;
   a.use_q = !adjoint_of_inverse;
   a.mlo = mlo;
@@ -345,7 +382,7 @@ void sht_inverse(const Sht &H, const double2 *flm, bool flm_half, void *f, int64
   const int sw = real ? L : 2 * L - 1, mlo = real ? 0 : -(L - 1);
   double2 *spec = S.get<double2>((int64_t)nb * nt * sw);
   L2T a{};
-  a.tb = &wigner_table(L, std::abs(s), H.ss);
+  a.tb = &wigner_table(L, std::abs(s), H.ss, H.rc);
   a.n = -s;
   a.use_q = adjoint_of_forward;
   a.mlo = mlo;
@@ -396,7 +433,7 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
     const int sw = real ? bs : 2 * bs - 1, mlo = real ? 0 : -(bs - 1);
     double2 *spec = S.get<double2>((int64_t)nb * nts * sw);
     L2T a{};
-    a.tb = &wigner_table(bs, 0, P.ss);
+    a.tb = &P.table(bs, 0);
     a.n = 0;
     a.use_q = adj;
     a.mlo = mlo;
@@ -435,7 +472,7 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
         const int n = sd.ns[i];
         L2T &a = grp[q];
         a = L2T{};
-        a.tb = &wigner_table(bl, std::abs(n), P.ss);
+        a.tb = &P.table(bl, std::abs(n));
         a.n = n;
         a.use_q = adj;
         a.mlo = (real && n == 0) ? 0 : -(bl - 1);
@@ -502,7 +539,7 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
     ring_forward(f_scal, Ks, sstride, nts, spec, sw, sw, mlo, nb * nts, bs, P.ss, real, S.st);
     if (P.scal_lmin > 0) S2G_CUDA(cudaMemsetAsync(zs, 0, sizeof(double2) * nb * bs * bs, S.st));
     T2L a{};
-    a.tb = &wigner_table(bs, 0, P.ss);
+    a.tb = &P.table(bs, 0);
     a.n = 0;
     a.use_q = !adj;
     a.mlo = mlo;
@@ -554,7 +591,7 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
         const int n = sd.ns[i];
         T2L &a = grp[q];
         a = T2L{};
-        a.tb = &wigner_table(bl, std::abs(n), P.ss);
+        a.tb = &P.table(bl, std::abs(n));
         a.n = n;
         a.use_q = !adj;
         a.mlo = (real && n == 0) ? 0 : -(bl - 1);
@@ -582,6 +619,16 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
   }
   merge_lmn(flm, L, (int64_t)L * L, z, P.z_per_map, P.d_pairs, P.npairs, P.d_w, zs, (int64_t)bs * bs, bs,
             real, accumulate, nb, S.st);
+}
+
+// Device bytes that stored tables of one plan may take: 60 % of the memory
+// free when the plan is built (S2LET_GPU_TABLE_BUDGET_GB overrides).
+int64_t table_budget_bytes() {
+  const char *e = getenv("S2LET_GPU_TABLE_BUDGET_GB");
+  if (e && e[0]) return (int64_t)(atof(e) * 1073741824.0);
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return INT64_MAX;
+  return (int64_t)(0.6 * (double)fr);
 }
 
 // (-1)^s sqrt((2l+1)/4pi) on the device, cached per (L, s)
@@ -709,8 +756,10 @@ void run_sht(int dir, int L, int spin, bool real, int ss, void *f, double2 *flm,
   S2G_REQUIRE(std::abs(spin) < L, ERR_INVALID, "|spin| must be < L");
   if (real) S2G_REQUIRE(spin == 0, ERR_INVALID, "real signals are spin 0");
   Scratch S(st);
-  const Sht H{L, real ? 0 : spin, ss, real, cl_weights(L, real ? 0 : spin)};
-  wigner_table(L, std::abs(H.s), ss);
+  bool rc = t_table_mode == 2;
+  if (t_table_mode == 0) rc = stored_table_bytes(L, std::abs(real ? 0 : spin), ss) > table_budget_bytes();
+  const Sht H{L, real ? 0 : spin, ss, real, cl_weights(L, real ? 0 : spin), rc};
+  wigner_table(L, std::abs(H.s), ss, rc);
   const int64_t npx = (int64_t)grid_rings(L, ss) * grid_ring_len(L, ss);
   if (dir == 0 || dir == 3) {
     sht_forward(H, f, npx, flm, nb, S, dir == 3);
@@ -916,6 +965,16 @@ int s2let_gpu_set_precision(int mode) {
   return 0;
 }
 int s2let_gpu_get_precision(void) { return s2g::t_precision; }
+int s2let_gpu_set_table_mode(int mode) {
+  if (mode < 0 || mode > 2) {
+    s2g::set_status(s2g::ERR_INVALID, "s2let_gpu_set_table_mode: mode must be 0, 1 or 2");
+    s2g::report_failure();
+    return s2g::ERR_INVALID;
+  }
+  s2g::t_table_mode = mode;
+  return 0;
+}
+int s2let_gpu_get_table_mode(void) { return s2g::t_table_mode; }
 void s2let_gpu_release_plans(void) {
   s2g::guarded("s2let_gpu_release_plans", [] {
     {

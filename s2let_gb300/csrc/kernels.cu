@@ -13,6 +13,7 @@
 #include "dfconv.h"
 #include "kernels.h"
 #include "mixed.h"
+#include "recompute.h"
 #include "timing.h"
 
 namespace s2g {
@@ -1172,6 +1173,10 @@ void ring_inverse_c(const double2 *spec, int64_t spec_stride, int64_t spec_map_s
 
 void contract_l2t(const L2T &p, cudaStream_t st) {
   if (p.nb <= 0 || p.mhi < p.mlo) return;
+  if (p.tb->rc) {
+    contract_l2t_rc(p, st);
+    return;
+  }
   if (t_precision == 1 && contract_l2t_mixed(&p, 1, st)) return;
   ContractArgs a{};
   a.table = p.use_q ? p.tb->Q : p.tb->D;
@@ -1204,6 +1209,10 @@ void contract_l2t(const L2T &p, cudaStream_t st) {
 
 void contract_t2l(const T2L &p, cudaStream_t st) {
   if (p.nb <= 0 || p.mhi < p.mlo) return;
+  if (p.tb->rc) {
+    contract_t2l_rc(p, st);
+    return;
+  }
   if (t_precision == 1 && contract_t2l_mixed(&p, 1, st)) return;
   ContractArgs a{};
   a.table = p.use_q ? p.tb->Q : p.tb->D;
@@ -1234,13 +1243,13 @@ void contract_t2l(const T2L &p, cudaStream_t st) {
 
 void contract_l2t_group(const L2T *a, int n, cudaStream_t st) {
   if (n <= 0) return;
-  if (t_precision == 1 && n <= 2 && contract_l2t_mixed(a, n, st)) return;
+  if (t_precision == 1 && n <= 2 && !a[0].tb->rc && contract_l2t_mixed(a, n, st)) return;
   for (int i = 0; i < n; ++i) contract_l2t(a[i], st);
 }
 
 void contract_t2l_group(const T2L *a, int n, cudaStream_t st) {
   if (n <= 0) return;
-  if (t_precision == 1 && n <= 2 && contract_t2l_mixed(a, n, st)) return;
+  if (t_precision == 1 && n <= 2 && !a[0].tb->rc && contract_t2l_mixed(a, n, st)) return;
   for (int i = 0; i < n; ++i) contract_t2l(a[i], st);
 }
 

@@ -112,19 +112,16 @@ struct AngleDD {
   int north, pad;                             // theta <= pi/2
 };
 
-__global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ off, int bl, int nt, int an,
-                           int mlo, int nm, const double *__restrict__ start_hi,
-                           const double *__restrict__ start_lo, const int *__restrict__ start_exp,
-                           const AngleDD *__restrict__ ang) {
-  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= (int64_t)nm * nt) return;
-  const int mi = (int)(gid / nt), t = (int)(gid % nt);
-  const int m = mlo + mi;
+// One row of the recursion, (m, an) at one angle: calls sink(i, v, vp, E) for
+// i = l - l0 in [0, nl) with d^{l0+i} = v 2^E and d^{l0+i-1} = vp 2^E (vp = 0
+// at i = 0), or sink.zero() when the closed form, hence the row, vanishes.
+template <class Sink>
+__device__ void wigner_row(int bl, int an, int m, const AngleDD &A, double st_hi, double st_lo, int st_e,
+                           Sink &sink) {
   const int am = m < 0 ? -m : m;
   const int l0 = am > an ? am : an;
   const int nl = bl - l0;
   if (nl <= 0) return;
-  const AngleDD A = ang[t];
   const dd s{A.s_hi, A.s_lo}, c{A.c_hi, A.c_lo}, u{A.u_hi, A.u_lo};
   const bool north = A.north != 0;
   int ka, kb;
@@ -136,14 +133,12 @@ __global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ o
   } else {
     ka = l0 + m; kb = l0 - m;
   }
-  double *row = D + off[mi] + (int64_t)t * nl;
   if ((ka > 0 && c.hi == 0.0) || (kb > 0 && s.hi == 0.0)) {
-    // the closed form vanishes (a pole); so does the whole recursion
-    for (int i = 0; i < nl; ++i) row[i] = 0.0;
+    sink.zero();  // the closed form vanishes (a pole); so does the whole recursion
     return;
   }
-  int E = start_exp[mi], e1 = 0, e2 = 0;
-  dd v{start_hi[mi], start_lo[mi]};
+  int E = st_e, e1 = 0, e2 = 0;
+  dd v{st_hi, st_lo};
   if (ka) {
     v = dd_mul(v, dd_pow(c, ka, e1));
     E += e1;
@@ -155,14 +150,14 @@ __global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ o
   v.hi *= sign;
   v.lo *= sign;
   dd vp{0.0, 0.0};
-  row[0] = ldexp(v.hi, E);
+  sink(0, v.hi, 0.0, E);
   const double mn = (double)m * (double)an, m2 = (double)m * m, n2 = (double)an * an;
   int l = l0;
   if (l0 == 0 && nl > 1) { /* m = an = 0: d^1_{00} = cos(theta) */
     const dd x = north ? dd_add(dd{1.0, 0.0}, dd_neg(u)) : dd_add(u, dd{-1.0, 0.0});
     vp = v;
     v = dd_mul(x, v);
-    row[1] = ldexp(v.hi, E);
+    sink(1, v.hi, vp.hi, E);
     l = 1;
   }
   for (; l + 1 < bl; ++l) {
@@ -183,8 +178,79 @@ __global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ o
       vp.lo = ldexp(vp.lo, -500);
       E += 500;
     }
-    row[l + 1 - l0] = ldexp(v.hi, E);
+    sink(l + 1 - l0, v.hi, vp.hi, E);
   }
+}
+
+// the full row D[t][l - l0] of a stored table
+struct RowSink {
+  double *row;
+  int nl;
+  __device__ void zero() {
+    for (int i = 0; i < nl; ++i) row[i] = 0.0;
+  }
+  __device__ void operator()(int i, double v, double, int E) { row[i] = ldexp(v, E); }
+};
+
+__global__ void k_wigner_d(double *__restrict__ D, const int64_t *__restrict__ off, int bl, int nt, int an,
+                           int mlo, int nm, const double *__restrict__ start_hi,
+                           const double *__restrict__ start_lo, const int *__restrict__ start_exp,
+                           const AngleDD *__restrict__ ang) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (int64_t)nm * nt) return;
+  const int mi = (int)(gid / nt), t = (int)(gid % nt);
+  const int m = mlo + mi;
+  const int am = m < 0 ? -m : m;
+  const int nl = bl - (am > an ? am : an);
+  if (nl <= 0) return;
+  RowSink sink{D + off[mi] + (int64_t)t * nl, nl};
+  wigner_row(bl, an, m, ang[t], start_hi[mi], start_lo[mi], start_exp[mi], sink);
+}
+
+// Checkpoints of a recomputed table: for segment c (l from l0 + c kSeg), the
+// pair (d^{lc}, d^{lc+1}) = (a, b) 2^E with max(|a|, |b|) in [1/2, 1) (b = 0
+// when the segment holds one value; E = kCkZeroExp when the pair is zero),
+// stored at [off[mi] + c nt + t].
+struct CkptSink {
+  double2 *ab;
+  int *ex;
+  int64_t base;  // off[mi] + t
+  int nt, nl;
+  __device__ void put(int c, double a, double b, int E) {
+    const double mx = fmax(fabs(a), fabs(b));
+    if (mx == 0.0) {
+      ab[base + (int64_t)c * nt] = make_double2(0.0, 0.0);
+      ex[base + (int64_t)c * nt] = kCkZeroExp;
+      return;
+    }
+    int k;
+    frexp(mx, &k);
+    ab[base + (int64_t)c * nt] = make_double2(ldexp(a, -k), ldexp(b, -k));
+    ex[base + (int64_t)c * nt] = E + k;
+  }
+  __device__ void zero() {
+    for (int c = 0; c * kSeg < nl; ++c) put(c, 0.0, 0.0, 0);
+  }
+  __device__ void operator()(int i, double v, double vp, int E) {
+    const int r = i % kSeg;
+    if (r == 1) put(i / kSeg, vp, v, E);
+    else if (r == 0 && i == nl - 1) put(i / kSeg, v, 0.0, E);  // a segment of one value
+  }
+};
+
+__global__ void k_wigner_ckpt(double2 *__restrict__ ab, int *__restrict__ ex, const int64_t *__restrict__ off,
+                              int bl, int nt, int an, int mlo, int nm, const double *__restrict__ start_hi,
+                              const double *__restrict__ start_lo, const int *__restrict__ start_exp,
+                              const AngleDD *__restrict__ ang) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (int64_t)nm * nt) return;
+  const int mi = (int)(gid / nt), t = (int)(gid % nt);
+  const int m = mlo + mi;
+  const int am = m < 0 ? -m : m;
+  const int nl = bl - (am > an ? am : an);
+  if (nl <= 0) return;
+  CkptSink sink{ab, ex, off[mi] + t, nt, nl};
+  wigner_row(bl, an, m, ang[t], start_hi[mi], start_lo[mi], start_exp[mi], sink);
 }
 
 // w(p) = int_0^pi e^{ipt} sin t dt  (complex: +-i pi/2 at p = +-1)
@@ -330,7 +396,7 @@ void host_fft(std::vector<std::complex<double>> &x) {
 }
 
 std::mutex g_plan_mu;
-std::map<std::tuple<int, int, int>, std::unique_ptr<WignerTable>> g_tables;
+std::map<std::tuple<int, int, int, int>, std::unique_ptr<WignerTable>> g_tables;  // (bl, an, ss, rc)
 std::map<int, std::unique_ptr<RingFFT>> g_rings;
 size_t g_bytes = 0;
 
@@ -342,11 +408,38 @@ T *dev_alloc(size_t n) {
   return p;
 }
 
-std::unique_ptr<WignerTable> build_table(int bl, int an, int ss) {
+// the quadrature operators W_+ and W_- of (bl, ss), nt x nt each, cached
+// (caller holds g_plan_mu)
+std::map<std::pair<int, int>, std::pair<double *, double *>> g_wmat;
+std::pair<double *, double *> wmat_locked(int bl, int ss) {
+  auto key = std::make_pair(bl, ss);
+  auto it = g_wmat.find(key);
+  if (it != g_wmat.end()) return it->second;
+  const int nt = grid_rings(bl, ss), K = 2 * bl - 1;
+  double2 *TA = nullptr;
+  S2G_CUDA(cudaMalloc(&TA, sizeof(double2) * (size_t)K * nt));
+  double *W[2];
+  for (int e = 0; e < 2; ++e) {
+    W[e] = dev_alloc<double>((size_t)nt * nt);
+    const int eps = e == 0 ? 1 : -1;
+    k_wmat_ta<<<ceil_div((int64_t)K * nt, 128), 128>>>(TA, bl, nt, ss, eps);
+    S2G_LAUNCHED();
+    k_wmat_w<<<ceil_div((int64_t)nt * nt, 128), 128>>>(W[e], TA, bl, nt, ss, eps);
+    S2G_LAUNCHED();
+  }
+  S2G_CUDA(cudaDeviceSynchronize());
+  cudaFree(TA);
+  auto w = std::make_pair(W[0], W[1]);
+  g_wmat.emplace(key, w);
+  return w;
+}
+
+std::unique_ptr<WignerTable> build_table(int bl, int an, int ss, bool rc) {
   auto tb = std::make_unique<WignerTable>();
   tb->bl = bl;
   tb->an = an;
   tb->ss = ss;
+  tb->rc = rc;
   tb->nt = grid_rings(bl, ss);
   const int nt = tb->nt;
   tb->mlo = an == 0 ? 0 : -(bl - 1);
@@ -410,11 +503,9 @@ std::unique_ptr<WignerTable> build_table(int bl, int an, int ss) {
       ang[t].pad = 0;
     }
   }
-  const int64_t n = tb->elems();
-  tb->D = dev_alloc<double>(n);
-  tb->Q = dev_alloc<double>(n);
-  tb->d_off = dev_alloc<int64_t>(tb->nm + 1);
-  S2G_CUDA(cudaMemcpy(tb->d_off, tb->off.data(), sizeof(int64_t) * (tb->nm + 1), cudaMemcpyHostToDevice));
+  const auto W = wmat_locked(bl, ss);
+  tb->W[0] = W.first;
+  tb->W[1] = W.second;
   double *d_hi = nullptr, *d_lo = nullptr;
   int *d_ex = nullptr;
   AngleDD *d_ang = nullptr;
@@ -426,34 +517,37 @@ std::unique_ptr<WignerTable> build_table(int bl, int an, int ss) {
   S2G_CUDA(cudaMemcpy(d_lo, st_lo.data(), sizeof(double) * tb->nm, cudaMemcpyHostToDevice));
   S2G_CUDA(cudaMemcpy(d_ex, ex.data(), sizeof(int) * tb->nm, cudaMemcpyHostToDevice));
   S2G_CUDA(cudaMemcpy(d_ang, ang.data(), sizeof(AngleDD) * nt, cudaMemcpyHostToDevice));
-  {
-    const int64_t nthr = (int64_t)tb->nm * nt;
+  const int64_t nthr = (int64_t)tb->nm * nt;
+  if (!rc) {
+    const int64_t n = tb->elems();
+    tb->D = dev_alloc<double>(n);
+    tb->Q = dev_alloc<double>(n);
+    tb->d_off = dev_alloc<int64_t>(tb->nm + 1);
+    S2G_CUDA(cudaMemcpy(tb->d_off, tb->off.data(), sizeof(int64_t) * (tb->nm + 1), cudaMemcpyHostToDevice));
     k_wigner_d<<<ceil_div(nthr, 128), 128>>>(tb->D, tb->d_off, bl, nt, an, tb->mlo, tb->nm, d_hi, d_lo, d_ex,
                                              d_ang);
     S2G_LAUNCHED();
-  }
-  // W_+ and W_- (exact forward quadrature operators), then Q = D^T W per m
-  const int K = 2 * bl - 1;
-  double2 *TA = nullptr;
-  double *W[2] = {nullptr, nullptr};
-  S2G_CUDA(cudaMalloc(&TA, sizeof(double2) * (size_t)K * nt));
-  for (int e = 0; e < 2; ++e) {
-    S2G_CUDA(cudaMalloc(&W[e], sizeof(double) * (size_t)nt * nt));
-    const int eps = e == 0 ? 1 : -1;
-    k_wmat_ta<<<ceil_div((int64_t)K * nt, 128), 128>>>(TA, bl, nt, ss, eps);
-    S2G_LAUNCHED();
-    k_wmat_w<<<ceil_div((int64_t)nt * nt, 128), 128>>>(W[e], TA, bl, nt, ss, eps);
-    S2G_LAUNCHED();
-  }
-  {
+    // Q = D^T W per m
     dim3 grid(ceil_div(nt, QG_T), ceil_div(bl, QG_T), tb->nm);
-    k_qgemm<<<grid, 256>>>(tb->Q, tb->D, tb->d_off, W[0], W[1], bl, nt, an, tb->mlo);
+    k_qgemm<<<grid, 256>>>(tb->Q, tb->D, tb->d_off, W.first, W.second, bl, nt, an, tb->mlo);
+    S2G_LAUNCHED();
+  } else {
+    tb->coff.assign(tb->nm + 1, 0);
+    for (int mi = 0; mi < tb->nm; ++mi) tb->coff[mi + 1] = tb->coff[mi] + (int64_t)tb->nseg(tb->mlo + mi) * nt;
+    const int64_t nc = tb->coff.back();
+    tb->ck = dev_alloc<double2>(nc);
+    tb->ck_e = dev_alloc<int>(nc);
+    tb->d_coff = dev_alloc<int64_t>(tb->nm + 1);
+    S2G_CUDA(cudaMemcpy(tb->d_coff, tb->coff.data(), sizeof(int64_t) * (tb->nm + 1), cudaMemcpyHostToDevice));
+    std::vector<double2> uq(nt);
+    for (int t = 0; t < nt; ++t) uq[t] = make_double2(ang[t].u_hi, ang[t].north ? 1.0 : 0.0);
+    tb->uq = dev_alloc<double2>(nt);
+    S2G_CUDA(cudaMemcpy(tb->uq, uq.data(), sizeof(double2) * nt, cudaMemcpyHostToDevice));
+    k_wigner_ckpt<<<ceil_div(nthr, 128), 128>>>(tb->ck, tb->ck_e, tb->d_coff, bl, nt, an, tb->mlo, tb->nm, d_hi,
+                                                d_lo, d_ex, d_ang);
     S2G_LAUNCHED();
   }
   S2G_CUDA(cudaDeviceSynchronize());
-  cudaFree(TA);
-  cudaFree(W[0]);
-  cudaFree(W[1]);
   cudaFree(d_hi);
   cudaFree(d_lo);
   cudaFree(d_ex);
@@ -510,12 +604,12 @@ std::unique_ptr<RingFFT> build_ring(int K) {
 
 }  // namespace
 
-const WignerTable &wigner_table(int bl, int an, int ss) {
+const WignerTable &wigner_table(int bl, int an, int ss, bool rc) {
   std::lock_guard<std::mutex> lk(g_plan_mu);
-  auto key = std::make_tuple(bl, an, ss);
+  auto key = std::make_tuple(bl, an, ss, rc ? 1 : 0);
   auto it = g_tables.find(key);
   if (it != g_tables.end()) return *it->second;
-  auto tb = build_table(bl, an, ss);
+  auto tb = build_table(bl, an, ss, rc);
   const WignerTable &ref = *tb;
   g_tables.emplace(key, std::move(tb));
   return ref;
@@ -538,7 +632,16 @@ void release_plans() {
     cudaFree(kv.second->D);
     cudaFree(kv.second->Q);
     cudaFree(kv.second->d_off);
+    cudaFree(kv.second->ck);
+    cudaFree(kv.second->ck_e);
+    cudaFree(kv.second->d_coff);
+    cudaFree(kv.second->uq);
   }
+  for (auto &kv : g_wmat) {
+    cudaFree(kv.second.first);
+    cudaFree(kv.second.second);
+  }
+  g_wmat.clear();
   for (auto &kv : g_rings) {
     cudaFree(kv.second->chirp);
     cudaFree(kv.second->bhat);
@@ -550,6 +653,17 @@ void release_plans() {
   g_tables.clear();
   g_rings.clear();
   g_bytes = 0;
+}
+
+int64_t stored_table_bytes(int bl, int an, int ss) {
+  // sum over m of (bl - l0(m)) nt entries, D and Q, 8 B each
+  const int nt = grid_rings(bl, ss), mlo = an == 0 ? 0 : -(bl - 1);
+  int64_t e = 0;
+  for (int m = mlo; m < bl; ++m) {
+    const int am = m < 0 ? -m : m, l0 = am > an ? am : an;
+    if (l0 < bl) e += (int64_t)(bl - l0) * nt;
+  }
+  return 16 * e;
 }
 
 size_t plan_bytes() {

@@ -22,14 +22,36 @@ namespace s2g {
 // eps (kt = 2bl-1 or 2bl samples), Fourier transform, convolution with
 // w(p) = int_0^pi e^{ipt} sin t dt, and folding back, divided by kt^2.
 // Entries for n < 0 are read from the |n| table at -m with sign (-1)^{m+|n|}.
+//
+// A recomputed table (rc = true) stores neither D nor Q.  It keeps, per m,
+// theta ring t and segment c of kSeg degrees starting at lc = l0 + c kSeg,
+// the checkpoint pair (d^{lc}, d^{lc+1}) = (a, b) 2^E from the double-double
+// recursion (ck / ck_e at [coff[mi] + c nt + t]); the contraction kernels
+// regenerate the segment from it with the FP64 three-term recursion, written
+// in u = 2 sin^2(theta/2) (north) or 2 cos^2(theta/2) (south) as uq[t] =
+// (u, north).  The forward quadrature is applied as the nt x nt operators
+// W_eps (W[0]: eps = +1, W[1]: eps = -1), shared by all tables of (bl, ss).
+// Memory: 20 B per kSeg entries instead of 16 B per entry.
+constexpr int kSeg = 64;
+constexpr int kCkZeroExp = -100000;  // exponent of an all-zero checkpoint
+
 struct WignerTable {
   int bl = 0, an = 0, ss = 0, nt = 0, mlo = 0, nm = 0;
+  bool rc = false;
   std::vector<int64_t> off;  // host copy, nm+1 entries (elements)
   int64_t *d_off = nullptr;
   double *D = nullptr;
   double *Q = nullptr;
+  // recomputed tables
+  std::vector<int64_t> coff;  // host copy, nm+1 entries (checkpoints)
+  int64_t *d_coff = nullptr;
+  double2 *ck = nullptr;
+  int *ck_e = nullptr;
+  double2 *uq = nullptr;
+  const double *W[2] = {nullptr, nullptr};
   int64_t elems() const { return off.empty() ? 0 : off.back(); }
   int l0(int m) const { return (m < 0 ? -m : m) > an ? (m < 0 ? -m : m) : an; }
+  int nseg(int m) const { return (bl - l0(m) + kSeg - 1) / kSeg; }
 };
 
 // Ring geometry of a sampling scheme at band-limit bl: rings per map and
@@ -49,7 +71,11 @@ struct RingFFT {
   float4 *chirp_df = nullptr, *bhat_df = nullptr, *tw_df = nullptr;
 };
 
-const WignerTable &wigner_table(int bl, int an, int ss = 0);
+// rc: recomputed (checkpointed) table instead of stored D and Q
+const WignerTable &wigner_table(int bl, int an, int ss = 0, bool rc = false);
+// device bytes of the stored D and Q tables of (bl, an) on the sampling's grid
+// (for the choice between stored and recomputed tables)
+int64_t stored_table_bytes(int bl, int an, int ss);
 const RingFFT &ring_fft(int K);
 void release_plans();
 size_t plan_bytes();
