@@ -1039,6 +1039,14 @@ __global__ void k_scale_copy(const double *x, double *y, int64_t n, double s) {
   if (i < n) y[i] = x[i] * s;
 }
 
+// y[b * ys + i] = a x[b * xs + i] + c y[b * ys + i], i < n, b < nb
+__global__ void k_axpby(const double *x, int64_t xs, double *y, int64_t ys, int64_t n, int nb, double a, double c) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n * nb) return;
+  const int64_t b = g / n, i = g - b * n;
+  y[b * ys + i] = fma(a, x[b * xs + i], c * y[b * ys + i]);
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1363,6 +1371,13 @@ void symmetrize_flm(double2 *flm, int L, int64_t fs, int nb, cudaStream_t st) {
 void scale_copy(const double *x, double *y, int64_t n, double s, cudaStream_t st) {
   if (n <= 0) return;
   k_scale_copy<<<ceil_div(n, 256), 256, 0, st>>>(x, y, n, s);
+  S2G_LAUNCHED();
+}
+
+void axpby(const double *x, int64_t xs, double *y, int64_t ys, int64_t n, int nb, double a, double c,
+           cudaStream_t st) {
+  if (n <= 0 || nb <= 0) return;
+  k_axpby<<<ceil_div(n * nb, 256), 256, 0, st>>>(x, xs, y, ys, n, nb, a, c);
   S2G_LAUNCHED();
 }
 

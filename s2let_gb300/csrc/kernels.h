@@ -122,6 +122,9 @@ void symmetrize_flm(double2 *flm, int L, int64_t fs, int nb, cudaStream_t st);
 
 // elementwise: y[i] = x[i] * s (complex or real, as doubles)
 void scale_copy(const double *x, double *y, int64_t n, double s, cudaStream_t st);
+// batched elementwise on doubles: y_b = a x_b + c y_b (rows of n at strides xs, ys)
+void axpby(const double *x, int64_t xs, double *y, int64_t ys, int64_t n, int nb, double a, double c,
+           cudaStream_t st);
 
 }  // namespace s2g
 
