@@ -75,10 +75,12 @@ def args_():
     ap.add_argument("--N", type=int, default=4)
     ap.add_argument("--B", type=float, default=2.0)
     ap.add_argument("--J_min", type=int, default=2)
-    ap.add_argument("--workload", default="metric", choices=["metric", "spin2", "sparsity"],
+    ap.add_argument("--workload", default="metric", choices=["metric", "spin2", "sparsity", "uneven", "L2048"],
                     help="metric: the headline (real maps, L=1024, N=4); spin2: complex spin-2 maps, "
                          "L=1024, N=5, J_min=3, error per scale; sparsity: differentiable wavelet-sparsity "
-                         "loss, 32 real maps at L=256, forward + backward")
+                         "loss, 32 real maps at L=256, forward + backward; uneven: 256 maps of their own L, N "
+                         "and spin in one graph-replayed call against a call-per-map loop; L2048: one real map "
+                         "at L=2048, N=4 with recomputed Wigner tables")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -260,6 +262,8 @@ def run_workload(a, world, rank, local):
 
     rel = lambda x, y: float(((x - y).abs().max() / y.abs().max()).item())
     clocks = ClockSampler(local)
+    if a.workload in ("uneven", "L2048"):
+        return run_recompute_workload(a, world, rank, local)
     out = {"n_gpus": world, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "data": "synthetic"}
     if a.workload == "spin2":
@@ -342,6 +346,175 @@ def run_workload(a, world, rank, local):
             "max_rel_err_grad_vs_fp64": rel(grads["mixed"], grads["fp64"]),
             "clocks": clk,
         })
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def uneven_parameters(rng, n):
+    """The uneven configuration: L log-uniform on [64, 512] rounded to even,
+    N uniform in {1, 3, 5}, spin uniform in {0, 2} (spin-0 maps real, spin-2
+    maps complex), B = 2, J_min = 1."""
+    out = []
+    for _ in range(n):
+        L = int(2 * round(np.exp(rng.uniform(np.log(64), np.log(512))) / 2))
+        out.append((L, int(rng.choice([1, 3, 5])), int(rng.choice([0, 2]))))
+    return out
+
+
+def run_recompute_workload(a, world, rank, local):
+    """Workloads on recomputed Wigner tables (FP64 contraction): the uneven
+    batch and the L = 2048 map, whose stored tables would not fit."""
+    import time
+
+    import torch
+
+    import s2let_gb300
+    from s2let_gb300.capi import S2letParameters, make_parameters
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    api = s2let_gb300.api()
+    lib = api.lib
+    lib.s2let_gpu_set_precision(0)
+    stream = torch.cuda.Stream(dev)
+    sp = C.c_void_p(stream.cuda_stream)
+    clocks = ClockSampler(local)
+
+    def event_ms(fn, steps):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    out = {"n_gpus": world, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "data": "synthetic", "unit": "maps/s", "dtype": "f64"}
+    if a.workload == "uneven":
+        lib.s2let_gpu_set_table_mode(2)
+        rng = np.random.default_rng(replica_seed(rank))
+        maps = uneven_parameters(rng, 256)
+        n = len(maps)
+        params = (S2letParameters * n)()
+        real = (C.c_int * n)()
+        px, wav, scal, rec = [], [], [], []
+        for k, (L, N, spin) in enumerate(maps):
+            params[k] = make_parameters(L, 2.0, 1, N, spin, 0)
+            real[k] = 1 if spin == 0 else 0
+            sz = api.sizes(params[k])
+            dt = torch.float64 if real[k] else torch.complex128
+            flm = power_law_real_flm(rng, L) if real[k] else spin2_flm(rng, L, spin)
+            f = api.alm2map(flm, L, spin, real=bool(real[k]))
+            px.append(torch.from_numpy(f).to(dev))
+            wav.append(torch.zeros(sz["n_wav"], dtype=dt, device=dev))
+            scal.append(torch.zeros(sz["n_scal"], dtype=dt, device=dev))
+            rec.append(torch.zeros_like(px[-1]))
+
+        def arrays(idx):
+            m = len(idx)
+            pa = (S2letParameters * m)(*[params[k] for k in idx])
+            ra = (C.c_int * m)(*[real[k] for k in idx])
+            ptr = lambda ts: (C.c_void_p * m)(*[ts[k].data_ptr() for k in idx])
+            return pa, ra, ptr(px), ptr(wav), ptr(scal), ptr(rec), m
+
+        def multi_step(arr):
+            pa, ra, P, W, S_, R, m = arr
+            assert lib.s2let_gpu_px2wav_multi(W, S_, P, pa, ra, m, 1, sp) == 0
+            assert lib.s2let_gpu_wav2px_multi(R, W, S_, pa, ra, m, 1, sp) == 0
+
+        def loop_step():
+            for k in range(n):
+                p = C.byref(params[k])
+                if real[k]:
+                    lib.s2let_gpu_analysis_px2wav_real_batch(wav[k].data_ptr(), scal[k].data_ptr(),
+                                                             px[k].data_ptr(), 1, p, sp)
+                    lib.s2let_gpu_synthesis_wav2px_real_batch(rec[k].data_ptr(), wav[k].data_ptr(),
+                                                              scal[k].data_ptr(), 1, p, sp)
+                else:
+                    lib.s2let_gpu_analysis_px2wav_batch(wav[k].data_ptr(), scal[k].data_ptr(),
+                                                        px[k].data_ptr(), 1, p, sp)
+                    lib.s2let_gpu_synthesis_wav2px_batch(rec[k].data_ptr(), wav[k].data_ptr(),
+                                                         scal[k].data_ptr(), 1, p, sp)
+
+        allidx = list(range(n))
+        arr = arrays(allidx)
+        t0 = time.time()
+        multi_step(arr)  # builds every plan (eager pass)
+        torch.cuda.synchronize()
+        build_s = time.time() - t0
+        for _ in range(max(a.warmup, 2)):  # the second call captures the graph
+            multi_step(arr)
+        clocks.start()
+        ms = event_ms(lambda: multi_step(arr), a.steps)
+        clk = clocks.stop()
+        err = max(float(((rec[k] - px[k]).abs().max() / px[k].abs().max()).item()) for k in range(n))
+        for _ in range(a.warmup):
+            loop_step()
+        loop_ms = event_ms(loop_step, a.steps)
+        buckets = {}
+        for lo, hi in ((64, 128), (128, 256), (256, 513)):
+            idx = [k for k in range(n) if lo <= maps[k][0] < hi]
+            if not idx:
+                continue
+            arr_b = arrays(idx)
+            for _ in range(3):
+                multi_step(arr_b)
+            bms = event_ms(lambda: multi_step(arr_b), a.steps)
+            buckets[f"L{lo}-{min(hi, 512)}"] = {"maps": len(idx), "maps_per_s": len(idx) / (bms * 1e-3),
+                                                "ms": bms}
+        out.update({
+            "metric": "uneven batch px2wav+wav2px maps/s (256 maps, own L/N/spin each, one graph-replayed call)",
+            "value": whole_job_rate(n, world, ms * 1e-3), "ms_per_step": ms,
+            "config": {"workload": "256 maps, L log-uniform on [64, 512] rounded to even, N in {1,3,5}, "
+                                   "spin in {0,2} (spin 0 real, spin 2 complex), B=2, J_min=1, MW, "
+                                   "power-law flm; FP64 storage, recomputed Wigner tables, FP64 contraction",
+                       "distinct_parameter_sets": len({(m[0], m[1], m[2]) for m in maps}),
+                       "l2": "inputs and outputs of the 256 maps exceed L2"},
+            "one_call_per_map_loop": {"value": whole_job_rate(n, world, loop_ms * 1e-3), "ms_per_step": loop_ms},
+            "per_L_bucket": buckets,
+            "plan_build_s": build_s,
+            "max_rel_err_round_trip": err,
+            "clocks": clk,
+        })
+    else:
+        L = 2048
+        p = make_parameters(L, 2.0, 2, 4, 0, 0)
+        rng = np.random.default_rng(replica_seed(rank))
+        lib.s2let_gpu_set_table_mode(2)
+        f = torch.from_numpy(api.sht(1, power_law_real_flm(rng, L), L, 0, True)).to(dev)[None, :].contiguous()
+        lib.s2let_gpu_set_table_mode(0)
+        sz = api.sizes(p)
+        w = torch.zeros((1, sz["n_wav"]), dtype=torch.float64, device=dev)
+        s_ = torch.zeros((1, sz["n_scal"]), dtype=torch.float64, device=dev)
+        r = torch.zeros_like(f)
+        pp = C.byref(p)
+
+        def step():
+            lib.s2let_gpu_analysis_px2wav_real_batch(w.data_ptr(), s_.data_ptr(), f.data_ptr(), 1, pp, sp)
+            lib.s2let_gpu_synthesis_wav2px_real_batch(r.data_ptr(), w.data_ptr(), s_.data_ptr(), 1, pp, sp)
+
+        t0 = time.time()
+        step()
+        torch.cuda.synchronize()
+        build_s = time.time() - t0
+        for _ in range(max(1, a.warmup - 1)):
+            step()
+        clocks.start()
+        ms = event_ms(step, a.steps)
+        clk = clocks.stop()
+        out.update({
+            "metric": "px2wav+wav2px maps/s at L=2048, N=4 (recomputed Wigner tables, FP64)",
+            "value": whole_job_rate(1, world, ms * 1e-3), "ms_per_step": ms,
+            "config": {"workload": "one real spin-0 map, L=2048, N=4, B=2, J_min=2, upsample=0, MW, "
+                                   "power-law band-limited flm", "table_bytes_device": lib.s2let_gpu_plan_bytes()},
+            "plan_build_s": build_s,
+            "max_rel_err_round_trip": float(((r - f).abs().max() / f.abs().max()).item()),
+            "clocks": clk,
+        })
+    lib.s2let_gpu_set_table_mode(0)
     if rank == 0:
         print(json.dumps(out), flush=True)
 

@@ -430,6 +430,23 @@ void s2let_gpu_release_plans(void);
 /* Bytes of device memory currently held by cached plans. */
 size_t s2let_gpu_plan_bytes(void);
 
+/* Heterogeneous batches: map k has its own parameters params[k] (band-limit,
+ * N, spin, B, J_min, upsample, sampling) and reality real[k] (nonzero: a real
+ * map, double buffers; else complex).  f[k], f_wav[k], f_scal[k] are DEVICE
+ * pointers to one map's buffers of the reference's layout (s2let_n_px /
+ * s2let_n_wav / s2let_n_scal of params[k]); work is enqueued on `stream`.
+ * Maps with equal parameters run as one batch.  use_graph != 0 with a
+ * non-default stream: the first call with a given set of parameters and
+ * pointers runs eagerly and builds the plans, the second captures the whole
+ * launch sequence into a CUDA graph, later calls replay the graph (one launch).
+ * s2let_gpu_release_plans() drops the graphs.  Returns the status. */
+int s2let_gpu_px2wav_multi(void *const *f_wav, void *const *f_scal, void *const *f,
+                           const s2let_parameters_t *params, const int *real, int nmaps, int use_graph,
+                           void *stream);
+int s2let_gpu_wav2px_multi(void *const *f, void *const *f_wav, void *const *f_scal,
+                           const s2let_parameters_t *params, const int *real, int nmaps, int use_graph,
+                           void *stream);
+
 /*
  * Batched device-pointer entry points.  All pointers are DEVICE pointers; `stream`
  * is a cudaStream_t (NULL = default stream).  `nbatch` maps share one parameter

@@ -27,6 +27,7 @@
 #include "mixed.h"
 #include "plan.h"
 #include "runtime.h"
+#include "timing.h"
 
 namespace s2g {
 
@@ -795,6 +796,126 @@ void run_sht(int dir, int L, int spin, bool real, int ss, void *f, double2 *flm,
   }
 }
 
+// ---------------------------------------------------------------------------
+// heterogeneous batches: every map with its own parameters
+// ---------------------------------------------------------------------------
+
+// One pass over the maps on stream st.  Maps with equal parameters (and
+// reality) run as one batch on contiguous scratch: inputs gathered and outputs
+// scattered with device-to-device copies; a map alone runs in place.
+void multi_pass(Op op, int n, const s2let_parameters_t *params, const int *real, void *const *px,
+                void *const *wav, void *const *scal, cudaStream_t st) {
+  std::map<std::string, std::vector<int>> groups;
+  for (int k = 0; k < n; ++k) {
+    std::string key((const char *)&params[k], sizeof(s2let_parameters_t));
+    key.push_back(real[k] ? 1 : 0);
+    groups[key].push_back(k);
+  }
+  for (auto &kv : groups) {
+    const std::vector<int> &g = kv.second;
+    const s2let_parameters_t &p = params[g[0]];
+    const bool re = real[g[0]] != 0;
+    if (g.size() == 1) {
+      run_directional(op, p, re, px[g[0]], nullptr, wav[g[0]], scal[g[0]], 1, st);
+      continue;
+    }
+    const int nb = (int)g.size();
+    const size_t esz = re ? sizeof(double) : sizeof(double2);
+    const size_t bpx = esz * s2let_n_px(&p), bw = esz * s2let_n_wav(&p), bs = esz * s2let_n_scal(&p);
+    Scratch S(st);
+    char *dpx = S.get<char>((int64_t)nb * bpx), *dw = S.get<char>((int64_t)nb * bw),
+         *ds = S.get<char>((int64_t)nb * bs);
+    const bool fwd = (op == OP_PX2WAV || op == OP_ADJ_PX2WAV);
+    for (int i = 0; i < nb; ++i) {
+      const int k = g[i];
+      if (fwd) {
+        S2G_CUDA(cudaMemcpyAsync(dpx + i * bpx, px[k], bpx, cudaMemcpyDeviceToDevice, st));
+      } else {
+        S2G_CUDA(cudaMemcpyAsync(dw + i * bw, wav[k], bw, cudaMemcpyDeviceToDevice, st));
+        S2G_CUDA(cudaMemcpyAsync(ds + i * bs, scal[k], bs, cudaMemcpyDeviceToDevice, st));
+      }
+    }
+    run_directional(op, p, re, dpx, nullptr, dw, ds, nb, st);
+    for (int i = 0; i < nb; ++i) {
+      const int k = g[i];
+      if (fwd) {
+        S2G_CUDA(cudaMemcpyAsync(wav[k], dw + i * bw, bw, cudaMemcpyDeviceToDevice, st));
+        S2G_CUDA(cudaMemcpyAsync(scal[k], ds + i * bs, bs, cudaMemcpyDeviceToDevice, st));
+      } else {
+        S2G_CUDA(cudaMemcpyAsync(px[k], dpx + i * bpx, bpx, cudaMemcpyDeviceToDevice, st));
+      }
+    }
+  }
+}
+
+// Graphs of repeated heterogeneous batches, keyed by everything the launch
+// sequence depends on (operation, parameters, reality, pointers, precision,
+// table mode, wavelet kernel).  The first call with a key runs eagerly (it
+// builds the plans: device allocation and host synchronisation, which a
+// capture cannot contain); the second captures the pass into a CUDA graph; later
+// calls replay it.  Plans released => graphs released.
+std::mutex g_multi_mu;
+std::map<std::string, cudaGraphExec_t> g_multi_graphs;
+std::set<std::string> g_multi_seen;
+
+void release_multi_graphs() {
+  std::lock_guard<std::mutex> lk(g_multi_mu);
+  for (auto &kv : g_multi_graphs) cudaGraphExecDestroy(kv.second);
+  g_multi_graphs.clear();
+  g_multi_seen.clear();
+}
+
+void run_multi(Op op, int n, const s2let_parameters_t *params, const int *real, void *const *px,
+               void *const *wav, void *const *scal, bool use_graph, cudaStream_t st) {
+  S2G_REQUIRE(n >= 0, ERR_INVALID, "negative map count");
+  S2G_REQUIRE(n == 0 || (params && real && px && wav && scal), ERR_INVALID, "NULL array");
+  for (int k = 0; k < n; ++k) validate(&params[k]);
+  if (!use_graph || st == nullptr || timing_enabled()) {
+    multi_pass(op, n, params, real, px, wav, scal, st);
+    return;
+  }
+  std::string key;
+  auto put = [&key](const void *x, size_t b) { key.append((const char *)x, b); };
+  const int op_i = (int)op, kern = current_kernel_type();
+  put(&op_i, sizeof op_i);
+  put(&n, sizeof n);
+  put(params, sizeof(s2let_parameters_t) * n);
+  put(real, sizeof(int) * n);
+  put(px, sizeof(void *) * n);
+  put(wav, sizeof(void *) * n);
+  put(scal, sizeof(void *) * n);
+  put(&t_precision, sizeof t_precision);
+  put(&t_table_mode, sizeof t_table_mode);
+  put(&kern, sizeof kern);
+  std::lock_guard<std::mutex> lk(g_multi_mu);
+  auto it = g_multi_graphs.find(key);
+  if (it != g_multi_graphs.end()) {
+    S2G_CUDA(cudaGraphLaunch(it->second, st));
+    return;
+  }
+  if (!g_multi_seen.count(key)) {
+    multi_pass(op, n, params, real, px, wav, scal, st);
+    g_multi_seen.insert(key);
+    return;
+  }
+  cudaGraph_t graph = nullptr;
+  S2G_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  try {
+    multi_pass(op, n, params, real, px, wav, scal, st);
+  } catch (...) {
+    cudaStreamEndCapture(st, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    throw;
+  }
+  S2G_CUDA(cudaStreamEndCapture(st, &graph));
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  S2G_CUDA(e);
+  g_multi_graphs.emplace(key, exec);
+  S2G_CUDA(cudaGraphLaunch(exec, st));
+}
+
 }  // namespace s2g
 
 // ===========================================================================
@@ -1009,6 +1130,7 @@ void s2let_gpu_release_plans(void) {
       for (auto &kv : s2g::g_plans) kv.second->release();
       s2g::g_plans.clear();
     }
+    s2g::release_multi_graphs();
     s2g::release_sliced_tables();
     s2g::release_plans();
   });
@@ -1177,6 +1299,24 @@ int s2let_gpu_sht(int dir, int sampling_scheme, int L, int spin, int real, void 
   }
   host_sht(__func__, dir, L, spin, real != 0, f, flm, sampling_scheme == S2LET_SAMPLING_MW_SS);
   return s2g::last_status();
+}
+
+// ---- heterogeneous batches (device pointers, per-map parameters)
+int s2let_gpu_px2wav_multi(void *const *f_wav, void *const *f_scal, void *const *f,
+                           const s2let_parameters_t *params, const int *real, int nmaps, int use_graph,
+                           void *stream) {
+  return s2g::guarded(__func__, [&] {
+    s2g::ensure_device();
+    s2g::run_multi(s2g::OP_PX2WAV, nmaps, params, real, f, f_wav, f_scal, use_graph != 0, (cudaStream_t)stream);
+  });
+}
+int s2let_gpu_wav2px_multi(void *const *f, void *const *f_wav, void *const *f_scal,
+                           const s2let_parameters_t *params, const int *real, int nmaps, int use_graph,
+                           void *stream) {
+  return s2g::guarded(__func__, [&] {
+    s2g::ensure_device();
+    s2g::run_multi(s2g::OP_WAV2PX, nmaps, params, real, f, f_wav, f_scal, use_graph != 0, (cudaStream_t)stream);
+  });
 }
 
 // ---- batched device-pointer extensions
