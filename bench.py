@@ -636,6 +636,7 @@ def main():
     lib.s2let_gpu_timing_report(rep, 6)
     lib.s2let_gpu_timing_enable(0)
     cats = ["fp64_contraction", "ring_dft", "gamma_dft", "tiling_merge", "tensor_contraction", "other"]
+    # (categories 6 and 7, the recomputed-table contractions and quadrature, do not run here)
     kernels = {c: {"launches": int(rep[4 * i]), "ms": rep[4 * i + 1], "flops": rep[4 * i + 2],
                    "bytes": rep[4 * i + 3]} for i, c in enumerate(cats)}
     dom = max(kernels, key=lambda c: kernels[c]["ms"])

@@ -218,11 +218,14 @@ size_t rc_t2l_smem() {
 }
 
 // grid: x = m, y = segment, z = batch chunk.  Threads generate one ring's row of
-// the tile each, then contract as (degree li = tid % kSeg, map half tid / kSeg).
+// the tile each, then contract as (degree li = tid % kSeg, half bh = tid / kSeg):
+// with NBT >= 2 each half takes half of the maps over all rings of the tile;
+// with NBT = 1 each half takes half of the rings, and the halves add up at the end.
 template <int NBT>
 __global__ void __launch_bounds__(kRcT) k_rc_t2l(RcArgs a) {
-  static_assert(NBT % 2 == 0, "two map halves");
-  constexpr int NH = NBT / 2;
+  static_assert(NBT == 1 || NBT % 2 == 0, "one map, or two map halves");
+  constexpr int NH = NBT == 1 ? 1 : NBT / 2;
+  constexpr bool SPLIT_T = NBT == 1;
   extern __shared__ double smem_rc[];
   double *tile = smem_rc;                                   // [kRcT][kTileLd]
   double2 *sg = (double2 *)(smem_rc + kRcT * kTileLd);      // [kRcT][NBT]
@@ -292,24 +295,34 @@ __global__ void __launch_bounds__(kRcT) k_rc_t2l(RcArgs a) {
     }
     __syncthreads();
     const int tl_end = min(kRcT, a.nt - t0);
+    const int tl_lo = SPLIT_T ? bh * (kRcT / 2) : 0;
+    const int tl_hi = SPLIT_T ? min(tl_end, tl_lo + kRcT / 2) : tl_end;
 #pragma unroll 4
-    for (int tl = 0; tl < tl_end; ++tl) {
+    for (int tl = tl_lo; tl < tl_hi; ++tl) {
       const double d = tile[tl * kTileLd + li];
 #pragma unroll
       for (int j = 0; j < NH; ++j) {
-        const double2 g = sg[tl * NBT + bh * NH + j];
+        const double2 g = sg[tl * NBT + (SPLIT_T ? 0 : bh * NH) + j];
         acc[j].x = fma(d, g.x, acc[j].x);
         acc[j].y = fma(d, g.y, acc[j].y);
       }
     }
     __syncthreads();
   }
+  if (SPLIT_T) {  // second half of the rings hands its sums to the first
+    double2 *red = sg;  // free after the last tile
+    if (bh == 1) red[li] = acc[0];
+    __syncthreads();
+    if (bh == 1) return;
+    acc[0].x += red[li].x;
+    acc[0].y += red[li].y;
+  }
   const int l = lc + li;
   if (li >= n || l < lst) return;
   const double2 wt = weight_of(a, l);
 #pragma unroll
   for (int j = 0; j < NH; ++j) {
-    const int b = b0 + bh * NH + j;
+    const int b = b0 + (SPLIT_T ? 0 : bh * NH) + j;
     if (b >= a.nb) break;
     const double2 v = make_double2(acc[j].x * r.sign, acc[j].y * r.sign);
     a.dst[(int64_t)b * a.ds + (int64_t)l * l + l + m] = cmul_(v, wt);
@@ -431,7 +444,7 @@ void apply_w(const WignerTable &tb, bool trans, int mlo, int mhi, const double2 
              double2 *out, int64_t os, int ow, int o_mlo, int nb, cudaStream_t st) {
   const int nm = mhi - mlo + 1;
   const int ncols = 2 * ((nm + 1) / 2) * nb;
-  KTimer kt(KC_CONTRACT, st, 2.0 * tb.nt * (double)tb.nt * nm * nb * 2.0, 16.0 * nb * (double)nm * tb.nt * 2.0);
+  KTimer kt(KC_QUAD, st, 2.0 * tb.nt * (double)tb.nt * nm * nb * 2.0, 16.0 * nb * (double)nm * tb.nt * 2.0);
   dim3 grid(ceil_div(ncols, AW_T), ceil_div(tb.nt, AW_T), 2);
   k_apply_w<<<grid, 256, 0, st>>>(tb.W[0], tb.W[1], trans ? 1 : 0, tb.nt, tb.an, mlo, mhi, in, is, iw, i_mlo,
                                   out, os, ow, o_mlo, nb);
@@ -482,7 +495,7 @@ void contract_l2t_rc(const L2T &p, cudaStream_t st) {
   {
     double fl = 0, by = 0;
     if (timing_enabled()) rc_work(tb, p.mlo, p.mhi, p.lmin, p.nb, &fl, &by);
-    KTimer kt(KC_CONTRACT, st, fl, by);
+    KTimer kt(KC_RECOMPUTE, st, fl, by);
     if (p.nb >= 8)
       launch_l2t<8>(a, nm, st);
     else if (p.nb >= 4)
@@ -522,15 +535,17 @@ void contract_t2l_rc(const T2L &p, cudaStream_t st) {
   {
     double fl = 0, by = 0;
     if (timing_enabled()) rc_work(tb, p.mlo, p.mhi, p.lmin, p.nb, &fl, &by);
-    KTimer kt(KC_CONTRACT, st, fl, by);
+    KTimer kt(KC_RECOMPUTE, st, fl, by);
     if (p.nb >= 16)
       launch_t2l<16>(a, nm, maxseg, st);
     else if (p.nb >= 8)
       launch_t2l<8>(a, nm, maxseg, st);
     else if (p.nb >= 4)
       launch_t2l<4>(a, nm, maxseg, st);
-    else
+    else if (p.nb >= 2)
       launch_t2l<2>(a, nm, maxseg, st);
+    else
+      launch_t2l<1>(a, nm, maxseg, st);
   }
   if (tmp) cudaFreeAsync(tmp, st);
 }

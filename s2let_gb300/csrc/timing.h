@@ -14,7 +14,9 @@ enum KCat {
   KC_MERGE = 3,     // tiling merge / split / symmetrise
   KC_MIXED = 4,     // split-precision tensor-core contractions
   KC_OTHER = 5,
-  KC_N = 6
+  KC_RECOMPUTE = 6,  // FP64 contractions regenerating the Wigner values (recomputed tables)
+  KC_QUAD = 7,       // forward quadrature operator applied to ring spectra (recomputed tables)
+  KC_N = 8
 };
 
 bool timing_enabled();
