@@ -448,6 +448,24 @@ int s2let_gpu_wav2px_multi(void *const *f, void *const *f_wav, void *const *f_sc
                            void *stream);
 
 /*
+ * Host-pointer batches: the drop-in functions above for `nbatch` maps in one
+ * call (HOST buffers, map b at b * s2let_n_px / s2let_n_wav / s2let_n_scal
+ * elements, synchronous).  The maps run as batches of up to 8 on the GPU
+ * (S2LET_GPU_HOST_CHUNK overrides), chunks alternating between two streams so
+ * that one chunk's copies overlap another's transforms; the per-map work of
+ * streaming the Wigner tables is shared by the chunk.
+ * Returns the status.
+ */
+int s2let_gpu_analysis_px2wav_real_host_batch(double *f_wav, double *f_scal, const double *f, int nbatch,
+                                              const s2let_parameters_t *parameters);
+int s2let_gpu_synthesis_wav2px_real_host_batch(double *f, const double *f_wav, const double *f_scal,
+                                               int nbatch, const s2let_parameters_t *parameters);
+int s2let_gpu_analysis_px2wav_host_batch(void *f_wav, void *f_scal, const void *f, int nbatch,
+                                         const s2let_parameters_t *parameters);
+int s2let_gpu_synthesis_wav2px_host_batch(void *f, const void *f_wav, const void *f_scal, int nbatch,
+                                          const s2let_parameters_t *parameters);
+
+/*
  * Batched device-pointer entry points.  All pointers are DEVICE pointers; `stream`
  * is a cudaStream_t (NULL = default stream).  `nbatch` maps share one parameter
  * set; map b starts at b*stride of each array, strides being the single-map sizes

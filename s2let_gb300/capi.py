@@ -131,6 +131,10 @@ GPU_SIGNATURES = {
     "s2let_gpu_mw_adjoint_map2alm": (None, [V, V, I, I]),
     "s2let_gpu_mw_adjoint_alm2map": (None, [V, V, I, I]),
     "s2let_gpu_sht": (I, [I, I, I, I, I, V, V]),
+    "s2let_gpu_analysis_px2wav_real_host_batch": (I, [V, V, V, I, P]),
+    "s2let_gpu_synthesis_wav2px_real_host_batch": (I, [V, V, V, I, P]),
+    "s2let_gpu_analysis_px2wav_host_batch": (I, [V, V, V, I, P]),
+    "s2let_gpu_synthesis_wav2px_host_batch": (I, [V, V, V, I, P]),
     "s2let_gpu_px2wav_multi": (I, [V, V, V, P, V, I, I, V]),
     "s2let_gpu_wav2px_multi": (I, [V, V, V, P, V, I, I, V]),
     "s2let_gpu_analysis_px2wav_real_batch": (I, [V, V, V, I, P, V]),

@@ -999,6 +999,68 @@ int batch_directional(const char *fn, s2g::Op op, const s2let_parameters_t *p, b
   });
 }
 
+// Host-pointer batches: nb contiguous maps in host memory (the drop-in layout,
+// map b at b * the single-map size), run in chunks of kHostChunk maps on two
+// streams so that one chunk's copies overlap the other's transforms.  Only the
+// used prefix of each f_wav (the transforms advance with N_j, the buffer is
+// sized with N) crosses the bus, as in the drop-in functions.  Synchronous.
+constexpr int kHostChunk = 8;
+int host_chunk() {
+  const char *e = getenv("S2LET_GPU_HOST_CHUNK");
+  const int v = e ? atoi(e) : 0;
+  return v > 0 ? v : kHostChunk;
+}
+
+int host_batch(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool real, void *px, void *wav,
+               void *scal, int nb) {
+  return s2g::guarded(fn, [&] {
+    using namespace s2g;
+    validate(p);
+    ensure_device();
+    S2G_REQUIRE(nb >= 0, ERR_INVALID, "negative batch size");
+    if (nb == 0) return;
+    S2G_REQUIRE(px && wav && scal, ERR_INVALID, "NULL buffer");
+    static thread_local cudaStream_t sts[2] = {nullptr, nullptr};
+    for (auto &x : sts)
+      if (!x) S2G_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+    const size_t esz = real ? sizeof(double) : sizeof(double2);
+    s2let_parameters_t q = *p;
+    if (real) {
+      q.reality = 1;
+      q.spin = 0;
+    }
+    const int64_t npx = s2let_n_px(p), nw = s2let_n_wav(p), ns = s2let_n_scal(p);
+    const int64_t nwu = make_layout(q, real).woff.back();  // used prefix of one f_wav
+    const bool fwd = (op == OP_PX2WAV || op == OP_ADJ_PX2WAV);
+    (void)directional_plan(*p, real);  // build the plan before the two streams use it
+    char *hpx = (char *)px, *hw = (char *)wav, *hs = (char *)scal;
+    const int chunk = host_chunk();
+    for (int c0 = 0, k = 0; c0 < nb; c0 += chunk, ++k) {
+      const int n = std::min(chunk, nb - c0);
+      cudaStream_t st = sts[k & 1];
+      Scratch S(st);
+      char *dpx = S.get<char>((int64_t)n * npx * esz), *dw = S.get<char>((int64_t)n * nw * esz),
+           *ds = S.get<char>((int64_t)n * ns * esz);
+      if (fwd) {
+        S2G_CUDA(cudaMemcpyAsync(dpx, hpx + (size_t)c0 * npx * esz, (size_t)n * npx * esz, cudaMemcpyHostToDevice, st));
+      } else {
+        S2G_CUDA(cudaMemcpy2DAsync(dw, nw * esz, hw + (size_t)c0 * nw * esz, nw * esz, nwu * esz, n,
+                                   cudaMemcpyHostToDevice, st));
+        S2G_CUDA(cudaMemcpyAsync(ds, hs + (size_t)c0 * ns * esz, (size_t)n * ns * esz, cudaMemcpyHostToDevice, st));
+      }
+      run_directional(op, *p, real, dpx, nullptr, dw, ds, n, st);
+      if (fwd) {
+        S2G_CUDA(cudaMemcpy2DAsync(hw + (size_t)c0 * nw * esz, nw * esz, dw, nw * esz, nwu * esz, n,
+                                   cudaMemcpyDeviceToHost, st));
+        S2G_CUDA(cudaMemcpyAsync(hs + (size_t)c0 * ns * esz, ds, (size_t)n * ns * esz, cudaMemcpyDeviceToHost, st));
+      } else {
+        S2G_CUDA(cudaMemcpyAsync(hpx + (size_t)c0 * npx * esz, dpx, (size_t)n * npx * esz, cudaMemcpyDeviceToHost, st));
+      }
+    }
+    for (auto &x : sts) S2G_CUDA(cudaStreamSynchronize(x));
+  });
+}
+
 // ---- axisymmetric pixel-space transforms (src/c/s2let_transform_axisym_mw.c:124-1171)
 void host_axisym(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool real, bool multires,
                  void *f, void *wav, void *scal) {
@@ -1299,6 +1361,24 @@ int s2let_gpu_sht(int dir, int sampling_scheme, int L, int spin, int real, void 
   }
   host_sht(__func__, dir, L, spin, real != 0, f, flm, sampling_scheme == S2LET_SAMPLING_MW_SS);
   return s2g::last_status();
+}
+
+// ---- host-pointer batches (drop-in layout, nbatch maps per call)
+int s2let_gpu_analysis_px2wav_real_host_batch(double *f_wav, double *f_scal, const double *f, int nb,
+                                              const s2let_parameters_t *p) {
+  return host_batch(__func__, s2g::OP_PX2WAV, p, true, (void *)f, f_wav, f_scal, nb);
+}
+int s2let_gpu_synthesis_wav2px_real_host_batch(double *f, const double *f_wav, const double *f_scal, int nb,
+                                               const s2let_parameters_t *p) {
+  return host_batch(__func__, s2g::OP_WAV2PX, p, true, f, (void *)f_wav, (void *)f_scal, nb);
+}
+int s2let_gpu_analysis_px2wav_host_batch(void *f_wav, void *f_scal, const void *f, int nb,
+                                         const s2let_parameters_t *p) {
+  return host_batch(__func__, s2g::OP_PX2WAV, p, false, (void *)f, f_wav, f_scal, nb);
+}
+int s2let_gpu_synthesis_wav2px_host_batch(void *f, const void *f_wav, const void *f_scal, int nb,
+                                          const s2let_parameters_t *p) {
+  return host_batch(__func__, s2g::OP_WAV2PX, p, false, f, (void *)f_wav, (void *)f_scal, nb);
 }
 
 // ---- heterogeneous batches (device pointers, per-map parameters)

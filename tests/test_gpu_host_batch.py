@@ -1,0 +1,44 @@
+"""Host-pointer batches (s2let_gpu_*_host_batch): nbatch maps per call in the
+drop-in host layout.  Each map must equal the one-map drop-in call (FP64
+path, 1e-12), across chunk boundaries (two streams) and with the unused tail
+of f_wav (a scale with N_j < N) left as the caller wrote it."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from s2let_gb300.capi import make_parameters, ptr
+
+TOL = 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,N,spin,real,nb", [(32, 4, 0, True, 3), (24, 5, 2, False, 20), (16, 8, 0, True, 17)])
+def test_host_batch_equals_single_calls(gpu, L, N, spin, real, nb):
+    lib = gpu.lib
+    p = make_parameters(L, 2.0, 1, N, 0 if real else spin, 0)
+    s = gpu.sizes(p)
+    rng = np.random.default_rng(L + nb)
+    dt = np.float64 if real else np.complex128
+    shape = lambda n: (nb, n)
+    f = rng.normal(size=shape(s["n_px"])) if real else rng.normal(size=shape(s["n_px"])) + 1j * rng.normal(size=shape(s["n_px"]))
+    f = np.ascontiguousarray(f.astype(dt))
+    w = np.full(shape(s["n_wav"]), 7.0, dt)  # the unused tail must keep this
+    sc = np.zeros(shape(s["n_scal"]), dt)
+    fn = lib.s2let_gpu_analysis_px2wav_real_host_batch if real else lib.s2let_gpu_analysis_px2wav_host_batch
+    assert fn(ptr(w), ptr(sc), ptr(f), nb, C.byref(p)) == 0
+    r = np.zeros_like(f)
+    fn = lib.s2let_gpu_synthesis_wav2px_real_host_batch if real else lib.s2let_gpu_synthesis_wav2px_host_batch
+    assert fn(ptr(r), ptr(w), ptr(sc), nb, C.byref(p)) == 0
+    for b in range(nb):
+        w1 = np.full(s["n_wav"], 7.0, dt)
+        s1 = np.zeros(s["n_scal"], dt)
+        if real:
+            lib.s2let_analysis_px2wav_real(ptr(w1), ptr(s1), ptr(np.ascontiguousarray(f[b])), C.byref(p))
+        else:
+            lib.s2let_analysis_px2wav(ptr(w1), ptr(s1), ptr(np.ascontiguousarray(f[b])), C.byref(p))
+        assert rel_err(w[b], w1) < TOL and rel_err(sc[b], s1) < TOL, b
+        r1 = gpu.wav2px(w1, s1, p, real=real)
+        assert rel_err(r[b], r1) < TOL, b
+    assert lib.s2let_gpu_last_error() == 0
