@@ -175,7 +175,9 @@ def measured_peaks():
 # (dram__bytes_read.sum + dram__bytes_write.sum over the bytes the launch must
 # move); profiles/fp64_contraction_L512_N4_batch8.md.  Traffic grows with the
 # table size, so the ratio carries to the L=1024 launches.
-TRAFFIC_RATIO = {"fp64_contraction": 1.126}
+# DRAM traffic / algorithmic bytes per launch, from one ncu capture each
+# (profiles/fp64_contraction_L512_N4_batch8.md, profiles/ring_dft_df_L1024_N4_batch8.md)
+TRAFFIC_RATIO = {"fp64_contraction": 1.126, "ring_dft": 0.91}
 
 
 def profile_traffic(kernel, alg_bytes_per_launch):
@@ -674,6 +676,11 @@ def main():
             ti = kd["flops"] / (kd["ms"] * 1e-3) / 1e12
             roof["fp32_pipe"] = {"achieved_tinst_per_s": ti, "peak_tinst_per_s": peak_ti, "frac": ti / peak_ti,
                                  "work": "double-float FP32 instructions (model)"}
+            roof["binding_unit"] = {
+                "unit": "FP32 instruction issue", "frac": ti / peak_ti,
+                "note": "the ring DFTs are issue-bound on the FP32 pipe (ncu: FMA pipe 60 %, ALU 18-21 %, "
+                        "stall 'not selected' on top; DRAM 4 %), so the HBM fraction above is not their "
+                        "limit: profiles/ring_dft_df_L1024_N4_batch8.md"}
     km = kernels["tensor_contraction"]
     if km["launches"] and km["ms"]:
         g = km["bytes"] / (km["ms"] * 1e-3) / 1e9

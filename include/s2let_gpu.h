@@ -370,6 +370,24 @@ double s2let_mw_power_real(double *flm, int L);                                 
 double s2let_lm_power(S2LET_COMPLEX(double) *flm, int L);                                /* s2let_lm.h:14 */
 
 /* ------------------------------------------------------------------------ */
+/* FITS I/O of MW / MWSS maps (src/c/s2let_fits.c; s2let_fits.h), host code   */
+/* without cfitsio: an empty primary HDU and one binary table BINTABLE with    */
+/* the map column(s) and the keyword L (and MWSS = 1).  Readers accept 8-byte */
+/* (D) or 4-byte (E) float columns.  Writers refuse an existing file unless   */
+/* its name starts with '!', as cfitsio does.  Errors set the status.         */
+/* ------------------------------------------------------------------------ */
+int s2let_fits_hpx_read_nside(char *filename);                                            /* s2let_fits.h:18 */
+int s2let_fits_mw_read_bandlimit(char *filename);                                         /* s2let_fits.h:26 */
+void s2let_fits_mw_read_map(double *f, char *file, int L);                                /* s2let_fits.h:36 */
+void s2let_fits_mwss_read_map(double *f, char *file, int L);                              /* s2let_fits.h:46 */
+void s2let_fits_mw_write_map(char *file, double *f, int L);                               /* s2let_fits.h:56 */
+void s2let_fits_mwss_write_map(char *file, double *f, int L);                             /* s2let_fits.h:66 */
+void s2let_fits_mw_read_spin_maps(double *fQ, double *fU, char *file, int L);             /* s2let_fits.h:76 */
+void s2let_fits_mwss_read_spin_maps(double *fQ, double *fU, char *file, int L);           /* s2let_fits.h:86 */
+void s2let_fits_mw_write_spin_maps(char *file, double *fQ, double *fU, int L);            /* s2let_fits.h:96 */
+void s2let_fits_mwss_write_spin_maps(char *file, double *fQ, double *fU, int L);          /* s2let_fits.h:106 */
+
+/* ------------------------------------------------------------------------ */
 /* GB300 extensions (no reference counterpart)                              */
 /* ------------------------------------------------------------------------ */
 

@@ -8,7 +8,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from .capi import GPU_SIGNATURES, SIGNATURES, bind
+from .capi import FITS_SIGNATURES, GPU_SIGNATURES, SIGNATURES, bind
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libs2let_gpu.so")
 
@@ -25,6 +25,7 @@ def load() -> C.CDLL:
         lib = C.CDLL(LIB_PATH, mode=os.RTLD_LOCAL)
         bind(lib, SIGNATURES, required=False)
         bind(lib, GPU_SIGNATURES, required=False)
+        bind(lib, FITS_SIGNATURES, required=False)
         _lib = lib
     return _lib
 

@@ -114,6 +114,20 @@ for _op in ("analysis", "analysis_adjoint", "synthesis", "synthesis_adjoint"):
     for _suf in ("", "_multires", "_real", "_multires_real"):
         SIGNATURES[f"s2let_transform_axisym_wav_{_op}_mw{_suf}"] = (None, [V, V, V, P])
 
+# FITS I/O of MW / MWSS maps (host code of libs2let_gpu.so; not in the oracle)
+FITS_SIGNATURES = {
+    "s2let_fits_mw_read_bandlimit": (I, [C.c_char_p]),
+    "s2let_fits_hpx_read_nside": (I, [C.c_char_p]),
+    "s2let_fits_mw_read_map": (None, [V, C.c_char_p, I]),
+    "s2let_fits_mwss_read_map": (None, [V, C.c_char_p, I]),
+    "s2let_fits_mw_write_map": (None, [C.c_char_p, V, I]),
+    "s2let_fits_mwss_write_map": (None, [C.c_char_p, V, I]),
+    "s2let_fits_mw_read_spin_maps": (None, [V, V, C.c_char_p, I]),
+    "s2let_fits_mwss_read_spin_maps": (None, [V, V, C.c_char_p, I]),
+    "s2let_fits_mw_write_spin_maps": (None, [C.c_char_p, V, V, I]),
+    "s2let_fits_mwss_write_spin_maps": (None, [C.c_char_p, V, V, I]),
+}
+
 GPU_SIGNATURES = {
     "s2let_gpu_last_error": (I, []),
     "s2let_gpu_last_error_string": (C.c_char_p, []),

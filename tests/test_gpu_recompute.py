@@ -104,3 +104,36 @@ def test_L2048_recomputed_round_trip_and_oracle(gpu, oracle_port):
     w0, s0 = oracle_port.px2wav(f, p, real=True)
     assert rel_err(w, w0) < TOL and rel_err(s, s0) < TOL
     gpu.lib.s2let_gpu_release_plans()
+
+
+@pytest.mark.gpu
+def test_L2048_adjoint_dot_product_and_gradient(gpu):
+    """The differentiable path at L = 2048 (one map, recomputed tables): the
+    backward of px2wav is its exact adjoint, <W x, y> = <x, W* y> to 1e-10, and
+    a quadratic wavelet-space loss has the gradient W* W x."""
+    torch = pytest.importorskip("torch")
+    from s2let_gb300 import torch_ops as T
+
+    L = 2048
+    p = make_parameters(L, 2.0, 2, 4, 0, 0)
+    s = T.sizes(p)
+    gen = torch.Generator().manual_seed(7)
+    x = (torch.rand((1, s["n_px"]), generator=gen, dtype=torch.float64) - 0.5).cuda().requires_grad_(True)
+    yw = (torch.rand((1, s["n_wav"]), generator=gen, dtype=torch.float64) - 0.5).cuda()
+    ys = (torch.rand((1, s["n_scal"]), generator=gen, dtype=torch.float64) - 0.5).cuda()
+    with table_mode(gpu.lib, 0):
+        w, sc = T.px2wav(x, p, precision="fp64")
+        lhs = float((w * yw).sum() + (sc * ys).sum())
+        (g,) = torch.autograd.grad((w * yw).sum() + (sc * ys).sum(), [x])
+        rhs = float((x.detach() * g).sum())
+        assert abs(lhs - rhs) <= 1e-10 * abs(lhs)
+        # gradient of 0.5 ||W x||^2 is W* W x: compare with a central difference along x
+        loss = lambda z: 0.5 * sum(float((t ** 2).sum()) for t in T.px2wav(z, p, precision="fp64"))
+        w, sc = T.px2wav(x, p, precision="fp64")
+        (g2,) = torch.autograd.grad(0.5 * ((w ** 2).sum() + (sc ** 2).sum()), [x])
+        d = x.detach()
+        h = 1e-3
+        fd = (loss(d + h * d) - loss(d - h * d)) / (2 * h)
+        assert abs(fd - float((g2 * d).sum())) <= 1e-9 * abs(fd)
+    assert gpu.lib.s2let_gpu_device_fault() == 0
+    gpu.lib.s2let_gpu_release_plans()
