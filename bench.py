@@ -637,13 +637,15 @@ def main():
     lib.s2let_gpu_timing_enable(1)
     step()
     torch.cuda.synchronize()
-    rep = (C.c_double * 24)()
-    lib.s2let_gpu_timing_report(rep, 6)
+    rep = (C.c_double * 36)()
+    lib.s2let_gpu_timing_report(rep, 9)
     lib.s2let_gpu_timing_enable(0)
-    cats = ["fp64_contraction", "ring_dft", "gamma_dft", "tiling_merge", "tensor_contraction", "other"]
-    # (categories 6 and 7, the recomputed-table contractions and quadrature, do not run here)
+    # timing categories of s2let_gb300/csrc/timing.h (6 and 7, the recomputed-table
+    # contractions and quadrature, do not run here)
+    cats = {0: "fp64_contraction", 1: "ring_dft", 2: "gamma_dft", 3: "tiling_merge", 4: "tensor_contraction",
+            5: "other", 8: "digit_slicing"}
     kernels = {c: {"launches": int(rep[4 * i]), "ms": rep[4 * i + 1], "flops": rep[4 * i + 2],
-                   "bytes": rep[4 * i + 3]} for i, c in enumerate(cats)}
+                   "bytes": rep[4 * i + 3]} for i, c in cats.items()}
     dom = max(kernels, key=lambda c: kernels[c]["ms"])
     kd = kernels[dom]
     peaks, peak_kind = measured_peaks()
@@ -686,6 +688,10 @@ def main():
         g = km["bytes"] / (km["ms"] * 1e-3) / 1e9
         roof["tensor_contraction"] = {"bound": "hbm", "achieved_gbs": g, "frac": g / peak, "ms_per_step": km["ms"],
                                       "fp64_equiv_tflops": km["flops"] / (km["ms"] * 1e-3) / 1e12}
+    ks = kernels["digit_slicing"]
+    if ks["launches"] and ks["ms"]:
+        g = ks["bytes"] / (ks["ms"] * 1e-3) / 1e9
+        roof["digit_slicing"] = {"bound": "hbm", "achieved_gbs": g, "frac": g / peak, "ms_per_step": ks["ms"]}
 
     # ---- e2e through the host-pointer C ABI ----
     # The timed region holds every host <-> device copy: the maps in, the

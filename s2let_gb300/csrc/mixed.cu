@@ -888,12 +888,12 @@ void run_mixed(const Problem &p, cudaStream_t st) {
   for (int g = 0; g < ngroups; ++g) {
     const int b0 = g * mpp;
     const int nbg = p.nb - b0 < mpp ? p.nb - b0 : mpp;
-    double fl = 0, by = 0;
+    double fl = 0, by = 0, xby = 0;
     if (timing_enabled()) {
       fl = 4.0 * entries * nbg * p.nparts;
       by = entries * 2.0 * kS + (double)x_elems * 2.0 + 16.0 * nbg * p.nparts * (double)p.tb->nt * nmp;
+      xby = (double)x_elems * 2.0 * (1.0 + 8.0 / (2.0 * kS));  // panels written + FP64 values read
     }
-    KTimer kt(KC_MIXED, st, fl, by);
     XArgs xa{};
     xa.q = p.q ? 1 : 0;
     xa.bl = p.tb->bl;
@@ -909,9 +909,13 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     xa.xoff = xoff;
     xa.xpan = xpan;
     xa.eX = eX;
-    k_slice_x<NC><<<nmp, NC * 4, 0, st>>>(xa);
-    S2G_LAUNCHED();
+    {
+      KTimer kx(KC_SLICE, st, 0.0, xby);
+      k_slice_x<NC><<<nmp, NC * 4, 0, st>>>(xa);
+      S2G_LAUNCHED();
+    }
     if (L->ntiles == 0) continue;
+    KTimer kt(KC_MIXED, st, fl, by);
     MxArgs ma{};
     ma.q = xa.q;
     ma.panels = s->panels;

@@ -16,7 +16,8 @@ enum KCat {
   KC_OTHER = 5,
   KC_RECOMPUTE = 6,  // FP64 contractions regenerating the Wigner values (recomputed tables)
   KC_QUAD = 7,       // forward quadrature operator applied to ring spectra (recomputed tables)
-  KC_N = 8
+  KC_SLICE = 8,      // digit slicing of the coefficients for the tensor-core contractions
+  KC_N = 9
 };
 
 bool timing_enabled();
