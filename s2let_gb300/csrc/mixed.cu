@@ -222,6 +222,8 @@ struct XArgs {
   int nparts;
   Part part[kMaxParts];
   int nb, b0, mpp;  // maps per part in this launch: column pair cp -> part cp / mpp, map b0 + cp % mpp
+  int nmp;          // problem m count
+  int nkcmax, kst;  // largest K-chunk count over the problem m; staged column stride (double2)
   const int64_t *xoff;
   uint16_t *xpan;
   int *eX;
@@ -233,95 +235,168 @@ __device__ __forceinline__ double2 weight_of(const double2 *w, double wscale, in
   return make_double2(v.x * wscale, v.y * wscale);
 }
 
-// Complex coefficient of column pair cp (part cp / mpp, map b0 + cp % mpp) at K index k.
-__device__ __forceinline__ double2 x_value(const XArgs &a, int m, int am, const Geom &g, int k, int cp) {
-  const int pi = cp / a.mpp;
-  const int b = a.b0 + cp % a.mpp;
-  const double2 zero = make_double2(0.0, 0.0);
-  if (pi >= a.nparts || b >= a.nb) return zero;
-  const Part &P = a.part[pi];
-  if (!a.q) {
-    const int l = g.l0 + k;
-    if (l < P.lmin || l >= a.bl) return zero;
-    const int64_t base = (int64_t)b * P.ss + (int64_t)l * l + l;
-    double2 v;
-    if (P.x_half && m < 0) {
-      v = P.src[base - m];
-      v.y = -v.y;
-      if (am & 1) v = make_double2(-v.x, -v.y);
-    } else {
-      v = P.src[base + m];
-    }
-    const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
-    return make_double2(v.x * wt.x - v.y * wt.y, v.x * wt.y + v.y * wt.x);
-  }
-  if (k >= a.nt) return zero;
-  return P.src[(int64_t)b * P.ss + (int64_t)k * P.sw + (m - P.s_mlo)];
-}
+// Coefficient slicing: one block per (kMG consecutive problem m, column pair
+// cp = part cp / mpp, map b0 + cp % mpp).  Phase 1 stages the kMG complex
+// columns in shared memory, reading the source with m as the contiguous index
+// (flm-like l^2 + l + m for l -> t, spectra [t][m] for t -> l), so that a warp
+// load covers 64-byte runs, and records the largest exponent field of each
+// real and imaginary column.  Phase 2 writes the digit panels: 8 consecutive
+// lanes build one 128-byte panel row from 8 K values each.  The FP64 values
+// are read once and the panels written once.
+constexpr int kMG = 4;
+constexpr int kSliceThreads = 256;
+// staged index of K position k: one double2 of padding per 8, so that the
+// 16-byte reads of 8 lanes at K stride 8 fall in distinct banks
+__host__ __device__ __forceinline__ int sv_idx(int k) { return k + (k >> 3); }
 
-// One block per problem m; thread (cp, h): column pair cp (real part in column
-// 2cp, imaginary part in 2cp + 1) and the 8-wide K chunk h of every panel, so
-// that each slice row of a panel is written by 8 consecutive lanes as eight
-// 16-byte (8 x bf16) stores = one full 128-byte row.
 template <int NC>
-__global__ void __launch_bounds__(NC * 4) k_slice_x(XArgs a) {
+__global__ void __launch_bounds__(kSliceThreads, 3) k_slice_x(XArgs a) {
+  extern __shared__ double2 sv[];  // [kMG][a.kst]
+  __shared__ int gl0[kMG], gnkc[kMG], gkc0[kMG], gls[kMG], gex[kMG][2];
   constexpr int PX = Cfg<NC>::kPanelX;
-  const int pm = blockIdx.x, m = a.mlo + pm, am = m < 0 ? -m : m;
-  const Geom g = geom(a.bl, a.nt, a.an, m, a.q != 0);
-  const int cp = threadIdx.x >> 3, h = threadIdx.x & 7;
-  const int c0 = 2 * cp;
-  if (g.nkc == 0) {
-    if (h == 0) a.eX[pm * NC + c0] = a.eX[pm * NC + c0 + 1] = 0;
-    return;
-  }
-  const int lst = g.l0 > a.lmin ? g.l0 : a.lmin;
-  int kc0 = 0;
-  if (!a.q) kc0 = lst >= a.bl ? g.nkc : (lst - g.l0) / kPK;
-  int mr = 0, mi = 0;  // largest exponent fields
-  for (int kc = kc0; kc < g.nkc; ++kc)
-#pragma unroll 4
-    for (int e = 0; e < 8; ++e) {
-      const double2 v = x_value(a, m, am, g, kc * kPK + h * 8 + e, cp);
-      mr = max(mr, exp_field(v.x));
-      mi = max(mi, exp_field(v.y));
+  const int cp = blockIdx.y, pm0 = blockIdx.x * kMG, c0 = 2 * cp;
+  const int part = cp / a.mpp, b = a.b0 + cp % a.mpp;
+  const bool live = part < a.nparts && b < a.nb;
+  if (threadIdx.x < kMG) {
+    const int pm = pm0 + threadIdx.x;
+    int l0 = 0, nkc = 0, kc0 = 0, ls = 0;
+    if (pm < a.nmp) {
+      const Geom g = geom(a.bl, a.nt, a.an, a.mlo + pm, a.q != 0);
+      l0 = g.l0;
+      nkc = g.nkc;
+      if (!a.q) {
+        const int lst = g.l0 > a.lmin ? g.l0 : a.lmin;
+        kc0 = lst >= a.bl ? g.nkc : (lst - g.l0) / kPK;
+        // first degree with a value: below its part's lmin the column is zero
+        ls = live && a.part[part].lmin > g.l0 ? a.part[part].lmin : g.l0;
+      }
     }
-#pragma unroll
-  for (int o = 4; o > 0; o >>= 1) {
-    mr = max(mr, __shfl_xor_sync(0xffffffffu, mr, o));
-    mi = max(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+    gl0[threadIdx.x] = l0;
+    gnkc[threadIdx.x] = nkc;
+    gkc0[threadIdx.x] = kc0;
+    gls[threadIdx.x] = ls;
+    gex[threadIdx.x][0] = gex[threadIdx.x][1] = 0;
   }
-  // |v| < 2^e for every value of the column (e = largest unbiased exponent + 1)
-  const int er = block_scale(mr), ei = block_scale(mi);
-  if (h == 0) {
-    a.eX[pm * NC + c0] = er;
-    a.eX[pm * NC + c0 + 1] = ei;
-  }
-  uint16_t *base = a.xpan + a.xoff[pm] * (NC / 16);
-  for (int kc = kc0; kc < g.nkc; ++kc) {
-    uint32_t pr[kS][4], pi[kS][4];
+  for (int i = threadIdx.x; i < kMG * a.kst; i += kSliceThreads) ((int4 *)sv)[i] = make_int4(0, 0, 0, 0);
+  __syncthreads();
+  if (live) {
+    const Part &P = a.part[part];
+    const int mi = threadIdx.x % kMG;  // fixed per thread: kSliceThreads is a multiple of kMG
+    const int pm = pm0 + mi, m = a.mlo + pm, am = m < 0 ? -m : m;
+    const bool has = pm < a.nmp && gnkc[mi] > gkc0[mi];
+    double2 *col = sv + mi * a.kst;
+    int er = 0, ei = 0;
+    constexpr int kStep = kSliceThreads / kMG, kU = 4;  // kU loads in flight per thread
+    if (!a.q) {
+      // every lane walks the same degrees, so the kMG m of one degree are adjacent
+      int lb = a.bl;
+      for (int i = 0; i < kMG; ++i)
+        if (pm0 + i < a.nmp && gnkc[i] > gkc0[i]) lb = min(lb, gls[i]);
+      const int l0 = gl0[mi], ls = gls[mi];
+      const bool neg = P.x_half && m < 0;
+      const int mm = neg ? -m : m;
+      for (int l1 = lb + threadIdx.x / kMG; l1 < a.bl; l1 += kU * kStep) {
+        double2 v[kU];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const double2 v = x_value(a, m, am, g, kc * kPK + h * 8 + e, cp);
-      int dr[kS], di[kS];
-      int_digits(fixed48(v.x, er), dr);
-      int_digits(fixed48(v.y, ei), di);
+        for (int u = 0; u < kU; ++u) {
+          const int l = l1 + u * kStep;
+          v[u] = make_double2(0.0, 0.0);
+          if (has && l >= ls && l < a.bl) v[u] = P.src[(int64_t)b * P.ss + (int64_t)l * l + l + mm];
+        }
 #pragma unroll
-      for (int j = 0; j < kS; ++j) {
-        const uint32_t br = bf16_of_int(dr[j]), bi = bf16_of_int(di[j]);
-        if (e & 1) {
-          pr[j][e >> 1] |= br << 16;
-          pi[j][e >> 1] |= bi << 16;
-        } else {
-          pr[j][e >> 1] = br;
-          pi[j][e >> 1] = bi;
+        for (int u = 0; u < kU; ++u) {
+          const int l = l1 + u * kStep;
+          if (!has || l < ls || l >= a.bl) continue;
+          double2 x = v[u];
+          if (neg) {
+            x.y = -x.y;
+            if (am & 1) x = make_double2(-x.x, -x.y);
+          }
+          const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
+          x = make_double2(x.x * wt.x - x.y * wt.y, x.x * wt.y + x.y * wt.x);
+          col[sv_idx(l - l0)] = x;
+          er = max(er, exp_field(x.x));
+          ei = max(ei, exp_field(x.y));
+        }
+      }
+    } else if (has) {
+      const double2 *src = P.src + (int64_t)b * P.ss + (m - P.s_mlo);
+      for (int t1 = threadIdx.x / kMG; t1 < a.nt; t1 += kU * kStep) {
+        double2 v[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int t = t1 + u * kStep;
+          v[u] = t < a.nt ? src[(int64_t)t * P.sw] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int t = t1 + u * kStep;
+          if (t >= a.nt) continue;
+          col[sv_idx(t)] = v[u];
+          er = max(er, exp_field(v[u].x));
+          ei = max(ei, exp_field(v[u].y));
         }
       }
     }
-    uint16_t *p = base + (int64_t)kc * PX;
+    // lanes with the same m are kMG apart
 #pragma unroll
-    for (int j = 0; j < kS; ++j) {
-      *(uint4 *)(p + swz(j * NC + c0, h * 8)) = make_uint4(pr[j][0], pr[j][1], pr[j][2], pr[j][3]);
-      *(uint4 *)(p + swz(j * NC + c0 + 1, h * 8)) = make_uint4(pi[j][0], pi[j][1], pi[j][2], pi[j][3]);
+    for (int o = kMG; o < 32; o <<= 1) {
+      er = max(er, __shfl_xor_sync(0xffffffffu, er, o));
+      ei = max(ei, __shfl_xor_sync(0xffffffffu, ei, o));
+    }
+    if ((threadIdx.x & 31) < kMG) {
+      atomicMax(&gex[mi][0], er);
+      atomicMax(&gex[mi][1], ei);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < kMG) {
+    const int pm = pm0 + threadIdx.x;
+    // |v| < 2^e for every value of the column (e = largest unbiased exponent + 1)
+    const int er = block_scale(gex[threadIdx.x][0]), ei = block_scale(gex[threadIdx.x][1]);
+    gex[threadIdx.x][0] = er;
+    gex[threadIdx.x][1] = ei;
+    if (pm < a.nmp) {
+      a.eX[pm * NC + c0] = er;
+      a.eX[pm * NC + c0 + 1] = ei;
+    }
+  }
+  __syncthreads();
+  const int units = kMG * a.nkcmax * 8;
+  for (int u = threadIdx.x; u < units; u += kSliceThreads) {
+    const int h = u & 7, rest = u >> 3;
+    const int kc = rest % a.nkcmax, mi = rest / a.nkcmax;
+    const int pm = pm0 + mi;
+    if (pm >= a.nmp || kc < gkc0[mi] || kc >= gnkc[mi]) continue;
+    uint16_t *p = a.xpan + a.xoff[pm] * (NC / 16) + (int64_t)kc * PX;
+    const double *col = (const double *)(sv + mi * a.kst);
+#pragma unroll 1
+    for (int ri = 0; ri < 2; ++ri) {  // real part (column c0), then imaginary part (c0 + 1)
+      uint32_t pk[kS][4];
+      if (live) {
+        const int e = gex[mi][ri];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          int d[kS];
+          int_digits(fixed48(col[2 * sv_idx(kc * kPK + h * 8 + q) + ri], e), d);
+#pragma unroll
+          for (int j = 0; j < kS; ++j) {
+            const uint32_t bb = bf16_of_int(d[j]);
+            if (q & 1)
+              pk[j][q >> 1] |= bb << 16;
+            else
+              pk[j][q >> 1] = bb;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < kS; ++j)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) pk[j][q] = 0u;
+      }
+#pragma unroll
+      for (int j = 0; j < kS; ++j)
+        *(uint4 *)(p + swz(j * NC + c0 + ri, h * 8)) = make_uint4(pk[j][0], pk[j][1], pk[j][2], pk[j][3]);
     }
   }
 }
@@ -875,6 +950,17 @@ void run_mixed(const Problem &p, cudaStream_t st) {
   }
   const int nmp = p.mhi - p.mlo + 1;
   const int mpp = NC / (2 * p.nparts);  // maps per part per launch
+  int nkcmax = 0;
+  for (int pm = 0; pm < nmp; ++pm) nkcmax = std::max(nkcmax, geom(p.tb->bl, p.tb->nt, p.tb->an, p.mlo + pm, p.q).nkc);
+  const size_t slice_smem = sizeof(double2) * kMG * (size_t)sv_idx(nkcmax * kPK);
+  constexpr int kSliceSmemMax = 232448 - 1024;  // the opt-in maximum less the static arrays
+  S2G_REQUIRE(slice_smem <= (size_t)kSliceSmemMax, ERR_INVALID,
+              "coefficient slicing: K too large for shared-memory staging");
+  static bool attr_x = false;
+  if (!attr_x) {
+    S2G_CUDA(cudaFuncSetAttribute(k_slice_x<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSliceSmemMax));
+    attr_x = true;
+  }
   const int ngroups = (p.nb + mpp - 1) / mpp;
   // coefficient panels: the tile list's offsets count 16-column panels; an
   // NC-column panel is NC/16 times larger, so offsets scale by NC/16
@@ -909,9 +995,12 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     xa.xoff = xoff;
     xa.xpan = xpan;
     xa.eX = eX;
+    xa.nmp = nmp;
+    xa.nkcmax = nkcmax;
+    xa.kst = sv_idx(nkcmax * kPK);
     {
       KTimer kx(KC_SLICE, st, 0.0, xby);
-      k_slice_x<NC><<<nmp, NC * 4, 0, st>>>(xa);
+      k_slice_x<NC><<<dim3((nmp + kMG - 1) / kMG, NC / 2), kSliceThreads, slice_smem, st>>>(xa);
       S2G_LAUNCHED();
     }
     if (L->ntiles == 0) continue;
