@@ -10,16 +10,20 @@
 //   panel [7 slices x 16 columns][64 bf16] (16 real columns = 8 complex maps),
 //   column exponents eX (int32) per (m, column).
 //
-// Kernel k_contract_mx: persistent, one CTA per SM, 6 warps.
-//   warp 0    producer: cp.async.bulk of panels into a 10-deep ring of 16 KB
-//             table stages and a 2-deep ring of 14 KB coefficient stages.
+// Kernel k_contract_mx<NC>: persistent, one CTA per SM, 18 warps; NC real
+// coefficient columns (16, 32 or 64) per table pass.
+//   warp 0    producer: cp.async.bulk of panels into a ring of 16 KB table
+//             stages (10 deep; 6 at NC = 64) and a 2-deep ring of coefficient
+//             stages (7 slices x NC columns x 64 K).
 //   warp 1    MMA issuer: per K-chunk and digit slice j, one 128 x N x 64
-//             product (4 tcgen05.mma of K=16) of table slice j against the
-//             first 7-j coefficient slices, written to the accumulator columns
-//             of classes j..6 (N = 16 (7-j)); two TMEM accumulators alternate
-//             between tiles.
-//   warps 2-5 epilogue: tcgen05.ld of the 7 class accumulators, FP64 combine,
-//             row/column exponents, sign, per-l weight, store.
+//             product (tcgen05.mma of K=16, N <= 256 each) of table slice j
+//             against the first 7-j coefficient slices, written to the
+//             accumulator columns of classes j..6 (N = NC (7-j)); two TMEM
+//             accumulators alternate between tiles (one at NC = 64).
+//   warps 2-17 epilogue: four warps per TMEM lane quarter, 16 columns each:
+//             tcgen05.ld of the 7 class accumulators, double-float combine,
+//             row/column exponents, sign, per-l weight, store; the
+//             accumulator is released as soon as its values are in registers.
 // Every wait is bounded (about 2 s); on expiry the kernel raises an error flag,
 // drains its own copies and MMAs, frees TMEM and returns.
 #include <cstdint>
@@ -47,7 +51,7 @@ constexpr int kPM = 128;               // rows per panel
 constexpr int kPanelA = kPM * kPK;     // 8192 elements, 16 KB
 constexpr int kMaxParts = 2;           // scales sharing one table pass
 constexpr int kXST = 2;                // coefficient pipeline depth
-constexpr int kEpiWarps = 8;           // two warps per TMEM lane quarter, alternating 16-column chunks
+constexpr int kEpiWarps = 16;          // four warps per TMEM lane quarter, one 16-column chunk each
 constexpr int kThreads = 64 + 32 * kEpiWarps;
 constexpr int kMinBl = 128;            // below this the FP64 kernel is used
 constexpr long long kWaitCycles = 4000000000LL;
@@ -536,29 +540,27 @@ __device__ __forceinline__ TileInfo tile_info(const MxArgs &a, int t) {
   return ti;
 }
 
-// Combine the 7 class accumulators of 16 columns for this thread's row:
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+// the 7 class accumulators of 8 columns into registers (waits for the loads)
+__device__ __forceinline__ void load_classes8(uint32_t taddr, int ncols_per_class, float (*acc)[8]) {
+#pragma unroll
+  for (int c = 0; c < kS; ++c) tmem_ld8(taddr + (uint32_t)(c * ncols_per_class), acc[c]);
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+// Combine the 7 class accumulators of 8 columns for this thread's row:
 // S = sum_c acc_c 2^(-7c) by Horner in double-float on the FP32 pipe (the class
 // values and 2^-7 scalings are exact floats), then one widening to FP64 with
 // the power of two 2^(ea + eX - 12) applied while widening (dfconv.h).
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
+__device__ __forceinline__ void combine8(float (*acc)[8], int ea, const int *eX, double sign, double *y) {
 #pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-__device__ __forceinline__ void combine16(uint32_t taddr, int ncols_per_class, int ea, const int *eX, double sign,
-                                          double *y) {
-  float acc[kS][16];
-#pragma unroll
-  for (int c = 0; c < kS; ++c) tmem_ld16(taddr + (uint32_t)(c * ncols_per_class), acc[c]);
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int col = 0; col < 16; ++col) {
+  for (int col = 0; col < 8; ++col) {
     float hi = acc[kS - 1][col], lo = 0.0f;
 #pragma unroll
     for (int c = kS - 2; c >= 0; --c) {
@@ -709,8 +711,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
     }
   } else if (warp >= 2) {
     // ---------------- epilogue ----------------
+    // warp -> TMEM lane quarter (warp mod 4, the quarter it may address) and one
+    // 16-column chunk pi, read as two 8-column halves; the accumulator is
+    // handed back right after the second half is in registers, before it is
+    // combined and stored, so that the next tile's MMAs wait as little as possible
     const int quarter = warp & 3;
-    const int half = (warp - 2) / 4;  // which alternate 16-column chunks this warp combines
+    const int pi = (warp - 2) / 4;
     const int rr = quarter * 32 + lane;
     int ti_n = 0;
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++ti_n) {
@@ -720,32 +726,35 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
       if (!__all_sync(0xffffffffu, bar_wait(&tfull[ab], (ti_n / NBUF) & 1, abort_flag, a.err))) break;
       tc_fence_after();
       const bool live = ti.kc0 < ti.nkc;
+      if (pi >= NC / 16 || !live) {  // no columns here, or nothing accumulated: release at once
+        tc_fence_before();
+        bar_arrive(&tempty[ab]);
+        if (pi >= NC / 16) continue;
+      }
       const int ea = live ? (int)a.eA[a.e_off[ti.mi] + ti.rt * kPM + rr] : 0;
       const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * ACC);
       const int t_row = ti.rt * kPM + rr;
       const int l = ti.l0 + ti.rt * kPM + rr;
-      // chunks pi = half, half + 2, ...; a warp with no chunk left still arrives
-      const int last = ((NC / 16 - 1 - half) / 2) * 2 + half;
-      if (half >= NC / 16) {
-        tc_fence_before();
-        bar_arrive(&tempty[ab]);
-      }
-      for (int pi = half; pi < NC / 16; pi += 2) {
-        double y[16];
+#pragma unroll 1
+      for (int hh = 0; hh < 2; ++hh) {
+        const int c0 = pi * 16 + hh * 8;  // first column of this half
+        double y[8];
         if (live) {
-          combine16(taddr + (uint32_t)(pi * 16), NC, ea, a.eX + ti.pm * NC + pi * 16, ti.sign, y);
+          float acc[kS][8];
+          load_classes8(taddr + (uint32_t)c0, NC, acc);
+          if (hh == 1) {  // every column of this warp is in registers: hand the accumulator back
+            tc_fence_before();
+            bar_arrive(&tempty[ab]);
+          }
+          combine8(acc, ea, a.eX + ti.pm * NC + c0, ti.sign, y);
         } else {
 #pragma unroll
-          for (int col = 0; col < 16; ++col) y[col] = 0.0;
+          for (int col = 0; col < 8; ++col) y[col] = 0.0;
         }
-        if (pi == last) {  // this warp's columns read: hand the accumulator back
-          tc_fence_before();
-          bar_arrive(&tempty[ab]);
-        }
-        // column pair cp = 8 pi + bb: part cp / mpp, map b0 + cp % mpp
+        // column pair cp = c0 / 2 + bb: part cp / mpp, map b0 + cp % mpp
 #pragma unroll
-        for (int bb = 0; bb < 8; ++bb) {
-          const int cp = pi * 8 + bb;
+        for (int bb = 0; bb < 4; ++bb) {
+          const int cp = c0 / 2 + bb;
           const int part = cp / a.mpp;
           const int b = a.b0 + cp % a.mpp;
           if (part >= a.nparts || b >= a.nb) continue;
