@@ -514,17 +514,26 @@ struct MxArgs {
   int ntiles;
   int nparts;
   Part part[kMaxParts];
-  int nb, b0, mpp;
+  int nb, mpp;
+  // map groups of one launch: group g holds maps [b0 + g mpp, b0 + (g + 1) mpp)
+  // of every part, its coefficient panels at xpan + g xg and exponents at
+  // eX + g eXg.  Work item v is tile v / ngroups of group v % ngroups, so that
+  // neighbouring CTAs run the same table tile for different groups and the
+  // second read of the tile's panels is served by L2.
+  int b0, ngroups, eXg;
+  int64_t xg;
   int *err;
 };
 
 struct TileInfo {
   int pm, m, mi, rt, kc0, nkc, l0;
+  int g;  // map group
   double sign;
 };
-__device__ __forceinline__ TileInfo tile_info(const MxArgs &a, int t) {
+__device__ __forceinline__ TileInfo tile_info(const MxArgs &a, int v) {
   TileInfo ti;
-  const int2 tl = a.tiles[t];
+  ti.g = v % a.ngroups;
+  const int2 tl = a.tiles[v / a.ngroups];
   ti.pm = tl.x;
   ti.rt = tl.y;
   ti.m = a.mlo + ti.pm;
@@ -635,10 +644,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
   if (warp == 0 && lane == 0) {
     // ---------------- producer ----------------
     bool ok = true;
-    for (int t = blockIdx.x; ok && t < a.ntiles; t += gridDim.x) {
+    for (int t = blockIdx.x; ok && t < a.ntiles * a.ngroups; t += gridDim.x) {
       const TileInfo ti = tile_info(a, t);
       const uint16_t *pan = a.panels + a.pan_off[ti.mi] + (int64_t)ti.rt * ti.nkc * kS * kPanelA;
-      const uint16_t *xp = a.xpan + a.xoff[ti.pm] * (NC / 16);
+      const uint16_t *xp = a.xpan + ti.g * a.xg + a.xoff[ti.pm] * (NC / 16);
       for (int kc = ti.kc0; ok && kc < ti.nkc; ++kc) {
         const int xs = issuedX % kXST;
         if (!(ok = bar_wait(&emptyX[xs], ((issuedX / kXST) & 1) ^ 1, abort_flag, a.err))) break;
@@ -658,7 +667,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
     // ---------------- MMA issuer ----------------
     int ca = 0, cx = 0, ti_n = 0;
     bool ok = true, any = false;
-    for (int t = blockIdx.x; ok && t < a.ntiles; t += gridDim.x, ++ti_n) {
+    for (int t = blockIdx.x; ok && t < a.ntiles * a.ngroups; t += gridDim.x, ++ti_n) {
       const TileInfo ti = tile_info(a, t);
       const int ab = ti_n % NBUF;
       if (!(ok = bar_wait(&tempty[ab], ((ti_n / NBUF) & 1) ^ 1, abort_flag, a.err))) break;
@@ -719,7 +728,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
     const int pi = (warp - 2) / 4;
     const int rr = quarter * 32 + lane;
     int ti_n = 0;
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++ti_n) {
+    for (int t = blockIdx.x; t < a.ntiles * a.ngroups; t += gridDim.x, ++ti_n) {
       const TileInfo ti = tile_info(a, t);
       const int ab = ti_n % NBUF;
       // warp-uniform outcome: tcgen05.ld below is .sync.aligned
@@ -746,7 +755,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
             tc_fence_before();
             bar_arrive(&tempty[ab]);
           }
-          combine8(acc, ea, a.eX + ti.pm * NC + c0, ti.sign, y);
+          combine8(acc, ea, a.eX + ti.g * a.eXg + ti.pm * NC + c0, ti.sign, y);
         } else {
 #pragma unroll
           for (int col = 0; col < 8; ++col) y[col] = 0.0;
@@ -756,7 +765,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
         for (int bb = 0; bb < 4; ++bb) {
           const int cp = c0 / 2 + bb;
           const int part = cp / a.mpp;
-          const int b = a.b0 + cp % a.mpp;
+          const int b = a.b0 + ti.g * a.mpp + cp % a.mpp;
           if (part >= a.nparts || b >= a.nb) continue;
           const Part &P = a.part[part];
           if (!a.q) {
@@ -971,43 +980,49 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     attr_x = true;
   }
   const int ngroups = (p.nb + mpp - 1) / mpp;
+  // map groups run kGroupsPerLaunch at a time in one launch (their tiles
+  // interleaved, the table read once from HBM and again from L2)
+  constexpr int kGroupsPerLaunch = 4;
+  const int gpl = ngroups < kGroupsPerLaunch ? ngroups : kGroupsPerLaunch;
   // coefficient panels: the tile list's offsets count 16-column panels; an
   // NC-column panel is NC/16 times larger, so offsets scale by NC/16
   const int64_t x_elems = L->x_elems * (NC / 16);
   uint16_t *xpan = nullptr;
   int *eX = nullptr;
   const int64_t *xoff = L->d_xoff;
-  S2G_CUDA(cudaMallocAsync((void **)&xpan, sizeof(uint16_t) * (size_t)(x_elems ? x_elems : 1), st));
-  S2G_CUDA(cudaMallocAsync((void **)&eX, sizeof(int) * (size_t)nmp * NC, st));
+  S2G_CUDA(cudaMallocAsync((void **)&xpan, sizeof(uint16_t) * (size_t)(x_elems ? x_elems * gpl : 1), st));
+  S2G_CUDA(cudaMallocAsync((void **)&eX, sizeof(int) * (size_t)nmp * NC * gpl, st));
   const double entries = (double)L->work_entries;
-  for (int g = 0; g < ngroups; ++g) {
-    const int b0 = g * mpp;
-    const int nbg = p.nb - b0 < mpp ? p.nb - b0 : mpp;
-    double fl = 0, by = 0, xby = 0;
-    if (timing_enabled()) {
-      fl = 4.0 * entries * nbg * p.nparts;
-      by = entries * 2.0 * kS + (double)x_elems * 2.0 + 16.0 * nbg * p.nparts * (double)p.tb->nt * nmp;
-      xby = (double)x_elems * 2.0 * (1.0 + 8.0 / (2.0 * kS));  // panels written + FP64 values read
-    }
-    XArgs xa{};
-    xa.q = p.q ? 1 : 0;
-    xa.bl = p.tb->bl;
-    xa.nt = p.tb->nt;
-    xa.an = p.tb->an;
-    xa.mlo = p.mlo;
-    xa.lmin = lmin;
-    xa.nparts = p.nparts;
-    for (int i = 0; i < p.nparts; ++i) xa.part[i] = p.part[i];
-    xa.nb = p.nb;
-    xa.b0 = b0;
-    xa.mpp = mpp;
-    xa.xoff = xoff;
-    xa.xpan = xpan;
-    xa.eX = eX;
-    xa.nmp = nmp;
-    xa.nkcmax = nkcmax;
-    xa.kst = sv_idx(nkcmax * kPK);
-    {
+  for (int g0 = 0; g0 < ngroups; g0 += gpl) {
+    const int ng = ngroups - g0 < gpl ? ngroups - g0 : gpl;
+    double fl = 0, by = 0;
+    for (int g = g0; g < g0 + ng; ++g) {
+      const int b0 = g * mpp;
+      const int nbg = p.nb - b0 < mpp ? p.nb - b0 : mpp;
+      double xby = 0;
+      if (timing_enabled()) {
+        fl += 4.0 * entries * nbg * p.nparts;
+        by += entries * 2.0 * kS + (double)x_elems * 2.0 + 16.0 * nbg * p.nparts * (double)p.tb->nt * nmp;
+        xby = (double)x_elems * 2.0 * (1.0 + 8.0 / (2.0 * kS));  // panels written + FP64 values read
+      }
+      XArgs xa{};
+      xa.q = p.q ? 1 : 0;
+      xa.bl = p.tb->bl;
+      xa.nt = p.tb->nt;
+      xa.an = p.tb->an;
+      xa.mlo = p.mlo;
+      xa.lmin = lmin;
+      xa.nparts = p.nparts;
+      for (int i = 0; i < p.nparts; ++i) xa.part[i] = p.part[i];
+      xa.nb = p.nb;
+      xa.b0 = b0;
+      xa.mpp = mpp;
+      xa.xoff = xoff;
+      xa.xpan = xpan + (int64_t)(g - g0) * x_elems;
+      xa.eX = eX + (int64_t)(g - g0) * nmp * NC;
+      xa.nmp = nmp;
+      xa.nkcmax = nkcmax;
+      xa.kst = sv_idx(nkcmax * kPK);
       KTimer kx(KC_SLICE, st, 0.0, xby);
       k_slice_x<NC><<<dim3((nmp + kMG - 1) / kMG, NC / 2), kSliceThreads, slice_smem, st>>>(xa);
       S2G_LAUNCHED();
@@ -1015,7 +1030,7 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     if (L->ntiles == 0) continue;
     KTimer kt(KC_MIXED, st, fl, by);
     MxArgs ma{};
-    ma.q = xa.q;
+    ma.q = p.q ? 1 : 0;
     ma.panels = s->panels;
     ma.pan_off = s->d_pan_off;
     ma.eA = s->eA;
@@ -1035,10 +1050,14 @@ void run_mixed(const Problem &p, cudaStream_t st) {
     ma.nparts = p.nparts;
     for (int i = 0; i < p.nparts; ++i) ma.part[i] = p.part[i];
     ma.nb = p.nb;
-    ma.b0 = b0;
     ma.mpp = mpp;
+    ma.b0 = g0 * mpp;
+    ma.ngroups = ng;
+    ma.xg = x_elems;
+    ma.eXg = nmp * NC;
     ma.err = err;
-    const int grid = L->ntiles < num_sms() ? L->ntiles : num_sms();
+    const int nwork = L->ntiles * ng;
+    const int grid = nwork < num_sms() ? nwork : num_sms();
     k_contract_mx<NC><<<grid, kThreads, Cfg<NC>::kSmemBytes, st>>>(ma);
     S2G_LAUNCHED();
   }

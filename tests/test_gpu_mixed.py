@@ -71,10 +71,12 @@ def test_mixed_sht(gpu):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L,N,nb", [(256, 4, 12), (160, 3, 20)])
+@pytest.mark.parametrize("L,N,nb", [(256, 4, 12), (160, 3, 20), (128, 2, 70)])
 def test_mixed_large_batches(gpu, L, N, nb):
     """Batches that need 48-64 coefficient columns per table pass (one 448-column
-    TMEM accumulator, MMAs split at N = 256) against the FP64 path."""
+    TMEM accumulator, MMAs split at N = 256) against the FP64 path; 70 maps at
+    two scales per pass make five map groups of 16, run as one launch of four
+    interleaved groups and one of the remaining six maps."""
     torch = pytest.importorskip("torch")
     from s2let_gb300 import torch_ops as T
 
