@@ -285,9 +285,21 @@ __device__ __forceinline__ int pd(int i) { return i + (i >> 3); }
 __device__ __forceinline__ float4 dc_mul_mi(float4 a) { return make_float4(a.z, a.w, -a.x, -a.y); }  // a * (-i)
 __device__ __forceinline__ float4 dc_mul_pi(float4 a) { return make_float4(-a.z, -a.w, a.x, a.y); }  // a * (+i)
 
-// bit-reversed input, natural output, forward transform (w = e^{-2 pi i k / P})
+// bit-reversed input, natural output, forward transform (w = e^{-2 pi i k / P}).
+// The input is zero-padded past P/2 (the Bluestein sequences have K <= P/2
+// values), i.e. zero at every odd bit-reversed position, and the first two
+// stages have unit twiddles: that pass is a 4-point DFT of (a0, 0, a2, 0).
 __device__ void fft_dit_df(float4 *buf, const float4 *__restrict__ tw, int P, int logP) {
-  int s = 1;
+  for (int i = threadIdx.x; i < P / 4; i += blockDim.x) {
+    const int p0 = 4 * i;
+    const float4 a0 = buf[pd(p0)], a2 = buf[pd(p0 + 2)], a2m = dc_mul_mi(a2);
+    buf[pd(p0)] = dc_add(a0, a2);
+    buf[pd(p0 + 2)] = dc_sub(a0, a2);
+    buf[pd(p0 + 1)] = dc_add(a0, a2m);
+    buf[pd(p0 + 3)] = dc_sub(a0, a2m);
+  }
+  __syncthreads();
+  int s = 3;
   for (; s + 1 <= logP; s += 2) {
     const int h = 1 << (s - 1);
     for (int i = threadIdx.x; i < P / 4; i += blockDim.x) {
@@ -319,10 +331,13 @@ __device__ void fft_dit_df(float4 *buf, const float4 *__restrict__ tw, int P, in
     __syncthreads();
   }
 }
-// natural input, bit-reversed output, unnormalised inverse transform
+// natural input, bit-reversed output, unnormalised inverse transform.  Only
+// the outputs at even bit-reversed positions (natural index < P/2) are
+// produced: the Bluestein result needs K <= P/2 of them.  The last pass has
+// unit twiddles.
 __device__ void ifft_dif_df(float4 *buf, const float4 *__restrict__ tw, int P, int logP) {
   int s = logP;
-  for (; s - 1 >= 1; s -= 2) {
+  for (; s >= 3; s -= 2) {
     const int h = 1 << (s - 2);
     for (int i = threadIdx.x; i < P / 4; i += blockDim.x) {
       const int jp = i & (h - 1);
@@ -339,12 +354,16 @@ __device__ void ifft_dif_df(float4 *buf, const float4 *__restrict__ tw, int P, i
     }
     __syncthreads();
   }
-  if (s == 1) {
-    for (int i = threadIdx.x; i < P / 2; i += blockDim.x) {
-      const float4 u = buf[pd(2 * i)], v = buf[pd(2 * i + 1)];
-      buf[pd(2 * i)] = dc_add(u, v);
-      buf[pd(2 * i + 1)] = dc_sub(u, v);
+  if (s == 2) {  // stages 2 and 1, unit twiddles, even outputs only
+    for (int i = threadIdx.x; i < P / 4; i += blockDim.x) {
+      const int p0 = 4 * i;
+      const float4 a0 = buf[pd(p0)], a1 = buf[pd(p0 + 1)], a2 = buf[pd(p0 + 2)], a3 = buf[pd(p0 + 3)];
+      buf[pd(p0)] = dc_add(dc_add(a0, a2), dc_add(a1, a3));
+      buf[pd(p0 + 2)] = dc_add(dc_sub(a0, a2), dc_mul_pi(dc_sub(a1, a3)));
     }
+    __syncthreads();
+  } else if (s == 1) {
+    for (int i = threadIdx.x; i < P / 2; i += blockDim.x) buf[pd(2 * i)] = dc_add(buf[pd(2 * i)], buf[pd(2 * i + 1)]);
     __syncthreads();
   }
 }
@@ -1078,7 +1097,7 @@ void launch_ring(KF kernel, const RingArgs &a, int nblk, int P, cudaStream_t st,
 // spectrum and each chirp); the FP64 path counts 5 P log2 P flop per FFT.
 double ring_work(const RingArgs &a, int nblk) {
   const double P = a.P, lg = a.logP;
-  if (t_precision == 1) return (double)nblk * P * (64.0 * lg + 32.0 + 64.0 * a.K / P);
+  if (t_precision == 1) return (double)nblk * P * (64.0 * lg - 56.0 + 64.0 * a.K / P);
   return (double)nblk * (10.0 * P * lg + 6.0 * P + 12.0 * a.K);
 }
 
