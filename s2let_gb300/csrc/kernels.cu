@@ -224,10 +224,6 @@ __device__ __forceinline__ float2 df_two_sum(float a, float b) {
   const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
   return make_float2(s, e);
 }
-__device__ __forceinline__ float2 df_fast(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
-}
 __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
   float2 s = df_two_sum(a.x, b.x);
   s.y = __fadd_rn(s.y, __fadd_rn(a.y, b.y));
@@ -830,26 +826,28 @@ __global__ void k_gamma_px_synth(const double2 *__restrict__ F, void *__restrict
   }
   __syncthreads();
   const int64_t total = (int64_t)nb * npx;
-  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= total) return;
-  const int b = (int)(gid / npx);
-  const int64_t px = gid - (int64_t)b * npx;
-  double2 v[NN];
+  // grid-stride: a few blocks per SM, so the twiddle table above is built once per block
+  for (int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < total;
+       gid += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(gid / npx);
+    const int64_t px = gid - (int64_t)b * npx;
+    double2 v[NN];
 #pragma unroll
-  for (int k = 0; k < NN; ++k) v[k] = F[((int64_t)b * NN + k) * npx + px];
-  for (int g = 0; g < ng; ++g) {
-    double re = 0.0, im = 0.0;
+    for (int k = 0; k < NN; ++k) v[k] = F[((int64_t)b * NN + k) * npx + px];
+    for (int g = 0; g < ng; ++g) {
+      double re = 0.0, im = 0.0;
 #pragma unroll
-    for (int k = 0; k < NN; ++k) {
-      const double2 e = tw[g * NN + k];
-      re = fma(e.x, v[k].x, fma(-e.y, v[k].y, re));
-      if (!real) im = fma(e.x, v[k].y, fma(e.y, v[k].x, im));
+      for (int k = 0; k < NN; ++k) {
+        const double2 e = tw[g * NN + k];
+        re = fma(e.x, v[k].x, fma(-e.y, v[k].y, re));
+        if (!real) im = fma(e.x, v[k].y, fma(e.y, v[k].x, im));
+      }
+      const int64_t o = (int64_t)b * out_ms + (int64_t)g * npx + px;
+      if (real)
+        ((double *)out)[o] = re * c;
+      else
+        ((double2 *)out)[o] = make_double2(re * c, im * c);
     }
-    const int64_t o = (int64_t)b * out_ms + (int64_t)g * npx + px;
-    if (real)
-      ((double *)out)[o] = re * c;
-    else
-      ((double2 *)out)[o] = make_double2(re * c, im * c);
   }
 }
 
@@ -865,36 +863,38 @@ __global__ void k_gamma_px_anal(const void *__restrict__ in, int64_t in_ms, doub
   }
   __syncthreads();
   const int64_t total = (int64_t)nb * npx;
-  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= total) return;
-  const int b = (int)(gid / npx);
-  const int64_t px = gid - (int64_t)b * npx;
-  double2 acc[NN];
+  // grid-stride: a few blocks per SM, so the twiddle table above is built once per block
+  for (int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < total;
+       gid += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(gid / npx);
+    const int64_t px = gid - (int64_t)b * npx;
+    double2 acc[NN];
 #pragma unroll
-  for (int k = 0; k < NN; ++k) acc[k] = make_double2(0.0, 0.0);
-  if (real) {
-    for (int g = 0; g < ng; ++g) {
-      const double f = ((const double *)in)[(int64_t)b * in_ms + (int64_t)g * npx + px];
+    for (int k = 0; k < NN; ++k) acc[k] = make_double2(0.0, 0.0);
+    if (real) {
+      for (int g = 0; g < ng; ++g) {
+        const double f = ((const double *)in)[(int64_t)b * in_ms + (int64_t)g * npx + px];
 #pragma unroll
-      for (int k = 0; k < NN; ++k) {
-        const double2 e = tw[g * NN + k];
-        acc[k].x = fma(e.x, f, acc[k].x);
-        acc[k].y = fma(e.y, f, acc[k].y);
+        for (int k = 0; k < NN; ++k) {
+          const double2 e = tw[g * NN + k];
+          acc[k].x = fma(e.x, f, acc[k].x);
+          acc[k].y = fma(e.y, f, acc[k].y);
+        }
+      }
+    } else {
+      for (int g = 0; g < ng; ++g) {
+        const double2 f = ((const double2 *)in)[(int64_t)b * in_ms + (int64_t)g * npx + px];
+#pragma unroll
+        for (int k = 0; k < NN; ++k) {
+          const double2 e = tw[g * NN + k];
+          acc[k].x = fma(e.x, f.x, fma(-e.y, f.y, acc[k].x));
+          acc[k].y = fma(e.x, f.y, fma(e.y, f.x, acc[k].y));
+        }
       }
     }
-  } else {
-    for (int g = 0; g < ng; ++g) {
-      const double2 f = ((const double2 *)in)[(int64_t)b * in_ms + (int64_t)g * npx + px];
 #pragma unroll
-      for (int k = 0; k < NN; ++k) {
-        const double2 e = tw[g * NN + k];
-        acc[k].x = fma(e.x, f.x, fma(-e.y, f.y, acc[k].x));
-        acc[k].y = fma(e.x, f.y, fma(e.y, f.x, acc[k].y));
-      }
-    }
+    for (int k = 0; k < NN; ++k) F[((int64_t)b * NN + k) * npx + px] = scl2(acc[k], c);
   }
-#pragma unroll
-  for (int k = 0; k < NN; ++k) F[((int64_t)b * NN + k) * npx + px] = scl2(acc[k], c);
 }
 
 // The same gamma DFTs in double-float arithmetic on the FP32 pipe (split-
@@ -926,34 +926,36 @@ __global__ void k_gamma_px_synth_df(const double2 *__restrict__ F, void *__restr
   }
   __syncthreads();
   const int64_t total = (int64_t)nb * npx;
-  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= total) return;
-  const int b = (int)(gid / npx);
-  const int64_t px = gid - (int64_t)b * npx;
-  double2 v[NN];
-  int em = 0;
-#pragma unroll
-  for (int k = 0; k < NN; ++k) {
-    v[k] = F[((int64_t)b * NN + k) * npx + px];
-    em = max(em, max(exp_field(v[k].x), exp_field(v[k].y)));
-  }
-  const int e = block_scale(em);
-  float4 z[NN];
-#pragma unroll
-  for (int k = 0; k < NN; ++k) z[k] = dc_split(v[k], e);
-  for (int g = 0; g < ng; ++g) {
-    float2 re = make_float2(0.f, 0.f), im = make_float2(0.f, 0.f);
+  // grid-stride: a few blocks per SM, so the twiddle table above is built once per block
+  for (int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < total;
+       gid += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(gid / npx);
+    const int64_t px = gid - (int64_t)b * npx;
+    double2 v[NN];
+    int em = 0;
 #pragma unroll
     for (int k = 0; k < NN; ++k) {
-      const float4 w = tw[g * NN + k];
-      re = df_add(re, df_dot2(dre(w), dre(z[k]), df_neg(dim_(w)), dim_(z[k])));
-      if (!real) im = df_add(im, df_dot2(dre(w), dim_(z[k]), dim_(w), dre(z[k])));
+      v[k] = F[((int64_t)b * NN + k) * npx + px];
+      em = max(em, max(exp_field(v[k].x), exp_field(v[k].y)));
     }
-    const int64_t o = (int64_t)b * out_ms + (int64_t)g * npx + px;
-    if (real)
-      ((double *)out)[o] = join_scaled(re.x, re.y, e);
-    else
-      ((double2 *)out)[o] = make_double2(join_scaled(re.x, re.y, e), join_scaled(im.x, im.y, e));
+    const int e = block_scale(em);
+    float4 z[NN];
+#pragma unroll
+    for (int k = 0; k < NN; ++k) z[k] = dc_split(v[k], e);
+    for (int g = 0; g < ng; ++g) {
+      float2 re = make_float2(0.f, 0.f), im = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < NN; ++k) {
+        const float4 w = tw[g * NN + k];
+        re = df_add(re, df_dot2(dre(w), dre(z[k]), df_neg(dim_(w)), dim_(z[k])));
+        if (!real) im = df_add(im, df_dot2(dre(w), dim_(z[k]), dim_(w), dre(z[k])));
+      }
+      const int64_t o = (int64_t)b * out_ms + (int64_t)g * npx + px;
+      if (real)
+        ((double *)out)[o] = join_scaled(re.x, re.y, e);
+      else
+        ((double2 *)out)[o] = make_double2(join_scaled(re.x, re.y, e), join_scaled(im.x, im.y, e));
+    }
   }
 }
 
@@ -972,40 +974,42 @@ __global__ void k_gamma_px_anal_df(const void *__restrict__ in, int64_t in_ms, d
   }
   __syncthreads();
   const int64_t total = (int64_t)nb * npx;
-  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= total) return;
-  const int b = (int)(gid / npx);
-  const int64_t px = gid - (int64_t)b * npx;
-  float4 acc[NN];
+  // grid-stride: a few blocks per SM, so the twiddle table above is built once per block
+  for (int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < total;
+       gid += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(gid / npx);
+    const int64_t px = gid - (int64_t)b * npx;
+    float4 acc[NN];
 #pragma unroll
-  for (int k = 0; k < NN; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-  const int64_t base = (int64_t)b * in_ms + px;
-  int em = 0;
-  for (int g = 0; g < ng; ++g) {
-    if (real) {
-      em = max(em, exp_field(((const double *)in)[base + (int64_t)g * npx]));
-    } else {
-      const double2 f = ((const double2 *)in)[base + (int64_t)g * npx];
-      em = max(em, max(exp_field(f.x), exp_field(f.y)));
-    }
-  }
-  const int e = block_scale(em);
-  for (int g = 0; g < ng; ++g) {
-    if (real) {
-      const float2 f = df_split(((const double *)in)[base + (int64_t)g * npx], e);
-#pragma unroll
-      for (int k = 0; k < NN; ++k) {
-        const float4 w = tw[g * NN + k];
-        acc[k] = dmk(df_add(dre(acc[k]), df_mul(dre(w), f)), df_add(dim_(acc[k]), df_mul(dim_(w), f)));
+    for (int k = 0; k < NN; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int64_t base = (int64_t)b * in_ms + px;
+    int em = 0;
+    for (int g = 0; g < ng; ++g) {
+      if (real) {
+        em = max(em, exp_field(((const double *)in)[base + (int64_t)g * npx]));
+      } else {
+        const double2 f = ((const double2 *)in)[base + (int64_t)g * npx];
+        em = max(em, max(exp_field(f.x), exp_field(f.y)));
       }
-    } else {
-      const float4 f = dc_split(((const double2 *)in)[base + (int64_t)g * npx], e);
-#pragma unroll
-      for (int k = 0; k < NN; ++k) acc[k] = dc_add(acc[k], dc_mul(tw[g * NN + k], f));
     }
-  }
+    const int e = block_scale(em);
+    for (int g = 0; g < ng; ++g) {
+      if (real) {
+        const float2 f = df_split(((const double *)in)[base + (int64_t)g * npx], e);
 #pragma unroll
-  for (int k = 0; k < NN; ++k) F[((int64_t)b * NN + k) * npx + px] = dc_to(acc[k], e);
+        for (int k = 0; k < NN; ++k) {
+          const float4 w = tw[g * NN + k];
+          acc[k] = dmk(df_add(dre(acc[k]), df_mul(dre(w), f)), df_add(dim_(acc[k]), df_mul(dim_(w), f)));
+        }
+      } else {
+        const float4 f = dc_split(((const double2 *)in)[base + (int64_t)g * npx], e);
+#pragma unroll
+        for (int k = 0; k < NN; ++k) acc[k] = dc_add(acc[k], dc_mul(tw[g * NN + k], f));
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NN; ++k) F[((int64_t)b * NN + k) * npx + px] = dc_to(acc[k], e);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1328,6 +1332,18 @@ void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int 
   S2G_LAUNCHED();
 }
 
+// blocks for the grid-stride pixel gamma kernels: at most 8 per SM
+static unsigned gamma_px_grid(int64_t total) {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    S2G_CUDA(cudaGetDevice(&dev));
+    S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const int64_t want = ceil_div(total, 256), cap = (int64_t)nsm * 8;
+  return (unsigned)(want < cap ? want : cap);
+}
+
 void gamma_px_synthesis(const double2 *F, void *out, int64_t out_ms, const int *ns, int nn, int ng, int bl,
                         int ss, int nb, bool real, double c, cudaStream_t st) {
   S2G_REQUIRE(nn >= 1 && nn <= 16 && ng * nn <= kMaxGammaTw, ERR_UNSUPPORTED, "more than 16 directions per scale");
@@ -1335,7 +1351,7 @@ void gamma_px_synthesis(const double2 *F, void *out, int64_t out_ms, const int *
   const int64_t total = (int64_t)nb * npx;
   if (total <= 0) return;
   KTimer kt(KC_GAMMA, st, 0.0, (double)total * (16.0 * nn + (real ? 8.0 : 16.0) * ng));
-  const unsigned grid = (unsigned)ceil_div(total, 256);
+  const unsigned grid = gamma_px_grid(total);
   switch (nn) {
 #define S2G_GPS(N)                                                                       \
   case N:                                                                                \
@@ -1359,7 +1375,7 @@ void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns,
   const int64_t total = (int64_t)nb * npx;
   if (total <= 0) return;
   KTimer kt(KC_GAMMA, st, 0.0, (double)total * (16.0 * nn + (real ? 8.0 : 16.0) * ng));
-  const unsigned grid = (unsigned)ceil_div(total, 256);
+  const unsigned grid = gamma_px_grid(total);
   switch (nn) {
 #define S2G_GPA(N)                                                                      \
   case N:                                                                               \

@@ -54,12 +54,20 @@ def _check(t: torch.Tensor, name: str, n: int, real: bool) -> torch.Tensor:
 
 
 def _call(fn: str, args, precision: str, device) -> None:
+    """One library call at the given precision; the calling thread's precision
+    mode is restored afterwards, so C-ABI calls made later on the same thread
+    keep their own setting."""
     lib = _lib_handle()
+    if precision not in _PREC:
+        raise ValueError(f"precision must be one of {list(_PREC)}")
     with torch.cuda.device(device):
         stream = C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
-        if lib.s2let_gpu_set_precision(_PREC[precision]) != 0:
-            raise ValueError(f"precision must be one of {list(_PREC)}")
-        rc = getattr(lib, fn)(*args, stream)
+        old = lib.s2let_gpu_get_precision()
+        lib.s2let_gpu_set_precision(_PREC[precision])
+        try:
+            rc = getattr(lib, fn)(*args, stream)
+        finally:
+            lib.s2let_gpu_set_precision(old)
     if rc != 0:
         raise RuntimeError(f"{fn}: {lib.s2let_gpu_last_error_string().decode()}")
 

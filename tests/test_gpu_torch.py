@@ -131,3 +131,23 @@ def test_rejects_bad_shapes():
         T.px2wav(torch.zeros((2, 7), dtype=torch.float64, device=DEV), p)
     with pytest.raises(ValueError):
         T.px2wav(torch.zeros((2, T.sizes(p)["n_px"]), dtype=torch.float64), p)
+
+
+@pytest.mark.gpu
+def test_precision_mode_restored(gpu):
+    """A mixed-precision torch call leaves the thread's precision mode as it
+    found it, so later C-ABI calls on the thread keep their own setting."""
+    lib = gpu.lib
+    old = lib.s2let_gpu_get_precision()
+    assert lib.s2let_gpu_set_precision(0) == 0
+    try:
+        p = make_parameters(160, 2.0, 2, 3, 0, 0)
+        x = _rand((2, T.sizes(p)["n_px"]), False, torch.Generator().manual_seed(3))
+        w, s = T.px2wav(x, p, precision="mixed")
+        T.wav2px(w, s, p, precision="mixed")
+        assert lib.s2let_gpu_get_precision() == 0
+        with pytest.raises(ValueError):
+            T.px2wav(x, p, precision="fp16")
+        assert lib.s2let_gpu_get_precision() == 0
+    finally:
+        lib.s2let_gpu_set_precision(old)
