@@ -468,8 +468,8 @@ int s2let_gpu_wav2px_multi(void *const *f, void *const *f_wav, void *const *f_sc
 /*
  * Host-pointer batches: the drop-in functions above for `nbatch` maps in one
  * call (HOST buffers, map b at b * s2let_n_px / s2let_n_wav / s2let_n_scal
- * elements, synchronous).  The maps run as batches of up to 8 on the GPU
- * (S2LET_GPU_HOST_CHUNK overrides), chunks alternating between two streams so
+ * elements, synchronous).  The maps run as chunks of half the batch, 8 to 16
+ * maps (S2LET_GPU_HOST_CHUNK overrides), alternating between two streams so
  * that one chunk's copies overlap another's transforms; the per-map work of
  * streaming the Wigner tables is shared by the chunk.
  * Returns the status.

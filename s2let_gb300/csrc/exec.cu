@@ -1000,15 +1000,21 @@ int batch_directional(const char *fn, s2g::Op op, const s2let_parameters_t *p, b
 }
 
 // Host-pointer batches: nb contiguous maps in host memory (the drop-in layout,
-// map b at b * the single-map size), run in chunks of kHostChunk maps on two
-// streams so that one chunk's copies overlap the other's transforms.  Only the
-// used prefix of each f_wav (the transforms advance with N_j, the buffer is
-// sized with N) crosses the bus, as in the drop-in functions.  Synchronous.
-constexpr int kHostChunk = 8;
-int host_chunk() {
+// map b at b * the single-map size), run in chunks on two streams so that one
+// chunk's copies overlap the other's transforms.  Only the used prefix of each
+// f_wav (the transforms advance with N_j, the buffer is sized with N) crosses
+// the bus, as in the drop-in functions.  Synchronous.
+//
+// Chunk size: half the batch, between 8 and 16 maps.  Larger chunks stream
+// the Wigner tables for more maps at once; smaller ones expose less of the
+// first copy in and the last copy out (L=1024, N=4, 32 real maps per call:
+// 131.8 / 150.0 / 164.5 maps/s at chunks of 4 / 8 / 16).
+int host_chunk(int nb) {
   const char *e = getenv("S2LET_GPU_HOST_CHUNK");
   const int v = e ? atoi(e) : 0;
-  return v > 0 ? v : kHostChunk;
+  if (v > 0) return v;
+  const int half = (nb + 1) / 2;
+  return half < 8 ? 8 : (half > 16 ? 16 : half);
 }
 
 int host_batch(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool real, void *px, void *wav,
@@ -1034,7 +1040,7 @@ int host_batch(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool rea
     const bool fwd = (op == OP_PX2WAV || op == OP_ADJ_PX2WAV);
     (void)directional_plan(*p, real);  // build the plan before the two streams use it
     char *hpx = (char *)px, *hw = (char *)wav, *hs = (char *)scal;
-    const int chunk = host_chunk();
+    const int chunk = host_chunk(nb);
     for (int c0 = 0, k = 0; c0 < nb; c0 += chunk, ++k) {
       const int n = std::min(chunk, nb - c0);
       cudaStream_t st = sts[k & 1];
