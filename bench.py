@@ -719,16 +719,22 @@ def main():
                 lib.s2let_synthesis_wav2px_real(vp(frh[b]), vp(wh[b]), vp(sh[b]), C.byref(p))
             s2let_gb300.check(lib, "host API")
 
-        def host_rate(fn, steps):
-            fn()
+        step_ms = []
+
+        def host_rate(fn, steps, record=False, warmup=1):
+            for _ in range(warmup):
+                fn()
             if dist:
                 dist.barrier()
             t0 = time.perf_counter()
             for _ in range(steps):
+                t1 = time.perf_counter()
                 fn()
+                if record:
+                    step_ms.append(1e3 * (time.perf_counter() - t1))
             return max_over_ranks((time.perf_counter() - t0) / steps, dist, dev)
 
-        e2e_s = host_rate(e2e_batch_step, a.steps)
+        e2e_s = host_rate(e2e_batch_step, a.steps, record=True, warmup=max(1, a.warmup))
         e2e_rt = float((frh - fh).abs().max() / fh.abs().max())
         single_s = host_rate(e2e_single_step, max(1, min(a.steps, 2)))
         e2e = {"value": whole_job_rate(nb, world, e2e_s), "unit": "maps/s",
@@ -736,6 +742,7 @@ def main():
                "api": "s2let_gpu_analysis_px2wav_real_host_batch + s2let_gpu_synthesis_wav2px_real_host_batch "
                       f"({nb} maps per call, pinned host buffers)",
                "max_rel_err_round_trip": e2e_rt,
+               "step_ms": [round(x, 1) for x in step_ms],
                "dropin_one_map_per_call": {"value": whole_job_rate(nb, world, single_s), "unit": "maps/s",
                                            "api": "s2let_analysis_px2wav_real + s2let_synthesis_wav2px_real"}}
 

@@ -468,10 +468,12 @@ int s2let_gpu_wav2px_multi(void *const *f, void *const *f_wav, void *const *f_sc
 /*
  * Host-pointer batches: the drop-in functions above for `nbatch` maps in one
  * call (HOST buffers, map b at b * s2let_n_px / s2let_n_wav / s2let_n_scal
- * elements, synchronous).  The maps run as chunks of half the batch, 8 to 16
- * maps (S2LET_GPU_HOST_CHUNK overrides), alternating between two streams so
- * that one chunk's copies overlap another's transforms; the per-map work of
- * streaming the Wigner tables is shared by the chunk.
+ * elements, synchronous).  Up to 32 maps run as one device batch
+ * (S2LET_GPU_HOST_PASS overrides), so the Wigner tables are streamed once for
+ * all of them, and f_wav crosses the bus on a second stream in pieces (one
+ * scale of a group of up to 8 maps) overlapped with the transforms: the
+ * analysis copies each piece out as soon as it is written, largest scales
+ * first; the synthesis starts each group's kernels as soon as its piece is in.
  * Returns the status.
  */
 int s2let_gpu_analysis_px2wav_real_host_batch(double *f_wav, double *f_scal, const double *f, int nbatch,

@@ -436,6 +436,62 @@ void sht_forward(const Sht &H, const void *f, int64_t fstride, double2 *flm, int
 
 enum SplitMode { SPLIT_ANALYSIS, SPLIT_SYNTH_ADJ };
 enum MergeMode { MERGE_SYNTHESIS, MERGE_ANALYSIS_ADJ };
+
+// Host f_wav copies overlapped with the transforms of one batch.  A piece is
+// one scale of a group of consecutive maps: elements woff .. woff + len of
+// each map's f_wav (seglen[woff] = len).  Analysis: the copy stream takes each
+// piece to the host as soon as the kernels on the compute stream have written
+// it.  Synthesis: every piece is queued on the copy stream up front, in the
+// order the transforms read them, and the compute stream waits for a piece's
+// event before its first kernel reads it.
+struct WavPipe {
+  cudaStream_t cs = nullptr;  // copy stream
+  char *host = nullptr;       // map b's f_wav at host + b * hstride * esz
+  int64_t hstride = 0;
+  size_t esz = 0;
+  int group = 8;                           // maps per piece
+  std::map<int64_t, int64_t> seglen;       // scale offset -> elements of the scale
+  std::map<std::pair<int64_t, int>, cudaEvent_t> ready;  // (scale offset, first map) -> copied in
+  std::vector<cudaEvent_t> events;
+  WavPipe() = default;
+  WavPipe(const WavPipe &) = delete;
+  WavPipe &operator=(const WavPipe &) = delete;
+  ~WavPipe() {
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+  }
+  cudaEvent_t event() {
+    cudaEvent_t e;
+    S2G_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    events.push_back(e);
+    return e;
+  }
+  // analysis: piece (woff, maps b0 .. b0 + nbg) written by the kernels queued so far on st
+  void out(cudaStream_t st, const void *dev, int64_t dstride, int64_t woff, int b0, int nbg) {
+    cudaEvent_t e = event();
+    S2G_CUDA(cudaEventRecord(e, st));
+    S2G_CUDA(cudaStreamWaitEvent(cs, e, 0));
+    const int64_t len = seglen.at(woff);
+    S2G_CUDA(cudaMemcpy2DAsync(host + ((size_t)b0 * hstride + woff) * esz, hstride * esz,
+                               (const char *)dev + ((size_t)b0 * dstride + woff) * esz, dstride * esz, len * esz,
+                               nbg, cudaMemcpyDeviceToHost, cs));
+  }
+  // synthesis: queue the copy of piece (woff, b0 .. b0 + nbg) into dev
+  void in(void *dev, int64_t dstride, int64_t woff, int b0, int nbg) {
+    const int64_t len = seglen.at(woff);
+    S2G_CUDA(cudaMemcpy2DAsync((char *)dev + ((size_t)b0 * dstride + woff) * esz, dstride * esz,
+                               host + ((size_t)b0 * hstride + woff) * esz, hstride * esz, len * esz, nbg,
+                               cudaMemcpyHostToDevice, cs));
+    cudaEvent_t e = event();
+    S2G_CUDA(cudaEventRecord(e, cs));
+    ready[{woff, b0}] = e;
+  }
+  // synthesis: the compute stream waits for piece (woff, b0)
+  void wait(cudaStream_t st, int64_t woff, int b0) {
+    auto it = ready.find({woff, b0});
+    S2G_REQUIRE(it != ready.end(), ERR_INVALID, "host pipeline: piece not queued");
+    S2G_CUDA(cudaStreamWaitEvent(st, it->second, 0));
+  }
+};
 const double kSqrt2Pi = 2.5066282746310005024;
 
 // flm -> (f_wav, f_scal).  SPLIT_ANALYSIS: lm2wav.  SPLIT_SYNTH_ADJ: adjoint of wav2lm.
@@ -449,7 +505,7 @@ bool rings_on_n(const WavPlan &P, const Scale &sd) {
 }
 
 void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_half, void *f_wav,
-               int64_t wstride, void *f_scal, int64_t sstride, int nb, Scratch &S) {
+               int64_t wstride, void *f_scal, int64_t sstride, int nb, Scratch &S, WavPipe *pipe = nullptr) {
   const bool real = P.real;
   const int L = P.L;
   const size_t esz = real ? sizeof(double) : sizeof(double2);
@@ -485,10 +541,19 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
   const int64_t gsz = (int64_t)nb * P.max_nn * ntmax * Wmax;
   double2 *Gbuf = S.get<double2>(2 * gsz);
   double2 *spec = S.get<double2>((int64_t)nb * std::max(P.max_ng, P.max_nn) * ntmax * Kmax);
+  // scales sharing band-limit and directions share each table pass
+  std::vector<std::pair<size_t, size_t>> passes;
   for (size_t k0 = 0; k0 < P.sc.size();) {
-    // scales sharing band-limit and directions share each table pass
     size_t k1 = k0 + 1;
     if (k1 < P.sc.size() && P.sc[k1].bl == P.sc[k0].bl && P.sc[k1].ns == P.sc[k0].ns) ++k1;
+    passes.emplace_back(k0, k1);
+    k0 = k1;
+  }
+  // with host copies the largest scales go first, so that most of f_wav can
+  // cross the bus while the smaller scales are transformed
+  if (pipe) std::reverse(passes.begin(), passes.end());
+  for (const auto &pk : passes) {
+    const size_t k0 = pk.first, k1 = pk.second;
     const int ngrp = (int)(k1 - k0);
     const int bl = P.sc[k0].bl, W = 2 * bl - 1, nn = (int)P.sc[k0].ns.size();
     const int nt = P.nt(bl), K = P.K(bl);
@@ -531,28 +596,38 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
       char *out = (char *)f_wav + (size_t)sd.woff * esz;
       const double2 *Gq = Gbuf + q * gsz;
       if (rings_on_n(P, sd)) {
-        // F_n(t, p) = sum_m G_n(t, m) e^{i m phi_p}; spec holds F[b][i][t][p]
-        for (int i = 0; i < nn; ++i) {
-          const bool herm = real && sd.ns[i] == 0;  // real signal, n = 0: only m >= 0 computed
-          ring_inverse_c(Gq + (int64_t)i * nt * W + (herm ? bl - 1 : 0), W, (int64_t)nn * nt * W, nt,
-                         herm ? bl : W, herm ? 0 : -(bl - 1), herm, spec + (int64_t)i * nt * K, K,
-                         (int64_t)nn * nt * K, nt, nb * nt, bl, P.ss, S.st);
+        // F_n(t, p) = sum_m G_n(t, m) e^{i m phi_p}; spec holds F[b][i][t][p].
+        // With host copies, in groups of maps, each group copied out when done.
+        const int G = pipe ? pipe->group : nb;
+        for (int b0 = 0; b0 < nb; b0 += G) {
+          const int nbg = std::min(G, nb - b0);
+          const double2 *Gb = Gq + (int64_t)b0 * nn * nt * W;
+          double2 *sb = spec + (int64_t)b0 * nn * nt * K;
+          for (int i = 0; i < nn; ++i) {
+            const bool herm = real && sd.ns[i] == 0;  // real signal, n = 0: only m >= 0 computed
+            ring_inverse_c(Gb + (int64_t)i * nt * W + (herm ? bl - 1 : 0), W, (int64_t)nn * nt * W, nt,
+                           herm ? bl : W, herm ? 0 : -(bl - 1), herm, sb + (int64_t)i * nt * K, K,
+                           (int64_t)nn * nt * K, nt, nbg * nt, bl, P.ss, S.st);
+          }
+          gamma_px_synthesis(sb, out + (size_t)b0 * wstride * esz, wstride, sd.d_ns, nn, ng, bl, P.ss, nbg, real,
+                             c, S.st);
+          if (pipe) pipe->out(S.st, f_wav, wstride, sd.woff, b0, nbg);
         }
-        gamma_px_synthesis(spec, out, wstride, sd.d_ns, nn, ng, bl, P.ss, nb, real, c, S.st);
       } else {
         const int sw = real ? bl : W, mlo = real ? 0 : -(bl - 1);
         gamma_synthesis(Gq, spec, sd.d_ns, nn, ng, bl, P.ss, nb, real, c, S.st);
         ring_inverse(spec, sw, sw, mlo, out, K, wstride, ng * nt, nb * ng * nt, bl, P.ss, real, S.st);
+        if (pipe) pipe->out(S.st, f_wav, wstride, sd.woff, 0, nb);
       }
     }
-    k0 = k1;
   }
 }
 
 // (f_wav, f_scal) -> flm.  MERGE_SYNTHESIS: wav2lm.  MERGE_ANALYSIS_ADJ: adjoint of lm2wav.
 // For real signals flm holds m >= 0 only.  accumulate: add to flm instead of overwriting.
 void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstride, const void *f_scal,
-               int64_t sstride, double2 *flm, int nb, Scratch &S, bool accumulate = false) {
+               int64_t sstride, double2 *flm, int nb, Scratch &S, bool accumulate = false,
+               WavPipe *pipe = nullptr) {
   const bool real = P.real;
   const int L = P.L;
   const size_t esz = real ? sizeof(double) : sizeof(double2);
@@ -601,12 +676,22 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
       const char *in = (const char *)f_wav + (size_t)sd.woff * esz;
       double2 *Gq = Gbuf + q * gsz;
       if (rings_on_n(P, sd)) {
-        // F_n(t, p) = c sum_g e^{-i n gamma_g} f_g(t, p), then one DFT per (n, t)
-        gamma_px_analysis(in, wstride, spec, sd.d_ns, nn, ng, bl, P.ss, nb, real, c, S.st);
-        for (int i = 0; i < nn; ++i)
-          ring_forward_c(spec + (int64_t)i * nt * K, K, (int64_t)nn * nt * K, nt, Gq + (int64_t)i * nt * W, W,
-                         (int64_t)nn * nt * W, nt, W, -(bl - 1), nb * nt, bl, P.ss, S.st);
+        // F_n(t, p) = c sum_g e^{-i n gamma_g} f_g(t, p), then one DFT per (n, t).
+        // With host copies, in groups of maps, each after its copy has landed.
+        const int G = pipe ? pipe->group : nb;
+        for (int b0 = 0; b0 < nb; b0 += G) {
+          const int nbg = std::min(G, nb - b0);
+          if (pipe) pipe->wait(S.st, sd.woff, b0);
+          double2 *sb = spec + (int64_t)b0 * nn * nt * K;
+          gamma_px_analysis(in + (size_t)b0 * wstride * esz, wstride, sb, sd.d_ns, nn, ng, bl, P.ss, nbg, real, c,
+                            S.st);
+          for (int i = 0; i < nn; ++i)
+            ring_forward_c(sb + (int64_t)i * nt * K, K, (int64_t)nn * nt * K, nt,
+                           Gq + (int64_t)b0 * nn * nt * W + (int64_t)i * nt * W, W, (int64_t)nn * nt * W, nt, W,
+                           -(bl - 1), nbg * nt, bl, P.ss, S.st);
+        }
       } else {
+        if (pipe) pipe->wait(S.st, sd.woff, 0);
         ring_forward(in, K, wstride, ng * nt, spec, sw, sw, mlo, nb * ng * nt, bl, P.ss, real, S.st);
         gamma_analysis(spec, Gq, sd.d_ns, nn, ng, bl, P.ss, nb, real, c, S.st);
       }
@@ -725,7 +810,7 @@ enum Op { OP_PX2WAV, OP_WAV2PX, OP_ADJ_WAV2PX, OP_ADJ_PX2WAV, OP_LM2WAV, OP_WAV2
 // One wavelet transform of `nb` maps with plan P.  Pixel maps, wavelet and
 // scaling arrays are batched with their single-map sizes as strides.
 void run_plan(Op op, const WavPlan &P, void *px, void *lm, void *wav, int64_t nw, void *scal, int64_t ns,
-              int nb, cudaStream_t st, bool accumulate_lm = false) {
+              int nb, cudaStream_t st, bool accumulate_lm = false, WavPipe *pipe = nullptr) {
   if (nb <= 0) return;
   Scratch S(st);
   const int L = P.L;
@@ -736,20 +821,20 @@ void run_plan(Op op, const WavPlan &P, void *px, void *lm, void *wav, int64_t nw
   switch (op) {
   case OP_PX2WAV:
     sht_forward(sht_of(P), px, npx, flm, nb, S, false);
-    wav_split(P, SPLIT_ANALYSIS, flm, real, wav, nw, scal, ns, nb, S);
+    wav_split(P, SPLIT_ANALYSIS, flm, real, wav, nw, scal, ns, nb, S, pipe);
     break;
   case OP_LM2WAV:
     wav_split(P, SPLIT_ANALYSIS, flm, false, wav, nw, scal, ns, nb, S);
     break;
   case OP_ADJ_PX2WAV:
     sht_forward(sht_of(P), px, npx, flm, nb, S, true);
-    wav_split(P, SPLIT_SYNTH_ADJ, flm, real, wav, nw, scal, ns, nb, S);
+    wav_split(P, SPLIT_SYNTH_ADJ, flm, real, wav, nw, scal, ns, nb, S, pipe);
     break;
   case OP_ADJ_LM2WAV:
     wav_split(P, SPLIT_SYNTH_ADJ, flm, false, wav, nw, scal, ns, nb, S);
     break;
   case OP_WAV2PX:
-    wav_merge(P, MERGE_SYNTHESIS, wav, nw, scal, ns, flm, nb, S);
+    wav_merge(P, MERGE_SYNTHESIS, wav, nw, scal, ns, flm, nb, S, false, pipe);
     sht_inverse(sht_of(P), flm, real, px, npx, nb, S, false);
     break;
   case OP_WAV2LM:
@@ -757,7 +842,7 @@ void run_plan(Op op, const WavPlan &P, void *px, void *lm, void *wav, int64_t nw
     if (real) symmetrize_flm(flm, L, (int64_t)L * L, nb, st);
     break;
   case OP_ADJ_WAV2PX:
-    wav_merge(P, MERGE_ANALYSIS_ADJ, wav, nw, scal, ns, flm, nb, S);
+    wav_merge(P, MERGE_ANALYSIS_ADJ, wav, nw, scal, ns, flm, nb, S, false, pipe);
     sht_inverse(sht_of(P), flm, real, px, npx, nb, S, true);
     break;
   case OP_ADJ_WAV2LM:
@@ -1000,21 +1085,21 @@ int batch_directional(const char *fn, s2g::Op op, const s2let_parameters_t *p, b
 }
 
 // Host-pointer batches: nb contiguous maps in host memory (the drop-in layout,
-// map b at b * the single-map size), run in chunks on two streams so that one
-// chunk's copies overlap the other's transforms.  Only the used prefix of each
-// f_wav (the transforms advance with N_j, the buffer is sized with N) crosses
-// the bus, as in the drop-in functions.  Synchronous.
-//
-// Chunk size: half the batch, between 8 and 16 maps.  Larger chunks stream
-// the Wigner tables for more maps at once; smaller ones expose less of the
-// first copy in and the last copy out (L=1024, N=4, 32 real maps per call:
-// 131.8 / 150.0 / 164.5 maps/s at chunks of 4 / 8 / 16).
-int host_chunk(int nb) {
-  const char *e = getenv("S2LET_GPU_HOST_CHUNK");
+// map b at b * the single-map size).  Up to kHostPass maps run as one device
+// batch (the Wigner tables streamed once for all of them), and f_wav crosses
+// the bus in pieces of one scale for a group of maps on a second stream,
+// overlapped with the transforms (WavPipe): analysis copies each piece out as
+// soon as it is written, the largest scales first; synthesis queues every
+// piece up front and each group's first kernel waits for its piece.  Only the
+// used part of each f_wav (the transforms advance with N_j, the buffer is
+// sized with N) crosses the bus, as in the drop-in functions.  Synchronous.
+constexpr int kHostPass = 32;   // maps per device batch
+constexpr int kHostGroups = 4;  // map groups per scale (pieces of at most 8 maps)
+int host_pass(int nb) {
+  const char *e = getenv("S2LET_GPU_HOST_PASS");
   const int v = e ? atoi(e) : 0;
-  if (v > 0) return v;
-  const int half = (nb + 1) / 2;
-  return half < 8 ? 8 : (half > 16 ? 16 : half);
+  const int cap = v > 0 ? v : kHostPass;
+  return nb < cap ? nb : cap;
 }
 
 int host_batch(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool real, void *px, void *wav,
@@ -1029,6 +1114,7 @@ int host_batch(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool rea
     static thread_local cudaStream_t sts[2] = {nullptr, nullptr};
     for (auto &x : sts)
       if (!x) S2G_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+    cudaStream_t st = sts[0], cs = sts[1];
     const size_t esz = real ? sizeof(double) : sizeof(double2);
     s2let_parameters_t q = *p;
     if (real) {
@@ -1036,34 +1122,53 @@ int host_batch(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool rea
       q.spin = 0;
     }
     const int64_t npx = s2let_n_px(p), nw = s2let_n_wav(p), ns = s2let_n_scal(p);
-    const int64_t nwu = make_layout(q, real).woff.back();  // used prefix of one f_wav
+    const int64_t nwu = make_layout(q, real).woff.back();  // used part of one f_wav
     const bool fwd = (op == OP_PX2WAV || op == OP_ADJ_PX2WAV);
-    (void)directional_plan(*p, real);  // build the plan before the two streams use it
+    const WavPlan &P = directional_plan(*p, real);
     char *hpx = (char *)px, *hw = (char *)wav, *hs = (char *)scal;
-    const int chunk = host_chunk(nb);
-    for (int c0 = 0, k = 0; c0 < nb; c0 += chunk, ++k) {
-      const int n = std::min(chunk, nb - c0);
-      cudaStream_t st = sts[k & 1];
+    const int pass = host_pass(nb);
+    for (int c0 = 0; c0 < nb; c0 += pass) {
+      const int n = std::min(pass, nb - c0);
       Scratch S(st);
       char *dpx = S.get<char>((int64_t)n * npx * esz), *dw = S.get<char>((int64_t)n * nw * esz),
            *ds = S.get<char>((int64_t)n * ns * esz);
+      // both streams idle before the buffers are released, also on an error
+      struct Drain {
+        cudaStream_t a, b;
+        ~Drain() {
+          cudaStreamSynchronize(a);
+          cudaStreamSynchronize(b);
+        }
+      } drain{cs, st};
+      WavPipe pipe;
+      pipe.cs = cs;
+      pipe.host = hw + (size_t)c0 * nw * esz;
+      pipe.hstride = nw;
+      pipe.esz = esz;
+      pipe.group = std::max(1, std::min(8, (n + kHostGroups - 1) / kHostGroups));
+      for (size_t k = 0; k < P.sc.size(); ++k)
+        pipe.seglen[P.sc[k].woff] = (k + 1 < P.sc.size() ? P.sc[k + 1].woff : nwu) - P.sc[k].woff;
+      // the copy stream uses the new buffers only after their allocation on st
+      cudaEvent_t e0 = pipe.event();
+      S2G_CUDA(cudaEventRecord(e0, st));
+      S2G_CUDA(cudaStreamWaitEvent(cs, e0, 0));
       if (fwd) {
         S2G_CUDA(cudaMemcpyAsync(dpx, hpx + (size_t)c0 * npx * esz, (size_t)n * npx * esz, cudaMemcpyHostToDevice, st));
-      } else {
-        S2G_CUDA(cudaMemcpy2DAsync(dw, nw * esz, hw + (size_t)c0 * nw * esz, nw * esz, nwu * esz, n,
-                                   cudaMemcpyHostToDevice, st));
-        S2G_CUDA(cudaMemcpyAsync(ds, hs + (size_t)c0 * ns * esz, (size_t)n * ns * esz, cudaMemcpyHostToDevice, st));
-      }
-      run_directional(op, *p, real, dpx, nullptr, dw, ds, n, st);
-      if (fwd) {
-        S2G_CUDA(cudaMemcpy2DAsync(hw + (size_t)c0 * nw * esz, nw * esz, dw, nw * esz, nwu * esz, n,
-                                   cudaMemcpyDeviceToHost, st));
+        run_plan(op, P, dpx, nullptr, dw, nw, ds, ns, n, st, false, &pipe);
         S2G_CUDA(cudaMemcpyAsync(hs + (size_t)c0 * ns * esz, ds, (size_t)n * ns * esz, cudaMemcpyDeviceToHost, st));
       } else {
+        S2G_CUDA(cudaMemcpyAsync(ds, hs + (size_t)c0 * ns * esz, (size_t)n * ns * esz, cudaMemcpyHostToDevice, st));
+        for (const Scale &sd : P.sc) {  // in the order the synthesis reads them
+          if (rings_on_n(P, sd)) {
+            for (int b0 = 0; b0 < n; b0 += pipe.group) pipe.in(dw, nw, sd.woff, b0, std::min(pipe.group, n - b0));
+          } else {
+            pipe.in(dw, nw, sd.woff, 0, n);
+          }
+        }
+        run_plan(op, P, dpx, nullptr, dw, nw, ds, ns, n, st, false, &pipe);
         S2G_CUDA(cudaMemcpyAsync(hpx + (size_t)c0 * npx * esz, dpx, (size_t)n * npx * esz, cudaMemcpyDeviceToHost, st));
       }
     }
-    for (auto &x : sts) S2G_CUDA(cudaStreamSynchronize(x));
   });
 }
 

@@ -1,23 +1,27 @@
 """Host-pointer batches (s2let_gpu_*_host_batch): nbatch maps per call in the
 drop-in host layout.  Each map must equal the one-map drop-in call (FP64
-path, 1e-12), across chunk boundaries (two streams) and with the unused tail
-of f_wav (a scale with N_j < N) left as the caller wrote it."""
+path, 1e-12): f_wav crosses the bus in pieces (one scale of a group of maps)
+on a second stream while the transforms run, device batches hold up to 32
+maps (40 maps make two), and the unused tail of f_wav (a scale with N_j < N)
+stays as the caller wrote it."""
 import ctypes as C
 
 import numpy as np
 import pytest
 
 from conftest import rel_err
-from s2let_gb300.capi import make_parameters, ptr
+from s2let_gb300.capi import SAMPLING_MW_SS, make_parameters, ptr
 
 TOL = 1e-12
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L,N,spin,real,nb", [(32, 4, 0, True, 3), (24, 5, 2, False, 20), (16, 8, 0, True, 17)])
-def test_host_batch_equals_single_calls(gpu, L, N, spin, real, nb):
+@pytest.mark.parametrize("L,N,spin,real,nb,ss", [(32, 4, 0, True, 3, 0), (24, 5, 2, False, 20, 0),
+                                                 (16, 8, 0, True, 17, 0), (16, 3, 0, True, 40, 0),
+                                                 (20, 4, 0, True, 6, 1), (18, 3, 1, False, 5, 1)])
+def test_host_batch_equals_single_calls(gpu, L, N, spin, real, nb, ss):
     lib = gpu.lib
-    p = make_parameters(L, 2.0, 1, N, 0 if real else spin, 0)
+    p = make_parameters(L, 2.0, 1, N, 0 if real else spin, 0, sampling_scheme=SAMPLING_MW_SS if ss else 0)
     s = gpu.sizes(p)
     rng = np.random.default_rng(L + nb)
     dt = np.float64 if real else np.complex128
