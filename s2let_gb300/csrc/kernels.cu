@@ -9,6 +9,8 @@
 //              their contiguous axis, coefficient tiles broadcast).
 //  k_gamma_*   DFT over the 2N-1 gamma samples of the rotation group.
 //  k_merge     harmonic tiling merge (lmn -> lm) fused over scales/directions.
+#include <map>
+
 #include "common.h"
 #include "dfconv.h"
 #include "kernels.h"
@@ -1332,15 +1334,23 @@ void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int 
   S2G_LAUNCHED();
 }
 
-// blocks for the grid-stride pixel gamma kernels: at most 8 per SM
-static unsigned gamma_px_grid(int64_t total) {
+// blocks for a grid-stride pixel gamma kernel: as many as are resident at
+// once (one wave), fewer for small inputs
+static unsigned gamma_px_grid(int64_t total, const void *kernel) {
   static int nsm = 0;
+  static std::map<const void *, int> per_sm;
   if (!nsm) {
     int dev = 0;
     S2G_CUDA(cudaGetDevice(&dev));
     S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   }
-  const int64_t want = ceil_div(total, 256), cap = (int64_t)nsm * 8;
+  auto it = per_sm.find(kernel);
+  if (it == per_sm.end()) {
+    int b = 0;
+    S2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, 256, 0));
+    it = per_sm.emplace(kernel, b > 0 ? b : 1).first;
+  }
+  const int64_t want = ceil_div(total, 256), cap = (int64_t)nsm * it->second;
   return (unsigned)(want < cap ? want : cap);
 }
 
@@ -1351,14 +1361,15 @@ void gamma_px_synthesis(const double2 *F, void *out, int64_t out_ms, const int *
   const int64_t total = (int64_t)nb * npx;
   if (total <= 0) return;
   KTimer kt(KC_GAMMA, st, 0.0, (double)total * (16.0 * nn + (real ? 8.0 : 16.0) * ng));
-  const unsigned grid = gamma_px_grid(total);
   switch (nn) {
-#define S2G_GPS(N)                                                                       \
-  case N:                                                                                \
-    if (t_precision == 1)                                                                \
-      k_gamma_px_synth_df<N><<<grid, 256, 0, st>>>(F, out, out_ms, ns, ng, npx, nb, real, c); \
-    else                                                                                 \
-      k_gamma_px_synth<N><<<grid, 256, 0, st>>>(F, out, out_ms, ns, ng, npx, nb, real, c);    \
+#define S2G_GPS(N)                                                                                    \
+  case N:                                                                                             \
+    if (t_precision == 1)                                                                             \
+      k_gamma_px_synth_df<N><<<gamma_px_grid(total, (const void *)k_gamma_px_synth_df<N>), 256, 0, st>>>( \
+          F, out, out_ms, ns, ng, npx, nb, real, c);                                                  \
+    else                                                                                              \
+      k_gamma_px_synth<N><<<gamma_px_grid(total, (const void *)k_gamma_px_synth<N>), 256, 0, st>>>(       \
+          F, out, out_ms, ns, ng, npx, nb, real, c);                                                  \
     break;
     S2G_GPS(1) S2G_GPS(2) S2G_GPS(3) S2G_GPS(4) S2G_GPS(5) S2G_GPS(6) S2G_GPS(7) S2G_GPS(8)
     S2G_GPS(9) S2G_GPS(10) S2G_GPS(11) S2G_GPS(12) S2G_GPS(13) S2G_GPS(14) S2G_GPS(15) S2G_GPS(16)
@@ -1375,14 +1386,15 @@ void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns,
   const int64_t total = (int64_t)nb * npx;
   if (total <= 0) return;
   KTimer kt(KC_GAMMA, st, 0.0, (double)total * (16.0 * nn + (real ? 8.0 : 16.0) * ng));
-  const unsigned grid = gamma_px_grid(total);
   switch (nn) {
-#define S2G_GPA(N)                                                                      \
-  case N:                                                                               \
-    if (t_precision == 1)                                                               \
-      k_gamma_px_anal_df<N><<<grid, 256, 0, st>>>(in, in_ms, F, ns, ng, npx, nb, real, c); \
-    else                                                                                \
-      k_gamma_px_anal<N><<<grid, 256, 0, st>>>(in, in_ms, F, ns, ng, npx, nb, real, c);    \
+#define S2G_GPA(N)                                                                                  \
+  case N:                                                                                           \
+    if (t_precision == 1)                                                                           \
+      k_gamma_px_anal_df<N><<<gamma_px_grid(total, (const void *)k_gamma_px_anal_df<N>), 256, 0, st>>>( \
+          in, in_ms, F, ns, ng, npx, nb, real, c);                                                  \
+    else                                                                                            \
+      k_gamma_px_anal<N><<<gamma_px_grid(total, (const void *)k_gamma_px_anal<N>), 256, 0, st>>>(       \
+          in, in_ms, F, ns, ng, npx, nb, real, c);                                                  \
     break;
     S2G_GPA(1) S2G_GPA(2) S2G_GPA(3) S2G_GPA(4) S2G_GPA(5) S2G_GPA(6) S2G_GPA(7) S2G_GPA(8)
     S2G_GPA(9) S2G_GPA(10) S2G_GPA(11) S2G_GPA(12) S2G_GPA(13) S2G_GPA(14) S2G_GPA(15) S2G_GPA(16)
