@@ -743,6 +743,7 @@ def main():
                       f"({nb} maps per call, pinned host buffers)",
                "max_rel_err_round_trip": e2e_rt,
                "step_ms": [round(x, 1) for x in step_ms],
+               "median_step_value": whole_job_rate(nb, world, statistics.median(step_ms) / 1e3) if step_ms else None,
                "dropin_one_map_per_call": {"value": whole_job_rate(nb, world, single_s), "unit": "maps/s",
                                            "api": "s2let_analysis_px2wav_real + s2let_synthesis_wav2px_real"}}
 
