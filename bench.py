@@ -680,9 +680,10 @@ def main():
                                  "work": "double-float FP32 instructions (model)"}
             roof["binding_unit"] = {
                 "unit": "FP32 instruction issue", "frac": ti / peak_ti,
-                "note": "the ring DFTs are issue-bound on the FP32 pipe (ncu: FMA pipe 60 %, ALU 18-21 %, "
-                        "stall 'not selected' on top; DRAM 4 %), so the HBM fraction above is not their "
-                        "limit: profiles/ring_dft_df_L1024_N4_batch8.md"}
+                "note": "the ring DFTs are bound by FP32 instruction issue and the latency of their "
+                        "twiddle loads (ncu, P = 4096: FMA pipe 52 %, ALU 21 %, LSU 11 %, issue active 69 %, "
+                        "stalls 'not selected' then 'long scoreboard'; DRAM 5 %), so the HBM fraction above is "
+                        "not their limit: profiles/ring_dft_df_L1024_N4_batch8.md"}
     km = kernels["tensor_contraction"]
     if km["launches"] and km["ms"]:
         g = km["bytes"] / (km["ms"] * 1e-3) / 1e9

@@ -100,4 +100,44 @@ S2G_HD double widen_scaled(float x, int k) {
 // (hi + lo) 2^k as a double: one FP64 add
 S2G_HD double join_scaled(float hi, float lo, int k) { return widen_scaled(hi, k) + widen_scaled(lo, k); }
 
+// FP32 operations rounded to nearest: explicit intrinsics on the device (no
+// contraction), IEEE single precision on the host (built with
+// -ffp-contract=off)
+#ifdef __CUDA_ARCH__
+#define S2G_FADD(a, b) __fadd_rn((a), (b))
+#define S2G_FSUB(a, b) __fsub_rn((a), (b))
+#define S2G_FMUL(a, b) __fmul_rn((a), (b))
+#else
+#define S2G_FADD(a, b) ((a) + (b))
+#define S2G_FSUB(a, b) ((a) - (b))
+#define S2G_FMUL(a, b) ((a) * (b))
+#endif
+
+// Balanced base-128 digits of v 2^-e (|v| < 2^e) by FP32 arithmetic:
+// v 2^-e ~ sum_{j<nd} d_j 2^(-6-7j) with integer |d_j| <= 64.  x = v 2^-e as a
+// double-float (split_scaled), then per digit d = x rounded to an integer
+// (adding and subtracting 1.5 * 2^23 rounds any |x| < 2^22) and x = (x - d)
+// 128, kept exact in double-float (fast two-sum: the difference is either 0
+// or at least the low word).  The remainder after nd = 7 digits is below
+// 2^-49.  Each d is an integer-valued float of at most 7 significant bits, so
+// its bf16 bit pattern is the float's top half, returned in the low 16 bits
+// of out[j].
+template <int nd>
+S2G_HD void split_digits_fp32(double v, int e, uint32_t *out) {
+  const float kRound = 12582912.0f;  // 1.5 * 2^23
+  float h, l;
+  split_scaled(v, e, h, l);
+  h = S2G_FMUL(h, 64.0f);
+  l = S2G_FMUL(l, 64.0f);
+  for (int j = 0; j < nd; ++j) {
+    const float r = S2G_FSUB(S2G_FADD(h, kRound), kRound);
+    out[j] = bits_of(r) >> 16;
+    const float sd = S2G_FSUB(h, r);  // exact
+    const float t = S2G_FADD(sd, l);
+    l = S2G_FSUB(l, S2G_FSUB(t, sd));
+    h = S2G_FMUL(t, 128.0f);
+    l = S2G_FMUL(l, 128.0f);
+  }
+}
+
 }  // namespace s2g

@@ -1098,9 +1098,11 @@ void launch_ring(KF kernel, const RingArgs &a, int nblk, int P, cudaStream_t st,
 }
 
 // Work model of one Bluestein transform of padded length P (for the timing
-// report): the split path counts double-float FP32 instructions (41 per
-// element per radix-2 stage and FFT, a complex multiply of 38 for the kernel
-// spectrum and each chirp); the FP64 path counts 5 P log2 P flop per FFT.
+// report): the split path counts double-float FP32 instructions (32 per
+// element per radix-2 stage and FFT with unnormalised adds of 8 and complex
+// multiplies of 32 instructions, less the pruned first and last passes; 32
+// for the kernel-spectrum multiply and 64 K / P for the two chirps); the FP64
+// path counts 5 P log2 P flop per FFT.
 double ring_work(const RingArgs &a, int nblk) {
   const double P = a.P, lg = a.logP;
   if (t_precision == 1) return (double)nblk * P * (64.0 * lg - 56.0 + 64.0 * a.K / P);

@@ -136,33 +136,6 @@ __device__ __forceinline__ long long fixed48(double v, int e) {
   return (u >> 63) ? -q : q;
 }
 
-// The same balanced digits by FP32 arithmetic (the per-call coefficient
-// slicing, where the integer version keeps the ALU pipe busiest): v 2^-e as a
-// double-float x = hi + lo (|x| < 1, from the significand bits, dfconv.h), then
-// per digit d = x rounded to an integer (adding and subtracting 1.5 * 2^23
-// rounds any |x| < 2^22), x = (x - d) 128 kept exact in double-float.  |d| <=
-// 64 for every digit; the remainder after the last is below 2^-49.  Each digit
-// is an integer-valued float of at most 7 significant bits, so its bf16 bit
-// pattern is the float's top half: slice j's pattern goes to the low 16 bits of
-// out[j].
-__device__ __forceinline__ void df_digits(double v, int e, uint32_t *out) {
-  constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
-  float h, l;
-  split_scaled(v, e, h, l);
-  h = __fmul_rn(h, 64.0f);
-  l = __fmul_rn(l, 64.0f);
-#pragma unroll
-  for (int j = 0; j < kS; ++j) {
-    const float r = __fsub_rn(__fadd_rn(h, kRound), kRound);
-    out[j] = __float_as_uint(r) >> 16;
-    const float sd = __fsub_rn(h, r);  // exact
-    const float t = __fadd_rn(sd, l);  // fast two-sum: |sd| >= |l| or sd = 0
-    l = __fsub_rn(l, __fsub_rn(t, sd));
-    h = __fmul_rn(t, 128.0f);
-    l = __fmul_rn(l, 128.0f);
-  }
-}
-
 // digits of v 2^-e as bf16 bit patterns
 __device__ __forceinline__ void split_digits(double v, int e, uint16_t *out) {
   int d[kS];
@@ -409,7 +382,7 @@ __global__ void __launch_bounds__(kSliceThreads, 3) k_slice_x(XArgs a) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
           uint32_t d[kS];
-          df_digits(col[2 * sv_idx(kc * kPK + h * 8 + q) + ri], e, d);
+          split_digits_fp32<kS>(col[2 * sv_idx(kc * kPK + h * 8 + q) + ri], e, d);  // dfconv.h
 #pragma unroll
           for (int j = 0; j < kS; ++j) {
             if (q & 1)

@@ -68,3 +68,58 @@ def test_dfconv_round_trip(tmp_path):
     # floor being where the low word leaves the float normal range
     assert float(ws) <= 1.0 and float(wj) <= 1.0
     assert int(flushed_wrong) == 0 and int(bad_norm) == 0
+
+
+DIGITS = r"""
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include "dfconv.h"
+using namespace s2g;
+int main() {
+  std::mt19937_64 g(11);
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  std::uniform_int_distribution<int> ex(-200, 200);
+  double worst = 0.0;
+  long big = 0, inexact = 0;
+  for (int it = 0; it < 2000000; ++it) {
+    double v = std::ldexp(u(g), ex(g));
+    if (it % 101 == 0) v = 0.0;
+    const int emax = exp_field(v) + (it % 7 == 0 ? it % 50 : 0);  // column maximum at or above v
+    const int e = block_scale(emax);
+    uint32_t d[7];
+    split_digits_fp32<7>(v, e, d);
+    long double acc = 0.0L;
+    for (int j = 0; j < 7; ++j) {
+      const uint32_t b = d[j] << 16;
+      float f;
+      std::memcpy(&f, &b, 4);
+      if (std::fabs(f) > 64.0f) ++big;
+      if (f != std::nearbyint(f)) ++inexact;
+      acc += (long double)f * std::pow(2.0L, -6 - 7 * j);
+    }
+    const double err = (double)std::fabs(acc - std::ldexp((long double)v, -e));
+    if (err > worst) worst = err;
+  }
+  std::printf("%.6e %ld %ld\n", worst, big, inexact);
+  return 0;
+}
+"""
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_fp32_digit_split(tmp_path):
+    """split_digits_fp32 (the coefficient slicing of the tensor-core
+    contraction): 7 balanced base-128 digits, each an integer of magnitude
+    <= 64 exactly held by its bf16 pattern, reconstructing v 2^-e to 2^-47."""
+    src = tmp_path / "d.cpp"
+    exe = tmp_path / "d"
+    src.write_text(DIGITS)
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", f"-I{CSRC}", str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.returncode
+    worst, big, inexact = out.stdout.split()
+    assert int(big) == 0 and int(inexact) == 0
+    assert float(worst) <= 2.0 ** -47
