@@ -2,8 +2,9 @@
 drop-in host layout.  Each map must equal the one-map drop-in call (FP64
 path, 1e-12): f_wav crosses the bus in pieces (one scale of a group of maps)
 on a second stream while the transforms run, device batches hold up to 32
-maps (40 maps make two), and the unused tail of f_wav (a scale with N_j < N)
-stays as the caller wrote it."""
+maps (40 maps make two), full-resolution (upsampled) layouts and single maps
+included, and the unused tail of f_wav (a scale with N_j < N) stays as the
+caller wrote it."""
 import ctypes as C
 
 import numpy as np
@@ -16,12 +17,13 @@ TOL = 1e-12
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L,N,spin,real,nb,ss", [(32, 4, 0, True, 3, 0), (24, 5, 2, False, 20, 0),
-                                                 (16, 8, 0, True, 17, 0), (16, 3, 0, True, 40, 0),
-                                                 (20, 4, 0, True, 6, 1), (18, 3, 1, False, 5, 1)])
-def test_host_batch_equals_single_calls(gpu, L, N, spin, real, nb, ss):
+@pytest.mark.parametrize("L,N,spin,real,nb,ss,up", [(32, 4, 0, True, 3, 0, 0), (24, 5, 2, False, 20, 0, 0),
+                                                    (16, 8, 0, True, 17, 0, 0), (16, 3, 0, True, 40, 0, 0),
+                                                    (20, 4, 0, True, 6, 1, 0), (18, 3, 1, False, 5, 1, 0),
+                                                    (16, 3, 0, True, 9, 0, 1), (12, 2, 2, False, 1, 0, 1)])
+def test_host_batch_equals_single_calls(gpu, L, N, spin, real, nb, ss, up):
     lib = gpu.lib
-    p = make_parameters(L, 2.0, 1, N, 0 if real else spin, 0, sampling_scheme=SAMPLING_MW_SS if ss else 0)
+    p = make_parameters(L, 2.0, 1, N, 0 if real else spin, up, sampling_scheme=SAMPLING_MW_SS if ss else 0)
     s = gpu.sizes(p)
     rng = np.random.default_rng(L + nb)
     dt = np.float64 if real else np.complex128
