@@ -316,8 +316,12 @@ __global__ void __launch_bounds__(kSliceThreads, 3) k_slice_x(XArgs a) {
             x.y = -x.y;
             if (am & 1) x = make_double2(-x.x, -x.y);
           }
-          const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
-          x = make_double2(x.x * wt.x - x.y * wt.y, x.x * wt.y + x.y * wt.x);
+          if (P.w) {
+            const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
+            x = make_double2(x.x * wt.x - x.y * wt.y, x.x * wt.y + x.y * wt.x);
+          } else {
+            x = make_double2(x.x * P.wscale, x.y * P.wscale);
+          }
           col[sv_idx(l - l0)] = x;
           er = max(er, exp_field(x.x));
           ei = max(ei, exp_field(x.y));
@@ -774,10 +778,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
           } else {
             const int lst = ti.l0 > P.lmin ? ti.l0 : P.lmin;
             if (l >= lst && l < a.bl) {
-              const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
               const double yr = y[2 * bb], yi = y[2 * bb + 1];
-              P.dst[(int64_t)b * P.ds + (int64_t)l * l + l + ti.m] =
-                  make_double2(yr * wt.x - yi * wt.y, yr * wt.y + yi * wt.x);
+              double2 o;
+              if (P.w) {
+                const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
+                o = make_double2(yr * wt.x - yi * wt.y, yr * wt.y + yi * wt.x);
+              } else {  // a real scale factor (the directional synthesis): two FP64 multiplies
+                o = make_double2(yr * P.wscale, yi * P.wscale);
+              }
+              P.dst[(int64_t)b * P.ds + (int64_t)l * l + l + ti.m] = o;
             }
           }
         }
