@@ -570,7 +570,13 @@ __device__ __forceinline__ void load_classes8(uint32_t taddr, int ncols_per_clas
 // S = sum_c acc_c 2^(-7c) by Horner in double-float on the FP32 pipe (the class
 // values and 2^-7 scalings are exact floats), then one widening to FP64 with
 // the power of two 2^(ea + eX - 12) applied while widening (dfconv.h).
-__device__ __forceinline__ void combine8(float (*acc)[8], int ea, const int *eX, double sign, double *y) {
+__device__ __forceinline__ int ex_at(int4 e0, int4 e1, int col) {
+  const int4 e = col < 4 ? e0 : e1;
+  const int c = col & 3;
+  return c == 0 ? e.x : (c == 1 ? e.y : (c == 2 ? e.z : e.w));
+}
+// eX of the 8 columns in e0 (columns 0-3) and e1 (4-7)
+__device__ __forceinline__ void combine8(float (*acc)[8], int ea, int4 e0, int4 e1, double sign, double *y) {
 #pragma unroll
   for (int col = 0; col < 8; ++col) {
     float hi = acc[kS - 1][col], lo = 0.0f;
@@ -589,7 +595,7 @@ __device__ __forceinline__ void combine8(float (*acc)[8], int ea, const int *eX,
       hi = -hi;
       lo = -lo;
     }
-    y[col] = join_scaled(hi, lo, ea + eX[col] - 2 * kB0);
+    y[col] = join_scaled(hi, lo, ea + ex_at(e0, e1, col) - 2 * kB0);
   }
 }
 
@@ -734,16 +740,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
     for (int t = blockIdx.x; t < a.ntiles * a.ngroups; t += gridDim.x, ++ti_n) {
       const TileInfo ti = tile_info(a, t);
       const int ab = ti_n % NBUF;
+      const bool live = ti.kc0 < ti.nkc;
+      // the row and column exponents do not depend on the accumulator: read
+      // them before waiting, so that their latency is not spent holding TMEM
+      int ea = 0;
+      int4 ex4[4];
+      if (pi < NC / 16 && live) {
+        ea = (int)a.eA[a.e_off[ti.mi] + ti.rt * kPM + rr];
+        const int4 *ep = (const int4 *)(a.eX + ti.g * a.eXg + ti.pm * NC + pi * 16);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) ex4[q] = ep[q];
+      }
       // warp-uniform outcome: tcgen05.ld below is .sync.aligned
       if (!__all_sync(0xffffffffu, bar_wait(&tfull[ab], (ti_n / NBUF) & 1, abort_flag, a.err))) break;
       tc_fence_after();
-      const bool live = ti.kc0 < ti.nkc;
       if (pi >= NC / 16 || !live) {  // no columns here, or nothing accumulated: release at once
         tc_fence_before();
         bar_arrive(&tempty[ab]);
         if (pi >= NC / 16) continue;
       }
-      const int ea = live ? (int)a.eA[a.e_off[ti.mi] + ti.rt * kPM + rr] : 0;
       const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * ACC);
       const int t_row = ti.rt * kPM + rr;
       const int l = ti.l0 + ti.rt * kPM + rr;
@@ -758,7 +773,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
             tc_fence_before();
             bar_arrive(&tempty[ab]);
           }
-          combine8(acc, ea, a.eX + ti.g * a.eXg + ti.pm * NC + c0, ti.sign, y);
+          combine8(acc, ea, hh ? ex4[2] : ex4[0], hh ? ex4[3] : ex4[1], ti.sign, y);
         } else {
 #pragma unroll
           for (int col = 0; col < 8; ++col) y[col] = 0.0;
