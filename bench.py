@@ -735,7 +735,12 @@ def main():
                     step_ms.append(1e3 * (time.perf_counter() - t1))
             return max_over_ranks((time.perf_counter() - t0) / steps, dist, dev)
 
+        # clocks sampled over the e2e steps as over the device-timed region
+        # (GPU-idle gaps between copy-bound phases make P-state behaviour matter here)
+        e2e_clocks = ClockSampler(local)
+        e2e_clocks.start()
         e2e_s = host_rate(e2e_batch_step, a.steps, record=True, warmup=max(1, a.warmup))
+        e2e_clk = e2e_clocks.stop()
         e2e_rt = float((frh - fh).abs().max() / fh.abs().max())
         single_s = host_rate(e2e_single_step, max(1, min(a.steps, 2)))
         e2e = {"value": whole_job_rate(nb, world, e2e_s), "unit": "maps/s",
@@ -744,6 +749,7 @@ def main():
                       f"({nb} maps per call, pinned host buffers)",
                "max_rel_err_round_trip": e2e_rt,
                "step_ms": [round(x, 1) for x in step_ms],
+               "clocks": e2e_clk,
                "median_step_value": whole_job_rate(nb, world, statistics.median(step_ms) / 1e3) if step_ms else None,
                "dropin_one_map_per_call": {"value": whole_job_rate(nb, world, single_s), "unit": "maps/s",
                                            "api": "s2let_analysis_px2wav_real + s2let_synthesis_wav2px_real"}}
