@@ -10,6 +10,7 @@
 //  k_gamma_*   DFT over the 2N-1 gamma samples of the rotation group.
 //  k_merge     harmonic tiling merge (lmn -> lm) fused over scales/directions.
 #include <map>
+#include <mutex>
 
 #include "common.h"
 #include "dfconv.h"
@@ -1339,20 +1340,26 @@ void gamma_analysis(const double2 *spec, double2 *G, const int *ns, int nn, int 
 // blocks for a grid-stride pixel gamma kernel: as many as are resident at
 // once (one wave), fewer for small inputs
 static unsigned gamma_px_grid(int64_t total, const void *kernel) {
-  static int nsm = 0;
-  static std::map<const void *, int> per_sm;
-  if (!nsm) {
-    int dev = 0;
+  static const int nsm = [] {
+    int dev = 0, n = 0;
     S2G_CUDA(cudaGetDevice(&dev));
-    S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    S2G_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    return n;
+  }();
+  static std::mutex mu;
+  static std::map<const void *, int> per_sm;
+  int blocks;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = per_sm.find(kernel);
+    if (it == per_sm.end()) {
+      int b = 0;
+      S2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, 256, 0));
+      it = per_sm.emplace(kernel, b > 0 ? b : 1).first;
+    }
+    blocks = it->second;
   }
-  auto it = per_sm.find(kernel);
-  if (it == per_sm.end()) {
-    int b = 0;
-    S2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, 256, 0));
-    it = per_sm.emplace(kernel, b > 0 ? b : 1).first;
-  }
-  const int64_t want = ceil_div(total, 256), cap = (int64_t)nsm * it->second;
+  const int64_t want = ceil_div(total, 256), cap = (int64_t)nsm * blocks;
   return (unsigned)(want < cap ? want : cap);
 }
 

@@ -944,12 +944,12 @@ const TileList &tile_list(SlicedTable &s, int n, int mlo, int mhi, int lmin, cud
 }
 
 int num_sms() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
+  static const int n = [] {
+    int dev = 0, v = 0;
     S2G_CUDA(cudaGetDevice(&dev));
-    S2G_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
-  }
+    S2G_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    return v;
+  }();
   return n;
 }
 
@@ -972,12 +972,12 @@ struct Problem {
 
 template <int NC>
 void run_mixed(const Problem &p, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [] {  // once per instantiation (thread-safe static initialisation)
     S2G_CUDA(cudaFuncSetAttribute(k_contract_mx<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)Cfg<NC>::kSmemBytes));
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   int lmin = p.part[0].lmin;
   for (int i = 1; i < p.nparts; ++i) lmin = std::min(lmin, p.part[i].lmin);
   SlicedTable *s;
@@ -997,11 +997,11 @@ void run_mixed(const Problem &p, cudaStream_t st) {
   constexpr int kSliceSmemMax = 232448 - 1024;  // the opt-in maximum less the static arrays
   S2G_REQUIRE(slice_smem <= (size_t)kSliceSmemMax, ERR_INVALID,
               "coefficient slicing: K too large for shared-memory staging");
-  static bool attr_x = false;
-  if (!attr_x) {
+  static const bool attr_x = [] {
     S2G_CUDA(cudaFuncSetAttribute(k_slice_x<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSliceSmemMax));
-    attr_x = true;
-  }
+    return true;
+  }();
+  (void)attr_x;
   const int ngroups = (p.nb + mpp - 1) / mpp;
   // map groups run kGroupsPerLaunch at a time in one launch (their tiles
   // interleaved, the table read once from HBM and again from L2)

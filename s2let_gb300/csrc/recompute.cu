@@ -461,11 +461,11 @@ void launch_l2t(const RcArgs &a, int nm, cudaStream_t st) {
 template <int NBT>
 void launch_t2l(const RcArgs &a, int nm, int maxseg, cudaStream_t st) {
   const size_t smem = rc_t2l_smem<NBT>();
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [smem] {  // once per instantiation (thread-safe static initialisation)
     S2G_CUDA(cudaFuncSetAttribute(k_rc_t2l<NBT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   dim3 grid(nm, maxseg, ceil_div(a.nb, NBT));
   k_rc_t2l<NBT><<<grid, kRcT, smem, st>>>(a);
   S2G_LAUNCHED();
