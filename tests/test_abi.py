@@ -5,6 +5,7 @@ s2let_parameters_t as the reference does, computes the host-side helpers
 its status API instead of exiting."""
 import ctypes as C
 import os
+import shutil
 import re
 import subprocess
 import tempfile
@@ -146,3 +147,45 @@ def test_precision_mode_switch(lib):
     assert lib.s2let_gpu_get_precision() == 1
     assert lib.s2let_gpu_set_precision(5) == 1
     assert lib.s2let_gpu_set_precision(0) == 0
+
+
+RELINK = r"""
+/* A caller written against the reference's API (s2let.h), relinked against
+   libs2let_gpu: allocation helpers, sizes, the tiling, and a transform whose
+   status it reads back. */
+#include <stdio.h>
+#include <stdlib.h>
+#include <s2let_gpu.h>
+int main(void) {
+  s2let_parameters_t p = {0};
+  p.L = 16; p.B = 2.0; p.J_min = 1; p.N = 3; p.reality = 1;
+  p.sampling_scheme = S2LET_SAMPLING_MW;
+  double *f, *f_wav, *f_scal;
+  s2let_allocate_mw_real(&f, p.L);
+  s2let_allocate_f_wav_real(&f_wav, &f_scal, &p);
+  for (int i = 0; i < p.L * (2 * p.L - 1); ++i) f[i] = 0.01 * i;
+  s2let_analysis_px2wav_real(f_wav, f_scal, f, &p);
+  printf("%d %d %d %d\n", s2let_n_px(&p), s2let_j_max(&p), s2let_bandlimit(2, &p), s2let_gpu_last_error());
+  free(f); free(f_wav); free(f_scal);
+  return 0;
+}
+"""
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="needs gcc")
+def test_reference_style_c_caller_relinks(lib, tmp_path):
+    """The drop-in claim at the C level: a program using only reference
+    names builds against include/s2let_gpu.h and links -ls2let_gpu; sizes and
+    band-limits come out as the reference computes them, and the transform's
+    status is 0 with a GPU, S2LET_GPU_ERR_NO_DEVICE without."""
+    import s2let_gb300
+
+    src, exe = tmp_path / "caller.c", tmp_path / "caller"
+    src.write_text(RELINK)
+    libdir = os.path.dirname(s2let_gb300.LIB_PATH)
+    subprocess.run(["gcc", "-std=c99", f"-I{ROOT}/include", str(src), f"-L{libdir}", "-ls2let_gpu",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    n_px, j_max, bl2, status = map(int, out)
+    assert n_px == 16 * 31 and j_max == 4 and bl2 == 8
+    assert status == (0 if _has_gpu() else 5)
