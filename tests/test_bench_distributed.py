@@ -55,3 +55,21 @@ def test_two_replicas_take_the_slowest_time():
 def test_single_process_needs_no_group():
     assert bench.max_over_ranks(3.5) == 3.5
     assert bench.whole_job_rate(16, 1, 0.5) == 32.0
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` (the CPU reference path, no GPU) prints one
+    JSON line with the metric, the reference marker, a cpu_baseline and an e2e
+    entry without copies (a small band-limit keeps it to seconds)."""
+    import json
+    import subprocess
+
+    out = subprocess.run([sys.executable, os.path.join(HERE, "..", "bench.py"), "--impl", "reference",
+                          "--L", "64", "--steps", "1", "--warmup", "1"],
+                         capture_output=True, text=True, timeout=300, check=True).stdout.strip().splitlines()
+    d = json.loads(out[-1])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == "maps/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 1 and d["warmup"] == 1
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert d["config"]["L"] == 64
