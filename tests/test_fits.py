@@ -156,3 +156,20 @@ def test_reads_the_reference_data_file(lib):
     assert h["TFORM1"] == "1E"
     np.testing.assert_array_equal(f, column(raw, h, off, 1))
     assert np.abs(f).max() > 0
+
+
+def test_header_readers_on_the_reference_data_files(lib):
+    """NSIDE of the reference's HEALPix files and L of its MW files; a missing
+    keyword reads as -1 (src/c/s2let_fits.c:17-85)."""
+    from oracle.oracle import REF_SRC
+
+    data = os.path.join(REF_SRC, "data")
+    files = {"somecmbsimu_hpx_128.fits": (128, -1), "wmap_mcmc_base_k_synch_stk_q_9yr_v5.fits": (64, -1),
+             "earth_tomo_mw_128.fits": (-1, 128), "earth_tomo_mw_128_rot.fits": (-1, 128)}
+    present = [f for f in files if os.path.exists(os.path.join(data, f))]
+    if not present:
+        pytest.skip("reference data not present")
+    for f in present:
+        path = os.path.join(data, f).encode()
+        assert (lib.s2let_fits_hpx_read_nside(path), lib.s2let_fits_mw_read_bandlimit(path)) == files[f], f
+        assert lib.s2let_gpu_last_error() == 0
