@@ -52,9 +52,18 @@ extern "C" {
 /* Types (layout identical to include/s2let/s2let_types.h:18-137)           */
 /* ------------------------------------------------------------------------ */
 
-#ifndef S2LET_GPU_NO_SSHT_TYPES
 /* Wigner recursion selector of SSHT; accepted and ignored (results are the
- * same linear map either way).  int-sized enum as in SSHT. */
+ * same linear map either way).  Where SSHT's own header is installed it
+ * provides the type, as in the reference's headers; otherwise an int-sized
+ * enum of the same values is declared here.  Define S2LET_GPU_NO_SSHT_TYPES
+ * to supply the type yourself. */
+#if !defined(S2LET_GPU_NO_SSHT_TYPES) && defined(__has_include)
+#if __has_include(<ssht/ssht.h>)
+#include <ssht/ssht.h>
+#define S2LET_GPU_NO_SSHT_TYPES
+#endif
+#endif
+#ifndef S2LET_GPU_NO_SSHT_TYPES
 typedef enum { SSHT_DL_RISBO = 0, SSHT_DL_TRAPANI = 1 } ssht_dl_method_t;
 #endif
 
@@ -520,6 +529,18 @@ int s2let_gpu_synthesis_adjoint_px2wav_batch(void *f_wav, void *f_scal, const vo
  * the last call (the affected outputs are invalid).  0 when all went well. */
 int s2let_gpu_device_fault(void);
 
+/* One device per process.  Plans, Wigner tables, streams and kernel
+ * attributes are cached for the device that was current at the first compute
+ * call of the process; every later call made while another device is current
+ * fails with S2LET_GPU_ERR_UNSUPPORTED (use one process per GPU, as the
+ * multi-GPU benchmark does).  s2let_gpu_bind_device(d) names that device ahead
+ * of the first call: it returns S2LET_GPU_OK if the library is unbound or
+ * already serves d, S2LET_GPU_ERR_UNSUPPORTED if it serves another device,
+ * S2LET_GPU_ERR_INVALID for d < 0.  s2let_gpu_bound_device() returns the
+ * device served, or -1 before the first call. */
+int s2let_gpu_bind_device(int device);
+int s2let_gpu_bound_device(void);
+
 /* Number of this library's kernel launches since load (instrumentation). */
 uint64_t s2let_gpu_launch_count(void);
 
@@ -530,6 +551,15 @@ uint64_t s2let_gpu_launch_count(void);
  * merge, 4 split-precision tensor-core contraction, 5 other). */
 int s2let_gpu_timing_enable(int on);
 int s2let_gpu_timing_report(double *out, int ncat);
+
+/* Optional trace of the host <-> device copies made by the host-pointer batch
+ * entry points, with CUDA events on the copying streams.  enable(1) clears
+ * previous records and starts tracing, enable(0) stops.  report fills
+ * out[d*4 + {0,1,2,3}] = {copies, bytes, busy milliseconds (sum of the copies'
+ * own durations), span milliseconds (first start to last end)} for direction
+ * d = 0 (host to device) and d = 1 (device to host). */
+int s2let_gpu_copy_trace_enable(int on);
+int s2let_gpu_copy_trace_report(double *out);
 
 #ifdef __cplusplus
 }

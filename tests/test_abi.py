@@ -152,12 +152,14 @@ def test_precision_mode_switch(lib):
 RELINK = r"""
 /* A caller written against the reference's API (s2let.h), relinked against
    libs2let_gpu: allocation helpers, sizes, the tiling, and a transform whose
-   status it reads back. */
+   status it reads back.  S2LET_HEADER is <s2let.h> or <s2let/s2let.h>. */
+#include <string.h>
 #include <stdio.h>
 #include <stdlib.h>
-#include <s2let_gpu.h>
+#include S2LET_HEADER
 int main(void) {
-  s2let_parameters_t p = {0};
+  s2let_parameters_t p;
+  memset(&p, 0, sizeof p);
   p.L = 16; p.B = 2.0; p.J_min = 1; p.N = 3; p.reality = 1;
   p.sampling_scheme = S2LET_SAMPLING_MW;
   double *f, *f_wav, *f_scal;
@@ -175,17 +177,47 @@ int main(void) {
 @pytest.mark.skipif(shutil.which("gcc") is None, reason="needs gcc")
 def test_reference_style_c_caller_relinks(lib, tmp_path):
     """The drop-in claim at the C level: a program using only reference
-    names builds against include/s2let_gpu.h and links -ls2let_gpu; sizes and
+    names and the reference's header (s2let.h, forwarding to
+    include/s2let_gpu.h) builds unchanged and links -ls2let_gpu; sizes and
     band-limits come out as the reference computes them, and the transform's
     status is 0 with a GPU, S2LET_GPU_ERR_NO_DEVICE without."""
     import s2let_gb300
 
-    src, exe = tmp_path / "caller.c", tmp_path / "caller"
-    src.write_text(RELINK)
     libdir = os.path.dirname(s2let_gb300.LIB_PATH)
-    subprocess.run(["gcc", "-std=c99", f"-I{ROOT}/include", str(src), f"-L{libdir}", "-ls2let_gpu",
-                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
-    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
-    n_px, j_max, bl2, status = map(int, out)
-    assert n_px == 16 * 31 and j_max == 4 and bl2 == 8
-    assert status == (0 if _has_gpu() else 5)
+    # the reference's own include forms: <s2let.h> with -I.../include/s2let, and
+    # <s2let/s2let.h> with -I.../include; as C99 and as C++ (std::complex)
+    builds = [("gcc", "c", "-std=c99", "<s2let.h>", f"-I{ROOT}/include/s2let"),
+              ("gcc", "c", "-std=c99", "<s2let/s2let.h>", f"-I{ROOT}/include"),
+              ("g++", "cpp", "-std=c++17", "<s2let.h>", f"-I{ROOT}/include/s2let")]
+    for k, (cc, ext, std, header, inc) in enumerate(builds):
+        if shutil.which(cc) is None:
+            continue
+        src, exe = tmp_path / f"caller{k}.{ext}", tmp_path / f"caller{k}"
+        src.write_text(RELINK.replace("S2LET_HEADER", header))
+        subprocess.run([cc, std, "-Wall", "-Werror", inc, str(src), f"-L{libdir}", "-ls2let_gpu",
+                        f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+        out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+        n_px, j_max, bl2, status = map(int, out)
+        assert n_px == 16 * 31 and j_max == 4 and bl2 == 8
+        assert status == (0 if _has_gpu() else 5)
+
+
+def test_device_binding_guard():
+    """One device per process: the first device (named explicitly here, as no
+    GPU is present) is kept; naming another is refused with
+    S2LET_GPU_ERR_UNSUPPORTED and leaves the binding unchanged.  Runs in a
+    fresh interpreter so that no earlier call has bound the library."""
+    code = r'''
+import s2let_gb300
+lib = s2let_gb300.load()
+out = [lib.s2let_gpu_bound_device(), lib.s2let_gpu_bind_device(-1), lib.s2let_gpu_bound_device(),
+       lib.s2let_gpu_bind_device(0), lib.s2let_gpu_bound_device(), lib.s2let_gpu_bind_device(0),
+       lib.s2let_gpu_bind_device(1), lib.s2let_gpu_last_error(), lib.s2let_gpu_bound_device()]
+print(" ".join(map(str, out)))
+'''
+    r = subprocess.run([os.sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    got = [int(x) for x in r.stdout.split()]
+    #      unbound, bind(-1) invalid, still unbound, bind(0), bound 0, again ok, bind(1) refused, status, still 0
+    assert got == [-1, 1, -1, 0, 0, 0, 2, 2, 0]
+    assert "already serves CUDA device 0" in r.stderr
