@@ -158,84 +158,118 @@ def axisym_wav_l(B, L, J_min):
 
 
 def verify_tiling(L, scal_l, wav_l, scal_bandlimit, wav_bandlimits):
-    """Band-limits and the admissibility sum of a manual tiling (prints like the reference)."""
-    scal_l, wav_l = _f64(scal_l), _f64(wav_l)
-    wav_bandlimits = np.asarray(wav_bandlimits)
-    J = wav_bandlimits.size - 1
+    """Checks a manual axisymmetric tiling before it is used with the *_manual
+    transforms (pys2let's verify_tiling, src/pys2let/pys2let.pyx:442-478).
 
-    def measured(c):
-        return int(np.where(c == 1)[0][0]) + 1
-
-    total = scal_l ** 2
-    cs = np.cumsum(scal_l)
-    cs = cs / cs[-1]
-    if cs[int(scal_bandlimit - 1)] < 1:
-        print('Wrong band-limit given for scaling function (', scal_bandlimit, ')')
-        print('Measured band-limit is ', measured(cs))
-        return False
-    print('Measured / given band-limits for scaling fct are', measured(cs), '/', scal_bandlimit)
-    for j in range(J + 1):
-        w = wav_l[j * L:(j + 1) * L]
-        total = total + w ** 2
-        cs = np.cumsum(w)
-        cs = cs / cs[-1]
-        if cs[int(wav_bandlimits[j] - 1)] < 1:
-            print('Wrong band-limit given for wavelet', j + 1, 'on', J + 1, '(', wav_bandlimits[j], ')')
-            print('Measured band-limit is ', measured(cs))
-            print('Wavelet:', w)
+    scal_l (L values) and wav_l ((J+1)*L values, scale-major) are harmonic
+    profiles; scal_bandlimit and wav_bandlimits[j] are the band-limits claimed
+    for them.  A profile is band-limited at b when its running sum has reached
+    its total at l = b - 1 (nothing beyond contributes).  The tiling is
+    admissible when scal_l^2 + sum_j wav_l[j]^2 = 1 at every l (np.allclose).
+    Prints the measured and the given band-limit of every profile (or the first
+    one that is wrong, with the profile) and, when the sum is off, the sum;
+    returns True when every band-limit holds and the sum is 1.
+    """
+    profiles = [("scaling function", np.asarray(scal_l, dtype=np.float64), scal_bandlimit)]
+    wav = np.asarray(wav_l, dtype=np.float64).reshape(-1)
+    bls = np.asarray(wav_bandlimits)
+    for j in range(bls.size):
+        profiles.append((f"wavelet {j}", wav[j * L:(j + 1) * L], bls[j]))
+    square_sum = np.zeros(L)
+    for name, prof, given in profiles:
+        square_sum += prof ** 2
+        # running sum over l as a fraction of the total; exactly 1 once the
+        # profile has ended
+        frac = np.cumsum(prof)
+        frac = frac / frac[-1]
+        measured = int(np.flatnonzero(frac == 1)[0]) + 1
+        if frac[int(given - 1)] < 1:
+            print(f"{name}: band-limit {given} is too small, the profile reaches l = {measured - 1}")
+            if name != "scaling function":
+                print("profile:", prof)
             return False
-        print('Measured / given band-limits for wavelet', j, 'are', measured(cs), '/', wav_bandlimits[j])
-    if np.allclose(total, 1.0):
-        return True
-    print('Admissibility condition not satisfied:')
-    print(total)
-    return False
+        print(f"{name}: band-limit measured {measured}, given {given}")
+    if not np.allclose(square_sum, 1.0):
+        print("not admissible: scal_l^2 + sum_j wav_l[j]^2 differs from 1:")
+        print(square_sum)
+        return False
+    return True
 
 
 def construct_hybrid_tiling(L, J_min0, Bs, L_transitions):
-    """Axisymmetric tiling that changes its dilation factor B at the multipoles
-    L_transitions: each band [L_k, L_{k+1}) takes the wavelets of B_k, and the
-    wavelet at each seam absorbs its neighbour in quadrature so that the
-    admissibility sum stays 1.  Returns (scal_l, wav_l[L, J+1],
-    scal_bandlimit, wav_bandlimits, J, L_bounds)."""
+    """Axisymmetric tiling whose dilation factor changes with the multipole
+    (pys2let's construct_hybrid_tiling, src/pys2let/pys2let.pyx:1132-1179).
+
+    The multipoles [0, L) are cut into bands, one per factor B_k of Bs.  Band
+    k uses the axisymmetric wavelets of B_k (J_min = J_min0 for the first band,
+    0 for the others), restricted to the band's multipoles:
+
+    * band k keeps the scales j = first_k .. last_k of B_k, where first_0 =
+      J_min0, first_k = floor(log(lo_k) / log(B_k)) + 1 for k > 0 (the first
+      scale that ends above the band's start lo_k), last_k = floor(log(T_k) /
+      log(B_k)) for the transition multipole T_k = L_transitions[k] (the last
+      band keeps every scale up to j_max(B_k));
+    * the band ends where its last scale peaks: hi_k = round(B_k^last_k) (= L
+      for the last band), and the next band starts there;
+    * seams: the first scale of a band absorbs, in quadrature, the scale of
+      B_k just below it, and (except in the last band) its last scale absorbs
+      the one just above it, so that the squares still sum to 1 inside the band
+      (the absorbed profile is used only where the kept one is below 1 at the
+      band's first multipole);
+    * columns: the scales are numbered across bands; the last scale of band k
+      and the first of band k+1 share one column (they live on the two sides of
+      the seam), so there are J + 1 = 1 + sum_k (last_k - first_k) columns;
+    * band-limits: round(min(B_k^(j+1), L)) per column, the later band's where
+      a column is shared; the scaling function is that of B_0 with band-limit
+      B_0^J_min0.
+
+    Two behaviours of the reference are kept: in the first band the "scale
+    below" of the first scale is B_0's LAST wavelet (the reference indexes
+    scale -1, which wraps), which is zero there unless the first band reaches
+    that wavelet's support (with a single band it does, and the tiling is then
+    not admissible); and band-limits of non-integer powers are rounded, which
+    can leave a profile one multipole past its band-limit.
+
+    Returns (scal_l, wav_l of shape (L, J + 1), scal_bandlimit,
+    wav_bandlimits, J, band boundaries [lo_0 = 0, lo_1, ..., L]).
+    """
     Bs = np.asarray(Bs, dtype=float)
-    nb = Bs.size
-    J_mins = np.zeros(nb, dtype=int)
-    J_mins[0] = J_min0
-    Js = [pys2let_j_max(b, L, jm) for b, jm in zip(Bs, J_mins)]
-    L_bounds = np.zeros(nb + 1, dtype=np.int32)
-    jl = np.zeros(nb, dtype=np.int32)
-    jr = np.zeros(nb, dtype=np.int32)
-    J = 0
-    for k in range(nb):
-        jl[k] = J_mins[k] if k == 0 else int(np.log(L_bounds[k]) / np.log(Bs[k])) + 1
-        jr[k] = Js[k] + 1 if k == nb - 1 else int(np.log(L_transitions[k]) / np.log(Bs[k])) + 1
-        if k < nb - 1:
-            L_bounds[k + 1] = np.rint(Bs[k] ** (jr[k] - 1))
-        J += int(jr[k] - jl[k] - 1)
-    L_bounds[-1] = L
+    nband = Bs.size
+    # the per-band axisymmetric tilings: (J_min, j_max, profiles[l, j - J_min])
+    tilings = []
+    for k in range(nband):
+        jmin = J_min0 if k == 0 else 0
+        _, w = axisym_wav_l(Bs[k], L, jmin)
+        tilings.append((jmin, pys2let_j_max(Bs[k], L, jmin), w))
+    # band boundaries and the scales each band keeps
+    bounds, first, last = [0], [], []
+    for k in range(nband):
+        jmin, jmax, _ = tilings[k]
+        first.append(jmin if k == 0 else int(np.log(bounds[k]) / np.log(Bs[k])) + 1)
+        last.append(jmax if k == nband - 1 else int(np.log(L_transitions[k]) / np.log(Bs[k])))
+        bounds.append(L if k == nband - 1 else int(np.rint(Bs[k] ** last[k])))
+    J = sum(b - a for a, b in zip(first, last))
     wav = np.zeros((L, J + 1))
-    bls = np.zeros(J + 1, dtype=np.int32)
-    scal_bandlimit, scal = None, None
+    wav_bandlimits = np.zeros(J + 1, dtype=np.int32)
     col = 0
-    for k in range(nb):
-        s_l, w_l = axisym_wav_l(Bs[k], L, J_mins[k])
-        js = np.arange(J_mins[k], Js[k] + 1)
-        band = np.array([np.rint(min(x, L)) for x in Bs[k] ** (js + 1)]).astype(np.int32)
-        if k == 0:
-            scal_bandlimit = Bs[k] ** J_mins[k]
-            scal = s_l.copy()
-        lo, hi = L_bounds[k], L_bounds[k + 1]
-        for j in range(jl[k] - J_mins[k], jr[k] - J_mins[k]):
-            bls[col] = band[j]
-            wav[lo:hi, col] = w_l[lo:hi, j]
-            if j == jl[k] - J_mins[k] and w_l[lo, j] < 1.0:
-                wav[lo:hi, col] = np.sqrt(wav[lo:hi, col] ** 2 + w_l[lo:hi, j - 1] ** 2)
-            if k < nb - 1 and j == jr[k] - 1 - J_mins[k] and w_l[lo, j] < 1.0:
-                wav[lo:hi, col] = np.sqrt(wav[lo:hi, col] ** 2 + w_l[lo:hi, j + 1] ** 2)
-            if j < jr[k] - 1 - J_mins[k]:
+    for k in range(nband):
+        jmin, _, w = tilings[k]
+        lo, hi = bounds[k], bounds[k + 1]
+        for j in range(first[k], last[k] + 1):
+            c = j - jmin  # column of scale j in B_k's profiles
+            prof = w[lo:hi, c]
+            below_one = w[lo, c] < 1.0
+            if j == first[k] and below_one:
+                # c - 1 = -1 in the first band: B_0's last wavelet (see above)
+                prof = np.sqrt(prof ** 2 + w[lo:hi, c - 1] ** 2)
+            if k < nband - 1 and j == last[k] and below_one:
+                prof = np.sqrt(prof ** 2 + w[lo:hi, c + 1] ** 2)
+            wav[lo:hi, col] = prof
+            wav_bandlimits[col] = np.rint(min(Bs[k] ** (j + 1), L))
+            if j < last[k]:
                 col += 1
-    return scal, wav, scal_bandlimit, bls, J, L_bounds
+    scal_l, _ = axisym_wav_l(Bs[0], L, J_min0)
+    return scal_l, wav, Bs[0] ** J_min0, wav_bandlimits, J, np.asarray(bounds, dtype=np.int32)
 
 
 # ---- axisymmetric transforms ---------------------------------------------------

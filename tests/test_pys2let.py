@@ -64,6 +64,64 @@ def test_hybrid_tiling_is_admissible():
     assert np.allclose(scal ** 2 + np.sum(wav ** 2, axis=1), 1.0)
 
 
+def test_hybrid_tiling_rule():
+    """The hybrid tiling against the rule worked out by hand for L = 64,
+    J_min = 2, B = (2, 1.5), transition at l = 20.  Band 0 (B = 2) keeps scales
+    2..floor(log2 20) = 4 and ends at 2^4 = 16; band 1 (B = 1.5, J_min = 0)
+    starts with scale floor(log 16 / log 1.5) + 1 = 7 and keeps up to
+    j_max = 11: columns 0, 1 are B=2 scales 2, 3; column 2 is B=2 scale 4 below
+    l = 16 and B=1.5 scale 7 above; columns 3..6 are B=1.5 scales 8..11."""
+    L = 64
+    scal, wav, sbl, wbl, J, bounds = ps.construct_hybrid_tiling(L, 2, np.array([2.0, 1.5]), np.array([20]))
+    assert J == 6 and list(bounds) == [0, 16, 64] and sbl == 4.0
+    # round(min(B^(j+1), L)); the shared column takes the later band's value
+    assert list(wbl) == [8, 16, 26, 38, 58, 64, 64]
+    s2, w2 = ps.axisym_wav_l(2.0, L, 2)    # profiles[l, j - 2]
+    _, w15 = ps.axisym_wav_l(1.5, L, 0)    # profiles[l, j]
+    np.testing.assert_array_equal(scal, s2)
+    lo = slice(0, 16)
+    hi = slice(16, 64)
+    # band 0: scale 2 absorbs "scale 1", which wraps to B=2's last wavelet (zero below 16)
+    assert not w2[lo, -1].any()
+    np.testing.assert_array_equal(wav[lo, 0], np.sqrt(w2[lo, 0] ** 2 + w2[lo, -1] ** 2))
+    np.testing.assert_array_equal(wav[lo, 1], w2[lo, 1])
+    # the seam: B=2 scale 4 absorbs scale 5 below 16; B=1.5 scale 7 absorbs scale 6 above
+    np.testing.assert_array_equal(wav[lo, 2], np.sqrt(w2[lo, 2] ** 2 + w2[lo, 3] ** 2))
+    np.testing.assert_array_equal(wav[hi, 2], np.sqrt(w15[hi, 7] ** 2 + w15[hi, 6] ** 2))
+    for col, j in zip(range(3, 7), range(8, 12)):
+        np.testing.assert_array_equal(wav[hi, col], w15[hi, j])
+        assert not wav[lo, col].any()
+    assert not wav[hi, :2].any()
+    # admissible in each band
+    np.testing.assert_allclose(scal ** 2 + (wav ** 2).sum(axis=1), 1.0, atol=1e-12)
+
+
+def test_hybrid_single_band_keeps_reference_wrap():
+    """With one band the first scale absorbs B's last wavelet (the reference's
+    scale -1 wraps), so that wavelet is counted twice and verify_tiling rejects
+    the tiling, as the reference does."""
+    L = 64
+    scal, wav, sbl, wbl, J, bounds = ps.construct_hybrid_tiling(L, 3, np.array([2.0]), np.array([], dtype=int))
+    _, w = ps.axisym_wav_l(2.0, L, 3)
+    np.testing.assert_array_equal(wav[:, 0], np.sqrt(w[:, 0] ** 2 + w[:, -1] ** 2))
+    np.testing.assert_array_equal(wav[:, -1], w[:, -1])
+    assert not ps.verify_tiling(L, scal, wav.T.ravel(), sbl, wbl)
+
+
+def test_verify_tiling(capsys):
+    L = 96
+    scal, wav, sbl, wbl, J, bounds = ps.construct_hybrid_tiling(L, 0, np.array([3.0, 2.0]), np.array([40]))
+    assert ps.verify_tiling(L, scal, wav.T.ravel(), sbl, wbl)
+    # a band-limit that is too small is caught and reported
+    bad = wbl.copy()
+    bad[1] -= 2
+    assert not ps.verify_tiling(L, scal, wav.T.ravel(), sbl, bad)
+    assert "wavelet 1: band-limit" in capsys.readouterr().out
+    # a tiling whose squares do not sum to 1 is not admissible
+    assert not ps.verify_tiling(L, scal, 0.5 * wav.T.ravel(), sbl, wbl)
+    assert "not admissible" in capsys.readouterr().out
+
+
 def test_wigner_d_table_against_oracle(oracle_port):
     lib = oracle_port.lib
     lib.oracle_wigner_d_column.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double]
