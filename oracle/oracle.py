@@ -22,14 +22,16 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libs2let_ref.so")
-REF_SRC = os.environ.get("S2LET_REFERENCE_DIR", "/root/reference")
 
 
-def build(ref: bool = True) -> None:
-    """Compile the port (always) and the in-place reference build (when present)."""
+def build(ref_dir: str | None = None) -> None:
+    """Compile the port (always) and, when a reference checkout is named
+    (``ref_dir``, else the S2LET_REFERENCE_DIR environment variable) and holds
+    src/c, the in-place reference build."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    if ref and os.path.isdir(os.path.join(REF_SRC, "src", "c")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+    ref_dir = ref_dir or os.environ.get("S2LET_REFERENCE_DIR")
+    if ref_dir and os.path.isdir(os.path.join(ref_dir, "src", "c")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_dir}"], check=True)
 
 
 def _load(path):
@@ -46,7 +48,7 @@ _cache = {}
 def port():
     if "port" not in _cache:
         if not os.path.exists(PORT_SO):
-            build(ref=False)
+            build()
         _cache["port"] = _load(PORT_SO)
     return _cache["port"]
 

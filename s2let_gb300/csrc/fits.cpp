@@ -207,7 +207,8 @@ Hdu open_table(const char *name, std::vector<char> &buf) {
 std::vector<double> read_column(const std::vector<char> &buf, const Hdu &h, int col) {
   bool f1, f2, f3;
   const long row = key_long(h, "NAXIS1", &f1), nrows = key_long(h, "NAXIS2", &f2), nf = key_long(h, "TFIELDS", &f3);
-  S2G_REQUIRE(f1 && f2 && f3 && col <= nf, ERR_INVALID, "binary table without the requested column");
+  S2G_REQUIRE(f1 && f2 && f3 && col >= 1 && col <= nf, ERR_INVALID, "binary table without the requested column");
+  S2G_REQUIRE(row > 0 && nrows >= 0, ERR_INVALID, "binary table with a bad NAXIS1 / NAXIS2");
   size_t off = 0;
   long rep = 0;
   char type = 0;
@@ -231,6 +232,9 @@ std::vector<double> read_column(const std::vector<char> &buf, const Hdu &h, int 
     }
   }
   S2G_REQUIRE(type == 'D' || type == 'E', ERR_INVALID, "map column is neither 8-byte (D) nor 4-byte (E) float");
+  // the column must lie inside one row, and the rows inside the file
+  S2G_REQUIRE(rep >= 0 && off + (size_t)rep * (type == 'D' ? 8 : 4) <= (size_t)row, ERR_INVALID,
+              "binary table column extends past the end of its row (TFORMs wider than NAXIS1)");
   const size_t need = h.data_offset + (size_t)row * nrows;
   S2G_REQUIRE(need <= buf.size(), ERR_INVALID, "truncated FITS data unit");
   std::vector<double> out;

@@ -3,9 +3,12 @@ in place (oracle/_ref/libs2let_ref.so, see oracle/Makefile) over the project's
 SSHT/SO3 restatement.  Inputs are seeded numpy draws stored with the outputs, so
 the fixtures pin the oracle port (oracle/s2let_port.c) without the reference.
 
-Run from the repository root:  python tests/golden/make_golden.py [name-prefix ...]
+Run from the repository root, naming the reference checkout:
+  S2LET_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py [name-prefix ...]
 (with prefixes, only the fixtures whose names start with one of them are written).
-MWSS fixtures (mwss_*) store the sampling scheme as a seventh parameter.
+MWSS fixtures (mwss_*) store the sampling scheme as a seventh parameter;
+spin-lowered fixtures (os_*, wavelets with original_spin != 0) store the
+sampling scheme and the original spin as seventh and eighth parameters.
 """
 import os
 import sys
@@ -37,21 +40,33 @@ MWSS = {
     "mwss_L13_N5_s1_Jmin1": (13, 5, 2.0, 1, 1, 0),
 }
 
+# spin-lowered wavelets: the tiling carries the spin normalisation of
+# original_spin (src/c/s2let_tiling.c:404-423); MW sampling
+ORIG = {
+    # name: (L, N, B, J_min, spin, upsample, original_spin)
+    "os_L16_N4_s0_os2_multires": (16, 4, 2.0, 2, 0, 0, 2),
+    "os_L16_N3_s1_osm3_fullres": (16, 3, 2.0, 1, 1, 1, -3),
+}
+
 
 def main(prefixes=()):
-    oracle.build(ref=True)
+    oracle.build()
+    if not oracle.ref_available():
+        sys.exit("no in-place reference build: set S2LET_REFERENCE_DIR to the S2LET checkout")
     R = oracle.ref()
     rng = np.random.default_rng(20261203)
     rng_ss = np.random.default_rng(20261204)  # MWSS inputs: a stream of their own
     want = lambda name: not prefixes or any(name.startswith(x) for x in prefixes)
-    todo = [(k, v, 0) for k, v in CASES.items()] + [(k, v, 1) for k, v in MWSS.items()]
+    rng_os = np.random.default_rng(20261205)  # spin-lowered inputs: a stream of their own
+    todo = [(k, v + (0,), 0) for k, v in CASES.items()] + [(k, v + (0,), 1) for k, v in MWSS.items()] + \
+        [(k, v, 0) for k, v in ORIG.items()]
     written = 0
-    for name, (L, N, B, J_min, spin, up), ss in todo:
-        p = make_parameters(L, B, J_min, N, spin, up, sampling_scheme=ss)
+    for name, (L, N, B, J_min, spin, up, osp), ss in todo:
+        p = make_parameters(L, B, J_min, N, spin, up, sampling_scheme=ss, original_spin=osp)
         npx = (L + 1) * 2 * L if ss else L * (2 * L - 1)
-        par = [L, N, B, J_min, spin, up] + ([ss] if ss else [])
+        par = [L, N, B, J_min, spin, up] + ([ss] if ss or osp else []) + ([osp] if osp else [])
         out = {"params": np.array(par, dtype=np.float64)}
-        rng_case = rng_ss if ss else rng
+        rng_case = rng_os if osp else (rng_ss if ss else rng)
         f = rng_case.normal(size=npx) + 1j * rng_case.normal(size=npx)
         flm = rng_case.normal(size=L * L) + 1j * rng_case.normal(size=L * L)
         out["f"] = f

@@ -140,10 +140,14 @@ def test_existing_file_needs_bang_and_wrong_L_warns(lib, tmp_path, capfd):
     assert lib.s2let_gpu_last_error() != 0
 
 
-def test_reads_the_reference_data_file(lib):
-    from oracle.oracle import REF_SRC
+def _reference_data_dir():
+    from __graft_entry__ import REFERENCE_CHECKOUT
 
-    path = os.path.join(REF_SRC, "data", "earth_tomo_mw_128.fits")
+    return os.path.join(REFERENCE_CHECKOUT, "data")
+
+
+def test_reads_the_reference_data_file(lib):
+    path = os.path.join(_reference_data_dir(), "earth_tomo_mw_128.fits")
     if not os.path.exists(path):
         pytest.skip("reference data not present")
     L = lib.s2let_fits_mw_read_bandlimit(path.encode())
@@ -161,9 +165,7 @@ def test_reads_the_reference_data_file(lib):
 def test_header_readers_on_the_reference_data_files(lib):
     """NSIDE of the reference's HEALPix files and L of its MW files; a missing
     keyword reads as -1 (src/c/s2let_fits.c:17-85)."""
-    from oracle.oracle import REF_SRC
-
-    data = os.path.join(REF_SRC, "data")
+    data = _reference_data_dir()
     files = {"somecmbsimu_hpx_128.fits": (128, -1), "wmap_mcmc_base_k_synch_stk_q_9yr_v5.fits": (64, -1),
              "earth_tomo_mw_128.fits": (-1, 128), "earth_tomo_mw_128_rot.fits": (-1, 128)}
     present = [f for f in files if os.path.exists(os.path.join(data, f))]
@@ -173,3 +175,29 @@ def test_header_readers_on_the_reference_data_files(lib):
         path = os.path.join(data, f).encode()
         assert (lib.s2let_fits_hpx_read_nside(path), lib.s2let_fits_mw_read_bandlimit(path)) == files[f], f
         assert lib.s2let_gpu_last_error() == 0
+
+
+def _set_card(raw, key, value):
+    """raw bytes with the first header card `key` given the integer `value`"""
+    k = raw.index(key.ljust(8).encode() + b"= ")
+    card = (key.ljust(8) + "= " + str(value).rjust(20)).ljust(80).encode()
+    return raw[:k] + card + raw[k + 80:]
+
+
+@pytest.mark.parametrize("key,value", [("NAXIS1", 4), ("NAXIS1", 0), ("NAXIS2", -3)])
+def test_malformed_table_header_is_rejected(lib, tmp_path, key, value):
+    """A binary table whose column does not fit in its row (a header that
+    claims narrower rows than its TFORMs), or with nonsensical row counts, is
+    refused with a status; the output buffer is left as it was."""
+    L = 6
+    f = np.arange(L * (2 * L - 1), dtype=np.float64)
+    good = tmp_path / "good.fits"
+    lib.s2let_fits_mw_write_map(str(good).encode(), ptr(f), L)
+    raw = good.read_bytes()
+    ext = raw.index(b"XTENSION")
+    bad = tmp_path / "bad.fits"
+    bad.write_bytes(raw[:ext] + _set_card(raw[ext:], key, value))
+    g = np.full_like(f, -7.0)
+    lib.s2let_fits_mw_read_map(ptr(g), str(bad).encode(), L)
+    assert lib.s2let_gpu_last_error() == 1
+    assert (g == -7.0).all()
