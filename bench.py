@@ -709,9 +709,27 @@ def main():
         sh = torch.empty((nb, ns), dtype=torch.float64, pin_memory=True)
         frh = torch.empty((nb, npx), dtype=torch.float64, pin_memory=True)
 
+        calls = []  # per call: wall ms and the copy trace (CUDA events on the copying streams)
+        trace = (C.c_double * 8)()
+
+        def traced_call(name, fn, *args):
+            lib.s2let_gpu_copy_trace_enable(1)
+            t0 = time.perf_counter()
+            fn(*args)
+            ms = 1e3 * (time.perf_counter() - t0)
+            lib.s2let_gpu_copy_trace_report(trace)
+            rec = {"call": name, "ms": round(ms, 2)}
+            for d, tag in ((0, "h2d"), (1, "d2h")):
+                gb, busy, span = trace[4 * d + 1] / 1e9, trace[4 * d + 2], trace[4 * d + 3]
+                rec[tag] = {"GB": round(gb, 3), "span_ms": round(span, 2),
+                            "GBps": round(gb / span * 1e3, 1) if span > 0 else None}
+            calls.append(rec)
+
         def e2e_batch_step():
-            lib.s2let_gpu_analysis_px2wav_real_host_batch(vp(wh), vp(sh), vp(fh), nb, C.byref(p))
-            lib.s2let_gpu_synthesis_wav2px_real_host_batch(vp(frh), vp(wh), vp(sh), nb, C.byref(p))
+            traced_call("analysis", lib.s2let_gpu_analysis_px2wav_real_host_batch, vp(wh), vp(sh), vp(fh), nb,
+                        C.byref(p))
+            traced_call("synthesis", lib.s2let_gpu_synthesis_wav2px_real_host_batch, vp(frh), vp(wh), vp(sh), nb,
+                        C.byref(p))
             s2let_gb300.check(lib, "host batch API")
 
         def e2e_single_step():
@@ -741,6 +759,16 @@ def main():
         e2e_clocks.start()
         e2e_s = host_rate(e2e_batch_step, a.steps, record=True, warmup=max(1, a.warmup))
         e2e_clk = e2e_clocks.stop()
+        lib.s2let_gpu_copy_trace_enable(0)
+        timed_calls = calls[-2 * a.steps:]
+
+        def call_stats(name):
+            cs = [c for c in timed_calls if c["call"] == name]
+            big = "d2h" if name == "analysis" else "h2d"  # the f_wav direction of the call
+            return {"median_ms": statistics.median(c["ms"] for c in cs),
+                    "min_ms": min(c["ms"] for c in cs), "max_ms": max(c["ms"] for c in cs),
+                    f"f_wav_{big}_GBps_median": statistics.median(c[big]["GBps"] for c in cs),
+                    f"f_wav_{big}_GBps_min": min(c[big]["GBps"] for c in cs)}
         e2e_rt = float((frh - fh).abs().max() / fh.abs().max())
         single_s = host_rate(e2e_single_step, max(1, min(a.steps, 2)))
         e2e = {"value": whole_job_rate(nb, world, e2e_s), "unit": "maps/s",
@@ -749,6 +777,8 @@ def main():
                       f"({nb} maps per call, pinned host buffers)",
                "max_rel_err_round_trip": e2e_rt,
                "step_ms": [round(x, 1) for x in step_ms],
+               "per_call": {"analysis": call_stats("analysis"), "synthesis": call_stats("synthesis")},
+               "copy_trace": timed_calls,
                "clocks": e2e_clk,
                "median_step_value": whole_job_rate(nb, world, statistics.median(step_ms) / 1e3) if step_ms else None,
                "dropin_one_map_per_call": {"value": whole_job_rate(nb, world, single_s), "unit": "maps/s",

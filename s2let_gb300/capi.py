@@ -141,6 +141,10 @@ GPU_SIGNATURES = {
     "s2let_gpu_device_fault": (I, []),
     "s2let_gpu_timing_enable": (I, [I]),
     "s2let_gpu_timing_report": (I, [V, I]),
+    "s2let_gpu_copy_trace_enable": (I, [I]),
+    "s2let_gpu_copy_trace_report": (I, [V]),
+    "s2let_gpu_bind_device": (I, [I]),
+    "s2let_gpu_bound_device": (I, []),
     "s2let_gpu_axisym_wav_hardthreshold_real_noalloc": (I, [V, V, P, I]),
     "s2let_gpu_mw_adjoint_map2alm": (None, [V, V, I, I]),
     "s2let_gpu_mw_adjoint_alm2map": (None, [V, V, I, I]),
@@ -362,6 +366,45 @@ class S2let:
             tot += bl * (2 * bl - 1)
         bs = min(self.lib.s2let_bandlimit(p.J_min - 1, C.byref(p)), L)
         return tot, bs * (2 * bs - 1)
+
+    def axisym_lm_kernels(self, p):
+        """(wav_lm, scal_lm) of s2let_transform_axisym_lm_wav: rows of L per scale."""
+        J = self.lib.s2let_j_max(C.byref(p))
+        wav = np.zeros((J + 1) * p.L, np.float64)
+        scal = np.zeros(p.L, np.float64)
+        self.lib.s2let_transform_axisym_lm_wav(ptr(wav), ptr(scal), C.byref(p))
+        return wav, scal
+
+    def axisym_lm_sizes(self, p, multires):
+        """Sizes of f_wav_lm and f_scal_lm (s2let_transform_axisym_lm_allocate_f_wav[_multires])."""
+        J = self.lib.s2let_j_max(C.byref(p))
+        L = p.L
+        if not multires:
+            return (J + 1 - p.J_min) * L * L, L * L
+        tot = sum(min(self.lib.s2let_bandlimit(j, C.byref(p)), L) ** 2 for j in range(p.J_min, J + 1))
+        bs = min(self.lib.s2let_bandlimit(p.J_min - 1, C.byref(p)), L)
+        return tot, bs * bs
+
+    def axisym_lm_analysis(self, flm, p, multires=False):
+        wav, scal = self.axisym_lm_kernels(p)
+        nw, ns = self.axisym_lm_sizes(p, multires)
+        flm = np.ascontiguousarray(flm, dtype=np.complex128)
+        fw = np.zeros(nw, np.complex128)
+        fs = np.zeros(ns, np.complex128)
+        fn = (self.lib.s2let_transform_axisym_lm_wav_analysis_multires if multires
+              else self.lib.s2let_transform_axisym_lm_wav_analysis)
+        fn(ptr(fw), ptr(fs), ptr(flm), ptr(wav), ptr(scal), C.byref(p))
+        return fw, fs
+
+    def axisym_lm_synthesis(self, fw, fs, p, multires=False):
+        wav, scal = self.axisym_lm_kernels(p)
+        fw = np.ascontiguousarray(fw, dtype=np.complex128)
+        fs = np.ascontiguousarray(fs, dtype=np.complex128)
+        flm = np.zeros(p.L * p.L, np.complex128)
+        fn = (self.lib.s2let_transform_axisym_lm_wav_synthesis_multires if multires
+              else self.lib.s2let_transform_axisym_lm_wav_synthesis)
+        fn(ptr(flm), ptr(fw), ptr(fs), ptr(wav), ptr(scal), C.byref(p))
+        return flm
 
     def axisym(self, op, arrays, p, multires=False, real=False):
         """op in {'analysis', 'analysis_adjoint', 'synthesis', 'synthesis_adjoint'}."""

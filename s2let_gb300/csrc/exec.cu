@@ -471,16 +471,16 @@ struct WavPipe {
     S2G_CUDA(cudaEventRecord(e, st));
     S2G_CUDA(cudaStreamWaitEvent(cs, e, 0));
     const int64_t len = seglen.at(woff);
-    S2G_CUDA(cudaMemcpy2DAsync(host + ((size_t)b0 * hstride + woff) * esz, hstride * esz,
-                               (const char *)dev + ((size_t)b0 * dstride + woff) * esz, dstride * esz, len * esz,
-                               nbg, cudaMemcpyDeviceToHost, cs));
+    copy_async(host + ((size_t)b0 * hstride + woff) * esz, hstride * esz,
+               (const char *)dev + ((size_t)b0 * dstride + woff) * esz, dstride * esz, len * esz, nbg,
+               cudaMemcpyDeviceToHost, cs);
   }
   // synthesis: queue the copy of piece (woff, b0 .. b0 + nbg) into dev
   void in(void *dev, int64_t dstride, int64_t woff, int b0, int nbg) {
     const int64_t len = seglen.at(woff);
-    S2G_CUDA(cudaMemcpy2DAsync((char *)dev + ((size_t)b0 * dstride + woff) * esz, dstride * esz,
-                               host + ((size_t)b0 * hstride + woff) * esz, hstride * esz, len * esz, nbg,
-                               cudaMemcpyHostToDevice, cs));
+    copy_async((char *)dev + ((size_t)b0 * dstride + woff) * esz, dstride * esz,
+               host + ((size_t)b0 * hstride + woff) * esz, hstride * esz, len * esz, nbg, cudaMemcpyHostToDevice,
+               cs);
     cudaEvent_t e = event();
     S2G_CUDA(cudaEventRecord(e, cs));
     ready[{woff, b0}] = e;
@@ -502,6 +502,21 @@ bool rings_on_n(const WavPlan &P, const Scale &sd) {
   const double on_n = (double)sd.ns.size();
   const double on_g = P.real ? 0.5 * sd.ng : (double)sd.ng;
   return on_n < on_g;
+}
+
+// Scale ranges [k0, k1) that share one table pass (consecutive scales with the
+// same band-limit and directions), smallest band-limits first, or largest
+// first when `largest_first`.
+std::vector<std::pair<size_t, size_t>> table_passes(const WavPlan &P, bool largest_first) {
+  std::vector<std::pair<size_t, size_t>> passes;
+  for (size_t k0 = 0; k0 < P.sc.size();) {
+    size_t k1 = k0 + 1;
+    if (k1 < P.sc.size() && P.sc[k1].bl == P.sc[k0].bl && P.sc[k1].ns == P.sc[k0].ns) ++k1;
+    passes.emplace_back(k0, k1);
+    k0 = k1;
+  }
+  if (largest_first) std::reverse(passes.begin(), passes.end());
+  return passes;
 }
 
 void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_half, void *f_wav,
@@ -541,17 +556,9 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
   const int64_t gsz = (int64_t)nb * P.max_nn * ntmax * Wmax;
   double2 *Gbuf = S.get<double2>(2 * gsz);
   double2 *spec = S.get<double2>((int64_t)nb * std::max(P.max_ng, P.max_nn) * ntmax * Kmax);
-  // scales sharing band-limit and directions share each table pass
-  std::vector<std::pair<size_t, size_t>> passes;
-  for (size_t k0 = 0; k0 < P.sc.size();) {
-    size_t k1 = k0 + 1;
-    if (k1 < P.sc.size() && P.sc[k1].bl == P.sc[k0].bl && P.sc[k1].ns == P.sc[k0].ns) ++k1;
-    passes.emplace_back(k0, k1);
-    k0 = k1;
-  }
   // with host copies the largest scales go first, so that most of f_wav can
   // cross the bus while the smaller scales are transformed
-  if (pipe) std::reverse(passes.begin(), passes.end());
+  const std::vector<std::pair<size_t, size_t>> passes = table_passes(P, pipe != nullptr);
   for (const auto &pk : passes) {
     const size_t k0 = pk.first, k1 = pk.second;
     const int ngrp = (int)(k1 - k0);
@@ -662,9 +669,12 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
   const int64_t gsz = (int64_t)nb * P.max_nn * ntmax * Wmax;
   double2 *Gbuf = S.get<double2>(2 * gsz);
   double2 *spec = S.get<double2>((int64_t)nb * std::max(P.max_ng, P.max_nn) * ntmax * Kmax);
-  for (size_t k0 = 0; k0 < P.sc.size();) {
-    size_t k1 = k0 + 1;
-    if (k1 < P.sc.size() && P.sc[k1].bl == P.sc[k0].bl && P.sc[k1].ns == P.sc[k0].ns) ++k1;
+  // with host copies the largest scales go first (their pieces are queued
+  // first, see merge_order), so that their ring DFTs run while the rest of
+  // f_wav is still crossing the bus
+  const std::vector<std::pair<size_t, size_t>> passes = table_passes(P, pipe != nullptr);
+  for (const auto &pk : passes) {
+    const size_t k0 = pk.first, k1 = pk.second;
     const int ngrp = (int)(k1 - k0);
     const int bl = P.sc[k0].bl, W = 2 * bl - 1, nn = (int)P.sc[k0].ns.size();
     const int nt = P.nt(bl), K = P.K(bl);
@@ -727,7 +737,6 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
       }
       contract_t2l_group(grp, ngrp, S.st);
     }
-    k0 = k1;
   }
   merge_lmn(flm, L, (int64_t)L * L, z, P.z_per_map, P.d_pairs, P.npairs, P.d_w, zs, (int64_t)bs * bs, bs,
             real, accumulate, nb, S.st);
@@ -775,10 +784,30 @@ void report_failure() {
 }
 int last_status() { return t_status; }
 
+// The device this process's library works on: the one current at the first
+// compute call (or named by s2let_gpu_bind_device).  Plans, Wigner tables,
+// streams and kernel attributes are cached process-wide for that device only,
+// so a call made while another device is current is refused.
+std::atomic<int> g_bound_device{-1};
+
+int bind_device(int dev) {
+  if (dev < 0) return ERR_INVALID;
+  int expected = -1;
+  if (g_bound_device.compare_exchange_strong(expected, dev) || expected == dev) return OK;
+  return ERR_UNSUPPORTED;
+}
+
 void ensure_device() {
   int n = 0;
   cudaError_t e = cudaGetDeviceCount(&n);
   S2G_REQUIRE(e == cudaSuccess && n > 0, ERR_NO_DEVICE, "no CUDA device available");
+  int dev = -1;
+  S2G_CUDA(cudaGetDevice(&dev));
+  if (bind_device(dev) != OK)
+    throw Error(ERR_UNSUPPORTED, "the library serves CUDA device " + std::to_string(g_bound_device.load()) +
+                                     " in this process (its first device); device " + std::to_string(dev) +
+                                     " is current: make device " + std::to_string(g_bound_device.load()) +
+                                     " current, or use one process per device");
   static std::once_flag f;
   std::call_once(f, [] {
     int dev = 0;
@@ -1153,20 +1182,22 @@ int host_batch(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool rea
       S2G_CUDA(cudaEventRecord(e0, st));
       S2G_CUDA(cudaStreamWaitEvent(cs, e0, 0));
       if (fwd) {
-        S2G_CUDA(cudaMemcpyAsync(dpx, hpx + (size_t)c0 * npx * esz, (size_t)n * npx * esz, cudaMemcpyHostToDevice, st));
+        copy_async(dpx, 0, hpx + (size_t)c0 * npx * esz, 0, (size_t)n * npx * esz, 1, cudaMemcpyHostToDevice, st);
         run_plan(op, P, dpx, nullptr, dw, nw, ds, ns, n, st, false, &pipe);
-        S2G_CUDA(cudaMemcpyAsync(hs + (size_t)c0 * ns * esz, ds, (size_t)n * ns * esz, cudaMemcpyDeviceToHost, st));
+        copy_async(hs + (size_t)c0 * ns * esz, 0, ds, 0, (size_t)n * ns * esz, 1, cudaMemcpyDeviceToHost, st);
       } else {
-        S2G_CUDA(cudaMemcpyAsync(ds, hs + (size_t)c0 * ns * esz, (size_t)n * ns * esz, cudaMemcpyHostToDevice, st));
-        for (const Scale &sd : P.sc) {  // in the order the synthesis reads them
-          if (rings_on_n(P, sd)) {
-            for (int b0 = 0; b0 < n; b0 += pipe.group) pipe.in(dw, nw, sd.woff, b0, std::min(pipe.group, n - b0));
-          } else {
-            pipe.in(dw, nw, sd.woff, 0, n);
+        copy_async(ds, 0, hs + (size_t)c0 * ns * esz, 0, (size_t)n * ns * esz, 1, cudaMemcpyHostToDevice, st);
+        for (const auto &pk : table_passes(P, true))  // in the order the synthesis reads them
+          for (size_t k = pk.first; k < pk.second; ++k) {
+            const Scale &sd = P.sc[k];
+            if (rings_on_n(P, sd)) {
+              for (int b0 = 0; b0 < n; b0 += pipe.group) pipe.in(dw, nw, sd.woff, b0, std::min(pipe.group, n - b0));
+            } else {
+              pipe.in(dw, nw, sd.woff, 0, n);
+            }
           }
-        }
         run_plan(op, P, dpx, nullptr, dw, nw, ds, ns, n, st, false, &pipe);
-        S2G_CUDA(cudaMemcpyAsync(hpx + (size_t)c0 * npx * esz, dpx, (size_t)n * npx * esz, cudaMemcpyDeviceToHost, st));
+        copy_async(hpx + (size_t)c0 * npx * esz, 0, dpx, 0, (size_t)n * npx * esz, 1, cudaMemcpyDeviceToHost, st);
       }
     }
   });
@@ -1295,6 +1326,17 @@ int s2let_gpu_set_table_mode(int mode) {
   return 0;
 }
 int s2let_gpu_get_table_mode(void) { return s2g::t_table_mode; }
+int s2let_gpu_bind_device(int device) {
+  const int st = s2g::bind_device(device);
+  if (st != s2g::OK) {
+    s2g::set_status(st, device < 0 ? "s2let_gpu_bind_device: negative device ordinal"
+                                   : "s2let_gpu_bind_device: the library already serves CUDA device " +
+                                         std::to_string(s2g::g_bound_device.load()) + " in this process");
+    s2g::report_failure();
+  }
+  return st;
+}
+int s2let_gpu_bound_device(void) { return s2g::g_bound_device.load(); }
 void s2let_gpu_release_plans(void) {
   s2g::guarded("s2let_gpu_release_plans", [] {
     {

@@ -34,10 +34,11 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-// Device address of g_scratch, looked up once per device with that device current.
+// Device address of g_scratch, looked up with that device current the first
+// time a call runs on it.  Only a successful lookup is kept: a failed one
+// raises ERR_CUDA for that call and is tried again by the next.
 struct DeviceSlot {
-  std::once_flag once;
-  cudaError_t err = cudaSuccess;
+  std::mutex mu;
   void *ptr = nullptr;
 };
 DeviceSlot g_slots[kMaxDevices];
@@ -47,9 +48,14 @@ unsigned char *scratch_on_current_device() {
   S2G_CUDA(cudaGetDevice(&dev));
   S2G_REQUIRE(dev >= 0 && dev < kMaxDevices, s2g::ERR_UNSUPPORTED, "device ordinal out of range");
   DeviceSlot &s = g_slots[dev];
-  std::call_once(s.once, [&s] { s.err = cudaGetSymbolAddress(&s.ptr, g_scratch); });
-  if (s.err != cudaSuccess || s.ptr == nullptr)
-    throw s2g::Error(s2g::ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(s.err));
+  std::lock_guard<std::mutex> lk(s.mu);
+  if (s.ptr == nullptr) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess || p == nullptr)
+      throw s2g::Error(s2g::ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    s.ptr = p;
+  }
   return static_cast<unsigned char *>(s.ptr);
 }
 
@@ -67,6 +73,7 @@ extern "C" int s2let_gpu_axisym_wav_hardthreshold_real_noalloc(double *g_wav, co
     q.N = 1;
     q.spin = 0;
     s2g::validate(&q, false);
+    s2g::ensure_device();
     const int L = q.L, J = s2g::j_max(q);
     const int nscale = J - q.J_min + 1;
     S2G_REQUIRE(nscale >= 1 && nscale <= kMaxScales, s2g::ERR_INVALID,

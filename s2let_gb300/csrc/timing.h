@@ -22,6 +22,13 @@ enum KCat {
 
 bool timing_enabled();
 
+// One host<->device copy of the host-pointer entry points (a plain copy when
+// height == 1, else pitched rows), asynchronous on st.  While copy tracing is
+// on (s2let_gpu_copy_trace_enable), CUDA events bracket the copy on st so its
+// duration and rate can be reported per direction.
+void copy_async(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
+                cudaMemcpyKind kind, cudaStream_t st);
+
 class KTimer {
  public:
   KTimer(int cat, cudaStream_t st, double flops, double bytes);
