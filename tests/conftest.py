@@ -55,14 +55,33 @@ def random_flm(rng, L, spin=0, real=False, power=None):
     return flm
 
 
+def power_law_flm(rng, L, spin=0, real=False):
+    """The benchmark configurations' spectra, vectorised: complex Gaussian flm
+    with variance C_l = (l+1)^-2 (spin 0) or l^-2 for l >= |spin| (zero below);
+    real=True enforces f_{l,-m} = (-1)^m conj(f_lm) (f_l0 real); f_00 = 0."""
+    l = np.repeat(np.arange(L), 2 * np.arange(L) + 1)
+    m = np.concatenate([np.arange(-k, k + 1) for k in range(L)]) if L else np.zeros(0, int)
+    amp = np.where(l >= abs(spin), 1.0 / np.maximum(l + (1 if spin == 0 else 0), 1), 0.0)
+    flm = (rng.normal(size=L * L) + 1j * rng.normal(size=L * L)) * amp / np.sqrt(2)
+    if real:
+        i0 = l * l + l
+        pos = m > 0
+        flm[m == 0] = flm[m == 0].real * np.sqrt(2)
+        flm[(i0 - m)[pos]] = (-1.0) ** m[pos] * np.conj(flm[pos])
+    flm[0] = 0.0
+    return flm
+
+
 def params_of(g):
     """make_parameters from a golden fixture's params (a seventh entry, when
-    present, is the sampling scheme)."""
+    present, is the sampling scheme; an eighth the original spin)."""
     from s2let_gb300.capi import make_parameters
 
     v = g["params"]
     ss = int(v[6]) if len(v) > 6 else 0
-    return make_parameters(int(v[0]), float(v[2]), int(v[3]), int(v[1]), int(v[4]), int(v[5]), sampling_scheme=ss)
+    osp = int(v[7]) if len(v) > 7 else 0
+    return make_parameters(int(v[0]), float(v[2]), int(v[3]), int(v[1]), int(v[4]), int(v[5]),
+                           sampling_scheme=ss, original_spin=osp)
 
 
 _SSHT_NAMES = {

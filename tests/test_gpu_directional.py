@@ -116,16 +116,19 @@ def test_lm2wav_wav2lm(gpu, oracle_port, case):
 import glob  # noqa: E402
 import os  # noqa: E402
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "dir_*.npz")))
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "dir_*.npz")) +
+                glob.glob(os.path.join(os.path.dirname(__file__), "golden", "os_*.npz")))
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
 def test_gpu_matches_reference_golden(gpu, path):
-    """GPU outputs against vectors produced by the reference's own S2LET sources."""
+    """GPU outputs against vectors produced by the reference's own S2LET sources
+    (os_*: spin-lowered wavelets, original_spin != 0, src/c/s2let_tiling.c:404-423)."""
+    from conftest import params_of
+
     g = np.load(path)
-    L, N, B, J_min, spin, up = g["params"]
-    p = make_parameters(int(L), B, int(J_min), int(N), int(spin), int(up))
+    p = params_of(g)
     w, s = gpu.px2wav(g["f"], p)
     assert rel_err(w, g["px2wav_wav"]) < TOL and rel_err(s, g["px2wav_scal"]) < TOL
     assert rel_err(gpu.wav2px(g["px2wav_wav"], g["px2wav_scal"], p), g["wav2px"]) < TOL

@@ -16,7 +16,7 @@ from s2let_gb300.capi import SAMPLING_MW_SS, make_parameters
 
 TOL = 1e-12
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
-GOLDEN = [p for p in GOLDEN if os.path.basename(p).startswith(("dir_", "mwss_"))]
+GOLDEN = [p for p in GOLDEN if os.path.basename(p).startswith(("dir_", "mwss_", "os_"))]
 
 
 class table_mode:

@@ -17,7 +17,7 @@ from s2let_gb300.capi import make_parameters, ptr
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
 
 
-@pytest.mark.parametrize("path", [p for p in GOLDEN if os.path.basename(p).startswith(("dir_", "mwss_"))],
+@pytest.mark.parametrize("path", [p for p in GOLDEN if os.path.basename(p).startswith(("dir_", "mwss_", "os_"))],
                          ids=lambda p: os.path.basename(p)[:-4])
 def test_port_matches_reference_golden_directional(oracle_port, path):
     g = np.load(path)
