@@ -37,7 +37,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "px2wav+wav2px maps/s at L=1024,N=4: mixed vs FP64 GPU at stated max err"
-NOMINAL_FP64_TFLOPS = 1.25  # GB300 FP64 (vendor nominal; no measured FP64 peak is available)
 
 
 def max_over_ranks(x, dist=None, device="cpu"):
@@ -185,6 +184,106 @@ def profile_traffic(kernel, alg_bytes_per_launch):
     return None if r is None else r * alg_bytes_per_launch
 
 
+# timing categories of s2let_gb300/csrc/timing.h (6 and 7, the recomputed-table
+# contractions and quadrature, do not run at the metric point)
+KERNEL_CATS = {0: "fp64_contraction", 1: "ring_dft", 2: "gamma_dft", 3: "tiling_merge", 4: "tensor_contraction",
+               5: "other", 8: "digit_slicing"}
+
+
+def sht_flops(ell, s, real):
+    """Direct-theta Legendre count of one spin-s SHT at band-limit ell: one
+    complex x real multiply-add (4 flop) per (l, m, theta ring), ell rings."""
+    ms = range(0, ell) if (real and s == 0) else range(-(ell - 1), ell)
+    return 4 * ell * sum(max(0, ell - max(abs(m), abs(s))) for m in ms)
+
+
+def work_flops_per_map(L, N, B, J_min):
+    """Algorithmic flops of px2wav + wav2px of one real spin-0 map (multires):
+    the SHT at L, the scaling SHT at B^J_min, and per scale j the SHTs of the
+    directions n >= 0 kept by a real signal at bl_j = min(ceil(B^(j+1)), L)."""
+    import math
+
+    J = math.ceil(math.log(L) / math.log(B) - 1e-12)
+    bl_scal = min(math.ceil(B ** J_min - 1e-12), L)
+    f = sht_flops(L, 0, True) + sht_flops(bl_scal, 0, True)
+    for j in range(J_min, J + 1):
+        bl = min(math.ceil(B ** (j + 1) - 1e-12), L)
+        Nj = min(N, bl)
+        Nj += (Nj + N) % 2
+        for n in range(-Nj + 1, Nj, 2):
+            if n >= 0:
+                f += sht_flops(bl, n, n == 0)
+    return 2 * f
+
+# bf16 MMA products per real multiply-add of the split-precision contraction
+# (7 x 7 digits, the 28 with i + j <= 6)
+DIGIT_PRODUCTS = 28
+
+
+def measured_fma_peaks(lib):
+    """FP32 and FP64 FMA throughput of this GPU, measured in this process
+    (best of three launches each, about 0.1 s)."""
+    out = {}
+    for name, fp64, iters in (("fp32_tflops", 0, 200000), ("fp64_tflops", 1, 4000)):
+        best = 0.0
+        for _ in range(3):
+            v = C.c_double(0.0)
+            if lib.s2let_gpu_fma_rate(fp64, iters, C.byref(v)) != 0:
+                raise RuntimeError("s2let_gpu_fma_rate failed")
+            best = max(best, v.value)
+        out[name] = best
+    return out
+
+
+def binding_roofline(kernels, peaks, peak_kind, fma, precision, mhz):
+    """Roofline of the step's dominant kernel against the unit that binds it:
+    the tensor pipe (split-precision contraction: bf16 MMA flops over the
+    measured cuBLAS bf16 peak), the FP32 pipe (double-float ring DFTs: FP32
+    instructions of the work model over the measured FP32 FMA instruction
+    rate), the FP64 pipe (FP64 kernels: flops over the measured FP64 FMA
+    peak), else HBM (algorithmic bytes over the measured copy bandwidth)."""
+    dom = max(kernels, key=lambda c: kernels[c]["ms"])
+    kd = kernels[dom]
+    sec = kd["ms"] * 1e-3
+    hbm = kd["bytes"] / sec / 1e9
+    hbm_peak = peaks.get("hbm_gbs")
+    if dom == "tensor_contraction":
+        ach = DIGIT_PRODUCTS * kd["flops"] / sec / 1e12
+        roof = {"bound": "tensor", "unit": "TFLOP/s", "achieved": ach, "peak": peaks.get("bf16_tflops"),
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json bf16 burst)",
+                "work": f"{DIGIT_PRODUCTS} bf16 products per FP64-equivalent multiply-add"}
+    elif dom == "ring_dft" and precision == "mixed":
+        ach = kd["flops"] / sec / 1e12  # the timing record carries the model FP32 instruction count
+        roof = {"bound": "fp32", "unit": "Tinst/s", "achieved": ach, "peak": fma["fp32_tflops"] / 2,
+                "peak_source": "measured in this run: FP32 FMA chains on every SM (s2let_gpu_fma_rate), "
+                               "one instruction per FMA",
+                "work": "double-float FP32 instructions of the Bluestein work model (csrc/kernels.cu ring_work)"}
+    elif dom in ("fp64_contraction", "ring_dft"):
+        ach = kd["flops"] / sec / 1e12
+        roof = {"bound": "fp64", "unit": "TFLOP/s", "achieved": ach, "peak": fma["fp64_tflops"],
+                "peak_source": "measured in this run: FP64 FMA chains on every SM (s2let_gpu_fma_rate)"}
+    else:
+        roof = {"bound": "hbm", "unit": "GB/s", "achieved": hbm, "peak": hbm_peak,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json copy)"}
+    roof["frac"] = roof["achieved"] / roof["peak"] if roof["peak"] else None
+    step_ms = sum(k["ms"] for k in kernels.values())
+    roof.update({
+        "kernel": dom, "launches_per_step": kd["launches"], "avg_launch_ms": kd["ms"] / max(kd["launches"], 1),
+        "traffic": profile_traffic(dom, kd["bytes"] / max(kd["launches"], 1)),
+        "share_of_step": kd["ms"] / step_ms if step_ms else None,
+        "hbm": {"achieved_gbs": hbm, "peak_gbs": hbm_peak, "frac": hbm / hbm_peak if hbm_peak else None},
+        "sm_mhz": mhz,
+        "per_kernel_ms_per_step": {c: k["ms"] for c, k in kernels.items() if k["launches"]},
+    })
+    km = kernels.get("tensor_contraction")
+    if km and km["launches"] and km["ms"] and dom != "tensor_contraction":
+        t = DIGIT_PRODUCTS * km["flops"] / (km["ms"] * 1e-3) / 1e12
+        roof["tensor_contraction"] = {"bound": "tensor", "achieved_tflops": t, "peak_tflops": peaks.get("bf16_tflops"),
+                                      "frac": t / peaks.get("bf16_tflops"), "ms_per_step": km["ms"],
+                                      "hbm_gbs": km["bytes"] / (km["ms"] * 1e-3) / 1e9}
+    return roof
+
+
 def cpu_baseline_sample(p_args, f0):
     """The oracle (C restatement of the reference path, OpenMP on all host cores):
     one map through px2wav_real + wav2px_real.  Returns (seconds, f_wav, f_scal)."""
@@ -197,6 +296,53 @@ def cpu_baseline_sample(p_args, f0):
     w, s = port.px2wav(f0, p, real=True)
     port.wav2px(w, s, p, real=True)
     return time.perf_counter() - t0, w, s
+
+
+def _one_map_single_thread(args):
+    """Worker of the CPU throughput mode (a spawned process): one map through
+    px2wav_real + wav2px_real on the oracle with one OpenMP thread.  Returns
+    (px2wav seconds, wav2px seconds)."""
+    L, B, J_min, N, seed = args
+    os.environ["OMP_NUM_THREADS"] = "1"
+    import ctypes
+
+    from oracle import oracle
+    from s2let_gb300.capi import make_parameters
+
+    port = oracle.port()
+    try:
+        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(1)
+    except OSError:
+        pass
+    p = make_parameters(L, B, J_min, N, 0, 0)
+    f = port.alm2map(power_law_real_flm(np.random.default_rng(seed), L), L, real=True)
+    t0 = time.perf_counter()
+    w, s = port.px2wav(f, p, real=True)
+    t1 = time.perf_counter()
+    port.wav2px(w, s, p, real=True)
+    return t1 - t0, time.perf_counter() - t1
+
+
+def cpu_modes(a):
+    """The reference is single-threaded: one map per host core, each on one
+    thread, all at once.  Throughput = cores / wall time; latency = the median
+    per-process round trip (1 thread, 1 map, under the memory traffic of the
+    other cores).  Processes are spawned, never forked."""
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_one_map_single_thread, [(a.L, a.B, a.J_min, a.N, 500 + k) for k in range(cores)])
+    wall = time.perf_counter() - t0
+    per = sorted(x + y for x, y in res)
+    return {"throughput": {"value": cores / wall, "unit": "maps/s", "cores": cores, "wall_s": wall,
+                           "sample": f"{cores} maps, one single-threaded process per core"},
+            "latency_1thread": {"seconds_per_map": statistics.median(per),
+                                "px2wav_s": statistics.median(x for x, _ in res),
+                                "wav2px_s": statistics.median(y for _, y in res),
+                                "value": 1.0 / statistics.median(per), "unit": "maps/s", "cores": 1}}
 
 
 def run_reference(a, rank):
@@ -634,65 +780,38 @@ def main():
         lib.s2let_gpu_set_precision(1)
 
     # ---- roofline: one instrumented step, CUDA events around each launch ----
-    lib.s2let_gpu_timing_enable(1)
-    step()
-    torch.cuda.synchronize()
-    rep = (C.c_double * 36)()
-    lib.s2let_gpu_timing_report(rep, 9)
-    lib.s2let_gpu_timing_enable(0)
-    # timing categories of s2let_gb300/csrc/timing.h (6 and 7, the recomputed-table
-    # contractions and quadrature, do not run here)
-    cats = {0: "fp64_contraction", 1: "ring_dft", 2: "gamma_dft", 3: "tiling_merge", 4: "tensor_contraction",
-            5: "other", 8: "digit_slicing"}
-    kernels = {c: {"launches": int(rep[4 * i]), "ms": rep[4 * i + 1], "flops": rep[4 * i + 2],
-                   "bytes": rep[4 * i + 3]} for i, c in cats.items()}
-    dom = max(kernels, key=lambda c: kernels[c]["ms"])
-    kd = kernels[dom]
     peaks, peak_kind = measured_peaks()
-    step_ms_instr = sum(k["ms"] for k in kernels.values())
-    # every kernel of the path streams HBM; the FP64 ones are bounded first by the
-    # FP64 pipe, reported beside the HBM figure
-    ach = kd["bytes"] / (kd["ms"] * 1e-3) / 1e9
-    peak = peaks.get("hbm_gbs")
-    roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak}
-    tr = profile_traffic(dom, kd["bytes"] / max(kd["launches"], 1))
-    roof.update({
-        "kernel": dom, "peak_source": peak_kind, "launches_per_step": kd["launches"],
-        "avg_launch_ms": kd["ms"] / max(kd["launches"], 1),
-        "traffic": tr,
-        "share_of_step": kd["ms"] / step_ms_instr if step_ms_instr else None,
-        "per_kernel_ms_per_step": {c: k["ms"] for c, k in kernels.items() if k["launches"]},
-    })
-    if dom == "fp64_contraction" and kd["ms"]:
-        t64 = kd["flops"] / (kd["ms"] * 1e-3) / 1e12
-        roof["fp64"] = {"achieved_tflops": t64, "nominal_peak_tflops": NOMINAL_FP64_TFLOPS,
-                        "frac_of_nominal": t64 / NOMINAL_FP64_TFLOPS}
-    if dom == "ring_dft" and kd["ms"]:
-        # double-float ring DFTs: bound by the FP32 pipe, not HBM.  Work = model
-        # count of FP32 instructions (s2let_gb300/csrc/kernels.cu ring_work);
-        # peak = SMs x 128 FP32 lanes x the SM clock sampled during the run.
-        props = torch.cuda.get_device_properties(dev)
-        mhz = (clk or {}).get("sm_mhz") or 2070.0
-        peak_ti = props.multi_processor_count * 128 * mhz * 1e6 / 1e12
-        if a.precision == "mixed":
-            ti = kd["flops"] / (kd["ms"] * 1e-3) / 1e12
-            roof["fp32_pipe"] = {"achieved_tinst_per_s": ti, "peak_tinst_per_s": peak_ti, "frac": ti / peak_ti,
-                                 "work": "double-float FP32 instructions (model)"}
-            roof["binding_unit"] = {
-                "unit": "FP32 instruction issue", "frac": ti / peak_ti,
-                "note": "the ring DFTs are bound by FP32 instruction issue and the latency of their "
-                        "twiddle loads (ncu, P = 4096: FMA pipe 52 %, ALU 21 %, LSU 11 %, issue active 69 %, "
-                        "stalls 'not selected' then 'long scoreboard'; DRAM 5 %), so the HBM fraction above is "
-                        "not their limit: profiles/ring_dft_df_L1024_N4_batch8.md"}
-    km = kernels["tensor_contraction"]
-    if km["launches"] and km["ms"]:
-        g = km["bytes"] / (km["ms"] * 1e-3) / 1e9
-        roof["tensor_contraction"] = {"bound": "hbm", "achieved_gbs": g, "frac": g / peak, "ms_per_step": km["ms"],
-                                      "fp64_equiv_tflops": km["flops"] / (km["ms"] * 1e-3) / 1e12}
-    ks = kernels["digit_slicing"]
-    if ks["launches"] and ks["ms"]:
-        g = ks["bytes"] / (ks["ms"] * 1e-3) / 1e9
-        roof["digit_slicing"] = {"bound": "hbm", "achieved_gbs": g, "frac": g / peak, "ms_per_step": ks["ms"]}
+    fma = measured_fma_peaks(lib)
+
+    def instrumented_step():
+        lib.s2let_gpu_timing_enable(1)
+        step()
+        torch.cuda.synchronize()
+        rep = (C.c_double * 36)()
+        lib.s2let_gpu_timing_report(rep, 9)
+        lib.s2let_gpu_timing_enable(0)
+        return {c: {"launches": int(rep[4 * i]), "ms": rep[4 * i + 1], "flops": rep[4 * i + 2],
+                    "bytes": rep[4 * i + 3]} for i, c in KERNEL_CATS.items()}
+
+    kernels = instrumented_step()
+    mhz = (clk or {}).get("sm_mhz")
+    roof = binding_roofline(kernels, peaks, peak_kind, fma, a.precision, mhz)
+    if fp64 is not None:
+        # the FP64 path on the same inputs: its step breakdown and roofline
+        lib.s2let_gpu_set_precision(0)
+        k64 = instrumented_step()
+        lib.s2let_gpu_set_precision(1)
+        wpm = work_flops_per_map(a.L, a.N, a.B, a.J_min)
+        f64_flops = wpm * nb  # algorithmic flops of one step
+        t64 = f64_flops / (fp64["ms_per_step"] * 1e-3) / 1e12
+        fp64["roofline"] = {
+            "bound": "fp64", "unit": "TFLOP/s", "achieved": t64, "peak": fma["fp64_tflops"],
+            "frac": t64 / fma["fp64_tflops"],
+            "peak_source": "measured in this run: FP64 FMA chains on every SM (s2let_gpu_fma_rate)",
+            "work": f"{wpm:.4g} flop per map (direct-theta Legendre count, both directions)",
+            "per_kernel_ms_per_step": {c: k["ms"] for c, k in k64.items() if k["launches"]},
+            "dominant_kernel": binding_roofline(k64, peaks, peak_kind, fma, "fp64", mhz),
+        }
 
     # ---- e2e through the host-pointer C ABI ----
     # The timed region holds every host <-> device copy: the maps in, the
@@ -710,7 +829,7 @@ def main():
         frh = torch.empty((nb, npx), dtype=torch.float64, pin_memory=True)
 
         calls = []  # per call: wall ms and the copy trace (CUDA events on the copying streams)
-        trace = (C.c_double * 8)()
+        trace = (C.c_double * 10)()
 
         def traced_call(name, fn, *args):
             lib.s2let_gpu_copy_trace_enable(1)
@@ -720,9 +839,10 @@ def main():
             lib.s2let_gpu_copy_trace_report(trace)
             rec = {"call": name, "ms": round(ms, 2)}
             for d, tag in ((0, "h2d"), (1, "d2h")):
-                gb, busy, span = trace[4 * d + 1] / 1e9, trace[4 * d + 2], trace[4 * d + 3]
+                gb, busy, span = trace[5 * d + 1] / 1e9, trace[5 * d + 2], trace[5 * d + 3]
                 rec[tag] = {"GB": round(gb, 3), "span_ms": round(span, 2),
-                            "GBps": round(gb / span * 1e3, 1) if span > 0 else None}
+                            "GBps": round(gb / span * 1e3, 1) if span > 0 else None,
+                            "copies": int(trace[5 * d]), "by_kernel": int(trace[5 * d + 4])}
             calls.append(rec)
 
         def e2e_batch_step():
@@ -789,9 +909,16 @@ def main():
     err_vs_oracle = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         sec, w_o, s_o = cpu_baseline_sample(a, f_host[0])
-        cpu = {"value": 1.0 / sec, "unit": "maps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"1 map (px2wav_real + wav2px_real) of the same workload, {sec:.1f} s; CPU oracle = C "
-                         "restatement of the reference S2LET layer over restated SSHT/SO3, OpenMP"}
+        modes = cpu_modes(a)
+        thr = modes["throughput"]
+        cpu = {"value": thr["value"], "unit": "maps/s", "cores": thr["cores"], "kind": "port",
+               "sample": f"{thr['cores']} maps of the same workload (px2wav_real + wav2px_real), one "
+                         f"single-threaded process per host core, {thr['wall_s']:.1f} s wall; CPU oracle = C "
+                         "restatement of the reference S2LET layer over restated SSHT/SO3 (the reference is "
+                         "single-threaded)",
+               "latency_1thread": modes["latency_1thread"],
+               "openmp_one_map": {"value": 1.0 / sec, "unit": "maps/s", "cores": os.cpu_count(),
+                                  "sample": f"1 map, the oracle's OpenMP loops on all cores, {sec:.1f} s"}}
         wg = w[0].cpu().numpy()
         sg = sc[0].cpu().numpy()
         err_vs_oracle = max(float(np.abs(wg - w_o).max() / np.abs(w_o).max()),

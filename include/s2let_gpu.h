@@ -555,11 +555,20 @@ int s2let_gpu_timing_report(double *out, int ncat);
 /* Optional trace of the host <-> device copies made by the host-pointer batch
  * entry points, with CUDA events on the copying streams.  enable(1) clears
  * previous records and starts tracing, enable(0) stops.  report fills
- * out[d*4 + {0,1,2,3}] = {copies, bytes, busy milliseconds (sum of the copies'
- * own durations), span milliseconds (first start to last end)} for direction
- * d = 0 (host to device) and d = 1 (device to host). */
+ * out[d*5 + {0,1,2,3,4}] = {copies, bytes, busy milliseconds (sum of the
+ * copies' own durations), span milliseconds (first start to last end), copies
+ * made by the copy kernel} for direction d = 0 (host to device) and d = 1
+ * (device to host).  Page-locked host buffers are moved by a copy kernel
+ * (SM loads and stores over the host link); other host memory, or every
+ * copy when S2LET_GPU_HOST_COPY=engine, by the copy engines. */
 int s2let_gpu_copy_trace_enable(int on);
 int s2let_gpu_copy_trace_report(double *out);
+
+/* Measured FMA throughput of the current GPU, for roofline fractions: one
+ * launch of 8 independent FMA chains per thread, `iters` iterations; fp64 != 0
+ * times FP64 FMAs, else FP32.  *tflops = 2 x FMAs per second / 1e12.
+ * Returns the status. */
+int s2let_gpu_fma_rate(int fp64, int iters, double *tflops);
 
 #ifdef __cplusplus
 }

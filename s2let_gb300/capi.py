@@ -144,6 +144,7 @@ GPU_SIGNATURES = {
     "s2let_gpu_copy_trace_enable": (I, [I]),
     "s2let_gpu_copy_trace_report": (I, [V]),
     "s2let_gpu_bind_device": (I, [I]),
+    "s2let_gpu_fma_rate": (I, [I, I, V]),
     "s2let_gpu_bound_device": (I, []),
     "s2let_gpu_axisym_wav_hardthreshold_real_noalloc": (I, [V, V, P, I]),
     "s2let_gpu_mw_adjoint_map2alm": (None, [V, V, I, I]),

@@ -80,6 +80,16 @@ struct WavPlan {
   int npairs = 0;
   int64_t z_per_map = 0;
   int max_bl = 1, max_nn = 1, max_ng = 1;
+  std::vector<double2> w_host;  // host copy of d_w, for the kinds of its weight arrays
+  // WKIND_* of the n weights at d_w + off
+  int wkind(int64_t off, int n) const {
+    bool re = true, im = true;
+    for (int i = 0; i < n; ++i) {
+      re = re && w_host[off + i].y == 0.0;
+      im = im && w_host[off + i].x == 0.0;
+    }
+    return re ? WKIND_REAL : (im ? WKIND_IMAG : WKIND_COMPLEX);
+  }
   std::vector<int> rc_bl;  // band-limits whose tables are recomputed (not stored)
   bool rc(int bl) const { return std::find(rc_bl.begin(), rc_bl.end(), bl) != rc_bl.end(); }
   const WignerTable &table(int bl, int an) const { return wigner_table(bl, an, ss, rc(bl)); }
@@ -200,6 +210,7 @@ std::unique_ptr<WavPlan> build_plan(const PlanSpec &ps) {
   }
   P->npairs = (int)pairs.size();
   P->d_w = upload(w);
+  P->w_host = w;
   P->d_pairs = upload(pairs);
   for (auto &sd : P->sc) sd.d_ns = upload(sd.ns);
   // stored or recomputed tables: stored while the plan's tables fit the budget,
@@ -367,6 +378,7 @@ void sht_forward_once(const Sht &H, const void *f, int64_t fstride, double2 *flm
   a.iw = sw;
   a.imlo = mlo;
   a.w = H.cl;
+  a.wkind = WKIND_REAL;
   a.wscale = adjoint_of_inverse ? 1.0 : 2.0 * kPi / K;
   a.lmin = std::abs(s);
   a.y = flm;
@@ -393,6 +405,7 @@ void sht_inverse(const Sht &H, const double2 *flm, bool flm_half, void *f, int64
   a.xL = L;
   a.x_half = flm_half;
   a.w = H.cl;
+  a.wkind = WKIND_REAL;
   a.wscale = adjoint_of_forward ? 2.0 * kPi / K : 1.0;
   a.lmin = std::abs(s);
   a.out = spec;
@@ -541,6 +554,7 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
     a.xL = L;
     a.x_half = flm_half;
     a.w = P.d_w + P.w_phi;
+    a.wkind = P.wkind(P.w_phi, bs);
     a.wscale = adj ? 2.0 * kPi / Ks : 1.0;
     a.lmin = P.scal_lmin;
     a.out = spec;
@@ -582,9 +596,11 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
         a.x_half = flm_half;
         if (P.axisym) {
           a.w = P.d_w + sd.w_axi;
+          a.wkind = P.wkind(sd.w_axi, bl);
           a.wscale = adj ? 2.0 * kPi / K * kSqrt2Pi : 1.0 / kSqrt2Pi;
         } else {
           a.w = P.d_w + sd.w_split[i];
+          a.wkind = P.wkind(sd.w_split[i], bl);
           a.wscale = adj ? 4.0 * kPi * kPi / K : 1.0;
         }
         a.lmin = std::max((real || P.axisym) ? 0 : std::abs(P.s), sd.lsup_split[i]);
@@ -658,6 +674,7 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
     a.iw = sw;
     a.imlo = mlo;
     a.w = P.d_w + P.w_phi;
+    a.wkind = P.wkind(P.w_phi, bs);
     a.wscale = adj ? 1.0 : 2.0 * kPi / Ks;
     a.lmin = P.scal_lmin;
     a.y = zs;
@@ -724,6 +741,7 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
         a.imlo = -(bl - 1);
         if (P.axisym) {
           a.w = P.d_w + sd.w_axi;
+          a.wkind = P.wkind(sd.w_axi, bl);
           a.wscale = adj ? 1.0 / kSqrt2Pi : 2.0 * kPi / K * kSqrt2Pi;
           a.lmin = sd.lsup_merge[i];
         } else {
@@ -1140,9 +1158,15 @@ int host_batch(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool rea
     S2G_REQUIRE(nb >= 0, ERR_INVALID, "negative batch size");
     if (nb == 0) return;
     S2G_REQUIRE(px && wav && scal, ERR_INVALID, "NULL buffer");
+    // the copy stream has the highest priority: its copy kernels take SM
+    // slots as soon as the transforms free some
     static thread_local cudaStream_t sts[2] = {nullptr, nullptr};
-    for (auto &x : sts)
-      if (!x) S2G_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+    if (!sts[0]) S2G_CUDA(cudaStreamCreateWithFlags(&sts[0], cudaStreamNonBlocking));
+    if (!sts[1]) {
+      int least = 0, greatest = 0;
+      S2G_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      S2G_CUDA(cudaStreamCreateWithPriority(&sts[1], cudaStreamNonBlocking, greatest));
+    }
     cudaStream_t st = sts[0], cs = sts[1];
     const size_t esz = real ? sizeof(double) : sizeof(double2);
     s2let_parameters_t q = *p;

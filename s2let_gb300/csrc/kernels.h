@@ -40,6 +40,11 @@ void ring_inverse_c(const double2 *spec, int64_t spec_stride, int64_t spec_map_s
                     int mlo, bool herm, double2 *rings, int64_t ring_stride, int64_t map_stride, int rpm, int nrings,
                     int bl, int ss, cudaStream_t st);
 
+// Kind of a per-l weight array: every entry real, every entry imaginary, or
+// general complex.  The directional weights are a real profile times 1 or i
+// (odd or even N), the axisymmetric and scaling weights are real.
+enum { WKIND_COMPLEX = 0, WKIND_REAL = 1, WKIND_IMAG = 2 };
+
 struct L2T {
   const WignerTable *tb;
   int n;
@@ -52,6 +57,7 @@ struct L2T {
   const double2 *w;  // per-l weight (length >= bl) or nullptr
   double wscale;
   bool wconj;
+  int wkind;  // WKIND_* of w: lets the kernels multiply by a real or imaginary weight with 2 products
   int lmin;
   double2 *out;
   int64_t os;  // batch stride of out
@@ -80,6 +86,7 @@ struct T2L {
   const double2 *w;
   double wscale;
   bool wconj;
+  int wkind;  // WKIND_* of w
   int lmin;
   double2 *y;
   int64_t ys;

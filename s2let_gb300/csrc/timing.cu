@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "common.h"
+#include "runtime.h"
 #include "timing.h"
 
 namespace s2g {
@@ -22,7 +23,7 @@ size_t g_used = 0;
 // copy trace: one record per traced copy, events owned here
 struct CopyRec {
   cudaEvent_t a = nullptr, b = nullptr;
-  int d2h = 0;
+  int d2h = 0, by_kernel = 0;
   double bytes = 0;
 };
 std::atomic<bool> g_copy_on{false};
@@ -38,27 +39,28 @@ void clear_copies() {
 }
 }  // namespace
 
-void copy_async(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
-                cudaMemcpyKind kind, cudaStream_t st) {
-  if (width == 0 || height == 0) return;
+CopyMark copy_trace_begin(cudaMemcpyKind kind, double bytes, cudaStream_t st) {
+  CopyMark m;
+  if (!g_copy_on.load(std::memory_order_relaxed)) return m;
+  S2G_CUDA(cudaEventCreate(&m.a));
+  S2G_CUDA(cudaEventCreate(&m.b));
+  m.d2h = kind == cudaMemcpyDeviceToHost;
+  m.bytes = bytes;
+  S2G_CUDA(cudaEventRecord(m.a, st));
+  return m;
+}
+
+void copy_trace_end(const CopyMark &m, bool by_kernel, cudaStream_t st) {
+  if (!m.a) return;
+  S2G_CUDA(cudaEventRecord(m.b, st));
   CopyRec r;
-  const bool on = g_copy_on.load(std::memory_order_relaxed);
-  if (on) {
-    S2G_CUDA(cudaEventCreate(&r.a));
-    S2G_CUDA(cudaEventCreate(&r.b));
-    r.d2h = kind == cudaMemcpyDeviceToHost;
-    r.bytes = (double)width * (double)height;
-    S2G_CUDA(cudaEventRecord(r.a, st));
-  }
-  if (height == 1)
-    S2G_CUDA(cudaMemcpyAsync(dst, src, width, kind, st));
-  else
-    S2G_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, st));
-  if (on) {
-    S2G_CUDA(cudaEventRecord(r.b, st));
-    std::lock_guard<std::mutex> lk(g_copy_mu);
-    g_copies.push_back(r);
-  }
+  r.a = m.a;
+  r.b = m.b;
+  r.d2h = m.d2h;
+  r.by_kernel = by_kernel ? 1 : 0;
+  r.bytes = m.bytes;
+  std::lock_guard<std::mutex> lk(g_copy_mu);
+  g_copies.push_back(r);
 }
 
 bool timing_enabled() { return g_on.load(std::memory_order_relaxed); }
@@ -88,7 +90,72 @@ KTimer::~KTimer() {
 
 }  // namespace s2g
 
+// FMA throughput probe: every thread runs 8 independent FMA chains (enough to
+// hide the pipe latency at the occupancy launched), so the kernel is bound by
+// the FMA issue rate of the type T.  The chains' sum is stored only when it
+// equals an unreachable value, which keeps the compiler from removing them.
+template <class T>
+__global__ void __launch_bounds__(256) k_fma_chains(T *out, int iters, T a, T b) {
+  T x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = (T)(threadIdx.x + k);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = x[k] * a + b;  // one FMA (contraction on in device code)
+  }
+  T s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == (T)-1.2345e30) out[0] = s;
+}
+
+namespace s2g {
+namespace {
+template <class T>
+int fma_rate(int iters, double *tflops) {
+  int dev = 0, nsm = 0;
+  S2G_CUDA(cudaGetDevice(&dev));
+  S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  T *out = nullptr;
+  S2G_CUDA(cudaMalloc(&out, sizeof(T)));
+  cudaEvent_t e0, e1;
+  S2G_CUDA(cudaEventCreate(&e0));
+  S2G_CUDA(cudaEventCreate(&e1));
+  const int blocks = nsm * 8, threads = 256;
+  // |a| < 1 and b > 0: the chains converge to b / (1 - a), no overflow or subnormals
+  k_fma_chains<T><<<blocks, threads>>>(out, 16, (T)0.999, (T)0.001);  // warm-up
+  S2G_LAUNCHED();
+  S2G_CUDA(cudaEventRecord(e0));
+  k_fma_chains<T><<<blocks, threads>>>(out, iters, (T)0.999, (T)0.001);
+  S2G_CUDA(cudaEventRecord(e1));
+  S2G_CUDA(cudaEventSynchronize(e1));
+  S2G_LAUNCHED();
+  float ms = 0.f;
+  S2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *tflops = 2.0 * 8.0 * (double)blocks * threads * iters / (ms * 1e-3) / 1e12;
+  return 0;
+}
+}  // namespace
+}  // namespace s2g
+
 extern "C" {
+
+// Measured FMA throughput of this GPU (the denominators of the FP64 and FP32
+// roofline fractions): fp64 != 0 for FP64, else FP32; *tflops = 2 x FMAs / s
+// over one launch of `iters` iterations of 8 chains per thread.
+int s2let_gpu_fma_rate(int fp64, int iters, double *tflops) {
+  return s2g::guarded("s2let_gpu_fma_rate", [&] {
+    S2G_REQUIRE(iters > 0 && tflops != nullptr, s2g::ERR_INVALID, "iters must be positive, tflops not NULL");
+    s2g::ensure_device();
+    if (fp64)
+      s2g::fma_rate<double>(iters, tflops);
+    else
+      s2g::fma_rate<float>(iters, tflops);
+  });
+}
 
 // Switches timing on (clearing previous records) or off.
 int s2let_gpu_timing_enable(int on) {
@@ -126,13 +193,14 @@ int s2let_gpu_copy_trace_enable(int on) {
   return 0;
 }
 
-// out[d*4 + 0..3] for d = 0 (host to device), 1 (device to host): copies,
-// bytes, busy milliseconds (sum of the copies' own durations) and span
-// milliseconds (first copy start to last copy end of that direction).
-// Synchronises the recorded events; keeps the records.
+// out[d*5 + 0..4] for d = 0 (host to device), 1 (device to host): copies,
+// bytes, busy milliseconds (sum of the copies' own durations), span
+// milliseconds (first copy start to last copy end of that direction) and the
+// copies made by the copy kernel.  Synchronises the recorded events; keeps the
+// records.
 int s2let_gpu_copy_trace_report(double *out) {
   std::lock_guard<std::mutex> lk(s2g::g_copy_mu);
-  for (int i = 0; i < 8; ++i) out[i] = 0.0;
+  for (int i = 0; i < 10; ++i) out[i] = 0.0;
   if (s2g::g_copies.empty()) return 0;
   const cudaEvent_t t0 = s2g::g_copies[0].a;
   double lo[2] = {1e300, 1e300}, hi[2] = {-1e300, -1e300};
@@ -142,15 +210,16 @@ int s2let_gpu_copy_trace_report(double *out) {
     if (cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess || cudaEventElapsedTime(&sa, t0, r.a) != cudaSuccess ||
         cudaEventElapsedTime(&sb, t0, r.b) != cudaSuccess)
       return s2g::ERR_CUDA;
-    double *o = out + 4 * r.d2h;
+    double *o = out + 5 * r.d2h;
     o[0] += 1.0;
     o[1] += r.bytes;
     o[2] += ms;
+    o[4] += r.by_kernel;
     lo[r.d2h] = std::min(lo[r.d2h], (double)sa);
     hi[r.d2h] = std::max(hi[r.d2h], (double)sb);
   }
   for (int d = 0; d < 2; ++d)
-    if (out[4 * d] > 0) out[4 * d + 3] = hi[d] - lo[d];
+    if (out[5 * d] > 0) out[5 * d + 3] = hi[d] - lo[d];
   return 0;
 }
 

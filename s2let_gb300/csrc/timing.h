@@ -22,10 +22,23 @@ enum KCat {
 
 bool timing_enabled();
 
+// Copy trace (s2let_gpu_copy_trace_enable): while tracing is on, begin/end
+// record CUDA events on st around one host<->device copy of `bytes`; off, they
+// do nothing.
+struct CopyMark {
+  cudaEvent_t a = nullptr, b = nullptr;
+  int d2h = 0;
+  double bytes = 0;
+};
+CopyMark copy_trace_begin(cudaMemcpyKind kind, double bytes, cudaStream_t st);
+// by_kernel: the copy was made by the copy kernel (else by the copy engines)
+void copy_trace_end(const CopyMark &m, bool by_kernel, cudaStream_t st);
+
 // One host<->device copy of the host-pointer entry points (a plain copy when
-// height == 1, else pitched rows), asynchronous on st.  While copy tracing is
-// on (s2let_gpu_copy_trace_enable), CUDA events bracket the copy on st so its
-// duration and rate can be reported per direction.
+// height == 1, else `height` rows of `width` bytes at the given pitches),
+// asynchronous on st, traced as above (hostcopy.cu).  Host memory that the
+// GPU can address (page-locked, or any memory where the device accesses
+// pageable memory) is moved by a copy kernel; other memory by the copy engines.
 void copy_async(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
                 cudaMemcpyKind kind, cudaStream_t st);
 

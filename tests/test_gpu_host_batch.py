@@ -4,7 +4,9 @@ path, 1e-12): f_wav crosses the bus in pieces (one scale of a group of maps)
 on a second stream while the transforms run, device batches hold up to 32
 maps (40 maps make two), full-resolution (upsampled) layouts and single maps
 included, and the unused tail of f_wav (a scale with N_j < N) stays as the
-caller wrote it."""
+caller wrote it.  Pageable numpy buffers go through the copy engines;
+page-locked buffers (pinned=True) through the copy kernel, as the copy trace
+reports."""
 import ctypes as C
 
 import numpy as np
@@ -21,7 +23,8 @@ TOL = 1e-12
                                                     (16, 8, 0, True, 17, 0, 0), (16, 3, 0, True, 40, 0, 0),
                                                     (20, 4, 0, True, 6, 1, 0), (18, 3, 1, False, 5, 1, 0),
                                                     (16, 3, 0, True, 9, 0, 1), (12, 2, 2, False, 1, 0, 1)])
-def test_host_batch_equals_single_calls(gpu, L, N, spin, real, nb, ss, up):
+@pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "pinned"])
+def test_host_batch_equals_single_calls(gpu, L, N, spin, real, nb, ss, up, pinned):
     lib = gpu.lib
     p = make_parameters(L, 2.0, 1, N, 0 if real else spin, up, sampling_scheme=SAMPLING_MW_SS if ss else 0)
     s = gpu.sizes(p)
@@ -32,11 +35,29 @@ def test_host_batch_equals_single_calls(gpu, L, N, spin, real, nb, ss, up):
     f = np.ascontiguousarray(f.astype(dt))
     w = np.full(shape(s["n_wav"]), 7.0, dt)  # the unused tail must keep this
     sc = np.zeros(shape(s["n_scal"]), dt)
+    r = np.zeros_like(f)
+    keep = []
+    if pinned:  # the same arrays in page-locked memory
+        torch = pytest.importorskip("torch")
+
+        def pin(a):
+            t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+            keep.append(t)
+            v = t.numpy().view(a.dtype).reshape(a.shape)
+            v[...] = a
+            return v
+
+        f, w, sc, r = pin(f), pin(w), pin(sc), pin(r)
+    trace = (C.c_double * 10)()
+    lib.s2let_gpu_copy_trace_enable(1)
     fn = lib.s2let_gpu_analysis_px2wav_real_host_batch if real else lib.s2let_gpu_analysis_px2wav_host_batch
     assert fn(ptr(w), ptr(sc), ptr(f), nb, C.byref(p)) == 0
-    r = np.zeros_like(f)
     fn = lib.s2let_gpu_synthesis_wav2px_real_host_batch if real else lib.s2let_gpu_synthesis_wav2px_host_batch
     assert fn(ptr(r), ptr(w), ptr(sc), nb, C.byref(p)) == 0
+    assert lib.s2let_gpu_copy_trace_report(trace) == 0
+    lib.s2let_gpu_copy_trace_enable(0)
+    copies, by_kernel = trace[0] + trace[5], trace[4] + trace[9]
+    assert copies > 0 and by_kernel == (copies if pinned else 0)
     for b in range(nb):
         w1 = np.full(s["n_wav"], 7.0, dt)
         s1 = np.zeros(s["n_scal"], dt)
