@@ -7,9 +7,10 @@ One step = analysis (s2let_analysis_px2wav_real) and synthesis
 through the batched device-pointer entry points of libs2let_gpu.so.
 
 Prints one JSON line (rank 0).  Fields beyond the headline:
-  e2e           same metric through the host-pointer C ABI (batch extension; the drop-in
-                one-map calls beside it), host<->device
-                copies inside the timed region
+  e2e           same metric through the host-pointer C ABI (batch extension, the
+                synthesis of one batch on a second host thread while the next
+                batch's analysis runs; sequential calls and the drop-in one-map
+                calls beside it), host<->device copies inside the timed region
   roofline      dominant kernel, measured live with CUDA events on its stream
   cpu_baseline  the CPU oracle (C restatement of the reference path, OpenMP) on
                 the host cores, one map of the same workload
@@ -873,6 +874,50 @@ def main():
                     step_ms.append(1e3 * (time.perf_counter() - t1))
             return max_over_ranks((time.perf_counter() - t0) / steps, dist, dev)
 
+        # Pipelined calls: the synthesis of batch k runs on a second host thread
+        # while this thread runs the analysis of batch k+1 (two sets of host
+        # f_wav / f_scal buffers, alternating).  Each call keeps its own CUDA
+        # streams, so the two calls' transforms share the GPU and their f_wav
+        # copies use the two directions of the link at the same time.  The
+        # timed region holds every call of `steps` round trips, pipeline fill
+        # and drain included: the first analysis and the last synthesis run
+        # alone.  The result maps of every synthesis go to host memory.
+        wh2 = [wh, torch.empty((nb, nw), dtype=torch.float64, pin_memory=True)]
+        sh2 = [sh, torch.empty((nb, ns), dtype=torch.float64, pin_memory=True)]
+        prec = 1 if a.precision == "mixed" else 0
+        import concurrent.futures as cf
+
+        def synth_thread_init():
+            torch.cuda.set_device(local)
+            lib.s2let_gpu_set_precision(prec)  # per-thread setting
+
+        pool = cf.ThreadPoolExecutor(max_workers=1, initializer=synth_thread_init)
+        pipe_calls = []
+
+        def synth_call(k):
+            t0 = time.perf_counter()
+            rc = lib.s2let_gpu_synthesis_wav2px_real_host_batch(vp(frh), vp(wh2[k % 2]), vp(sh2[k % 2]), nb,
+                                                                C.byref(p))
+            pipe_calls.append(("synthesis", k, t0, time.perf_counter()))
+            if rc:
+                raise RuntimeError(lib.s2let_gpu_last_error_string().decode())
+
+        def pipelined(steps):
+            fut = None
+            for k in range(steps + 1):
+                if k >= 1:
+                    fut = pool.submit(synth_call, k - 1)
+                if k < steps:
+                    t0 = time.perf_counter()
+                    rc = lib.s2let_gpu_analysis_px2wav_real_host_batch(vp(wh2[k % 2]), vp(sh2[k % 2]), vp(fh), nb,
+                                                                       C.byref(p))
+                    pipe_calls.append(("analysis", k, t0, time.perf_counter()))
+                    if rc:
+                        raise RuntimeError(lib.s2let_gpu_last_error_string().decode())
+                if fut is not None:
+                    fut.result()
+                    fut = None
+
         # clocks sampled over the e2e steps as over the device-timed region
         # (GPU-idle gaps between copy-bound phases make P-state behaviour matter here)
         e2e_clocks = ClockSampler(local)
@@ -881,6 +926,23 @@ def main():
         e2e_clk = e2e_clocks.stop()
         lib.s2let_gpu_copy_trace_enable(0)
         timed_calls = calls[-2 * a.steps:]
+        seq_rt = float((frh - fh).abs().max() / fh.abs().max())
+        pipelined(1)  # warm-up: the second thread's streams and pool
+        frh.zero_()
+        pipe_calls.clear()
+        pipe_clocks = ClockSampler(local)
+        pipe_clocks.start()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        pipelined(a.steps)
+        pipe_s = max_over_ranks((time.perf_counter() - t0) / a.steps, dist, dev)
+        pipe_clk = pipe_clocks.stop()
+        pool.shutdown()
+        pipe_rt = float((frh - fh).abs().max() / fh.abs().max())
+        tp0 = min(c[2] for c in pipe_calls)
+        pipe_trace = [{"call": c[0], "batch": c[1], "start_ms": round(1e3 * (c[2] - tp0), 1),
+                       "ms": round(1e3 * (c[3] - c[2]), 1)} for c in sorted(pipe_calls, key=lambda c: c[2])]
 
         def call_stats(name):
             cs = [c for c in timed_calls if c["call"] == name]
@@ -889,18 +951,26 @@ def main():
                     "min_ms": min(c["ms"] for c in cs), "max_ms": max(c["ms"] for c in cs),
                     f"f_wav_{big}_GBps_median": statistics.median(c[big]["GBps"] for c in cs),
                     f"f_wav_{big}_GBps_min": min(c[big]["GBps"] for c in cs)}
-        e2e_rt = float((frh - fh).abs().max() / fh.abs().max())
         single_s = host_rate(e2e_single_step, max(1, min(a.steps, 2)))
-        e2e = {"value": whole_job_rate(nb, world, e2e_s), "unit": "maps/s",
+        e2e = {"value": whole_job_rate(nb, world, pipe_s), "unit": "maps/s",
                "h2d_bytes_per_step": nb * (npx + nw + ns) * 8, "d2h_bytes_per_step": nb * (nw + ns + npx) * 8,
                "api": "s2let_gpu_analysis_px2wav_real_host_batch + s2let_gpu_synthesis_wav2px_real_host_batch "
-                      f"({nb} maps per call, pinned host buffers)",
-               "max_rel_err_round_trip": e2e_rt,
-               "step_ms": [round(x, 1) for x in step_ms],
-               "per_call": {"analysis": call_stats("analysis"), "synthesis": call_stats("synthesis")},
-               "copy_trace": timed_calls,
-               "clocks": e2e_clk,
-               "median_step_value": whole_job_rate(nb, world, statistics.median(step_ms) / 1e3) if step_ms else None,
+                      f"({nb} maps per call, pinned host buffers); synthesis of batch k on a second host thread "
+                      "while the analysis of batch k+1 runs",
+               "timed": f"{a.steps} round trips of {nb} maps, pipeline fill and drain included",
+               "max_rel_err_round_trip": pipe_rt,
+               "calls": pipe_trace,
+               "clocks": pipe_clk,
+               "sequential_calls": {
+                   "value": whole_job_rate(nb, world, e2e_s), "unit": "maps/s",
+                   "what": "analysis then synthesis, one call at a time",
+                   "max_rel_err_round_trip": seq_rt,
+                   "step_ms": [round(x, 1) for x in step_ms],
+                   "per_call": {"analysis": call_stats("analysis"), "synthesis": call_stats("synthesis")},
+                   "copy_trace": timed_calls,
+                   "clocks": e2e_clk,
+                   "median_step_value": whole_job_rate(nb, world, statistics.median(step_ms) / 1e3)
+                   if step_ms else None},
                "dropin_one_map_per_call": {"value": whole_job_rate(nb, world, single_s), "unit": "maps/s",
                                            "api": "s2let_analysis_px2wav_real + s2let_synthesis_wav2px_real"}}
 
