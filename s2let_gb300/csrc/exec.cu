@@ -517,6 +517,14 @@ bool rings_on_n(const WavPlan &P, const Scale &sd) {
   return on_n < on_g;
 }
 
+// Whether some scale of the plan runs its ring and gamma DFTs as separate
+// launches through a ring buffer (the fused launch keeps them on chip).
+bool needs_ring_buffer(const WavPlan &P) {
+  for (const Scale &sd : P.sc)
+    if (!rings_on_n(P, sd) || !ring_gamma_fusable((int)sd.ns.size(), sd.ng)) return true;
+  return false;
+}
+
 // Scale ranges [k0, k1) that share one table pass (consecutive scales with the
 // same band-limit and directions), smallest band-limits first, or largest
 // first when `largest_first`.
@@ -569,7 +577,9 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
   const int64_t Wmax = 2 * P.max_bl - 1, Kmax = 2 * P.max_bl, ntmax = P.nt(P.max_bl);
   const int64_t gsz = (int64_t)nb * P.max_nn * ntmax * Wmax;
   double2 *Gbuf = S.get<double2>(2 * gsz);
-  double2 *spec = S.get<double2>((int64_t)nb * std::max(P.max_ng, P.max_nn) * ntmax * Kmax);
+  // ring buffers only for the scales whose ring and gamma DFTs are separate launches
+  double2 *spec = needs_ring_buffer(P) ? S.get<double2>((int64_t)nb * std::max(P.max_ng, P.max_nn) * ntmax * Kmax)
+                                       : nullptr;
   // with host copies the largest scales go first, so that most of f_wav can
   // cross the bus while the smaller scales are transformed
   const std::vector<std::pair<size_t, size_t>> passes = table_passes(P, pipe != nullptr);
@@ -625,6 +635,12 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
         for (int b0 = 0; b0 < nb; b0 += G) {
           const int nbg = std::min(G, nb - b0);
           const double2 *Gb = Gq + (int64_t)b0 * nn * nt * W;
+          if (ring_gamma_fusable(nn, ng)) {  // one launch, the n-components stay on chip
+            ring_inverse_gamma(Gb, (int64_t)nn * nt * W, (int64_t)nt * W, sd.ns, ng, real, c,
+                               out + (size_t)b0 * wstride * esz, wstride, nbg, bl, P.ss, S.st);
+            if (pipe) pipe->out(S.st, f_wav, wstride, sd.woff, b0, nbg);
+            continue;
+          }
           double2 *sb = spec + (int64_t)b0 * nn * nt * K;
           for (int i = 0; i < nn; ++i) {
             const bool herm = real && sd.ns[i] == 0;  // real signal, n = 0: only m >= 0 computed
@@ -685,7 +701,8 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
   const int64_t Wmax = 2 * P.max_bl - 1, Kmax = 2 * P.max_bl, ntmax = P.nt(P.max_bl);
   const int64_t gsz = (int64_t)nb * P.max_nn * ntmax * Wmax;
   double2 *Gbuf = S.get<double2>(2 * gsz);
-  double2 *spec = S.get<double2>((int64_t)nb * std::max(P.max_ng, P.max_nn) * ntmax * Kmax);
+  double2 *spec = needs_ring_buffer(P) ? S.get<double2>((int64_t)nb * std::max(P.max_ng, P.max_nn) * ntmax * Kmax)
+                                       : nullptr;
   // with host copies the largest scales go first (their pieces are queued
   // first, see merge_order), so that their ring DFTs run while the rest of
   // f_wav is still crossing the bus
@@ -709,6 +726,12 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
         for (int b0 = 0; b0 < nb; b0 += G) {
           const int nbg = std::min(G, nb - b0);
           if (pipe) pipe->wait(S.st, sd.woff, b0);
+          if (ring_gamma_fusable(nn, ng)) {  // one launch, the n-components stay on chip
+            gamma_ring_forward(in + (size_t)b0 * wstride * esz, wstride, sd.ns, ng, real, c,
+                               Gq + (int64_t)b0 * nn * nt * W, (int64_t)nn * nt * W, (int64_t)nt * W, nbg, bl, P.ss,
+                               S.st);
+            continue;
+          }
           double2 *sb = spec + (int64_t)b0 * nn * nt * K;
           gamma_px_analysis(in + (size_t)b0 * wstride * esz, wstride, sb, sd.d_ns, nn, ng, bl, P.ss, nbg, real, c,
                             S.st);

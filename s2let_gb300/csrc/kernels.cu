@@ -9,6 +9,9 @@
 //              their contiguous axis, coefficient tiles broadcast).
 //  k_gamma_*   DFT over the 2N-1 gamma samples of the rotation group.
 //  k_merge     harmonic tiling merge (lmn -> lm) fused over scales/directions.
+#include <cooperative_groups.h>
+
+#include <cmath>
 #include <map>
 #include <mutex>
 
@@ -57,6 +60,24 @@ struct RingArgs {
   int nrings, bl, K, P, logP;
   const double2 *chirp, *bhat, *tw;
   const float4 *chirp_df, *bhat_df, *tw_df;
+};
+
+namespace cg = cooperative_groups;
+
+// One launch of ring DFTs fused with the gamma DFT (k_ring_inverse_gamma_df,
+// k_gamma_ring_forward_df): NN <= kFuseMaxNN n-components per ring.
+constexpr int kFuseMaxNN = 8;
+constexpr int kFuseMaxTw = 128;
+struct GammaFuse {
+  const double2 *G;  // synthesis input: spectrum of component k of ring (b, t) at G + b gms + k gks + t W
+  double2 *Gout;     // analysis output, the same addressing (all m from -(bl-1))
+  int64_t gms, gks;
+  int W, nt;
+  int herm_k;  // real signals: the component with n = 0 (m >= 0 stored, at offset bl-1), else -1
+  void *fw;    // gamma slice g of ring (b, t) at fw + b fms + g npx + t K (double, or double2 unless real)
+  int64_t fms, npx;
+  int ng, real;
+  float4 tw[kFuseMaxTw];  // [g NN + k] double-float twiddles with their normalisation
 };
 
 // element offset of ring r (rings of a map are ring_stride apart, maps map_stride)
@@ -1016,6 +1037,172 @@ __global__ void k_gamma_px_anal_df(const void *__restrict__ in, int64_t in_ms, d
 }
 
 // ---------------------------------------------------------------------------
+// Ring DFTs and gamma DFT in one launch (split-precision path)
+//
+// The n-components F_k(t, p) (k < NN) of one theta-ring are transformed by a
+// thread-block cluster of NN CTAs, one per component, each with the padded
+// Bluestein buffer of the single-ring kernels (3 CTAs per SM, as there).  The
+// gamma DFT exchanges values between the components of a pixel through
+// distributed shared memory, so the n-components never go to HBM:
+//   synthesis: each CTA runs the inverse ring DFT of its component and leaves
+//              F_k(p) (double-float) in its buffer; after a cluster barrier
+//              each CTA computes the gamma slices f_g(p) of its share of the
+//              pixels from all NN buffers and writes them to f_wav.
+//   analysis:  each CTA reads the gamma slices of its share of the pixels,
+//              forms every component F_k(p), premultiplies by the chirp and
+//              stores it into CTA k's buffer; after a cluster barrier each CTA
+//              runs the forward ring DFT of its component and writes its
+//              spectrum.
+// One power-of-two scale per ring, the largest over the cluster (exchanged
+// through shared memory before the transforms), so the components combine
+// without rescaling.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int cluster_max_int(cg::cluster_group &cl, int *slot, int v, int nn) {
+  const int m = block_max_int(v);
+  if (threadIdx.x == 0) *slot = m;
+  cl.sync();
+  int r = 0;
+  for (int j = 0; j < nn; ++j) r = max(r, *cl.map_shared_rank(slot, j));
+  return r;
+}
+
+template <int NN, bool REAL>
+__global__ void __launch_bounds__(512, 3) k_ring_inverse_gamma_df(RingArgs a, GammaFuse gf) {
+  extern __shared__ float4 bufd[];
+  __shared__ int s_em, s_e;
+  cg::cluster_group cl = cg::this_cluster();
+  const int k = (int)cl.block_rank();
+  const int r = blockIdx.x / NN;
+  const int b = r / gf.nt, t = r - b * gf.nt;
+  const int K = a.K, P = a.P, logP = a.logP, bl = a.bl;
+  const bool herm = (k == gf.herm_k);
+  const int sw = herm ? bl : gf.W, mlo = herm ? 0 : -(bl - 1);
+  const double2 *s0 = gf.G + (int64_t)b * gf.gms + (int64_t)k * gf.gks + (int64_t)t * gf.W + (herm ? bl - 1 : 0);
+  int em = 0;
+  for (int c = threadIdx.x; c < sw; c += blockDim.x) em = emax2(em, s0[c]);
+  const int e = block_scale(cluster_max_int(cl, &s_em, em, NN));
+  if (threadIdx.x == 0) s_e = e;  // read back after the transforms: fewer live registers in them
+  for (int j = threadIdx.x; j < P; j += blockDim.x) {
+    float4 zz = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (j < K) {
+      const int m = (j < bl) ? j : j - K;
+      const int c = m - mlo;
+      if (c >= 0 && c < sw)
+        zz = dc_split(s0[c], e);
+      else if (herm && m < 0 && -m < sw)
+        zz = dc_conj(dc_split(s0[-m], e));
+      zz = dc_conj(dc_mul(zz, __ldg(&a.chirp_df[j])));
+    }
+    bufd[pd(brev(j, logP))] = zz;
+  }
+  __syncthreads();
+  fft_dit_df(bufd, a.tw_df, P, logP);
+  for (int q = threadIdx.x; q < P; q += blockDim.x) bufd[pd(q)] = dc_mul(bufd[pd(q)], __ldg(&a.bhat_df[q]));
+  __syncthreads();
+  ifft_dif_df(bufd, a.tw_df, P, logP);
+  // F_k(p) = c_p conj(y_p), in place (p -> brev(p) is one-to-one)
+  for (int p = threadIdx.x; p < K; p += blockDim.x) {
+    const int i = pd(brev(p, logP));
+    bufd[i] = dc_mul(__ldg(&a.chirp_df[p]), dc_conj(bufd[i]));
+  }
+  cl.sync();
+  // gamma slices of this CTA's share of the pixels
+  const int eo = s_e - logP;
+  const int kk = (int)cl.block_rank(), rr = blockIdx.x / NN;
+  const int bb = rr / gf.nt, tt = rr - bb * gf.nt;
+  const int chunk = (K + NN - 1) / NN;
+  const int p1 = min(K, (kk + 1) * chunk);
+  const int64_t obase = (int64_t)bb * gf.fms + (int64_t)tt * K;
+  for (int p = kk * chunk + threadIdx.x; p < p1; p += blockDim.x) {
+    const int i = pd(brev(p, logP));
+    float4 z[NN];
+#pragma unroll
+    for (int j = 0; j < NN; ++j) z[j] = *cl.map_shared_rank(bufd + i, j);
+    for (int g = 0; g < gf.ng; ++g) {
+      float2 re = make_float2(0.f, 0.f), im = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < NN; ++j) {
+        const float4 w = gf.tw[g * NN + j];
+        re = df_add(re, df_dot2(dre(w), dre(z[j]), df_neg(dim_(w)), dim_(z[j])));
+        if (!REAL) im = df_add(im, df_dot2(dre(w), dim_(z[j]), dim_(w), dre(z[j])));
+      }
+      const int64_t o = obase + (int64_t)g * gf.npx + p;
+      if (REAL)
+        ((double *)gf.fw)[o] = join_scaled(re.x, re.y, eo);
+      else
+        ((double2 *)gf.fw)[o] = make_double2(join_scaled(re.x, re.y, eo), join_scaled(im.x, im.y, eo));
+    }
+  }
+  cl.sync();  // peers read this buffer until here
+}
+
+template <int NN, bool REAL>
+__global__ void __launch_bounds__(512, 3) k_gamma_ring_forward_df(RingArgs a, GammaFuse gf) {
+  extern __shared__ float4 bufd[];
+  __shared__ int s_em, s_e;
+  cg::cluster_group cl = cg::this_cluster();
+  const int k = (int)cl.block_rank();
+  const int r = blockIdx.x / NN;
+  const int b = r / gf.nt, t = r - b * gf.nt;
+  const int K = a.K, P = a.P, logP = a.logP;
+  const int chunk = (K + NN - 1) / NN;
+  const int p0 = k * chunk, p1 = min(K, p0 + chunk);
+  const int64_t ibase = (int64_t)b * gf.fms + (int64_t)t * K;
+  int em = 0;
+  for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x)
+    for (int g = 0; g < gf.ng; ++g) {
+      const int64_t o = ibase + (int64_t)g * gf.npx + p;
+      if (REAL)
+        em = max(em, exp_field(((const double *)gf.fw)[o]));
+      else
+        em = emax2(em, ((const double2 *)gf.fw)[o]);
+    }
+  const int e = block_scale(cluster_max_int(cl, &s_em, em, NN));
+  if (threadIdx.x == 0) s_e = e;  // read back after the transforms: fewer live registers in them
+  // the zero padding of this CTA's own buffer
+  for (int j = K + threadIdx.x; j < P; j += blockDim.x) bufd[pd(brev(j, logP))] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+    float4 acc[NN];
+#pragma unroll
+    for (int j = 0; j < NN; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int g = 0; g < gf.ng; ++g) {
+      const int64_t o = ibase + (int64_t)g * gf.npx + p;
+      if (REAL) {
+        const float2 f = df_split(((const double *)gf.fw)[o], e);
+#pragma unroll
+        for (int j = 0; j < NN; ++j) {
+          const float4 w = gf.tw[g * NN + j];
+          acc[j] = dmk(df_add(dre(acc[j]), df_mul(dre(w), f)), df_add(dim_(acc[j]), df_mul(dim_(w), f)));
+        }
+      } else {
+        const float4 f = dc_split(((const double2 *)gf.fw)[o], e);
+#pragma unroll
+        for (int j = 0; j < NN; ++j) acc[j] = dc_add(acc[j], dc_mul(gf.tw[g * NN + j], f));
+      }
+    }
+    const float4 ch = __ldg(&a.chirp_df[p]);
+    const int i = pd(brev(p, logP));
+#pragma unroll
+    for (int j = 0; j < NN; ++j) *cl.map_shared_rank(bufd + i, j) = dc_mulc(acc[j], ch);
+  }
+  cl.sync();  // every component's buffer is complete
+  fft_dit_df(bufd, a.tw_df, P, logP);
+  for (int q = threadIdx.x; q < P; q += blockDim.x) bufd[pd(q)] = dc_mul(bufd[pd(q)], __ldg(&a.bhat_df[q]));
+  __syncthreads();
+  ifft_dif_df(bufd, a.tw_df, P, logP);
+  const int eo = s_e - logP;
+  const int kk = (int)cl.block_rank(), rr = blockIdx.x / NN;
+  const int bb = rr / gf.nt, tt = rr - bb * gf.nt;
+  double2 *out = gf.Gout + (int64_t)bb * gf.gms + (int64_t)kk * gf.gks + (int64_t)tt * gf.W;
+  for (int c = threadIdx.x; c < gf.W; c += blockDim.x) {
+    const int m = c - (a.bl - 1);
+    const int q = ((m % K) + K) % K;
+    out[c] = dc_to(dc_mulc(bufd[pd(brev(q, logP))], __ldg(&a.chirp_df[q])), eo);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // lmn -> lm merge
 // ---------------------------------------------------------------------------
 
@@ -1141,6 +1328,126 @@ void run_ring_inverse(const RingArgs &a, int nrings, bool real, cudaStream_t st)
     launch_ring(k_ring_inverse<false>, a, nblk, a.P, st);
   }
 }
+
+// Twiddles of the fused gamma DFT: synthesis c e^{i n_k gamma_g} (x2 for
+// n_k != 0 on real signals, which stand for the +-n pair), analysis
+// c e^{-i n_k gamma_g}; gamma_g = 2 pi g / ng, as double-float pairs.
+void fuse_twiddles(GammaFuse &gf, const std::vector<int> &ns, int ng, bool real, double c, bool synth) {
+  const int nn = (int)ns.size();
+  for (int g = 0; g < ng; ++g)
+    for (int k = 0; k < nn; ++k) {
+      const long double x = 2.0L * (long double)((ns[k] * g) % ng) / (long double)ng;  // angle / pi
+      const long double pi = 3.141592653589793238462643383279502884L;
+      const double f = synth ? ((real && ns[k] != 0) ? 2.0 * c : c) : c;
+      const double re = (double)(f * cosl(pi * x)), im = (double)((synth ? f : -f) * sinl(pi * x));
+      const float rh = (float)re, ih = (float)im;
+      gf.tw[g * nn + k] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+    }
+}
+
+template <class KF>
+void launch_fused(KF kernel, const RingArgs &a, const GammaFuse &gf, int nrings, int nn, cudaStream_t st) {
+  const size_t smem = sizeof(float4) * (a.P + a.P / 8);
+  if (smem > 48 * 1024) S2G_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(nrings * nn));
+  cfg.blockDim = dim3(ring_threads(a.P));
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)nn;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  S2G_CUDA(cudaLaunchKernelEx(&cfg, kernel, a, gf));
+  S2G_LAUNCHED();
+}
+
+}  // namespace
+
+bool ring_gamma_fusable(int nn, int ng) { return t_precision == 1 && nn >= 2 && nn <= kFuseMaxNN && ng * nn <= kFuseMaxTw; }
+
+void ring_inverse_gamma(const double2 *G, int64_t gms, int64_t gks, const std::vector<int> &ns, int ng, bool real,
+                        double c, void *fw, int64_t fms, int nb, int bl, int ss, cudaStream_t st) {
+  const int nn = (int)ns.size();
+  S2G_REQUIRE(ring_gamma_fusable(nn, ng), ERR_UNSUPPORTED, "fused ring/gamma DFT: unsupported direction count");
+  const int nt = grid_rings(bl, ss), nrings = nb * nt;
+  if (nrings <= 0) return;
+  const RingFFT &rf = ring_fft(grid_ring_len(bl, ss));
+  RingArgs a = ring_args(rf, bl, nrings);
+  GammaFuse gf{};
+  gf.G = G;
+  gf.gms = gms;
+  gf.gks = gks;
+  gf.W = 2 * bl - 1;
+  gf.nt = nt;
+  gf.herm_k = -1;
+  for (int k = 0; k < nn; ++k)
+    if (real && ns[k] == 0) gf.herm_k = k;
+  gf.fw = fw;
+  gf.fms = fms;
+  gf.npx = (int64_t)nt * a.K;
+  gf.ng = ng;
+  gf.real = real ? 1 : 0;
+  fuse_twiddles(gf, ns, ng, real, c, true);
+  const double px = (double)nrings * a.K;
+  KTimer kt(KC_RING, st, timing_enabled() ? ring_work(a, nrings * nn) + px * ng * nn * (real ? 24.0 : 48.0) : 0.0,
+            (double)nrings * nn * gf.W * 16.0 + px * ng * (real ? 8.0 : 16.0));
+  switch (nn) {
+#define S2G_FUSE(N)                                                              \
+  case N:                                                                        \
+    if (real)                                                                    \
+      launch_fused(k_ring_inverse_gamma_df<N, true>, a, gf, nrings, N, st);     \
+    else                                                                         \
+      launch_fused(k_ring_inverse_gamma_df<N, false>, a, gf, nrings, N, st);    \
+    break;
+    S2G_FUSE(2) S2G_FUSE(3) S2G_FUSE(4) S2G_FUSE(5) S2G_FUSE(6) S2G_FUSE(7) S2G_FUSE(8)
+#undef S2G_FUSE
+    default: break;
+  }
+}
+
+void gamma_ring_forward(const void *fw, int64_t fms, const std::vector<int> &ns, int ng, bool real, double c,
+                        double2 *Gout, int64_t gms, int64_t gks, int nb, int bl, int ss, cudaStream_t st) {
+  const int nn = (int)ns.size();
+  S2G_REQUIRE(ring_gamma_fusable(nn, ng), ERR_UNSUPPORTED, "fused ring/gamma DFT: unsupported direction count");
+  const int nt = grid_rings(bl, ss), nrings = nb * nt;
+  if (nrings <= 0) return;
+  const RingFFT &rf = ring_fft(grid_ring_len(bl, ss));
+  RingArgs a = ring_args(rf, bl, nrings);
+  GammaFuse gf{};
+  gf.Gout = Gout;
+  gf.gms = gms;
+  gf.gks = gks;
+  gf.W = 2 * bl - 1;
+  gf.nt = nt;
+  gf.herm_k = -1;
+  gf.fw = const_cast<void *>(fw);
+  gf.fms = fms;
+  gf.npx = (int64_t)nt * a.K;
+  gf.ng = ng;
+  gf.real = real ? 1 : 0;
+  fuse_twiddles(gf, ns, ng, real, c, false);
+  const double px = (double)nrings * a.K;
+  KTimer kt(KC_RING, st, timing_enabled() ? ring_work(a, nrings * nn) + px * ng * nn * (real ? 24.0 : 48.0) : 0.0,
+            (double)nrings * nn * gf.W * 16.0 + px * ng * (real ? 8.0 : 16.0));
+  switch (nn) {
+#define S2G_FUSE(N)                                                              \
+  case N:                                                                        \
+    if (real)                                                                    \
+      launch_fused(k_gamma_ring_forward_df<N, true>, a, gf, nrings, N, st);     \
+    else                                                                         \
+      launch_fused(k_gamma_ring_forward_df<N, false>, a, gf, nrings, N, st);    \
+    break;
+    S2G_FUSE(2) S2G_FUSE(3) S2G_FUSE(4) S2G_FUSE(5) S2G_FUSE(6) S2G_FUSE(7) S2G_FUSE(8)
+#undef S2G_FUSE
+    default: break;
+  }
+}
+
+namespace {
 
 }  // namespace
 

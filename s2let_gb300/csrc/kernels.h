@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "plan.h"
 
@@ -111,6 +112,23 @@ void gamma_px_synthesis(const double2 *F, void *out, int64_t out_ms, const int *
                         int ss, int nb, bool real, double c, cudaStream_t st);
 void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns, int nn, int ng, int bl, int ss,
                        int nb, bool real, double c, cudaStream_t st);
+
+// Ring DFTs fused with the gamma DFT in one launch (split precision; a
+// thread-block cluster per ring, one CTA per n-component), usable when
+// ring_gamma_fusable(nn, ng).  Component k of ring (b, t), t < nt, has its
+// spectrum at G + b gms + k gks + t W (W = 2bl-1, m from -(bl-1); on real
+// signals the component with n = 0 holds m >= 0 at offset bl-1, the rest by
+// Hermitian symmetry); gamma slice g of ring (b, t) lives at
+// fw + b fms + g npx + t K (npx = nt K; double when real, else double2).
+//   ring_inverse_gamma:  f_g = c sum_k e^{i n_k gamma_g} F_k (real: 2 Re for
+//                        n_k > 0, Re for n_k = 0), F_k the inverse ring DFT
+//   gamma_ring_forward:  F_k = c sum_g e^{-i n_k gamma_g} f_g, then the
+//                        forward ring DFT of every F_k to G (all m)
+bool ring_gamma_fusable(int nn, int ng);
+void ring_inverse_gamma(const double2 *G, int64_t gms, int64_t gks, const std::vector<int> &ns, int ng, bool real,
+                        double c, void *fw, int64_t fms, int nb, int bl, int ss, cudaStream_t st);
+void gamma_ring_forward(const void *fw, int64_t fms, const std::vector<int> &ns, int ng, bool real, double c,
+                        double2 *Gout, int64_t gms, int64_t gks, int nb, int bl, int ss, cudaStream_t st);
 
 // Merge of per-(scale, direction) Wigner coefficients into flm (lmn2lm):
 //   flm(l,m) = sum_pairs [ psi_p(l) z_p(l,m) + real&&n>0 : (-1)^{m+n} conj(z_p(l,-m)) psin_p(l) ]
