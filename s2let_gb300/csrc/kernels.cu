@@ -299,54 +299,93 @@ __device__ __forceinline__ double2 dc_to(float4 z, int e) {
 
 // Stages are paired (radix 2^2): one pass over shared memory and one barrier
 // per two radix-2 stages; a leftover single stage when log2 P is odd.
-// Shared-memory index i is stored at i + i/8 (one float4 of padding per 8),
-// which spreads the small-span strided accesses of the early stages over the banks.
-__device__ __forceinline__ int pd(int i) { return i + (i >> 3); }
+//
+// Shared-memory layout: element i of the P = 2^lg point buffer (16-byte
+// complex double-float values, no padding) lives at swz(i) = i ^ X(i), where
+// X(i) XORs bits 3-4 of i into bits 1-2, bits 3-5 into bits 0-2 and bits
+// lg-3..lg-1 into bits 0-2 (the last term only for lg > 6).  X depends only on
+// bits >= 3 and sets only bits 0-2, so swz is a bijection and its own inverse,
+// and it is linear over GF(2): swz(a ^ b) = swz(a) ^ swz(b).  Every access
+// pattern below (bit-reversed scatter and gather, the radix-2^2 passes at every
+// span, stride-4 and linear sweeps) then touches 8 distinct 16-byte bank groups
+// per quarter warp for P >= 256 (checked by enumerating the patterns on the
+// CPU), without the 1/8 padding a skewed layout needs: a 4096-point buffer
+// takes 64 KB, which leaves room in L1 for the twiddle table.
+struct Swz {
+  int top;  // lg - 3 when lg > 6, else 31 (the term vanishes for non-negative i)
+};
+__device__ __forceinline__ Swz swz_of(int logP) { return Swz{logP > 6 ? logP - 3 : 31}; }
+__device__ __forceinline__ int swz(int i, Swz z) {
+  return i ^ ((i >> 2) & 6) ^ ((i >> 3) & 7) ^ ((i >> z.top) & 7);
+}
 __device__ __forceinline__ float4 dc_mul_mi(float4 a) { return make_float4(a.z, a.w, -a.x, -a.y); }  // a * (-i)
 __device__ __forceinline__ float4 dc_mul_pi(float4 a) { return make_float4(-a.z, -a.w, a.x, a.y); }  // a * (+i)
+
+// Read-only table loads with an L1 eviction priority: the twiddle table is
+// read by every pass of every ring on the SM (kept: evict_last); the chirp and
+// the chirp-kernel spectrum are read once per ring (evict_first).
+__device__ __forceinline__ float4 ld_keep(const float4 *p) {
+  float4 v;
+  asm("ld.global.nc.L1::evict_last.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float4 ld_once(const float4 *p) {
+  float4 v;
+  asm("ld.global.nc.L1::evict_first.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p));
+  return v;
+}
 
 // bit-reversed input, natural output, forward transform (w = e^{-2 pi i k / P}).
 // The input is zero-padded past P/2 (the Bluestein sequences have K <= P/2
 // values), i.e. zero at every odd bit-reversed position, and the first two
 // stages have unit twiddles: that pass is a 4-point DFT of (a0, 0, a2, 0).
+// In every pass the four points p0 + c h (c < 4) differ from p0 only in bits
+// that are zero in p0, so their buffer slots are swz(p0) ^ swz(c h).
 __device__ void fft_dit_df(float4 *buf, const float4 *__restrict__ tw, int P, int logP) {
+  const Swz z = swz_of(logP);
   for (int i = threadIdx.x; i < P / 4; i += blockDim.x) {
-    const int p0 = 4 * i;
-    const float4 a0 = buf[pd(p0)], a2 = buf[pd(p0 + 2)], a2m = dc_mul_mi(a2);
-    buf[pd(p0)] = dc_add(a0, a2);
-    buf[pd(p0 + 2)] = dc_sub(a0, a2);
-    buf[pd(p0 + 1)] = dc_add(a0, a2m);
-    buf[pd(p0 + 3)] = dc_sub(a0, a2m);
+    const int b = swz(4 * i, z);
+    const float4 a0 = buf[b], a2 = buf[b ^ 2], a2m = dc_mul_mi(a2);
+    buf[b] = dc_add(a0, a2);
+    buf[b ^ 2] = dc_sub(a0, a2);
+    buf[b ^ 1] = dc_add(a0, a2m);
+    buf[b ^ 3] = dc_sub(a0, a2m);
   }
   __syncthreads();
   int s = 3;
   for (; s + 1 <= logP; s += 2) {
     const int h = 1 << (s - 1);
+    const int q1 = swz(h, z), q2 = swz(2 * h, z), q3 = swz(3 * h, z);
     for (int i = threadIdx.x; i < P / 4; i += blockDim.x) {
       const int jp = i & (h - 1);
-      const int p0 = ((i >> (s - 1)) << (s + 1)) + jp;
-      const float4 w1 = __ldg(&tw[jp << (logP - s)]);
-      const float4 w2 = __ldg(&tw[jp << (logP - s - 1)]);
-      const float4 a0 = buf[pd(p0)], a1 = buf[pd(p0 + h)], a2 = buf[pd(p0 + 2 * h)], a3 = buf[pd(p0 + 3 * h)];
+      const int b = swz(((i >> (s - 1)) << (s + 1)) + jp, z);
+      const float4 w1 = ld_keep(&tw[jp << (logP - s)]);
+      const float4 w2 = ld_keep(&tw[jp << (logP - s - 1)]);
+      const float4 a0 = buf[b], a1 = buf[b ^ q1], a2 = buf[b ^ q2], a3 = buf[b ^ q3];
       const float4 t1 = dc_mul(a1, w1), t3 = dc_mul(a3, w1);
       const float4 b0 = dc_add(a0, t1), b1 = dc_sub(a0, t1), b2 = dc_add(a2, t3), b3 = dc_sub(a2, t3);
       const float4 u2 = dc_mul(b2, w2), u3 = dc_mul_mi(dc_mul(b3, w2));
-      buf[pd(p0)] = dc_add(b0, u2);
-      buf[pd(p0 + 2 * h)] = dc_sub(b0, u2);
-      buf[pd(p0 + h)] = dc_add(b1, u3);
-      buf[pd(p0 + 3 * h)] = dc_sub(b1, u3);
+      buf[b] = dc_add(b0, u2);
+      buf[b ^ q2] = dc_sub(b0, u2);
+      buf[b ^ q1] = dc_add(b1, u3);
+      buf[b ^ q3] = dc_sub(b1, u3);
     }
     __syncthreads();
   }
   if (s == logP) {
     const int half = 1 << (s - 1);
+    const int qh = swz(half, z);
     for (int i = threadIdx.x; i < P / 2; i += blockDim.x) {
       const int j = i & (half - 1);
-      const int i0 = ((i >> (s - 1)) << s) + j, i1 = i0 + half;
-      const float4 w = __ldg(&tw[j << (logP - s)]);
-      const float4 u = buf[pd(i0)], v = dc_mul(buf[pd(i1)], w);
-      buf[pd(i0)] = dc_add(u, v);
-      buf[pd(i1)] = dc_sub(u, v);
+      const int b = swz(((i >> (s - 1)) << s) + j, z);
+      const float4 w = ld_keep(&tw[j << (logP - s)]);
+      const float4 u = buf[b], v = dc_mul(buf[b ^ qh], w);
+      buf[b] = dc_add(u, v);
+      buf[b ^ qh] = dc_sub(u, v);
     }
     __syncthreads();
   }
@@ -356,37 +395,53 @@ __device__ void fft_dit_df(float4 *buf, const float4 *__restrict__ tw, int P, in
 // produced: the Bluestein result needs K <= P/2 of them.  The last pass has
 // unit twiddles.
 __device__ void ifft_dif_df(float4 *buf, const float4 *__restrict__ tw, int P, int logP) {
+  const Swz z = swz_of(logP);
   int s = logP;
   for (; s >= 3; s -= 2) {
     const int h = 1 << (s - 2);
+    const int q1 = swz(h, z), q2 = swz(2 * h, z), q3 = swz(3 * h, z);
     for (int i = threadIdx.x; i < P / 4; i += blockDim.x) {
       const int jp = i & (h - 1);
-      const int p0 = ((i >> (s - 2)) << s) + jp;
-      const float4 c2 = __ldg(&tw[jp << (logP - s)]);
-      const float4 c1 = __ldg(&tw[jp << (logP - s + 1)]);
-      const float4 a0 = buf[pd(p0)], a1 = buf[pd(p0 + h)], a2 = buf[pd(p0 + 2 * h)], a3 = buf[pd(p0 + 3 * h)];
+      const int b = swz(((i >> (s - 2)) << s) + jp, z);
+      const float4 c2 = ld_keep(&tw[jp << (logP - s)]);
+      const float4 c1 = ld_keep(&tw[jp << (logP - s + 1)]);
+      const float4 a0 = buf[b], a1 = buf[b ^ q1], a2 = buf[b ^ q2], a3 = buf[b ^ q3];
       const float4 b0 = dc_add(a0, a2), b1 = dc_add(a1, a3);
       const float4 b2 = dc_mulc(dc_sub(a0, a2), c2), b3 = dc_mul_pi(dc_mulc(dc_sub(a1, a3), c2));
-      buf[pd(p0)] = dc_add(b0, b1);
-      buf[pd(p0 + h)] = dc_mulc(dc_sub(b0, b1), c1);
-      buf[pd(p0 + 2 * h)] = dc_add(b2, b3);
-      buf[pd(p0 + 3 * h)] = dc_mulc(dc_sub(b2, b3), c1);
+      buf[b] = dc_add(b0, b1);
+      buf[b ^ q1] = dc_mulc(dc_sub(b0, b1), c1);
+      buf[b ^ q2] = dc_add(b2, b3);
+      buf[b ^ q3] = dc_mulc(dc_sub(b2, b3), c1);
     }
     __syncthreads();
   }
   if (s == 2) {  // stages 2 and 1, unit twiddles, even outputs only
     for (int i = threadIdx.x; i < P / 4; i += blockDim.x) {
-      const int p0 = 4 * i;
-      const float4 a0 = buf[pd(p0)], a1 = buf[pd(p0 + 1)], a2 = buf[pd(p0 + 2)], a3 = buf[pd(p0 + 3)];
-      buf[pd(p0)] = dc_add(dc_add(a0, a2), dc_add(a1, a3));
-      buf[pd(p0 + 2)] = dc_add(dc_sub(a0, a2), dc_mul_pi(dc_sub(a1, a3)));
+      const int b = swz(4 * i, z);
+      const float4 a0 = buf[b], a1 = buf[b ^ 1], a2 = buf[b ^ 2], a3 = buf[b ^ 3];
+      buf[b] = dc_add(dc_add(a0, a2), dc_add(a1, a3));
+      buf[b ^ 2] = dc_add(dc_sub(a0, a2), dc_mul_pi(dc_sub(a1, a3)));
     }
     __syncthreads();
   } else if (s == 1) {
-    for (int i = threadIdx.x; i < P / 2; i += blockDim.x) buf[pd(2 * i)] = dc_add(buf[pd(2 * i)], buf[pd(2 * i + 1)]);
+    for (int i = threadIdx.x; i < P / 2; i += blockDim.x) {
+      const int b = swz(2 * i, z);
+      buf[b] = dc_add(buf[b], buf[b ^ 1]);
+    }
     __syncthreads();
   }
 }
+// pointwise product with the chirp-kernel spectrum (every slot, any order)
+__device__ __forceinline__ void kernel_multiply_df(float4 *buf, const float4 *__restrict__ bhat, int P, int logP) {
+  const Swz z = swz_of(logP);
+  for (int k = threadIdx.x; k < P; k += blockDim.x) {
+    const int b = swz(k, z);
+    buf[b] = dc_mul(buf[b], ld_once(&bhat[k]));
+  }
+  __syncthreads();
+}
+// buffer slot of bit-reversed position k
+__device__ __forceinline__ int slot_brev(int k, int logP) { return swz(brev(k, logP), swz_of(logP)); }
 
 // block-wide max of an int (blockDim.x <= 1024)
 __device__ int block_max_int(int v) {
@@ -428,14 +483,13 @@ __global__ void __launch_bounds__(512, 3) k_ring_forward_df(RingArgs a) {
       } else {
         v = ((const double2 *)a.rings)[ring_base(a, r0) + j];
       }
-      z = dc_mulc(dc_split(v, e), __ldg(&a.chirp_df[j]));
+      z = dc_mulc(dc_split(v, e), ld_once(&a.chirp_df[j]));
     }
-    bufd[pd(brev(j, logP))] = z;
+    bufd[slot_brev(j, logP)] = z;
   }
   __syncthreads();
   fft_dit_df(bufd, a.tw_df, P, logP);
-  for (int k = threadIdx.x; k < P; k += blockDim.x) bufd[pd(k)] = dc_mul(bufd[pd(k)], __ldg(&a.bhat_df[k]));
-  __syncthreads();
+  kernel_multiply_df(bufd, a.bhat_df, P, logP);
   ifft_dif_df(bufd, a.tw_df, P, logP);
   const int eo = e - logP;  // undo the ring scaling and the 1/P of the unnormalised transforms
   if (!REAL) {
@@ -443,14 +497,14 @@ __global__ void __launch_bounds__(512, 3) k_ring_forward_df(RingArgs a) {
     for (int c = threadIdx.x; c < a.sw; c += blockDim.x) {
       const int m = a.mlo + c;
       const int k = ((m % K) + K) % K;
-      out[c] = dc_to(dc_mulc(bufd[pd(brev(k, logP))], __ldg(&a.chirp_df[k])), eo);
+      out[c] = dc_to(dc_mulc(bufd[slot_brev(k, logP)], ld_once(&a.chirp_df[k])), eo);
     }
   } else {
     double2 *out0 = a.spec_out + spec_base(a, r0);
     for (int m = threadIdx.x; m < a.sw; m += blockDim.x) {
       const int km = (K - m) % K;
-      const float4 zm = dc_mulc(bufd[pd(brev(m, logP))], __ldg(&a.chirp_df[m]));
-      const float4 zc = dc_conj(dc_mulc(bufd[pd(brev(km, logP))], __ldg(&a.chirp_df[km])));
+      const float4 zm = dc_mulc(bufd[slot_brev(m, logP)], ld_once(&a.chirp_df[m]));
+      const float4 zc = dc_conj(dc_mulc(bufd[slot_brev(km, logP)], ld_once(&a.chirp_df[km])));
       // A = (Z_m + conj Z_{-m})/2,  B = (Z_m - conj Z_{-m})/(2i)
       const double2 s = dc_to(dc_add(zm, zc), eo - 1);
       out0[m] = s;
@@ -501,18 +555,17 @@ __global__ void __launch_bounds__(512, 3) k_ring_inverse_df(RingArgs a) {
     }
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
     // inverse DFT = conj(forward(conj z)):  a_j = conj(z_j) conj(c_j)
-    if (j < K) v = dc_conj(dc_mul(zz, __ldg(&a.chirp_df[j])));
-    bufd[pd(brev(j, logP))] = v;
+    if (j < K) v = dc_conj(dc_mul(zz, ld_once(&a.chirp_df[j])));
+    bufd[slot_brev(j, logP)] = v;
   }
   __syncthreads();
   fft_dit_df(bufd, a.tw_df, P, logP);
-  for (int k = threadIdx.x; k < P; k += blockDim.x) bufd[pd(k)] = dc_mul(bufd[pd(k)], __ldg(&a.bhat_df[k]));
-  __syncthreads();
+  kernel_multiply_df(bufd, a.bhat_df, P, logP);
   ifft_dif_df(bufd, a.tw_df, P, logP);
   const int eo = e - logP;
   for (int p = threadIdx.x; p < K; p += blockDim.x) {
     // f_p = c_p conj(y_p)
-    const double2 f = dc_to(dc_mul(__ldg(&a.chirp_df[p]), dc_conj(bufd[pd(brev(p, logP))])), eo);
+    const double2 f = dc_to(dc_mul(ld_once(&a.chirp_df[p]), dc_conj(bufd[slot_brev(p, logP)])), eo);
     if (REAL) {
       ((double *)a.rings_out)[ring_base(a, r0) + p] = f.x;
       if (has1) ((double *)a.rings_out)[ring_base(a, r0 + 1) + p] = f.y;
@@ -1092,19 +1145,18 @@ __global__ void __launch_bounds__(512, 3) k_ring_inverse_gamma_df(RingArgs a, Ga
         zz = dc_split(s0[c], e);
       else if (herm && m < 0 && -m < sw)
         zz = dc_conj(dc_split(s0[-m], e));
-      zz = dc_conj(dc_mul(zz, __ldg(&a.chirp_df[j])));
+      zz = dc_conj(dc_mul(zz, ld_once(&a.chirp_df[j])));
     }
-    bufd[pd(brev(j, logP))] = zz;
+    bufd[slot_brev(j, logP)] = zz;
   }
   __syncthreads();
   fft_dit_df(bufd, a.tw_df, P, logP);
-  for (int q = threadIdx.x; q < P; q += blockDim.x) bufd[pd(q)] = dc_mul(bufd[pd(q)], __ldg(&a.bhat_df[q]));
-  __syncthreads();
+  kernel_multiply_df(bufd, a.bhat_df, P, logP);
   ifft_dif_df(bufd, a.tw_df, P, logP);
   // F_k(p) = c_p conj(y_p), in place (p -> brev(p) is one-to-one)
   for (int p = threadIdx.x; p < K; p += blockDim.x) {
-    const int i = pd(brev(p, logP));
-    bufd[i] = dc_mul(__ldg(&a.chirp_df[p]), dc_conj(bufd[i]));
+    const int i = slot_brev(p, logP);
+    bufd[i] = dc_mul(ld_once(&a.chirp_df[p]), dc_conj(bufd[i]));
   }
   cl.sync();
   // gamma slices of this CTA's share of the pixels
@@ -1115,7 +1167,7 @@ __global__ void __launch_bounds__(512, 3) k_ring_inverse_gamma_df(RingArgs a, Ga
   const int p1 = min(K, (kk + 1) * chunk);
   const int64_t obase = (int64_t)bb * gf.fms + (int64_t)tt * K;
   for (int p = kk * chunk + threadIdx.x; p < p1; p += blockDim.x) {
-    const int i = pd(brev(p, logP));
+    const int i = slot_brev(p, logP);
     float4 z[NN];
 #pragma unroll
     for (int j = 0; j < NN; ++j) z[j] = *cl.map_shared_rank(bufd + i, j);
@@ -1161,7 +1213,7 @@ __global__ void __launch_bounds__(512, 3) k_gamma_ring_forward_df(RingArgs a, Ga
   const int e = block_scale(cluster_max_int(cl, &s_em, em, NN));
   if (threadIdx.x == 0) s_e = e;  // read back after the transforms: fewer live registers in them
   // the zero padding of this CTA's own buffer
-  for (int j = K + threadIdx.x; j < P; j += blockDim.x) bufd[pd(brev(j, logP))] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int j = K + threadIdx.x; j < P; j += blockDim.x) bufd[slot_brev(j, logP)] = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
     float4 acc[NN];
 #pragma unroll
@@ -1181,15 +1233,14 @@ __global__ void __launch_bounds__(512, 3) k_gamma_ring_forward_df(RingArgs a, Ga
         for (int j = 0; j < NN; ++j) acc[j] = dc_add(acc[j], dc_mul(gf.tw[g * NN + j], f));
       }
     }
-    const float4 ch = __ldg(&a.chirp_df[p]);
-    const int i = pd(brev(p, logP));
+    const float4 ch = ld_once(&a.chirp_df[p]);
+    const int i = slot_brev(p, logP);
 #pragma unroll
     for (int j = 0; j < NN; ++j) *cl.map_shared_rank(bufd + i, j) = dc_mulc(acc[j], ch);
   }
   cl.sync();  // every component's buffer is complete
   fft_dit_df(bufd, a.tw_df, P, logP);
-  for (int q = threadIdx.x; q < P; q += blockDim.x) bufd[pd(q)] = dc_mul(bufd[pd(q)], __ldg(&a.bhat_df[q]));
-  __syncthreads();
+  kernel_multiply_df(bufd, a.bhat_df, P, logP);
   ifft_dif_df(bufd, a.tw_df, P, logP);
   const int eo = s_e - logP;
   const int kk = (int)cl.block_rank(), rr = blockIdx.x / NN;
@@ -1198,7 +1249,7 @@ __global__ void __launch_bounds__(512, 3) k_gamma_ring_forward_df(RingArgs a, Ga
   for (int c = threadIdx.x; c < gf.W; c += blockDim.x) {
     const int m = c - (a.bl - 1);
     const int q = ((m % K) + K) % K;
-    out[c] = dc_to(dc_mulc(bufd[pd(brev(q, logP))], __ldg(&a.chirp_df[q])), eo);
+    out[c] = dc_to(dc_mulc(bufd[slot_brev(q, logP)], ld_once(&a.chirp_df[q])), eo);
   }
 }
 
@@ -1277,10 +1328,23 @@ __global__ void k_axpby(const double *x, int64_t xs, double *y, int64_t ys, int6
 
 namespace {
 
+// Shared memory of the ring kernels: one P-point buffer of 16-byte values.
+// The double-float kernels (3 CTAs per SM) ask for a carveout just large
+// enough for three buffers, so that the rest of the SM's L1 keeps the twiddle
+// table (32 KB at P = 4096).
+void ring_smem_attrs(const void *kernel, size_t smem, bool df) {
+  if (smem > 48 * 1024) S2G_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (df) {
+    constexpr double kMaxSmemPerSm = 228.0 * 1024.0;
+    const int pct = std::min(100, (int)std::ceil(100.0 * 3.0 * (double)(smem + 2048) / kMaxSmemPerSm) + 1);
+    S2G_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+  }
+}
+
 template <class KF>
-void launch_ring(KF kernel, const RingArgs &a, int nblk, int P, cudaStream_t st, bool padded = false) {
-  const size_t smem = sizeof(double2) * (padded ? P + P / 8 : P);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+void launch_ring(KF kernel, const RingArgs &a, int nblk, int P, cudaStream_t st, bool df = false) {
+  const size_t smem = sizeof(double2) * (size_t)P;
+  ring_smem_attrs((const void *)kernel, smem, df);
   kernel<<<nblk, ring_threads(P), smem, st>>>(a);
   S2G_LAUNCHED();
 }
@@ -1347,8 +1411,8 @@ void fuse_twiddles(GammaFuse &gf, const std::vector<int> &ns, int ng, bool real,
 
 template <class KF>
 void launch_fused(KF kernel, const RingArgs &a, const GammaFuse &gf, int nrings, int nn, cudaStream_t st) {
-  const size_t smem = sizeof(float4) * (a.P + a.P / 8);
-  if (smem > 48 * 1024) S2G_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t smem = sizeof(float4) * (size_t)a.P;
+  ring_smem_attrs((const void *)kernel, smem, true);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(nrings * nn));
   cfg.blockDim = dim3(ring_threads(a.P));
