@@ -927,7 +927,7 @@ def main():
         lib.s2let_gpu_copy_trace_enable(0)
         timed_calls = calls[-2 * a.steps:]
         seq_rt = float((frh - fh).abs().max() / fh.abs().max())
-        pipelined(1)  # warm-up: the second thread's streams and pool
+        pipelined(2)  # warm-up: the second thread's streams, both host buffer sets, two calls at once
         frh.zero_()
         pipe_calls.clear()
         pipe_clocks = ClockSampler(local)

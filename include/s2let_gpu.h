@@ -524,6 +524,45 @@ int s2let_gpu_analysis_adjoint_wav2px_batch(void *f, const void *f_wav, const vo
 int s2let_gpu_synthesis_adjoint_px2wav_batch(void *f_wav, void *f_scal, const void *f, int nbatch,
                                              const s2let_parameters_t *parameters, void *stream);
 
+/*
+ * FP32 storage (configurations that keep maps and wavelet coefficients in
+ * single precision).  The batched device-pointer entry points above with
+ * `float` maps, f_wav and f_scal (complex signals as interleaved float
+ * pairs), the same strides in elements.  Inputs are widened to FP64 on the
+ * device, the transforms run as in the FP64-storage path at the precision set
+ * by s2let_gpu_set_precision, and outputs are rounded to FP32 (so the results
+ * are the FP64-storage results rounded, about 6e-8 relative).  Only the used
+ * part of each f_wav row is read or written.  Device scratch: the FP64 copies
+ * of the batch.  Asynchronous on `stream`; returns the status.  No counterpart
+ * in the reference (its transforms take double arrays only).
+ */
+int s2let_gpu_analysis_px2wav_real_batch_f32(float *f_wav, float *f_scal, const float *f, int nbatch,
+                                             const s2let_parameters_t *parameters, void *stream);
+int s2let_gpu_synthesis_wav2px_real_batch_f32(float *f, const float *f_wav, const float *f_scal, int nbatch,
+                                              const s2let_parameters_t *parameters, void *stream);
+int s2let_gpu_analysis_px2wav_batch_f32(void *f_wav, void *f_scal, const void *f, int nbatch,
+                                        const s2let_parameters_t *parameters, void *stream);
+int s2let_gpu_synthesis_wav2px_batch_f32(void *f, const void *f_wav, const void *f_scal, int nbatch,
+                                         const s2let_parameters_t *parameters, void *stream);
+int s2let_gpu_analysis_adjoint_wav2px_real_batch_f32(float *f, const float *f_wav, const float *f_scal,
+                                                     int nbatch, const s2let_parameters_t *parameters,
+                                                     void *stream);
+int s2let_gpu_synthesis_adjoint_px2wav_real_batch_f32(float *f_wav, float *f_scal, const float *f, int nbatch,
+                                                      const s2let_parameters_t *parameters, void *stream);
+int s2let_gpu_analysis_adjoint_wav2px_batch_f32(void *f, const void *f_wav, const void *f_scal, int nbatch,
+                                                const s2let_parameters_t *parameters, void *stream);
+int s2let_gpu_synthesis_adjoint_px2wav_batch_f32(void *f_wav, void *f_scal, const void *f, int nbatch,
+                                                 const s2let_parameters_t *parameters, void *stream);
+/* s2let_gpu_px2wav_multi / s2let_gpu_wav2px_multi with FP32 storage: every
+ * map's f, f_wav and f_scal are float arrays (device pointers), widened into
+ * FP64 batch scratch and rounded back, inside the CUDA graph when use_graph. */
+int s2let_gpu_px2wav_multi_f32(void *const *f_wav, void *const *f_scal, void *const *f,
+                               const s2let_parameters_t *params, const int *real, int nmaps, int use_graph,
+                               void *stream);
+int s2let_gpu_wav2px_multi_f32(void *const *f, void *const *f_wav, void *const *f_scal,
+                               const s2let_parameters_t *params, const int *real, int nmaps, int use_graph,
+                               void *stream);
+
 /* Reads and clears the device-side fault flag of the split-precision
  * tensor-core contraction: non-zero when one of its bounded waits expired since
  * the last call (the affected outputs are invalid).  0 when all went well. */
@@ -563,6 +602,23 @@ int s2let_gpu_timing_report(double *out, int ncat);
  * copy when S2LET_GPU_HOST_COPY=engine, by the copy engines. */
 int s2let_gpu_copy_trace_enable(int on);
 int s2let_gpu_copy_trace_report(double *out);
+
+/* Autotuning of launch shapes (maps per CTA of the FP64 and recomputed-table
+ * contractions; columns per table pass and map groups per launch of the
+ * split-precision contraction).  mode 1: the first call of each (kernel,
+ * band-limit bucket, batch bucket) times the candidates on the live call and
+ * keeps the fastest, which later calls use; the choices are kept in a cache
+ * file per GPU model (S2LET_GPU_AUTOTUNE_CACHE, else
+ * $XDG_CACHE_HOME/s2let_gb300/autotune.txt or ~/.cache/...) and read by later
+ * processes.  mode 0 (default, or S2LET_GPU_AUTOTUNE unset): built-in
+ * choices.  Every candidate computes the same result.  Returns the previous
+ * mode.  entries() lists the recorded choices: keys[5 i..5 i + 4] = {family,
+ * a, b, c, choice} (family 1 FP64 contraction, 2 / 3 recomputed l->t / t->l,
+ * 4 split precision), ms[2 i], ms[2 i + 1] = {best, built-in} milliseconds;
+ * returns the number of choices (at most max written).  No counterpart in the
+ * reference. */
+int s2let_gpu_autotune(int mode);
+int s2let_gpu_autotune_entries(int *keys, double *ms, int max);
 
 /* Measured FMA throughput of the current GPU, for roofline fractions: one
  * launch of 8 independent FMA chains per thread, `iters` iterations; fp64 != 0

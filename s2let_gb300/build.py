@@ -21,7 +21,7 @@ LIB = os.path.join(LIBDIR, "libs2let_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3,-ffp-contract=off", f"-I{ROOT}/include", f"-I{CSRC}"]
 SOURCES = ["host_layer.cpp", "plan.cu", "kernels.cu", "exec.cu", "capi_lm.cu", "timing.cu", "hostcopy.cu", "noalloc.cu",
-           "mixed.cu", "recompute.cu", "fits.cpp"]
+           "mixed.cu", "recompute.cu", "autotune.cu", "fits.cpp"]
 
 
 def nvcc() -> str:

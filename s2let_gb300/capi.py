@@ -164,6 +164,18 @@ GPU_SIGNATURES = {
     "s2let_gpu_synthesis_adjoint_px2wav_real_batch": (I, [V, V, V, I, P, V]),
     "s2let_gpu_analysis_adjoint_wav2px_batch": (I, [V, V, V, I, P, V]),
     "s2let_gpu_synthesis_adjoint_px2wav_batch": (I, [V, V, V, I, P, V]),
+    "s2let_gpu_analysis_px2wav_real_batch_f32": (I, [V, V, V, I, P, V]),
+    "s2let_gpu_synthesis_wav2px_real_batch_f32": (I, [V, V, V, I, P, V]),
+    "s2let_gpu_analysis_px2wav_batch_f32": (I, [V, V, V, I, P, V]),
+    "s2let_gpu_synthesis_wav2px_batch_f32": (I, [V, V, V, I, P, V]),
+    "s2let_gpu_analysis_adjoint_wav2px_real_batch_f32": (I, [V, V, V, I, P, V]),
+    "s2let_gpu_synthesis_adjoint_px2wav_real_batch_f32": (I, [V, V, V, I, P, V]),
+    "s2let_gpu_analysis_adjoint_wav2px_batch_f32": (I, [V, V, V, I, P, V]),
+    "s2let_gpu_synthesis_adjoint_px2wav_batch_f32": (I, [V, V, V, I, P, V]),
+    "s2let_gpu_autotune": (I, [I]),
+    "s2let_gpu_autotune_entries": (I, [V, V, I]),
+    "s2let_gpu_px2wav_multi_f32": (I, [V, V, V, P, V, I, I, V]),
+    "s2let_gpu_wav2px_multi_f32": (I, [V, V, V, P, V, I, I, V]),
 }
 
 

@@ -958,8 +958,22 @@ void run_sht(int dir, int L, int spin, bool real, int ss, void *f, double2 *flm,
 // One pass over the maps on stream st.  Maps with equal parameters (and
 // reality) run as one batch on contiguous scratch: inputs gathered and outputs
 // scattered with device-to-device copies; a map alone runs in place.
+// Reals per element and the used length (in reals) of one f_wav row: the
+// transforms advance with the parity-fixed N_j while s2let_n_wav counts N.
+int64_t used_wav_reals(const s2let_parameters_t &p, bool real) {
+  s2let_parameters_t q = p;
+  if (real) {
+    q.reality = 1;
+    q.spin = 0;
+  }
+  return make_layout(q, real).woff.back() * (real ? 1 : 2);
+}
+
+// f32: every map's arrays hold floats (interleaved pairs when complex); they
+// are widened into FP64 batch scratch on the way in and rounded on the way out
+// (only the used part of f_wav), so every map goes through the scratch.
 void multi_pass(Op op, int n, const s2let_parameters_t *params, const int *real, void *const *px,
-                void *const *wav, void *const *scal, cudaStream_t st) {
+                void *const *wav, void *const *scal, cudaStream_t st, bool f32 = false) {
   std::map<std::string, std::vector<int>> groups;
   for (int k = 0; k < n; ++k) {
     std::string key((const char *)&params[k], sizeof(s2let_parameters_t));
@@ -970,20 +984,29 @@ void multi_pass(Op op, int n, const s2let_parameters_t *params, const int *real,
     const std::vector<int> &g = kv.second;
     const s2let_parameters_t &p = params[g[0]];
     const bool re = real[g[0]] != 0;
-    if (g.size() == 1) {
+    if (g.size() == 1 && !f32) {
       run_directional(op, p, re, px[g[0]], nullptr, wav[g[0]], scal[g[0]], 1, st);
       continue;
     }
     const int nb = (int)g.size();
     const size_t esz = re ? sizeof(double) : sizeof(double2);
     const size_t bpx = esz * s2let_n_px(&p), bw = esz * s2let_n_wav(&p), bs = esz * s2let_n_scal(&p);
+    const int64_t rpx = (int64_t)(bpx / sizeof(double)), rw = (int64_t)(bw / sizeof(double)),
+                  rs = (int64_t)(bs / sizeof(double)), rwu = f32 ? used_wav_reals(p, re) : rw;
     Scratch S(st);
     char *dpx = S.get<char>((int64_t)nb * bpx), *dw = S.get<char>((int64_t)nb * bw),
          *ds = S.get<char>((int64_t)nb * bs);
     const bool fwd = (op == OP_PX2WAV || op == OP_ADJ_PX2WAV);
     for (int i = 0; i < nb; ++i) {
       const int k = g[i];
-      if (fwd) {
+      if (f32) {
+        if (fwd) {
+          widen_rows((const float *)px[k], 0, (double *)(dpx + i * bpx), 0, rpx, 1, st);
+        } else {
+          widen_rows((const float *)wav[k], 0, (double *)(dw + i * bw), 0, rwu, 1, st);
+          widen_rows((const float *)scal[k], 0, (double *)(ds + i * bs), 0, rs, 1, st);
+        }
+      } else if (fwd) {
         S2G_CUDA(cudaMemcpyAsync(dpx + i * bpx, px[k], bpx, cudaMemcpyDeviceToDevice, st));
       } else {
         S2G_CUDA(cudaMemcpyAsync(dw + i * bw, wav[k], bw, cudaMemcpyDeviceToDevice, st));
@@ -993,7 +1016,14 @@ void multi_pass(Op op, int n, const s2let_parameters_t *params, const int *real,
     run_directional(op, p, re, dpx, nullptr, dw, ds, nb, st);
     for (int i = 0; i < nb; ++i) {
       const int k = g[i];
-      if (fwd) {
+      if (f32) {
+        if (fwd) {
+          narrow_rows((const double *)(dw + i * bw), 0, (float *)wav[k], 0, rwu, 1, st);
+          narrow_rows((const double *)(ds + i * bs), 0, (float *)scal[k], 0, rs, 1, st);
+        } else {
+          narrow_rows((const double *)(dpx + i * bpx), 0, (float *)px[k], 0, rpx, 1, st);
+        }
+      } else if (fwd) {
         S2G_CUDA(cudaMemcpyAsync(wav[k], dw + i * bw, bw, cudaMemcpyDeviceToDevice, st));
         S2G_CUDA(cudaMemcpyAsync(scal[k], ds + i * bs, bs, cudaMemcpyDeviceToDevice, st));
       } else {
@@ -1021,12 +1051,12 @@ void release_multi_graphs() {
 }
 
 void run_multi(Op op, int n, const s2let_parameters_t *params, const int *real, void *const *px,
-               void *const *wav, void *const *scal, bool use_graph, cudaStream_t st) {
+               void *const *wav, void *const *scal, bool use_graph, cudaStream_t st, bool f32 = false) {
   S2G_REQUIRE(n >= 0, ERR_INVALID, "negative map count");
   S2G_REQUIRE(n == 0 || (params && real && px && wav && scal), ERR_INVALID, "NULL array");
   for (int k = 0; k < n; ++k) validate(&params[k]);
   if (!use_graph || st == nullptr || timing_enabled()) {
-    multi_pass(op, n, params, real, px, wav, scal, st);
+    multi_pass(op, n, params, real, px, wav, scal, st, f32);
     return;
   }
   std::string key;
@@ -1042,6 +1072,7 @@ void run_multi(Op op, int n, const s2let_parameters_t *params, const int *real, 
   put(&t_precision, sizeof t_precision);
   put(&t_table_mode, sizeof t_table_mode);
   put(&kern, sizeof kern);
+  put(&f32, sizeof f32);
   std::lock_guard<std::mutex> lk(g_multi_mu);
   auto it = g_multi_graphs.find(key);
   if (it != g_multi_graphs.end()) {
@@ -1049,14 +1080,14 @@ void run_multi(Op op, int n, const s2let_parameters_t *params, const int *real, 
     return;
   }
   if (!g_multi_seen.count(key)) {
-    multi_pass(op, n, params, real, px, wav, scal, st);
+    multi_pass(op, n, params, real, px, wav, scal, st, f32);
     g_multi_seen.insert(key);
     return;
   }
   cudaGraph_t graph = nullptr;
   S2G_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   try {
-    multi_pass(op, n, params, real, px, wav, scal, st);
+    multi_pass(op, n, params, real, px, wav, scal, st, f32);
   } catch (...) {
     cudaStreamEndCapture(st, &graph);
     if (graph) cudaGraphDestroy(graph);
@@ -1151,6 +1182,42 @@ int batch_directional(const char *fn, s2g::Op op, const s2let_parameters_t *p, b
     s2g::validate(p);
     s2g::ensure_device();
     s2g::run_directional(op, *p, real, px, nullptr, wav, scal, nb, (cudaStream_t)stream);
+  });
+}
+
+// FP32 storage: the batch widened into FP64 device scratch (only the used part
+// of each f_wav row), the FP64-storage path at the thread's precision, the
+// outputs rounded to FP32.
+int batch_directional_f32(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool real, void *px,
+                          void *wav, void *scal, int nb, void *stream) {
+  return s2g::guarded(fn, [&] {
+    using namespace s2g;
+    validate(p);
+    ensure_device();
+    S2G_REQUIRE(nb >= 0, ERR_INVALID, "negative batch size");
+    if (nb == 0) return;
+    S2G_REQUIRE(px && wav && scal, ERR_INVALID, "NULL buffer");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int dd = real ? 1 : 2;
+    const int64_t npx = s2let_n_px(p) * dd, nw = s2let_n_wav(p) * dd, ns = s2let_n_scal(p) * dd;
+    const int64_t nwu = used_wav_reals(*p, real);
+    Scratch S(st);
+    double *dpx = S.get<double>((int64_t)nb * npx), *dw = S.get<double>((int64_t)nb * nw),
+           *ds = S.get<double>((int64_t)nb * ns);
+    const bool fwd = (op == OP_PX2WAV || op == OP_ADJ_PX2WAV);
+    if (fwd) {
+      widen_rows((const float *)px, npx, dpx, npx, npx, nb, st);
+    } else {
+      widen_rows((const float *)wav, nw, dw, nw, nwu, nb, st);
+      widen_rows((const float *)scal, ns, ds, ns, ns, nb, st);
+    }
+    run_directional(op, *p, real, dpx, nullptr, dw, ds, nb, st);
+    if (fwd) {
+      narrow_rows(dw, nw, (float *)wav, nw, nwu, nb, st);
+      narrow_rows(ds, ns, (float *)scal, ns, ns, nb, st);
+    } else {
+      narrow_rows(dpx, npx, (float *)px, npx, npx, nb, st);
+    }
   });
 }
 
@@ -1631,6 +1698,60 @@ int s2let_gpu_analysis_adjoint_wav2px_batch(void *f, const void *f_wav, const vo
 int s2let_gpu_synthesis_adjoint_px2wav_batch(void *f_wav, void *f_scal, const void *f, int nb,
                                              const s2let_parameters_t *p, void *stream) {
   return batch_directional(__func__, s2g::OP_ADJ_PX2WAV, p, false, (void *)f, f_wav, f_scal, nb, stream);
+}
+
+// ---- FP32 storage (batched device pointers)
+int s2let_gpu_analysis_px2wav_real_batch_f32(float *f_wav, float *f_scal, const float *f, int nb,
+                                             const s2let_parameters_t *p, void *stream) {
+  return batch_directional_f32(__func__, s2g::OP_PX2WAV, p, true, (void *)f, f_wav, f_scal, nb, stream);
+}
+int s2let_gpu_synthesis_wav2px_real_batch_f32(float *f, const float *f_wav, const float *f_scal, int nb,
+                                              const s2let_parameters_t *p, void *stream) {
+  return batch_directional_f32(__func__, s2g::OP_WAV2PX, p, true, f, (void *)f_wav, (void *)f_scal, nb, stream);
+}
+int s2let_gpu_analysis_px2wav_batch_f32(void *f_wav, void *f_scal, const void *f, int nb,
+                                        const s2let_parameters_t *p, void *stream) {
+  return batch_directional_f32(__func__, s2g::OP_PX2WAV, p, false, (void *)f, f_wav, f_scal, nb, stream);
+}
+int s2let_gpu_synthesis_wav2px_batch_f32(void *f, const void *f_wav, const void *f_scal, int nb,
+                                         const s2let_parameters_t *p, void *stream) {
+  return batch_directional_f32(__func__, s2g::OP_WAV2PX, p, false, f, (void *)f_wav, (void *)f_scal, nb, stream);
+}
+int s2let_gpu_analysis_adjoint_wav2px_real_batch_f32(float *f, const float *f_wav, const float *f_scal, int nb,
+                                                     const s2let_parameters_t *p, void *stream) {
+  return batch_directional_f32(__func__, s2g::OP_ADJ_WAV2PX, p, true, f, (void *)f_wav, (void *)f_scal, nb,
+                               stream);
+}
+int s2let_gpu_synthesis_adjoint_px2wav_real_batch_f32(float *f_wav, float *f_scal, const float *f, int nb,
+                                                      const s2let_parameters_t *p, void *stream) {
+  return batch_directional_f32(__func__, s2g::OP_ADJ_PX2WAV, p, true, (void *)f, f_wav, f_scal, nb, stream);
+}
+int s2let_gpu_analysis_adjoint_wav2px_batch_f32(void *f, const void *f_wav, const void *f_scal, int nb,
+                                                const s2let_parameters_t *p, void *stream) {
+  return batch_directional_f32(__func__, s2g::OP_ADJ_WAV2PX, p, false, f, (void *)f_wav, (void *)f_scal, nb,
+                               stream);
+}
+int s2let_gpu_synthesis_adjoint_px2wav_batch_f32(void *f_wav, void *f_scal, const void *f, int nb,
+                                                 const s2let_parameters_t *p, void *stream) {
+  return batch_directional_f32(__func__, s2g::OP_ADJ_PX2WAV, p, false, (void *)f, f_wav, f_scal, nb, stream);
+}
+int s2let_gpu_px2wav_multi_f32(void *const *f_wav, void *const *f_scal, void *const *f,
+                               const s2let_parameters_t *params, const int *real, int nmaps, int use_graph,
+                               void *stream) {
+  return s2g::guarded(__func__, [&] {
+    s2g::ensure_device();
+    s2g::run_multi(s2g::OP_PX2WAV, nmaps, params, real, f, f_wav, f_scal, use_graph != 0, (cudaStream_t)stream,
+                   true);
+  });
+}
+int s2let_gpu_wav2px_multi_f32(void *const *f, void *const *f_wav, void *const *f_scal,
+                               const s2let_parameters_t *params, const int *real, int nmaps, int use_graph,
+                               void *stream) {
+  return s2g::guarded(__func__, [&] {
+    s2g::ensure_device();
+    s2g::run_multi(s2g::OP_WAV2PX, nmaps, params, real, f, f_wav, f_scal, use_graph != 0, (cudaStream_t)stream,
+                   true);
+  });
 }
 
 }  // extern "C"

@@ -15,6 +15,7 @@
 #include <map>
 #include <mutex>
 
+#include "autotune.h"
 #include "common.h"
 #include "dfconv.h"
 #include "kernels.h"
@@ -773,11 +774,7 @@ void contract_work(const ContractArgs &a, int nm, double *flops, double *bytes) 
 }
 
 template <int MODE>
-void launch_contract(const ContractArgs &a, int nm, int rows, cudaStream_t st) {
-  const int nbt = a.nb >= 8 ? 8 : (a.nb >= 4 ? 4 : (a.nb >= 2 ? 2 : 1));
-  double fl = 0, by = 0;
-  if (timing_enabled()) contract_work(a, nm, &fl, &by);
-  KTimer kt(KC_CONTRACT, st, fl, by);
+void launch_contract_nbt(const ContractArgs &a, int nm, int rows, int nbt, cudaStream_t st) {
   dim3 grid(nm, ceil_div(rows, CT_M), ceil_div(a.nb, nbt));
   switch (nbt) {
   case 8: k_contract<MODE, 8><<<grid, CT_M, 0, st>>>(a); break;
@@ -786,6 +783,20 @@ void launch_contract(const ContractArgs &a, int nm, int rows, cudaStream_t st) {
   default: k_contract<MODE, 1><<<grid, CT_M, 0, st>>>(a); break;
   }
   S2G_LAUNCHED();
+}
+
+// maps per CTA: the largest power of two up to 8 that the batch fills, or the
+// autotuned choice among those (per mode, band-limit bucket and batch bucket)
+template <int MODE>
+void launch_contract(const ContractArgs &a, int nm, int rows, cudaStream_t st) {
+  static const int kCand[4] = {1, 2, 4, 8};
+  const int ncand = a.nb >= 8 ? 4 : (a.nb >= 4 ? 3 : (a.nb >= 2 ? 2 : 1));
+  const int c = tuned(TF_CONTRACT, MODE, tune_bucket(a.bl), tune_bucket(a.nb), ncand, ncand - 1, st,
+                      [&](int i) { launch_contract_nbt<MODE>(a, nm, rows, kCand[i], st); });
+  double fl = 0, by = 0;
+  if (timing_enabled()) contract_work(a, nm, &fl, &by);
+  KTimer kt(KC_CONTRACT, st, fl, by);
+  launch_contract_nbt<MODE>(a, nm, rows, kCand[c], st);
 }
 
 // ---------------------------------------------------------------------------
@@ -1166,24 +1177,45 @@ __global__ void __launch_bounds__(512, 3) k_ring_inverse_gamma_df(RingArgs a, Ga
   const int chunk = (K + NN - 1) / NN;
   const int p1 = min(K, (kk + 1) * chunk);
   const int64_t obase = (int64_t)bb * gf.fms + (int64_t)tt * K;
+  // gamma_g and gamma_{ng-g} have conjugate twiddles: with w = C + i S,
+  //   real:    f_g = A - B, f_{ng-g} = A + B, A = sum_k C Re z_k, B = sum_k S Im z_k
+  //   complex: f_g = U + i V, f_{ng-g} = U - i V, U = sum_k C z_k, V = sum_k S z_k
   for (int p = kk * chunk + threadIdx.x; p < p1; p += blockDim.x) {
     const int i = slot_brev(p, logP);
     float4 z[NN];
 #pragma unroll
     for (int j = 0; j < NN; ++j) z[j] = *cl.map_shared_rank(bufd + i, j);
-    for (int g = 0; g < gf.ng; ++g) {
-      float2 re = make_float2(0.f, 0.f), im = make_float2(0.f, 0.f);
+    for (int g = 0; 2 * g <= gf.ng; ++g) {
+      const int g2 = gf.ng - g;  // the conjugate partner (g = 0 and g2 == g have none)
+      const int64_t o = obase + (int64_t)g * gf.npx + p, o2 = obase + (int64_t)g2 * gf.npx + p;
+      const bool pair = g > 0 && g2 != g;
+      if (REAL) {
+        float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int j = 0; j < NN; ++j) {
-        const float4 w = gf.tw[g * NN + j];
-        re = df_add(re, df_dot2(dre(w), dre(z[j]), df_neg(dim_(w)), dim_(z[j])));
-        if (!REAL) im = df_add(im, df_dot2(dre(w), dim_(z[j]), dim_(w), dre(z[j])));
+        for (int j = 0; j < NN; ++j) {
+          const float4 w = gf.tw[g * NN + j];
+          A = df_add(A, df_mul(dre(w), dre(z[j])));
+          B = df_add(B, df_mul(dim_(w), dim_(z[j])));
+        }
+        const float2 f1 = df_add(A, df_neg(B));
+        ((double *)gf.fw)[o] = join_scaled(f1.x, f1.y, eo);
+        if (pair) {
+          const float2 f2 = df_add(A, B);
+          ((double *)gf.fw)[o2] = join_scaled(f2.x, f2.y, eo);
+        }
+      } else {
+        float4 U = make_float4(0.f, 0.f, 0.f, 0.f), V = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < NN; ++j) {
+          const float4 w = gf.tw[g * NN + j];
+          U = dmk(df_add(dre(U), df_mul(dre(w), dre(z[j]))), df_add(dim_(U), df_mul(dre(w), dim_(z[j]))));
+          V = dmk(df_add(dre(V), df_mul(dim_(w), dre(z[j]))), df_add(dim_(V), df_mul(dim_(w), dim_(z[j]))));
+        }
+        const float4 iV = dc_mul_pi(V);
+        const float4 f1 = dc_add(U, iV);
+        ((double2 *)gf.fw)[o] = dc_to(f1, eo);
+        if (pair) ((double2 *)gf.fw)[o2] = dc_to(dc_sub(U, iV), eo);
       }
-      const int64_t o = obase + (int64_t)g * gf.npx + p;
-      if (REAL)
-        ((double *)gf.fw)[o] = join_scaled(re.x, re.y, eo);
-      else
-        ((double2 *)gf.fw)[o] = make_double2(join_scaled(re.x, re.y, eo), join_scaled(im.x, im.y, eo));
     }
   }
   cl.sync();  // peers read this buffer until here
@@ -1214,23 +1246,37 @@ __global__ void __launch_bounds__(512, 3) k_gamma_ring_forward_df(RingArgs a, Ga
   if (threadIdx.x == 0) s_e = e;  // read back after the transforms: fewer live registers in them
   // the zero padding of this CTA's own buffer
   for (int j = K + threadIdx.x; j < P; j += blockDim.x) bufd[slot_brev(j, logP)] = make_float4(0.f, 0.f, 0.f, 0.f);
+  // gamma_g and gamma_{ng-g} have conjugate twiddles w = C + i S and C - i S:
+  // each pair contributes C (f_g + f_{ng-g}) + i S (f_g - f_{ng-g})
   for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
     float4 acc[NN];
 #pragma unroll
     for (int j = 0; j < NN; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int g = 0; g < gf.ng; ++g) {
-      const int64_t o = ibase + (int64_t)g * gf.npx + p;
+    for (int g = 0; 2 * g <= gf.ng; ++g) {
+      const int g2 = gf.ng - g;
+      const bool pair = g > 0 && g2 != g;
+      const int64_t o = ibase + (int64_t)g * gf.npx + p, o2 = ibase + (int64_t)g2 * gf.npx + p;
       if (REAL) {
-        const float2 f = df_split(((const double *)gf.fw)[o], e);
+        const float2 fa = df_split(((const double *)gf.fw)[o], e);
+        const float2 fb = pair ? df_split(((const double *)gf.fw)[o2], e) : make_float2(0.f, 0.f);
+        const float2 Pp = df_add(fa, fb), Q = df_add(fa, df_neg(fb));
 #pragma unroll
         for (int j = 0; j < NN; ++j) {
           const float4 w = gf.tw[g * NN + j];
-          acc[j] = dmk(df_add(dre(acc[j]), df_mul(dre(w), f)), df_add(dim_(acc[j]), df_mul(dim_(w), f)));
+          acc[j] = dmk(df_add(dre(acc[j]), df_mul(dre(w), Pp)), df_add(dim_(acc[j]), df_mul(dim_(w), Q)));
         }
       } else {
-        const float4 f = dc_split(((const double2 *)gf.fw)[o], e);
+        const float4 fa = dc_split(((const double2 *)gf.fw)[o], e);
+        const float4 fb = pair ? dc_split(((const double2 *)gf.fw)[o2], e) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 Pp = dc_add(fa, fb), Q = dc_sub(fa, fb);
 #pragma unroll
-        for (int j = 0; j < NN; ++j) acc[j] = dc_add(acc[j], dc_mul(gf.tw[g * NN + j], f));
+        for (int j = 0; j < NN; ++j) {
+          const float4 w = gf.tw[g * NN + j];
+          // C P + i S Q
+          const float2 re = df_add(df_mul(dre(w), dre(Pp)), df_neg(df_mul(dim_(w), dim_(Q))));
+          const float2 im = df_add(df_mul(dre(w), dim_(Pp)), df_mul(dim_(w), dre(Q)));
+          acc[j] = dc_add(acc[j], dmk(re, im));
+        }
       }
     }
     const float4 ch = ld_once(&a.chirp_df[p]);
@@ -1305,6 +1351,25 @@ __global__ void k_symmetrize(double2 *flm, int L, int64_t fs, int nb) {
   double2 v = conj2(flm[(int64_t)b * fs + i]);
   if (m & 1) v = scl2(v, -1.0);
   flm[(int64_t)b * fs + l * l + l - m] = v;
+}
+
+// FP32 storage: `rows` rows of n values, row r at src + r ss and dst + r ds
+// (elements); widening is exact, narrowing rounds to nearest.
+__global__ void k_widen_rows(const float *__restrict__ src, int64_t ss, double *__restrict__ dst, int64_t ds,
+                             int64_t n, int rows) {
+  const int64_t total = (int64_t)rows * n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / n, c = i - r * n;
+    dst[r * ds + c] = (double)src[r * ss + c];
+  }
+}
+__global__ void k_narrow_rows(const double *__restrict__ src, int64_t ss, float *__restrict__ dst, int64_t ds,
+                              int64_t n, int rows) {
+  const int64_t total = (int64_t)rows * n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / n, c = i - r * n;
+    dst[r * ds + c] = __double2float_rn(src[r * ss + c]);
+  }
 }
 
 __global__ void k_scale_copy(const double *x, double *y, int64_t n, double s) {
@@ -1793,6 +1858,32 @@ void merge_lmn(double2 *flm, int L, int64_t fs, const double2 *z, int64_t zs, co
   KTimer kt(KC_MERGE, st, 0.0, 0.0);
   k_merge<<<ceil_div(total, 256), 256, 0, st>>>(flm, L, fs, z, zs, pairs, npairs, wts, zscal, zss,
                                                bl_scal, real, accumulate, nb);
+  S2G_LAUNCHED();
+}
+
+namespace {
+int conv_grid(int64_t total) {
+  static const int nsm = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  }();
+  const int64_t want = ceil_div(total, 256);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)nsm * 8));
+}
+}  // namespace
+
+void widen_rows(const float *src, int64_t ss, double *dst, int64_t ds, int64_t n, int rows, cudaStream_t st) {
+  if (n <= 0 || rows <= 0) return;
+  KTimer kt(KC_OTHER, st, 0.0, 12.0 * (double)n * rows);
+  k_widen_rows<<<conv_grid(n * rows), 256, 0, st>>>(src, ss, dst, ds, n, rows);
+  S2G_LAUNCHED();
+}
+void narrow_rows(const double *src, int64_t ss, float *dst, int64_t ds, int64_t n, int rows, cudaStream_t st) {
+  if (n <= 0 || rows <= 0) return;
+  KTimer kt(KC_OTHER, st, 0.0, 12.0 * (double)n * rows);
+  k_narrow_rows<<<conv_grid(n * rows), 256, 0, st>>>(src, ss, dst, ds, n, rows);
   S2G_LAUNCHED();
 }
 

@@ -130,6 +130,12 @@ void ring_inverse_gamma(const double2 *G, int64_t gms, int64_t gks, const std::v
 void gamma_ring_forward(const void *fw, int64_t fms, const std::vector<int> &ns, int ng, bool real, double c,
                         double2 *Gout, int64_t gms, int64_t gks, int nb, int bl, int ss, cudaStream_t st);
 
+// FP32 storage conversions: `rows` rows of n values, row r at src + r ss and
+// dst + r ds (elements; complex values as interleaved pairs).  Widening is
+// exact; narrowing rounds to nearest.
+void widen_rows(const float *src, int64_t ss, double *dst, int64_t ds, int64_t n, int rows, cudaStream_t st);
+void narrow_rows(const double *src, int64_t ss, float *dst, int64_t ds, int64_t n, int rows, cudaStream_t st);
+
 // Merge of per-(scale, direction) Wigner coefficients into flm (lmn2lm):
 //   flm(l,m) = sum_pairs [ psi_p(l) z_p(l,m) + real&&n>0 : (-1)^{m+n} conj(z_p(l,-m)) psin_p(l) ]
 //              + zs(l,m)

@@ -33,6 +33,7 @@
 #include <tuple>
 #include <vector>
 
+#include "autotune.h"
 #include "common.h"
 #include "dfconv.h"
 #include "kernels.h"
@@ -214,6 +215,7 @@ struct Part {
   const double2 *w;  // per-l weight (l -> t: on the input; t -> l: on the output)
   double wscale;
   int wconj;
+  int wkind;  // WKIND_* of w
   int lmin;
   double2 *dst;  // l -> t: spectra [t][m - d_mlo] (row width dw); t -> l: l^2 + l + m
   int64_t ds;
@@ -237,6 +239,23 @@ __device__ __forceinline__ double2 weight_of(const double2 *w, double wscale, in
   double2 v = w ? w[l] : make_double2(1.0, 0.0);
   if (wconj) v.y = -v.y;
   return make_double2(v.x * wscale, v.y * wscale);
+}
+// x times the part's weight at degree l (x times wscale without a weight).  A
+// real or imaginary weight takes three FP64 products instead of the eight of a
+// scaled complex product; the terms dropped are exact zeros, so the result is
+// the same.
+__device__ __forceinline__ double2 weighted(const Part &P, double2 x, int l) {
+  if (!P.w) return make_double2(x.x * P.wscale, x.y * P.wscale);
+  if (P.wkind == WKIND_REAL) {
+    const double r = P.w[l].x * P.wscale;
+    return make_double2(x.x * r, x.y * r);
+  }
+  if (P.wkind == WKIND_IMAG) {  // x (i r)
+    const double r = (P.wconj ? -P.w[l].y : P.w[l].y) * P.wscale;
+    return make_double2(-(x.y * r), x.x * r);
+  }
+  const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
+  return make_double2(x.x * wt.x - x.y * wt.y, x.x * wt.y + x.y * wt.x);
 }
 
 // Coefficient slicing: one block per (kMG consecutive problem m, column pair
@@ -316,12 +335,7 @@ __global__ void __launch_bounds__(kSliceThreads, 3) k_slice_x(XArgs a) {
             x.y = -x.y;
             if (am & 1) x = make_double2(-x.x, -x.y);
           }
-          if (P.w) {
-            const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
-            x = make_double2(x.x * wt.x - x.y * wt.y, x.x * wt.y + x.y * wt.x);
-          } else {
-            x = make_double2(x.x * P.wscale, x.y * P.wscale);
-          }
+          x = weighted(P, x, l);
           col[sv_idx(l - l0)] = x;
           er = max(er, exp_field(x.x));
           ei = max(ei, exp_field(x.y));
@@ -794,14 +808,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_mx(MxArgs a) {
             const int lst = ti.l0 > P.lmin ? ti.l0 : P.lmin;
             if (l >= lst && l < a.bl) {
               const double yr = y[2 * bb], yi = y[2 * bb + 1];
-              double2 o;
-              if (P.w) {
-                const double2 wt = weight_of(P.w, P.wscale, P.wconj, l);
-                o = make_double2(yr * wt.x - yi * wt.y, yr * wt.y + yi * wt.x);
-              } else {  // a real scale factor (the directional synthesis): two FP64 multiplies
-                o = make_double2(yr * P.wscale, yi * P.wscale);
-              }
-              P.dst[(int64_t)b * P.ds + (int64_t)l * l + l + ti.m] = o;
+              P.dst[(int64_t)b * P.ds + (int64_t)l * l + l + ti.m] = weighted(P, make_double2(yr, yi), l);
             }
           }
         }
@@ -971,7 +978,7 @@ struct Problem {
 };
 
 template <int NC>
-void run_mixed(const Problem &p, cudaStream_t st) {
+void run_mixed(const Problem &p, cudaStream_t st, int gpl_max) {
   static const bool attr = [] {  // once per instantiation (thread-safe static initialisation)
     S2G_CUDA(cudaFuncSetAttribute(k_contract_mx<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)Cfg<NC>::kSmemBytes));
@@ -1003,10 +1010,9 @@ void run_mixed(const Problem &p, cudaStream_t st) {
   }();
   (void)attr_x;
   const int ngroups = (p.nb + mpp - 1) / mpp;
-  // map groups run kGroupsPerLaunch at a time in one launch (their tiles
+  // map groups run up to gpl_max at a time in one launch (their tiles
   // interleaved, the table read once from HBM and again from L2)
-  constexpr int kGroupsPerLaunch = 4;
-  const int gpl = ngroups < kGroupsPerLaunch ? ngroups : kGroupsPerLaunch;
+  const int gpl = ngroups < gpl_max ? ngroups : gpl_max;
   // coefficient panels: the tile list's offsets count 16-column panels; an
   // NC-column panel is NC/16 times larger, so offsets scale by NC/16
   const int64_t x_elems = L->x_elems * (NC / 16);
@@ -1088,16 +1094,31 @@ void run_mixed(const Problem &p, cudaStream_t st) {
   cudaFreeAsync(eX, st);
 }
 
-// columns per table pass: 2 (re, im) x maps x parts, in the smallest of 16 /
-// 32 / 64 that holds the whole batch (larger batches loop over map groups)
+// Columns per table pass (2 (re, im) x maps x parts) and map groups per launch.
+// Built-in: the smallest of 16 / 32 / 64 columns that holds the whole batch
+// (larger batches loop over map groups), 4 groups per launch.  With tuning
+// on, the candidates below are timed per (band-limit bucket, column bucket,
+// direction) and the fastest kept.
 void run_problem(const Problem &p, cudaStream_t st) {
+  struct Shape {
+    int nc, gpl;
+  };
+  static const Shape kCand[7] = {{16, 1}, {16, 4}, {32, 1}, {32, 4}, {64, 1}, {64, 2}, {64, 4}};
   const int cols = 2 * p.nb * p.nparts;
-  if (cols <= 16)
-    run_mixed<16>(p, st);
-  else if (cols <= 32)
-    run_mixed<32>(p, st);
-  else
-    run_mixed<64>(p, st);
+  const int def = cols <= 16 ? 1 : (cols <= 32 ? 3 : 6);
+  // a candidate narrower than one part's two columns cannot hold a map
+  const int first = 2 * p.nparts > 16 ? (2 * p.nparts > 32 ? 4 : 2) : 0;
+  const auto run = [&](const Shape &sh) {
+    if (sh.nc == 16)
+      run_mixed<16>(p, st, sh.gpl);
+    else if (sh.nc == 32)
+      run_mixed<32>(p, st, sh.gpl);
+    else
+      run_mixed<64>(p, st, sh.gpl);
+  };
+  const int c = tuned(TF_MIXED, tune_bucket(p.tb->bl), tune_bucket(cols), p.q ? 1 : 0, 7 - first, def - first, st,
+                      [&](int i) { run(kCand[first + i]); });
+  run(kCand[first + c]);
 }
 
 Part part_of(const L2T &a) {
@@ -1108,6 +1129,7 @@ Part part_of(const L2T &a) {
   P.w = a.w;
   P.wscale = a.wscale;
   P.wconj = a.wconj ? 1 : 0;
+  P.wkind = a.wkind;
   P.lmin = a.lmin;
   P.dst = a.out;
   P.ds = a.os;
@@ -1125,6 +1147,7 @@ Part part_of(const T2L &a) {
   P.w = a.w;
   P.wscale = a.wscale;
   P.wconj = a.wconj ? 1 : 0;
+  P.wkind = a.wkind;
   P.lmin = a.lmin;
   P.dst = a.y;
   P.ds = a.ys;

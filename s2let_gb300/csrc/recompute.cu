@@ -20,6 +20,7 @@
 //              stored path's Q = D^T W becomes D^T applied after W (FP64 tiled GEMM)
 #include <algorithm>
 
+#include "autotune.h"
 #include "common.h"
 #include "kernels.h"
 #include "recompute.h"
@@ -495,15 +496,21 @@ void contract_l2t_rc(const L2T &p, cudaStream_t st) {
   {
     double fl = 0, by = 0;
     if (timing_enabled()) rc_work(tb, p.mlo, p.mhi, p.lmin, p.nb, &fl, &by);
+    // maps per CTA: the largest of 1/2/4/8 the batch fills, or the autotuned choice
+    const auto run = [&](int nbc) {
+      switch (nbc) {
+        case 8: launch_l2t<8>(a, nm, st); break;
+        case 4: launch_l2t<4>(a, nm, st); break;
+        case 2: launch_l2t<2>(a, nm, st); break;
+        default: launch_l2t<1>(a, nm, st); break;
+      }
+    };
+    static const int kCand[4] = {1, 2, 4, 8};
+    const int ncand = p.nb >= 8 ? 4 : (p.nb >= 4 ? 3 : (p.nb >= 2 ? 2 : 1));
+    const int c = tuned(TF_RC_L2T, tune_bucket(tb.bl), tune_bucket(p.nb), 0, ncand, ncand - 1, st,
+                        [&](int i) { run(kCand[i]); });
     KTimer kt(KC_RECOMPUTE, st, fl, by);
-    if (p.nb >= 8)
-      launch_l2t<8>(a, nm, st);
-    else if (p.nb >= 4)
-      launch_l2t<4>(a, nm, st);
-    else if (p.nb >= 2)
-      launch_l2t<2>(a, nm, st);
-    else
-      launch_l2t<1>(a, nm, st);
+    run(kCand[c]);
   }
   if (p.use_q) {
     apply_w(tb, true, p.mlo, p.mhi, tmp, (int64_t)tb.nt * p.ow, p.ow, p.omlo, p.out, p.os, p.ow, p.omlo, p.nb, st);
@@ -535,17 +542,22 @@ void contract_t2l_rc(const T2L &p, cudaStream_t st) {
   {
     double fl = 0, by = 0;
     if (timing_enabled()) rc_work(tb, p.mlo, p.mhi, p.lmin, p.nb, &fl, &by);
+    // maps per CTA: the largest of 1/2/4/8/16 the batch fills, or the autotuned choice
+    const auto run = [&](int nbc) {
+      switch (nbc) {
+        case 16: launch_t2l<16>(a, nm, maxseg, st); break;
+        case 8: launch_t2l<8>(a, nm, maxseg, st); break;
+        case 4: launch_t2l<4>(a, nm, maxseg, st); break;
+        case 2: launch_t2l<2>(a, nm, maxseg, st); break;
+        default: launch_t2l<1>(a, nm, maxseg, st); break;
+      }
+    };
+    static const int kCand[5] = {1, 2, 4, 8, 16};
+    const int ncand = p.nb >= 16 ? 5 : (p.nb >= 8 ? 4 : (p.nb >= 4 ? 3 : (p.nb >= 2 ? 2 : 1)));
+    const int c = tuned(TF_RC_T2L, tune_bucket(tb.bl), tune_bucket(p.nb), 0, ncand, ncand - 1, st,
+                        [&](int i) { run(kCand[i]); });
     KTimer kt(KC_RECOMPUTE, st, fl, by);
-    if (p.nb >= 16)
-      launch_t2l<16>(a, nm, maxseg, st);
-    else if (p.nb >= 8)
-      launch_t2l<8>(a, nm, maxseg, st);
-    else if (p.nb >= 4)
-      launch_t2l<4>(a, nm, maxseg, st);
-    else if (p.nb >= 2)
-      launch_t2l<2>(a, nm, maxseg, st);
-    else
-      launch_t2l<1>(a, nm, maxseg, st);
+    run(kCand[c]);
   }
   if (tmp) cudaFreeAsync(tmp, st);
 }
