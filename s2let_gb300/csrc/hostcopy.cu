@@ -22,20 +22,18 @@ namespace s2g {
 
 namespace {
 
-// Copy CTAs are small (128 threads, at most 32 registers: 4096 registers) so
-// that one fits on an SM beside the transforms that overlap the copies: three
-// double-float ring CTAs (3 x 512 threads x 40 registers = 61440) or the
-// persistent tensor-core contraction CTA.  A larger copy CTA would displace a
-// ring CTA on every SM it lands on.
-constexpr int kCopyThreads = 128;
+// 64 CTAs of 256 threads: 1 MB in flight.  Measured against 128 CTAs of 128
+// threads (which fit beside three ring-DFT CTAs on an SM): device-to-host
+// copies overlapping the transforms held 180 against 151 GB/s.
+constexpr int kCopyThreads = 256;
 constexpr int kCopyUnroll = 4;    // loads in flight per thread (latency of host reads)
-constexpr int kCopyBlocks = 128;  // CTAs per copy: 1 MB in flight (enough for the link), few SMs taken
+constexpr int kCopyBlocks = 64;   // CTAs per copy: enough bytes in flight for the link, few SMs taken
 
 // `height` rows of n elements of T: row r of src at src + r * spitch bytes,
 // of dst at dst + r * dpitch.  Rows run along blockIdx.y; each row is
 // grid-strided by the x blocks with kCopyUnroll independent loads per thread.
 template <class T>
-__global__ void __launch_bounds__(kCopyThreads, 16) k_copy_rows(char *__restrict__ dst, size_t dpitch,
+__global__ void __launch_bounds__(kCopyThreads) k_copy_rows(char *__restrict__ dst, size_t dpitch,
                                                             const char *__restrict__ src, size_t spitch,
                                                             size_t n) {
   const T *s = (const T *)(src + (size_t)blockIdx.y * spitch);
