@@ -6,9 +6,10 @@
 // host to device in every sample, while the copy engines delivered the same
 // rates only part of the time and dropped to 40-110 GB/s (device to host
 // most often) for stretches of tens to hundreds of milliseconds, with or
-// without other GPU activity.  So page-locked host memory is moved by
-// k_copy_rows on the caller's stream; anything else (or every copy, with
-// S2LET_GPU_HOST_COPY=engine) by the copy engines.
+// without other GPU activity.  So page-locked host memory is moved to the
+// host by k_copy_rows on the caller's stream (see copy_policy for the other
+// direction); anything else (or every copy, with S2LET_GPU_HOST_COPY=engine)
+// by the copy engines.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -54,12 +55,20 @@ __global__ void __launch_bounds__(kCopyThreads) k_copy_rows(char *__restrict__ d
   }
 }
 
-// 0: the copy engines for every copy; 1: a copy kernel where the host memory
-// is addressable by the device (S2LET_GPU_HOST_COPY=engine selects 0)
+// 0: the copy engines for every copy; 1: a copy kernel for both directions
+// where the host memory is addressable by the device; 2 (default): the copy
+// kernel for device-to-host copies, the copy engines host to device.  With a
+// synthesis call's host-to-device copies overlapping the next analysis call,
+// leaving them to the copy engines frees the copy kernel's SM slots for the
+// transforms (pipelined round trip 118 against 130 ms per 32 maps at L=1024
+// in most steps); the engines' slow stretches were mostly device to host.
+// S2LET_GPU_HOST_COPY=engine selects 0, =kernel 1.
 int copy_policy() {
   static const int p = [] {
     const char *e = getenv("S2LET_GPU_HOST_COPY");
-    return (e && strcmp(e, "engine") == 0) ? 0 : 1;
+    if (e && strcmp(e, "engine") == 0) return 0;
+    if (e && strcmp(e, "kernel") == 0) return 1;
+    return 2;
   }();
   return p;
 }
@@ -95,6 +104,7 @@ void launch_rows(void *dst, size_t dpitch, const void *src, size_t spitch, size_
 bool copy_by_kernel(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
                     cudaMemcpyKind kind, cudaStream_t st) {
   if (copy_policy() == 0 || height > 65535) return false;
+  if (copy_policy() == 2 && kind == cudaMemcpyHostToDevice) return false;
   if (kind != cudaMemcpyHostToDevice && kind != cudaMemcpyDeviceToHost) return false;
   if (!device_addressable(kind == cudaMemcpyHostToDevice ? src : dst)) return false;
   if (height == 1) dpitch = spitch = width;
