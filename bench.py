@@ -171,13 +171,14 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-# DRAM traffic / algorithmic bytes of the dominant kernel, from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum over the bytes the launch must
-# move); profiles/fp64_contraction_L512_N4_batch8.md.  Traffic grows with the
-# table size, so the ratio carries to the L=1024 launches.
-# DRAM traffic / algorithmic bytes per launch, from one ncu capture each
-# (profiles/fp64_contraction_L512_N4_batch8.md, profiles/ring_dft_df_L1024_N4_batch8.md)
-TRAFFIC_RATIO = {"fp64_contraction": 1.126, "ring_dft": 0.91}
+# DRAM traffic / algorithmic bytes per launch of the dominant kernel, from one
+# ncu capture each (DRAM bytes over the bytes the launch must move):
+# profiles/fp64_contraction_L512_N4_batch8.md (traffic grows with the table
+# size, so the ratio carries to the L=1024 launches) and
+# profiles/ring_gamma_fused_df_L1024_N4_batch8.md (the fused ring + gamma DFT
+# launches that carry most of the ring-DFT bytes: 1.437 GB of DRAM traffic for
+# 1.476 GB of spectra in and gamma slices out, per bl=1024 launch of 8 maps)
+TRAFFIC_RATIO = {"fp64_contraction": 1.126, "ring_dft": 0.974}
 
 
 def profile_traffic(kernel, alg_bytes_per_launch):
