@@ -104,6 +104,11 @@ void save_locked(const Key &k, const Entry &en) {
 
 }  // namespace
 
+int autotune_mode() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return mode_locked();
+}
+
 int tuned(int family, int a, int b, int c, int ncand, int def, cudaStream_t st,
           const std::function<void(int)> &trial) {
   if (ncand <= 1) return 0;

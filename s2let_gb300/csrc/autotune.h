@@ -29,6 +29,9 @@ enum TuneFamily {
 int tuned(int family, int a, int b, int c, int ncand, int def, cudaStream_t st,
           const std::function<void(int)> &trial);
 
+// current mode (0 off, 1 tuning on), for caches keyed by the launch shapes
+int autotune_mode();
+
 // power-of-two bucket of a size (the key's granularity)
 inline int tune_bucket(int x) {
   int b = 1;

@@ -21,6 +21,7 @@
 #include <string>
 #include <vector>
 
+#include "autotune.h"
 #include "common.h"
 #include "host_layer.h"
 #include "kernels.h"
@@ -1073,6 +1074,8 @@ void run_multi(Op op, int n, const s2let_parameters_t *params, const int *real, 
   put(&t_table_mode, sizeof t_table_mode);
   put(&kern, sizeof kern);
   put(&f32, sizeof f32);
+  const int tune = autotune_mode();  // tuned launch shapes: a graph of their own
+  put(&tune, sizeof tune);
   std::lock_guard<std::mutex> lk(g_multi_mu);
   auto it = g_multi_graphs.find(key);
   if (it != g_multi_graphs.end()) {
