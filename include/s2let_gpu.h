@@ -597,11 +597,10 @@ int s2let_gpu_timing_report(double *out, int ncat);
  * out[d*5 + {0,1,2,3,4}] = {copies, bytes, busy milliseconds (sum of the
  * copies' own durations), span milliseconds (first start to last end), copies
  * made by the copy kernel} for direction d = 0 (host to device) and d = 1
- * (device to host).  Copies to page-locked host buffers are made by a copy
- * kernel (SM loads and stores over the host link), copies from them by the
- * copy engines; S2LET_GPU_HOST_COPY=kernel uses the copy kernel both ways,
- * =engine the copy engines both ways.  Pageable host memory always goes
- * through the copy engines. */
+ * (device to host).  Page-locked host buffers are moved by a copy kernel
+ * (SM loads and stores over the host link); other host memory, or every copy
+ * when S2LET_GPU_HOST_COPY=engine, by the copy engines
+ * (S2LET_GPU_HOST_COPY=d2h_kernel: the copy kernel device to host only). */
 int s2let_gpu_copy_trace_enable(int on);
 int s2let_gpu_copy_trace_report(double *out);
 

@@ -522,7 +522,7 @@ bool rings_on_n(const WavPlan &P, const Scale &sd) {
 // launches through a ring buffer (the fused launch keeps them on chip).
 bool needs_ring_buffer(const WavPlan &P) {
   for (const Scale &sd : P.sc)
-    if (!rings_on_n(P, sd) || !ring_gamma_fusable((int)sd.ns.size(), sd.ng)) return true;
+    if (!rings_on_n(P, sd) || !ring_gamma_fusable((int)sd.ns.size(), sd.ng, sd.bl, P.ss)) return true;
   return false;
 }
 
@@ -636,7 +636,7 @@ void wav_split(const WavPlan &P, SplitMode mode, const double2 *flm, bool flm_ha
         for (int b0 = 0; b0 < nb; b0 += G) {
           const int nbg = std::min(G, nb - b0);
           const double2 *Gb = Gq + (int64_t)b0 * nn * nt * W;
-          if (ring_gamma_fusable(nn, ng)) {  // one launch, the n-components stay on chip
+          if (ring_gamma_fusable(nn, ng, bl, P.ss)) {  // one launch, the n-components stay on chip
             ring_inverse_gamma(Gb, (int64_t)nn * nt * W, (int64_t)nt * W, sd.ns, ng, real, c,
                                out + (size_t)b0 * wstride * esz, wstride, nbg, bl, P.ss, S.st);
             if (pipe) pipe->out(S.st, f_wav, wstride, sd.woff, b0, nbg);
@@ -727,7 +727,7 @@ void wav_merge(const WavPlan &P, MergeMode mode, const void *f_wav, int64_t wstr
         for (int b0 = 0; b0 < nb; b0 += G) {
           const int nbg = std::min(G, nb - b0);
           if (pipe) pipe->wait(S.st, sd.woff, b0);
-          if (ring_gamma_fusable(nn, ng)) {  // one launch, the n-components stay on chip
+          if (ring_gamma_fusable(nn, ng, bl, P.ss)) {  // one launch, the n-components stay on chip
             gamma_ring_forward(in + (size_t)b0 * wstride * esz, wstride, sd.ns, ng, real, c,
                                Gq + (int64_t)b0 * nn * nt * W, (int64_t)nn * nt * W, (int64_t)nt * W, nbg, bl, P.ss,
                                S.st);

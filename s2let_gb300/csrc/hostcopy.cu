@@ -6,10 +6,9 @@
 // host to device in every sample, while the copy engines delivered the same
 // rates only part of the time and dropped to 40-110 GB/s (device to host
 // most often) for stretches of tens to hundreds of milliseconds, with or
-// without other GPU activity.  So page-locked host memory is moved to the
-// host by k_copy_rows on the caller's stream (see copy_policy for the other
-// direction); anything else (or every copy, with S2LET_GPU_HOST_COPY=engine)
-// by the copy engines.
+// without other GPU activity.  So page-locked host memory is moved by
+// k_copy_rows on the caller's stream; anything else (or every copy, with
+// S2LET_GPU_HOST_COPY=engine) by the copy engines (see copy_policy).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -55,20 +54,20 @@ __global__ void __launch_bounds__(kCopyThreads) k_copy_rows(char *__restrict__ d
   }
 }
 
-// 0: the copy engines for every copy; 1: a copy kernel for both directions
-// where the host memory is addressable by the device; 2 (default): the copy
-// kernel for device-to-host copies, the copy engines host to device.  With a
-// synthesis call's host-to-device copies overlapping the next analysis call,
-// leaving them to the copy engines frees the copy kernel's SM slots for the
-// transforms (pipelined round trip 118 against 130 ms per 32 maps at L=1024
-// in most steps); the engines' slow stretches were mostly device to host.
-// S2LET_GPU_HOST_COPY=engine selects 0, =kernel 1.
+// 0: the copy engines for every copy; 1 (default): a copy kernel for both
+// directions where the host memory is addressable by the device; 2: the copy
+// kernel device to host, the copy engines host to device.  Policy 2 frees the
+// copy kernel's SM slots while a synthesis call's host-to-device copies
+// overlap the next analysis call (118 against 130 ms per pipelined round trip
+// of 32 maps at L=1024 in most steps), but over 20 steps the engines' slow
+// stretches hit several synthesis calls (260-378 ms instead of 118) and it lost
+// overall.  S2LET_GPU_HOST_COPY=engine selects 0, =d2h_kernel 2.
 int copy_policy() {
   static const int p = [] {
     const char *e = getenv("S2LET_GPU_HOST_COPY");
     if (e && strcmp(e, "engine") == 0) return 0;
-    if (e && strcmp(e, "kernel") == 0) return 1;
-    return 2;
+    if (e && strcmp(e, "d2h_kernel") == 0) return 2;
+    return 1;
   }();
   return p;
 }

@@ -1496,12 +1496,57 @@ void launch_fused(KF kernel, const RingArgs &a, const GammaFuse &gf, int nrings,
 
 }  // namespace
 
-bool ring_gamma_fusable(int nn, int ng) { return t_precision == 1 && nn >= 2 && nn <= kFuseMaxNN && ng * nn <= kFuseMaxTw; }
+namespace {
+// Whether a cluster of nn CTAs of the fused kernels (P-point buffers) can be
+// resident on this GPU: asked once per (nn, P) of the device in use.
+bool cluster_fits(int nn, int P) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, bool> known;
+  std::lock_guard<std::mutex> lk(mu);
+  const auto key = std::make_pair(nn, P);
+  auto it = known.find(key);
+  if (it != known.end()) return it->second;
+  const void *kern = nullptr;
+  switch (nn) {
+    case 2: kern = (const void *)k_ring_inverse_gamma_df<2, false>; break;
+    case 3: kern = (const void *)k_ring_inverse_gamma_df<3, false>; break;
+    case 4: kern = (const void *)k_ring_inverse_gamma_df<4, false>; break;
+    case 5: kern = (const void *)k_ring_inverse_gamma_df<5, false>; break;
+    case 6: kern = (const void *)k_ring_inverse_gamma_df<6, false>; break;
+    case 7: kern = (const void *)k_ring_inverse_gamma_df<7, false>; break;
+    default: kern = (const void *)k_ring_inverse_gamma_df<8, false>; break;
+  }
+  const size_t smem = sizeof(float4) * (size_t)P;
+  ring_smem_attrs(kern, smem, true);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)nn);
+  cfg.blockDim = dim3(ring_threads(P));
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)nn;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg);
+  if (e != cudaSuccess) cudaGetLastError();  // a refusal only means: not fusable here
+  const bool ok = e == cudaSuccess && nclusters > 0;
+  known[key] = ok;
+  return ok;
+}
+}  // namespace
+
+bool ring_gamma_fusable(int nn, int ng, int bl, int ss) {
+  if (t_precision != 1 || nn < 2 || nn > kFuseMaxNN || ng * nn > kFuseMaxTw) return false;
+  return cluster_fits(nn, ring_fft(grid_ring_len(bl, ss)).P);
+}
 
 void ring_inverse_gamma(const double2 *G, int64_t gms, int64_t gks, const std::vector<int> &ns, int ng, bool real,
                         double c, void *fw, int64_t fms, int nb, int bl, int ss, cudaStream_t st) {
   const int nn = (int)ns.size();
-  S2G_REQUIRE(ring_gamma_fusable(nn, ng), ERR_UNSUPPORTED, "fused ring/gamma DFT: unsupported direction count");
+  S2G_REQUIRE(ring_gamma_fusable(nn, ng, bl, ss), ERR_UNSUPPORTED, "fused ring/gamma DFT: unsupported shape");
   const int nt = grid_rings(bl, ss), nrings = nb * nt;
   if (nrings <= 0) return;
   const RingFFT &rf = ring_fft(grid_ring_len(bl, ss));
@@ -1541,7 +1586,7 @@ void ring_inverse_gamma(const double2 *G, int64_t gms, int64_t gks, const std::v
 void gamma_ring_forward(const void *fw, int64_t fms, const std::vector<int> &ns, int ng, bool real, double c,
                         double2 *Gout, int64_t gms, int64_t gks, int nb, int bl, int ss, cudaStream_t st) {
   const int nn = (int)ns.size();
-  S2G_REQUIRE(ring_gamma_fusable(nn, ng), ERR_UNSUPPORTED, "fused ring/gamma DFT: unsupported direction count");
+  S2G_REQUIRE(ring_gamma_fusable(nn, ng, bl, ss), ERR_UNSUPPORTED, "fused ring/gamma DFT: unsupported shape");
   const int nt = grid_rings(bl, ss), nrings = nb * nt;
   if (nrings <= 0) return;
   const RingFFT &rf = ring_fft(grid_ring_len(bl, ss));

@@ -115,7 +115,10 @@ void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns,
 
 // Ring DFTs fused with the gamma DFT in one launch (split precision; a
 // thread-block cluster per ring, one CTA per n-component), usable when
-// ring_gamma_fusable(nn, ng).  Component k of ring (b, t), t < nt, has its
+// ring_gamma_fusable(nn, ng, bl, ss): the split-precision path, 2 <= nn <= 8,
+// nn ng <= 128, and a cluster of nn CTAs fits on this GPU (asked once per
+// shape; otherwise the ring and gamma DFTs run as separate launches).
+// Component k of ring (b, t), t < nt, has its
 // spectrum at G + b gms + k gks + t W (W = 2bl-1, m from -(bl-1); on real
 // signals the component with n = 0 holds m >= 0 at offset bl-1, the rest by
 // Hermitian symmetry); gamma slice g of ring (b, t) lives at
@@ -124,7 +127,7 @@ void gamma_px_analysis(const void *in, int64_t in_ms, double2 *F, const int *ns,
 //                        n_k > 0, Re for n_k = 0), F_k the inverse ring DFT
 //   gamma_ring_forward:  F_k = c sum_g e^{-i n_k gamma_g} f_g, then the
 //                        forward ring DFT of every F_k to G (all m)
-bool ring_gamma_fusable(int nn, int ng);
+bool ring_gamma_fusable(int nn, int ng, int bl, int ss);
 void ring_inverse_gamma(const double2 *G, int64_t gms, int64_t gks, const std::vector<int> &ns, int ng, bool real,
                         double c, void *fw, int64_t fms, int nb, int bl, int ss, cudaStream_t st);
 void gamma_ring_forward(const void *fw, int64_t fms, const std::vector<int> &ns, int ng, bool real, double c,
