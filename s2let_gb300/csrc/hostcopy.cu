@@ -85,14 +85,28 @@ bool device_addressable(const void *h) {
   return at.type == cudaMemoryTypeHost && at.devicePointer == h;
 }
 
+// CTAs per copy: kCopyBlocks, or S2LET_GPU_COPY_CTAS (1-1024).  Measured on
+// the pipelined host batches at L=1024 (32 maps per call): 64 CTAs 239
+// maps/s, 32 CTAs 232, 16 CTAs 201 (fewer copy CTAs slow the copies more than
+// they help the transforms).
+int copy_blocks() {
+  static const int b = [] {
+    const char *e = getenv("S2LET_GPU_COPY_CTAS");
+    const int v = e ? atoi(e) : 0;
+    return (v >= 1 && v <= 1024) ? v : kCopyBlocks;
+  }();
+  return b;
+}
+
 template <class T>
 void launch_rows(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
                  cudaStream_t st) {
   const size_t n = width / sizeof(T);
   const size_t per = (size_t)kCopyThreads * kCopyUnroll;
   const size_t want = (n + per - 1) / per;
-  int bx = (int)(want < (size_t)kCopyBlocks ? want : (size_t)kCopyBlocks);
-  if (height > 1) bx = (bx + (int)height - 1) / (int)height;  // about kCopyBlocks CTAs in all
+  const int nblk = copy_blocks();
+  int bx = (int)(want < (size_t)nblk ? want : (size_t)nblk);
+  if (height > 1) bx = (bx + (int)height - 1) / (int)height;  // about nblk CTAs in all
   if (bx < 1) bx = 1;
   k_copy_rows<T><<<dim3(bx, (unsigned)height), kCopyThreads, 0, st>>>((char *)dst, dpitch, (const char *)src,
                                                                        spitch, n);
