@@ -1235,6 +1235,17 @@ int batch_directional_f32(const char *fn, s2g::Op op, const s2let_parameters_t *
 // sized with N) crosses the bus, as in the drop-in functions.  Synchronous.
 constexpr int kHostPass = 32;   // maps per device batch
 constexpr int kHostGroups = 4;  // map groups per scale (pieces of at most 8 maps)
+// map groups per scale: kHostGroups, or S2LET_GPU_HOST_GROUPS (1-32).
+// Pipelined host batches at L=1024 (32 maps per call) measured 238 / 242 / 241
+// maps/s with 4 / 8 / 2 groups: within the run-to-run spread.
+int host_groups() {
+  static const int g = [] {
+    const char *e = getenv("S2LET_GPU_HOST_GROUPS");
+    const int v = e ? atoi(e) : 0;
+    return (v >= 1 && v <= 32) ? v : kHostGroups;
+  }();
+  return g;
+}
 int host_pass(int nb) {
   const char *e = getenv("S2LET_GPU_HOST_PASS");
   const int v = e ? atoi(e) : 0;
@@ -1291,7 +1302,8 @@ int host_batch(const char *fn, s2g::Op op, const s2let_parameters_t *p, bool rea
       pipe.host = hw + (size_t)c0 * nw * esz;
       pipe.hstride = nw;
       pipe.esz = esz;
-      pipe.group = std::max(1, std::min(8, (n + kHostGroups - 1) / kHostGroups));
+      const int ngrp = host_groups();
+      pipe.group = std::max(1, std::min(8, (n + ngrp - 1) / ngrp));
       for (size_t k = 0; k < P.sc.size(); ++k)
         pipe.seglen[P.sc[k].woff] = (k + 1 < P.sc.size() ? P.sc[k + 1].woff : nwu) - P.sc[k].woff;
       // the copy stream uses the new buffers only after their allocation on st
