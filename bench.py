@@ -626,6 +626,23 @@ def run_recompute_workload(a, world, rank, local):
         ms32 = event_ms(multi_step_f32, a.steps)
         err32 = max(float(((rec32[k].to(rec[k].dtype) - rec[k]).abs().max() / rec[k].abs().max()).item())
                     for k in range(n))
+        # configuration 4 as specified: FP32 storage, split precision (double-float
+        # contractions on the recomputed tables), autotuned launch shapes, graph-replayed
+        lib.s2let_gpu_set_precision(1)
+        for _ in range(max(a.warmup, 2)):
+            multi_step_f32()
+        ms32_mx = event_ms(multi_step_f32, a.steps)
+        rec32_mx = [r.clone() for r in rec32]
+        err32_mx = max(float(((rec32_mx[k].to(rec[k].dtype) - rec[k]).abs().max() / rec[k].abs().max()).item())
+                       for k in range(n))
+        for _ in range(max(a.warmup, 2)):
+            multi_step(arr)
+        ms_mx = event_ms(lambda: multi_step(arr), a.steps)
+        err_mx = max(float(((rec[k] - px[k]).abs().max() / px[k].abs().max()).item()) for k in range(n))
+        for _ in range(a.warmup):
+            loop_step()
+        loop_mx_ms = event_ms(loop_step, a.steps)
+        lib.s2let_gpu_set_precision(0)
         # autotuned launch shapes (tuned on the first call of each shape, cache in a temporary file)
         import tempfile
 
@@ -638,6 +655,13 @@ def run_recompute_workload(a, world, rank, local):
         torch.cuda.synchronize()
         tune_s = time.time() - t0
         ms_tuned = event_ms(lambda: multi_step(arr), a.steps)
+        # the configuration-4 recipe with the tuned shapes (tuning again at split precision)
+        lib.s2let_gpu_set_precision(1)
+        for _ in range(max(a.warmup, 2) + 1):
+            multi_step_f32()
+        torch.cuda.synchronize()
+        ms_cfg4 = event_ms(multi_step_f32, a.steps)
+        lib.s2let_gpu_set_precision(0)
         ntuned = lib.s2let_gpu_autotune_entries((C.c_int * 5000)(), (C.c_double * 2000)(), 1000)
         lib.s2let_gpu_autotune(old_tune)
         buckets = {}
@@ -652,19 +676,33 @@ def run_recompute_workload(a, world, rank, local):
             buckets[f"L{lo}-{min(hi, 512)}"] = {"maps": len(idx), "maps_per_s": len(idx) / (bms * 1e-3),
                                                 "ms": bms}
         out.update({
-            "metric": "uneven batch px2wav+wav2px maps/s (256 maps, own L/N/spin each, one graph-replayed call)",
-            "value": whole_job_rate(n, world, ms * 1e-3), "ms_per_step": ms,
+            "metric": "uneven batch px2wav+wav2px maps/s (256 maps, own L/N/spin each, one graph-replayed call; "
+                      "FP32 storage, split precision, autotuned launch shapes)",
+            "value": whole_job_rate(n, world, ms_cfg4 * 1e-3), "ms_per_step": ms_cfg4,
+            "dtype": "f32 storage; double-float recomputed-table contractions and ring DFTs (split precision)",
             "config": {"workload": "256 maps, L log-uniform on [64, 512] rounded to even, N in {1,3,5}, "
                                    "spin in {0,2} (spin 0 real, spin 2 complex), B=2, J_min=1, MW, "
-                                   "power-law flm; FP64 storage, recomputed Wigner tables, FP64 contraction",
+                                   "power-law flm; recomputed Wigner tables",
                        "distinct_parameter_sets": len({(m[0], m[1], m[2]) for m in maps}),
                        "l2": "inputs and outputs of the 256 maps exceed L2"},
-            "one_call_per_map_loop": {"value": whole_job_rate(n, world, loop_ms * 1e-3), "ms_per_step": loop_ms},
+            "fp64": {"value": whole_job_rate(n, world, ms * 1e-3), "ms_per_step": ms,
+                     "what": "FP64 storage, FP64 contractions, graph-replayed"},
+            "split_precision": {"value": whole_job_rate(n, world, ms_mx * 1e-3), "ms_per_step": ms_mx,
+                                "what": "FP64 storage, split precision, graph-replayed",
+                                "max_rel_err_round_trip": err_mx},
+            "split_precision_fp32_storage": {"value": whole_job_rate(n, world, ms32_mx * 1e-3),
+                                             "ms_per_step": ms32_mx,
+                                             "max_rel_err_vs_fp64": err32_mx},
+            "one_call_per_map_loop": {"value": whole_job_rate(n, world, loop_ms * 1e-3), "ms_per_step": loop_ms,
+                                      "what": "FP64, one s2let_gpu_*_batch call per map"},
+            "one_call_per_map_loop_split": {"value": whole_job_rate(n, world, loop_mx_ms * 1e-3),
+                                            "ms_per_step": loop_mx_ms,
+                                            "what": "split precision, one call per map"},
             "fp32_storage": {"value": whole_job_rate(n, world, ms32 * 1e-3), "ms_per_step": ms32,
                              "api": "s2let_gpu_px2wav_multi_f32 + s2let_gpu_wav2px_multi_f32 (graph-replayed)",
                              "max_rel_err_vs_fp64_storage": err32},
             "autotuned": {"value": whole_job_rate(n, world, ms_tuned * 1e-3), "ms_per_step": ms_tuned,
-                          "tuning_s": tune_s, "shapes_recorded": ntuned},
+                          "what": "FP64, tuned launch shapes", "tuning_s": tune_s, "shapes_recorded": ntuned},
             "per_L_bucket": buckets,
             "plan_build_s": build_s,
             "max_rel_err_round_trip": err,
@@ -693,12 +731,23 @@ def run_recompute_workload(a, world, rank, local):
         build_s = time.time() - t0
         for _ in range(max(1, a.warmup - 1)):
             step()
+        ms64 = event_ms(step, a.steps)
+        err64 = float(((r - f).abs().max() / f.abs().max()).item())
+        w64 = w.clone()
+        lib.s2let_gpu_set_precision(1)  # split precision: double-float recomputed-table contractions
+        for _ in range(max(1, a.warmup - 1)):
+            step()
         clocks.start()
         ms = event_ms(step, a.steps)
         clk = clocks.stop()
+        lib.s2let_gpu_set_precision(0)
         out.update({
-            "metric": "px2wav+wav2px maps/s at L=2048, N=4 (recomputed Wigner tables, FP64)",
+            "metric": "px2wav+wav2px maps/s at L=2048, N=4 (recomputed Wigner tables, split precision)",
             "value": whole_job_rate(1, world, ms * 1e-3), "ms_per_step": ms,
+            "dtype": "double-float recomputed-table contractions and ring DFTs, FP64 quadrature",
+            "fp64_path": {"value": whole_job_rate(1, world, ms64 * 1e-3), "ms_per_step": ms64,
+                          "max_rel_err_round_trip": err64},
+            "max_rel_err_f_wav_vs_fp64": float(((w - w64).abs().max() / w64.abs().max()).item()),
             "config": {"workload": "one real spin-0 map, L=2048, N=4, B=2, J_min=2, upsample=0, MW, "
                                    "power-law band-limited flm", "table_bytes_device": lib.s2let_gpu_plan_bytes()},
             "plan_build_s": build_s,

@@ -17,6 +17,7 @@
 
 #include "autotune.h"
 #include "common.h"
+#include "dfarith.h"
 #include "dfconv.h"
 #include "kernels.h"
 #include "mixed.h"
@@ -242,61 +243,6 @@ __global__ void __launch_bounds__(512) k_ring_inverse(RingArgs a) {
 // emulated on the CPU) for 22 % fewer FP32 instructions per butterfly; the
 // FP64 widening at the end accepts any hi/lo split.
 // ---------------------------------------------------------------------------
-
-__device__ __forceinline__ float2 df_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  const float v = __fsub_rn(s, a);
-  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
-  return make_float2(s, e);
-}
-__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
-  float2 s = df_two_sum(a.x, b.x);
-  s.y = __fadd_rn(s.y, __fadd_rn(a.y, b.y));
-  return s;
-}
-__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
-// a*b + c*d (double-float in, double-float out)
-__device__ __forceinline__ float2 df_dot2(float2 a, float2 b, float2 c, float2 d) {
-  const float p1 = __fmul_rn(a.x, b.x);
-  const float e1 = __fmaf_rn(a.x, b.x, -p1);
-  const float p2 = __fmul_rn(c.x, d.x);
-  const float e2 = __fmaf_rn(c.x, d.x, -p2);
-  const float2 s = df_two_sum(p1, p2);
-  float e = __fadd_rn(s.y, __fadd_rn(e1, e2));
-  e = __fmaf_rn(a.x, b.y, e);
-  e = __fmaf_rn(a.y, b.x, e);
-  e = __fmaf_rn(c.x, d.y, e);
-  e = __fmaf_rn(c.y, d.x, e);
-  return make_float2(s.x, e);
-}
-// complex double-float as float4 (re.hi, re.lo, im.hi, im.lo)
-__device__ __forceinline__ float2 dre(float4 z) { return make_float2(z.x, z.y); }
-__device__ __forceinline__ float2 dim_(float4 z) { return make_float2(z.z, z.w); }
-__device__ __forceinline__ float4 dmk(float2 re, float2 im) { return make_float4(re.x, re.y, im.x, im.y); }
-__device__ __forceinline__ float4 dc_mul(float4 a, float4 b) {
-  return dmk(df_dot2(dre(a), dre(b), df_neg(dim_(a)), dim_(b)), df_dot2(dre(a), dim_(b), dim_(a), dre(b)));
-}
-__device__ __forceinline__ float4 dc_mulc(float4 a, float4 b) {  // a * conj(b)
-  return dmk(df_dot2(dre(a), dre(b), dim_(a), dim_(b)), df_dot2(dim_(a), dre(b), df_neg(dre(a)), dim_(b)));
-}
-__device__ __forceinline__ float4 dc_add(float4 a, float4 b) {
-  return dmk(df_add(dre(a), dre(b)), df_add(dim_(a), dim_(b)));
-}
-__device__ __forceinline__ float4 dc_sub(float4 a, float4 b) {
-  return dmk(df_add(dre(a), df_neg(dre(b))), df_add(dim_(a), df_neg(dim_(b))));
-}
-__device__ __forceinline__ float4 dc_conj(float4 a) { return make_float4(a.x, a.y, -a.z, -a.w); }
-// FP64 <-> double-float with a power-of-two block scale, by bit construction
-// (dfconv.h): no FP64 instructions but one add per value joined
-__device__ __forceinline__ float2 df_split(double v, int e) {
-  float h, l;
-  split_scaled(v, e, h, l);
-  return make_float2(h, l);
-}
-__device__ __forceinline__ float4 dc_split(double2 v, int e) { return dmk(df_split(v.x, e), df_split(v.y, e)); }
-__device__ __forceinline__ double2 dc_to(float4 z, int e) {
-  return make_double2(join_scaled(z.x, z.y, e), join_scaled(z.z, z.w, e));
-}
 
 // Stages are paired (radix 2^2): one pass over shared memory and one barrier
 // per two radix-2 stages; a leftover single stage when log2 P is odd.
@@ -990,13 +936,6 @@ __global__ void k_gamma_px_anal(const void *__restrict__ in, int64_t in_ms, doub
 // from their largest exponent field, the twiddles (times the normalisation c,
 // times 2 for the real +-n pairs) are double-float constants, and each output
 // costs one FP64 add to widen.
-__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
-  const float p = __fmul_rn(a.x, b.x);
-  float e = __fmaf_rn(a.x, b.x, -p);
-  e = __fmaf_rn(a.x, b.y, e);
-  e = __fmaf_rn(a.y, b.x, e);
-  return make_float2(p, e);
-}
 
 template <int NN>
 __global__ void k_gamma_px_synth_df(const double2 *__restrict__ F, void *__restrict__ out, int64_t out_ms,

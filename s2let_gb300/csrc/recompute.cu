@@ -22,7 +22,9 @@
 
 #include "autotune.h"
 #include "common.h"
+#include "dfarith.h"
 #include "kernels.h"
+#include "mixed.h"
 #include "recompute.h"
 #include "timing.h"
 
@@ -331,6 +333,291 @@ __global__ void __launch_bounds__(kRcT) k_rc_t2l(RcArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// double-float variants (split-precision path on recomputed tables)
+//
+// The same two contractions with the per-map multiply-adds in double-float
+// arithmetic on the FP32 pipe (dfarith.h), which GB300 issues at about 64
+// times its FP64 rate.  The three-term recursion stays in FP64 (3 instructions
+// per value, shared by all maps): in double-float its cancellation near the
+// turning points cost 1e-11 of accuracy (2^-47 against 2^-53 per step over a
+// 64-degree segment).  Each value is split into a double-float pair once
+// (integer bit operations, dfconv.h) and multiplied into every map's partial
+// sum; FP64 is otherwise left to the flush of the partial sums (two adds per
+// output value and segment, or per tile of rings for t -> l).  Values are
+// carried scaled by 2^-E per ring and segment as in the FP64 kernels, with a
+// lower rescaling threshold (2^kRenormDf) so that they stay in the float
+// range.  Coefficients (l -> t) and spectra (t -> l) enter as double-float
+// scaled by the largest power of two of their block (segment or tile, per
+// map).  Accumulators are renormalised after each add.
+// ---------------------------------------------------------------------------
+
+constexpr int kRenormDf = 60;
+
+__device__ __forceinline__ float2 df_of(double v) {  // |v| within the float range
+  float h, l;
+  split_scaled(v, 0, h, l);
+  return make_float2(h, l);
+}
+__device__ __forceinline__ float2 df_scale(float2 a, int k) { return make_float2(scale_pow2(a.x, k), scale_pow2(a.y, k)); }
+// s += v x (double-float real times complex), the accumulator renormalised
+// after each add (unnormalised sums of 64-128 terms lost about 6 bits)
+__device__ __forceinline__ void df_mac(float4 &s, float2 v, float4 x) {
+  s = dmk(df_add_norm(dre(s), df_mul(v, dre(x))), df_add_norm(dim_(s), df_mul(v, dim_(x))));
+}
+
+template <int NBT>
+__global__ void __launch_bounds__(kRcT) k_rc_l2t_df(RcArgs a) {
+  __shared__ double2 scn[kSeg], scs[kSeg];
+  __shared__ double sc2[kSeg];
+  __shared__ double2 sxd[kSeg][NBT];  // weighted coefficients of the segment
+  __shared__ float4 sx[kSeg][NBT];    // the same as double-float, scaled by 2^-sxs[b]
+  __shared__ int sxm[NBT], sxs[NBT];
+  const int m = a.mlo + blockIdx.x;
+  const int am = m < 0 ? -m : m;
+  const RcRef r = rc_ref(a, m);
+  const int amt = r.mt < 0 ? -r.mt : r.mt;
+  const int l0 = amt > a.an ? amt : a.an, bl = a.bl, nl = bl - l0;
+  const int lst = l0 > a.lmin ? l0 : a.lmin;
+  const int t = blockIdx.y * kRcT + threadIdx.x;
+  const bool live = t < a.nt;
+  const int b0 = blockIdx.z * NBT;
+  double2 acc[NBT];
+#pragma unroll
+  for (int b = 0; b < NBT; ++b) acc[b] = make_double2(0.0, 0.0);
+  double u = 0.0;
+  bool north = true;
+  if (live) {
+    const double2 q = a.uq[t];
+    u = q.x;
+    north = q.y != 0.0;
+  }
+  if (nl > 0 && lst < bl) {
+    const int nseg = (nl + kSeg - 1) / kSeg, c0 = (lst - l0) / kSeg;
+    const double2 *ck = a.ck + a.coff[r.mi];
+    const int *cke = a.ck_e + a.coff[r.mi];
+    const double2 *cc = north ? scn : scs;
+    for (int c = c0; c < nseg; ++c) {
+      const int lc = l0 + c * kSeg, n = min(kSeg, bl - lc);
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += kRcT)
+        if (i >= 1) rec_coef(lc + i, r.mt, a.an, scn[i], scs[i], sc2[i]);
+      if (threadIdx.x < NBT) sxm[threadIdx.x] = 0;
+      __syncthreads();
+      for (int i = threadIdx.x; i < kSeg * NBT; i += kRcT) {
+        const int kk = i / NBT, b = i % NBT, l = lc + kk;
+        double2 v = make_double2(0.0, 0.0);
+        if (kk < n && l >= lst && b0 + b < a.nb) {
+          const int64_t base = (int64_t)(b0 + b) * a.ss + (int64_t)l * l + l;
+          if (a.x_half && m < 0) {
+            v = a.src[base - m];
+            v.y = -v.y;
+            if (am & 1) v = make_double2(-v.x, -v.y);
+          } else {
+            v = a.src[base + m];
+          }
+          v = cmul_(v, weight_of(a, l));
+        }
+        sxd[kk][b] = v;
+        atomicMax(&sxm[b], max(exp_bits(v.x), exp_bits(v.y)));
+      }
+      __syncthreads();
+      if (threadIdx.x < NBT) sxs[threadIdx.x] = block_scale(sxm[threadIdx.x]);
+      __syncthreads();
+      for (int i = threadIdx.x; i < kSeg * NBT; i += kRcT) {
+        const int kk = i / NBT, b = i % NBT;
+        sx[kk][b] = dc_split(sxd[kk][b], sxs[b]);
+      }
+      __syncthreads();
+      if (!live) continue;
+      int E = cke[(int64_t)c * a.nt + t];
+      if (E < -1074 - 2 * kRenorm) continue;  // the whole segment is below the double range
+      const double2 ab = ck[(int64_t)c * a.nt + t];
+      double vp = ab.x, v = ab.y;
+      float4 sum[NBT];
+      {
+        const float2 dvp = df_of(vp), dv = df_of(v);
+#pragma unroll
+        for (int b = 0; b < NBT; ++b) {
+          sum[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+          df_mac(sum[b], dvp, sx[0][b]);
+          if (n > 1) df_mac(sum[b], dv, sx[1][b]);
+        }
+      }
+      for (int i = 1; i + 1 < n; ++i) {
+        const double2 k = cc[i];
+        const double xt = fma(k.x, u, k.y);
+        const double vn = fma(xt, v, -sc2[i] * vp);
+        vp = v;
+        v = vn;
+        if (exp_bits(v) > 1023 + kRenormDf) {  // flush at the old scale, continue at the new one
+#pragma unroll
+          for (int b = 0; b < NBT; ++b) {
+            const double2 f = dc_to(sum[b], E + sxs[b]);
+            acc[b].x += f.x;
+            acc[b].y += f.y;
+            sum[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+          v = ldexp(v, -kRenormDf);
+          vp = ldexp(vp, -kRenormDf);
+          E += kRenormDf;
+        }
+        const float2 dv = df_of(v);
+#pragma unroll
+        for (int b = 0; b < NBT; ++b) df_mac(sum[b], dv, sx[i + 1][b]);
+      }
+#pragma unroll
+      for (int b = 0; b < NBT; ++b) {
+        const double2 f = dc_to(sum[b], E + sxs[b]);
+        acc[b].x += f.x;
+        acc[b].y += f.y;
+      }
+    }
+  }
+  if (!live) return;
+#pragma unroll
+  for (int b = 0; b < NBT; ++b) {
+    if (b0 + b >= a.nb) break;
+    a.dst[(int64_t)(b0 + b) * a.ds + (int64_t)t * a.dw + (m - a.d_mlo)] =
+        make_double2(acc[b].x * r.sign, acc[b].y * r.sign);
+  }
+}
+
+template <int NBT>
+size_t rc_t2l_df_smem() {
+  return sizeof(float2) * kRcT * kTileLd + sizeof(float4) * kRcT * NBT;
+}
+
+// t -> l in double-float: the tile rows (one ring each, scaled by 2^-E_t)
+// as double-float pairs; the spectra enter scaled by 2^(E_t - es[b]) with es[b]
+// the largest exponent of spectrum times ring scale over the tile, so the
+// sums over the tile's rings share one power of two and are flushed to FP64
+// once per tile.
+template <int NBT>
+__global__ void __launch_bounds__(kRcT) k_rc_t2l_df(RcArgs a) {
+  static_assert(NBT == 1 || NBT % 2 == 0, "one map, or two map halves");
+  constexpr int NH = NBT == 1 ? 1 : NBT / 2;
+  constexpr bool SPLIT_T = NBT == 1;
+  extern __shared__ float2 smem_df[];
+  float2 *tile = smem_df;                                  // [kRcT][kTileLd]
+  float4 *sg = (float4 *)(smem_df + kRcT * kTileLd);       // [kRcT][NBT]
+  __shared__ double2 scn[kSeg], scs[kSeg];
+  __shared__ double sc2[kSeg];
+  __shared__ int sgm[NBT];
+  const int m = a.mlo + blockIdx.x, c = blockIdx.y;
+  const RcRef r = rc_ref(a, m);
+  const int amt = r.mt < 0 ? -r.mt : r.mt;
+  const int l0 = amt > a.an ? amt : a.an, bl = a.bl, nl = bl - l0;
+  const int lst = l0 > a.lmin ? l0 : a.lmin;
+  const int nseg = nl > 0 ? (nl + kSeg - 1) / kSeg : 0;
+  if (c >= nseg) return;
+  const int lc = l0 + c * kSeg, n = min(kSeg, bl - lc);
+  if (lc + n <= lst) return;  // every degree of the segment is below lmin: no output
+  const int b0 = blockIdx.z * NBT;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < n; i += kRcT)
+    if (i >= 1) rec_coef(lc + i, r.mt, a.an, scn[i], scs[i], sc2[i]);
+  const double2 *ck = a.ck + a.coff[r.mi] + (int64_t)c * a.nt;
+  const int *cke = a.ck_e + a.coff[r.mi] + (int64_t)c * a.nt;
+  const int li = tid % kSeg, bh = tid / kSeg;
+  double2 acc[NH];
+#pragma unroll
+  for (int j = 0; j < NH; ++j) acc[j] = make_double2(0.0, 0.0);
+  __syncthreads();
+  for (int t0 = 0; t0 < a.nt; t0 += kRcT) {
+    const int t = t0 + tid;
+    float2 *row = tile + tid * kTileLd;
+    int E = kCkZeroExp;
+    if (t < a.nt) E = cke[t];
+    const bool on = E >= -1074 - 2 * kRenorm;
+    if (on) {
+      const double2 q = a.uq[t];
+      const double u = q.x;
+      const double2 *cc = q.y != 0.0 ? scn : scs;
+      const double2 ab = ck[t];
+      double vp = ab.x, v = ab.y;
+      row[0] = df_of(vp);
+      if (n > 1) row[1] = df_of(v);
+      for (int i = 1; i + 1 < n; ++i) {
+        const double2 k = cc[i];
+        const double xt = fma(k.x, u, k.y);
+        const double vn = fma(xt, v, -sc2[i] * vp);
+        vp = v;
+        v = vn;
+        if (exp_bits(v) > 1023 + kRenormDf) {  // keep one scale per row: rescale what is written
+          for (int j = 0; j <= i; ++j) row[j] = df_scale(row[j], -kRenormDf);
+          v = ldexp(v, -kRenormDf);
+          vp = ldexp(vp, -kRenormDf);
+          E += kRenormDf;
+        }
+        row[i + 1] = df_of(v);
+      }
+      for (int i = n; i < kSeg; ++i) row[i] = make_float2(0.f, 0.f);
+    } else {
+      for (int i = 0; i < kSeg; ++i) row[i] = make_float2(0.f, 0.f);
+    }
+    // the spectra of this ring times 2^E, and the tile's largest exponent per map
+    if (tid < NBT) sgm[tid] = -(1 << 30);
+    __syncthreads();
+    double2 g[NBT];
+#pragma unroll
+    for (int b = 0; b < NBT; ++b) {
+      g[b] = make_double2(0.0, 0.0);
+      if (on && b0 + b < a.nb) {
+        g[b] = a.src[(int64_t)(b0 + b) * a.ss + (int64_t)t * a.sw + (m - a.s_mlo)];
+        const int ex = max(exp_bits(g[b].x), exp_bits(g[b].y));
+        if (ex > 0) atomicMax(&sgm[b], ex + E);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NBT; ++b) {
+      const int es = sgm[b] > -(1 << 29) ? block_scale(sgm[b]) : 0;
+      sg[tid * NBT + b] = on ? dc_split(g[b], es - E) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    const int tl_end = min(kRcT, a.nt - t0);
+    const int tl_lo = SPLIT_T ? bh * (kRcT / 2) : 0;
+    const int tl_hi = SPLIT_T ? min(tl_end, tl_lo + kRcT / 2) : tl_end;
+    float4 sum[NH];
+#pragma unroll
+    for (int j = 0; j < NH; ++j) sum[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
+    for (int tl = tl_lo; tl < tl_hi; ++tl) {
+      const float2 d = tile[tl * kTileLd + li];
+#pragma unroll
+      for (int j = 0; j < NH; ++j) df_mac(sum[j], d, sg[tl * NBT + (SPLIT_T ? 0 : bh * NH) + j]);
+    }
+#pragma unroll
+    for (int j = 0; j < NH; ++j) {
+      const int b = (SPLIT_T ? 0 : bh * NH) + j;
+      const int es = sgm[b] > -(1 << 29) ? block_scale(sgm[b]) : 0;
+      const double2 f = dc_to(sum[j], es);
+      acc[j].x += f.x;
+      acc[j].y += f.y;
+    }
+    __syncthreads();
+  }
+  if (SPLIT_T) {  // second half of the rings hands its sums to the first
+    double2 *red = (double2 *)sg;  // free after the last tile
+    if (bh == 1) red[li] = acc[0];
+    __syncthreads();
+    if (bh == 1) return;
+    acc[0].x += red[li].x;
+    acc[0].y += red[li].y;
+  }
+  const int l = lc + li;
+  if (li >= n || l < lst) return;
+  const double2 wt = weight_of(a, l);
+#pragma unroll
+  for (int j = 0; j < NH; ++j) {
+    const int b = b0 + (SPLIT_T ? 0 : bh * NH) + j;
+    if (b >= a.nb) break;
+    const double2 v = make_double2(acc[j].x * r.sign, acc[j].y * r.sign);
+    a.dst[(int64_t)b * a.ds + (int64_t)l * l + l + m] = cmul_(v, wt);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // quadrature operator on ring spectra
 // ---------------------------------------------------------------------------
 
@@ -472,6 +759,26 @@ void launch_t2l(const RcArgs &a, int nm, int maxseg, cudaStream_t st) {
   S2G_LAUNCHED();
 }
 
+template <int NBT>
+void launch_l2t_df(const RcArgs &a, int nm, cudaStream_t st) {
+  dim3 grid(nm, ceil_div(a.nt, kRcT), ceil_div(a.nb, NBT));
+  k_rc_l2t_df<NBT><<<grid, kRcT, 0, st>>>(a);
+  S2G_LAUNCHED();
+}
+
+template <int NBT>
+void launch_t2l_df(const RcArgs &a, int nm, int maxseg, cudaStream_t st) {
+  const size_t smem = rc_t2l_df_smem<NBT>();
+  static const bool attr = [smem] {  // once per instantiation (thread-safe static initialisation)
+    S2G_CUDA(cudaFuncSetAttribute(k_rc_t2l_df<NBT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return true;
+  }();
+  (void)attr;
+  dim3 grid(nm, maxseg, ceil_div(a.nb, NBT));
+  k_rc_t2l_df<NBT><<<grid, kRcT, smem, st>>>(a);
+  S2G_LAUNCHED();
+}
+
 }  // namespace
 
 void contract_l2t_rc(const L2T &p, cudaStream_t st) {
@@ -497,7 +804,18 @@ void contract_l2t_rc(const L2T &p, cudaStream_t st) {
     double fl = 0, by = 0;
     if (timing_enabled()) rc_work(tb, p.mlo, p.mhi, p.lmin, p.nb, &fl, &by);
     // maps per CTA: the largest of 1/2/4/8 the batch fills, or the autotuned choice
+    // split precision: the double-float kernels (same results to about 1e-13)
+    const bool df = t_precision == 1;
     const auto run = [&](int nbc) {
+      if (df) {
+        switch (nbc) {
+          case 8: launch_l2t_df<8>(a, nm, st); break;
+          case 4: launch_l2t_df<4>(a, nm, st); break;
+          case 2: launch_l2t_df<2>(a, nm, st); break;
+          default: launch_l2t_df<1>(a, nm, st); break;
+        }
+        return;
+      }
       switch (nbc) {
         case 8: launch_l2t<8>(a, nm, st); break;
         case 4: launch_l2t<4>(a, nm, st); break;
@@ -507,7 +825,7 @@ void contract_l2t_rc(const L2T &p, cudaStream_t st) {
     };
     static const int kCand[4] = {1, 2, 4, 8};
     const int ncand = p.nb >= 8 ? 4 : (p.nb >= 4 ? 3 : (p.nb >= 2 ? 2 : 1));
-    const int c = tuned(TF_RC_L2T, tune_bucket(tb.bl), tune_bucket(p.nb), 0, ncand, ncand - 1, st,
+    const int c = tuned(TF_RC_L2T, tune_bucket(tb.bl), tune_bucket(p.nb), df ? 1 : 0, ncand, ncand - 1, st,
                         [&](int i) { run(kCand[i]); });
     KTimer kt(KC_RECOMPUTE, st, fl, by);
     run(kCand[c]);
@@ -543,7 +861,18 @@ void contract_t2l_rc(const T2L &p, cudaStream_t st) {
     double fl = 0, by = 0;
     if (timing_enabled()) rc_work(tb, p.mlo, p.mhi, p.lmin, p.nb, &fl, &by);
     // maps per CTA: the largest of 1/2/4/8/16 the batch fills, or the autotuned choice
+    const bool df = t_precision == 1;  // split precision: the double-float kernels
     const auto run = [&](int nbc) {
+      if (df) {
+        switch (nbc) {
+          case 16: launch_t2l_df<16>(a, nm, maxseg, st); break;
+          case 8: launch_t2l_df<8>(a, nm, maxseg, st); break;
+          case 4: launch_t2l_df<4>(a, nm, maxseg, st); break;
+          case 2: launch_t2l_df<2>(a, nm, maxseg, st); break;
+          default: launch_t2l_df<1>(a, nm, maxseg, st); break;
+        }
+        return;
+      }
       switch (nbc) {
         case 16: launch_t2l<16>(a, nm, maxseg, st); break;
         case 8: launch_t2l<8>(a, nm, maxseg, st); break;
@@ -554,7 +883,7 @@ void contract_t2l_rc(const T2L &p, cudaStream_t st) {
     };
     static const int kCand[5] = {1, 2, 4, 8, 16};
     const int ncand = p.nb >= 16 ? 5 : (p.nb >= 8 ? 4 : (p.nb >= 4 ? 3 : (p.nb >= 2 ? 2 : 1)));
-    const int c = tuned(TF_RC_T2L, tune_bucket(tb.bl), tune_bucket(p.nb), 0, ncand, ncand - 1, st,
+    const int c = tuned(TF_RC_T2L, tune_bucket(tb.bl), tune_bucket(p.nb), df ? 1 : 0, ncand, ncand - 1, st,
                         [&](int i) { run(kCand[i]); });
     KTimer kt(KC_RECOMPUTE, st, fl, by);
     run(kCand[c]);
