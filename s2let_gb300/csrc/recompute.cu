@@ -695,6 +695,106 @@ __global__ void __launch_bounds__(256) k_apply_w(const double *__restrict__ Wp, 
   }
 }
 
+// The same operator in double-float (split-precision path).  Per K-slab of
+// AWD_K: W values as double-float pairs (unscaled: the operator's entries sit
+// well inside the float range), each real column's slab as double-float
+// scaled by its largest power of two; the slab's partial sums (renormalised
+// double-float) are flushed into FP64 accumulators with that power of two.
+// About 15 FP32 instructions per multiply-add against one FP64 instruction at
+// 1/64 of the rate.
+constexpr int AWD_K = 32;
+__global__ void __launch_bounds__(256) k_apply_w_df(const double *__restrict__ Wp, const double *__restrict__ Wm,
+                                                    int trans, int nt, int an, int mlo, int mhi,
+                                                    const double2 *__restrict__ in, int64_t is, int iw, int i_mlo,
+                                                    double2 *__restrict__ out, int64_t os, int ow, int o_mlo,
+                                                    int nb) {
+  const int par = blockIdx.z;
+  const int m_first = ((mlo + an) & 1) == par ? mlo : mlo + 1;
+  if (m_first > mhi) return;
+  const int nmp = (mhi - m_first) / 2 + 1;  // m's of this parity
+  const int ncols = 2 * nmp * nb;           // real columns
+  const int row0 = blockIdx.y * AW_T, col0 = blockIdx.x * AW_T;
+  if (row0 >= nt || col0 >= ncols) return;
+  const double *W = par == 0 ? Wp : Wm;
+  __shared__ float2 sA[AWD_K][AW_T + 1];  // [k][row]
+  // [k][col]: first the FP64 values, then (in place, each thread converting the
+  // entries it stored) their double-float pairs scaled by 2^-sBe[col]
+  __shared__ float2 sB[AWD_K][AW_T + 1];
+  __shared__ int sBm[AW_T], sBe[AW_T];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4] = {};
+  for (int k0 = 0; k0 < nt; k0 += AWD_K) {
+    if (threadIdx.x < AW_T) sBm[threadIdx.x] = 0;
+    for (int i = threadIdx.x; i < AWD_K * AW_T; i += 256) {
+      const int kk = trans ? i / AW_T : i % AWD_K, cc = trans ? i % AW_T : i / AWD_K;
+      const int k = k0 + kk;
+      double av = 0.0;
+      if (k < nt && row0 + cc < nt)
+        av = trans ? W[(int64_t)k * nt + row0 + cc] : W[(int64_t)(row0 + cc) * nt + k];
+      sA[kk][cc] = df_of(av);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < AWD_K * AW_T; i += 256) {
+      const int kk = i / AW_T, cc = i % AW_T;
+      const int k = k0 + kk, col = col0 + cc;
+      double bv = 0.0;
+      if (k < nt && col < ncols) {
+        const int pair = col >> 1, im = col & 1;
+        const int b = pair / nmp, m = m_first + 2 * (pair % nmp);
+        const double2 z = in[(int64_t)b * is + (int64_t)k * iw + (m - i_mlo)];
+        bv = im ? z.y : z.x;
+      }
+      *reinterpret_cast<double *>(&sB[kk][cc]) = bv;
+      atomicMax(&sBm[cc], exp_bits(bv));
+    }
+    __syncthreads();
+    if (threadIdx.x < AW_T) sBe[threadIdx.x] = block_scale(sBm[threadIdx.x]);
+    __syncthreads();
+    for (int i = threadIdx.x; i < AWD_K * AW_T; i += 256) {
+      const int kk = i / AW_T, cc = i % AW_T;
+      sB[kk][cc] = df_split(*reinterpret_cast<const double *>(&sB[kk][cc]), sBe[cc]);
+    }
+    __syncthreads();
+    float2 sum[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) sum[i][j] = make_float2(0.f, 0.f);
+#pragma unroll 4
+    for (int kk = 0; kk < AWD_K; ++kk) {
+      float2 x[4], y[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) x[i] = sA[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) y[j] = sB[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sum[i][j] = df_add_norm(sum[i][j], df_mul(x[i], y[j]));
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int e = sBe[tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i][j] += join_scaled(sum[i][j].x, sum[i][j].y, e);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int rr = row0 + ty * 4 + i;
+    if (rr >= nt) continue;
+#pragma unroll
+    for (int j = 0; j < 4; j += 2) {
+      const int col = col0 + tx * 4 + j;
+      if (col >= ncols) continue;
+      const int pair = col >> 1;
+      const int b = pair / nmp, m = m_first + 2 * (pair % nmp);
+      out[(int64_t)b * os + (int64_t)rr * ow + (m - o_mlo)] = make_double2(acc[i][j], acc[i][j + 1]);
+    }
+  }
+}
+
 RcArgs rc_args(const WignerTable &tb, int n, int mlo, int lmin, const double2 *w, double wscale, bool wconj,
                int nb) {
   RcArgs a{};
@@ -734,8 +834,12 @@ void apply_w(const WignerTable &tb, bool trans, int mlo, int mhi, const double2 
   const int ncols = 2 * ((nm + 1) / 2) * nb;
   KTimer kt(KC_QUAD, st, 2.0 * tb.nt * (double)tb.nt * nm * nb * 2.0, 16.0 * nb * (double)nm * tb.nt * 2.0);
   dim3 grid(ceil_div(ncols, AW_T), ceil_div(tb.nt, AW_T), 2);
-  k_apply_w<<<grid, 256, 0, st>>>(tb.W[0], tb.W[1], trans ? 1 : 0, tb.nt, tb.an, mlo, mhi, in, is, iw, i_mlo,
-                                  out, os, ow, o_mlo, nb);
+  if (t_precision == 1)  // split precision: double-float multiply-adds
+    k_apply_w_df<<<grid, 256, 0, st>>>(tb.W[0], tb.W[1], trans ? 1 : 0, tb.nt, tb.an, mlo, mhi, in, is, iw, i_mlo,
+                                       out, os, ow, o_mlo, nb);
+  else
+    k_apply_w<<<grid, 256, 0, st>>>(tb.W[0], tb.W[1], trans ? 1 : 0, tb.nt, tb.an, mlo, mhi, in, is, iw, i_mlo,
+                                    out, os, ow, o_mlo, nb);
   S2G_LAUNCHED();
 }
 
