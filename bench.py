@@ -503,6 +503,22 @@ def run_workload(a, world, rank, local):
         print(json.dumps(out), flush=True)
 
 
+ALL_CATS = {0: "fp64_contraction", 1: "ring_dft", 2: "gamma_dft", 3: "tiling_merge", 4: "tensor_contraction",
+            5: "other", 6: "recomputed_contraction", 7: "quadrature", 8: "digit_slicing"}
+
+
+def step_breakdown(lib, fn, sync):
+    """Milliseconds per kernel category of one call of fn (CUDA events around
+    each launch, csrc/timing.h categories)."""
+    lib.s2let_gpu_timing_enable(1)
+    fn()
+    sync()
+    rep = (C.c_double * 36)()
+    lib.s2let_gpu_timing_report(rep, 9)
+    lib.s2let_gpu_timing_enable(0)
+    return {c: round(rep[4 * i + 1], 2) for i, c in ALL_CATS.items() if rep[4 * i]}
+
+
 def uneven_parameters(rng, n):
     """The uneven configuration: L log-uniform on [64, 512] rounded to even,
     N uniform in {1, 3, 5}, spin uniform in {0, 2} (spin-0 maps real, spin-2
@@ -661,6 +677,7 @@ def run_recompute_workload(a, world, rank, local):
             multi_step_f32()
         torch.cuda.synchronize()
         ms_cfg4 = event_ms(multi_step_f32, a.steps)
+        bd_cfg4 = step_breakdown(lib, multi_step_f32, torch.cuda.synchronize)  # eager while timing
         lib.s2let_gpu_set_precision(0)
         ntuned = lib.s2let_gpu_autotune_entries((C.c_int * 5000)(), (C.c_double * 2000)(), 1000)
         lib.s2let_gpu_autotune(old_tune)
@@ -679,6 +696,7 @@ def run_recompute_workload(a, world, rank, local):
             "metric": "uneven batch px2wav+wav2px maps/s (256 maps, own L/N/spin each, one graph-replayed call; "
                       "FP32 storage, split precision, autotuned launch shapes)",
             "value": whole_job_rate(n, world, ms_cfg4 * 1e-3), "ms_per_step": ms_cfg4,
+            "per_kernel_ms_per_step": bd_cfg4,
             "dtype": "f32 storage; double-float recomputed-table contractions and ring DFTs (split precision)",
             "config": {"workload": "256 maps, L log-uniform on [64, 512] rounded to even, N in {1,3,5}, "
                                    "spin in {0,2} (spin 0 real, spin 2 complex), B=2, J_min=1, MW, "
@@ -732,6 +750,7 @@ def run_recompute_workload(a, world, rank, local):
         for _ in range(max(1, a.warmup - 1)):
             step()
         ms64 = event_ms(step, a.steps)
+        bd64 = step_breakdown(lib, step, torch.cuda.synchronize)
         err64 = float(((r - f).abs().max() / f.abs().max()).item())
         w64 = w.clone()
         lib.s2let_gpu_set_precision(1)  # split precision: double-float recomputed-table contractions
@@ -740,13 +759,15 @@ def run_recompute_workload(a, world, rank, local):
         clocks.start()
         ms = event_ms(step, a.steps)
         clk = clocks.stop()
+        bd = step_breakdown(lib, step, torch.cuda.synchronize)
         lib.s2let_gpu_set_precision(0)
         out.update({
             "metric": "px2wav+wav2px maps/s at L=2048, N=4 (recomputed Wigner tables, split precision)",
+            "per_kernel_ms_per_step": bd,
             "value": whole_job_rate(1, world, ms * 1e-3), "ms_per_step": ms,
             "dtype": "double-float recomputed-table contractions and ring DFTs, FP64 quadrature",
             "fp64_path": {"value": whole_job_rate(1, world, ms64 * 1e-3), "ms_per_step": ms64,
-                          "max_rel_err_round_trip": err64},
+                          "max_rel_err_round_trip": err64, "per_kernel_ms_per_step": bd64},
             "max_rel_err_f_wav_vs_fp64": float(((w - w64).abs().max() / w64.abs().max()).item()),
             "config": {"workload": "one real spin-0 map, L=2048, N=4, B=2, J_min=2, upsample=0, MW, "
                                    "power-law band-limited flm", "table_bytes_device": lib.s2let_gpu_plan_bytes()},

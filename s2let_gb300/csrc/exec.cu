@@ -970,9 +970,35 @@ int64_t used_wav_reals(const s2let_parameters_t &p, bool real) {
   return make_layout(q, real).woff.back() * (real ? 1 : 2);
 }
 
+// Streams of the calling thread for the parameter groups of a multi-map call:
+// groups are independent, so they are forked from the caller's stream onto
+// these (round robin), run concurrently, and joined back; inside a stream
+// capture the fork and join become edges of the graph.  Small band-limits
+// leave most of the GPU idle one group at a time (a quadrature launch of a
+// map at L = 100 has 16 CTAs).
+constexpr int kGroupStreams = 8;
+struct GroupStreams {
+  cudaStream_t s[kGroupStreams] = {};
+  cudaEvent_t fork = nullptr, join[kGroupStreams] = {};
+};
+GroupStreams &group_streams() {
+  static thread_local GroupStreams g;
+  if (!g.fork) {
+    for (int k = 0; k < kGroupStreams; ++k) {
+      S2G_CUDA(cudaStreamCreateWithFlags(&g.s[k], cudaStreamNonBlocking));
+      S2G_CUDA(cudaEventCreateWithFlags(&g.join[k], cudaEventDisableTiming));
+    }
+    S2G_CUDA(cudaEventCreateWithFlags(&g.fork, cudaEventDisableTiming));
+  }
+  return g;
+}
+
 // f32: every map's arrays hold floats (interleaved pairs when complex); they
 // are widened into FP64 batch scratch on the way in and rounded on the way out
 // (only the used part of f_wav), so every map goes through the scratch.
+void multi_pass_group(Op op, const std::vector<int> &g, const s2let_parameters_t *params, const int *real,
+                      void *const *px, void *const *wav, void *const *scal, cudaStream_t st, bool f32);
+
 void multi_pass(Op op, int n, const s2let_parameters_t *params, const int *real, void *const *px,
                 void *const *wav, void *const *scal, cudaStream_t st, bool f32 = false) {
   std::map<std::string, std::vector<int>> groups;
@@ -981,13 +1007,36 @@ void multi_pass(Op op, int n, const s2let_parameters_t *params, const int *real,
     key.push_back(real[k] ? 1 : 0);
     groups[key].push_back(k);
   }
-  for (auto &kv : groups) {
-    const std::vector<int> &g = kv.second;
+  const int K = std::min<int>(kGroupStreams, (int)groups.size());
+  if (K <= 1) {
+    for (auto &kv : groups) multi_pass_group(op, kv.second, params, real, px, wav, scal, st, f32);
+    return;
+  }
+  GroupStreams &gs = group_streams();
+  S2G_CUDA(cudaEventRecord(gs.fork, st));
+  for (int k = 0; k < K; ++k) S2G_CUDA(cudaStreamWaitEvent(gs.s[k], gs.fork, 0));
+  // largest band-limits first, so that the long groups start early
+  std::vector<const std::vector<int> *> order;
+  for (auto &kv : groups) order.push_back(&kv.second);
+  std::stable_sort(order.begin(), order.end(), [&](const std::vector<int> *x, const std::vector<int> *y) {
+    return params[(*x)[0]].L > params[(*y)[0]].L;
+  });
+  for (size_t i = 0; i < order.size(); ++i)
+    multi_pass_group(op, *order[i], params, real, px, wav, scal, gs.s[i % K], f32);
+  for (int k = 0; k < K; ++k) {
+    S2G_CUDA(cudaEventRecord(gs.join[k], gs.s[k]));
+    S2G_CUDA(cudaStreamWaitEvent(st, gs.join[k], 0));
+  }
+}
+
+void multi_pass_group(Op op, const std::vector<int> &g, const s2let_parameters_t *params, const int *real,
+                      void *const *px, void *const *wav, void *const *scal, cudaStream_t st, bool f32) {
+  {
     const s2let_parameters_t &p = params[g[0]];
     const bool re = real[g[0]] != 0;
     if (g.size() == 1 && !f32) {
       run_directional(op, p, re, px[g[0]], nullptr, wav[g[0]], scal[g[0]], 1, st);
-      continue;
+      return;
     }
     const int nb = (int)g.size();
     const size_t esz = re ? sizeof(double) : sizeof(double2);

@@ -359,6 +359,32 @@ __device__ __forceinline__ float2 df_of(double v) {  // |v| within the float ran
   return make_float2(h, l);
 }
 __device__ __forceinline__ float2 df_scale(float2 a, int k) { return make_float2(scale_pow2(a.x, k), scale_pow2(a.y, k)); }
+// Rescaled recursion of one segment (double-float kernels): with v_l =
+// lam_l w_l, lam_{lc} = lam_{lc+1} = 1 and lam_{l+1} = c2_l lam_{l-1}, the
+// three-term step v_{l+1} = (p u + q) v_l - c2_l v_{l-1} becomes
+// w_{l+1} = (p' u + q') w_l - w_{l-1} with (p', q') = (p, q) lam_l / (c2_l
+// lam_{l-1}): two FP64 instructions per value instead of three.  lam depends
+// on (l, m) only, so it is folded into the coefficients (l -> t) or the output
+// weight (t -> l).  On entry cn / cs / c2 hold the coefficients of degrees
+// lc + i, i in [1, n); on exit cn / cs the rescaled pairs and lam[i], i < n.
+// Called by all threads of the block (contains barriers).
+__device__ void rescale_segment(double2 *cn, double2 *cs, const double *c2, double *lam, int n) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    lam[0] = 1.0;
+    if (n > 1) lam[1] = 1.0;
+    for (int i = 1; i + 1 < n; ++i) lam[i + 1] = c2[i] * lam[i - 1];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    if (i >= 1) {
+      const double f = lam[i] / (c2[i] * lam[i - 1]);
+      cn[i] = make_double2(cn[i].x * f, cn[i].y * f);
+      cs[i] = make_double2(cs[i].x * f, cs[i].y * f);
+    }
+  __syncthreads();
+}
+
 // s += v x (double-float real times complex), the accumulator renormalised
 // after each add (unnormalised sums of 64-128 terms lost about 6 bits)
 __device__ __forceinline__ void df_mac(float4 &s, float2 v, float4 x) {
@@ -368,7 +394,7 @@ __device__ __forceinline__ void df_mac(float4 &s, float2 v, float4 x) {
 template <int NBT>
 __global__ void __launch_bounds__(kRcT) k_rc_l2t_df(RcArgs a) {
   __shared__ double2 scn[kSeg], scs[kSeg];
-  __shared__ double sc2[kSeg];
+  __shared__ double sc2[kSeg], slam[kSeg];
   __shared__ double2 sxd[kSeg][NBT];  // weighted coefficients of the segment
   __shared__ float4 sx[kSeg][NBT];    // the same as double-float, scaled by 2^-sxs[b]
   __shared__ int sxm[NBT], sxs[NBT];
@@ -402,7 +428,7 @@ __global__ void __launch_bounds__(kRcT) k_rc_l2t_df(RcArgs a) {
       for (int i = threadIdx.x; i < n; i += kRcT)
         if (i >= 1) rec_coef(lc + i, r.mt, a.an, scn[i], scs[i], sc2[i]);
       if (threadIdx.x < NBT) sxm[threadIdx.x] = 0;
-      __syncthreads();
+      rescale_segment(scn, scs, sc2, slam, n);
       for (int i = threadIdx.x; i < kSeg * NBT; i += kRcT) {
         const int kk = i / NBT, b = i % NBT, l = lc + kk;
         double2 v = make_double2(0.0, 0.0);
@@ -415,7 +441,8 @@ __global__ void __launch_bounds__(kRcT) k_rc_l2t_df(RcArgs a) {
           } else {
             v = a.src[base + m];
           }
-          v = cmul_(v, weight_of(a, l));
+          const double2 wl = weight_of(a, l);
+          v = cmul_(v, make_double2(wl.x * slam[kk], wl.y * slam[kk]));
         }
         sxd[kk][b] = v;
         atomicMax(&sxm[b], max(exp_bits(v.x), exp_bits(v.y)));
@@ -446,7 +473,7 @@ __global__ void __launch_bounds__(kRcT) k_rc_l2t_df(RcArgs a) {
       for (int i = 1; i + 1 < n; ++i) {
         const double2 k = cc[i];
         const double xt = fma(k.x, u, k.y);
-        const double vn = fma(xt, v, -sc2[i] * vp);
+        const double vn = fma(xt, v, -vp);  // rescaled recursion
         vp = v;
         v = vn;
         if (exp_bits(v) > 1023 + kRenormDf) {  // flush at the old scale, continue at the new one
@@ -501,7 +528,7 @@ __global__ void __launch_bounds__(kRcT) k_rc_t2l_df(RcArgs a) {
   float2 *tile = smem_df;                                  // [kRcT][kTileLd]
   float4 *sg = (float4 *)(smem_df + kRcT * kTileLd);       // [kRcT][NBT]
   __shared__ double2 scn[kSeg], scs[kSeg];
-  __shared__ double sc2[kSeg];
+  __shared__ double sc2[kSeg], slam[kSeg];
   __shared__ int sgm[NBT];
   const int m = a.mlo + blockIdx.x, c = blockIdx.y;
   const RcRef r = rc_ref(a, m);
@@ -516,13 +543,13 @@ __global__ void __launch_bounds__(kRcT) k_rc_t2l_df(RcArgs a) {
   const int tid = threadIdx.x;
   for (int i = tid; i < n; i += kRcT)
     if (i >= 1) rec_coef(lc + i, r.mt, a.an, scn[i], scs[i], sc2[i]);
+  rescale_segment(scn, scs, sc2, slam, n);
   const double2 *ck = a.ck + a.coff[r.mi] + (int64_t)c * a.nt;
   const int *cke = a.ck_e + a.coff[r.mi] + (int64_t)c * a.nt;
   const int li = tid % kSeg, bh = tid / kSeg;
   double2 acc[NH];
 #pragma unroll
   for (int j = 0; j < NH; ++j) acc[j] = make_double2(0.0, 0.0);
-  __syncthreads();
   for (int t0 = 0; t0 < a.nt; t0 += kRcT) {
     const int t = t0 + tid;
     float2 *row = tile + tid * kTileLd;
@@ -540,7 +567,7 @@ __global__ void __launch_bounds__(kRcT) k_rc_t2l_df(RcArgs a) {
       for (int i = 1; i + 1 < n; ++i) {
         const double2 k = cc[i];
         const double xt = fma(k.x, u, k.y);
-        const double vn = fma(xt, v, -sc2[i] * vp);
+        const double vn = fma(xt, v, -vp);  // rescaled recursion
         vp = v;
         v = vn;
         if (exp_bits(v) > 1023 + kRenormDf) {  // keep one scale per row: rescale what is written
@@ -608,11 +635,12 @@ __global__ void __launch_bounds__(kRcT) k_rc_t2l_df(RcArgs a) {
   const int l = lc + li;
   if (li >= n || l < lst) return;
   const double2 wt = weight_of(a, l);
+  const double sl = r.sign * slam[li];  // the rescaled recursion's lam_l
 #pragma unroll
   for (int j = 0; j < NH; ++j) {
     const int b = b0 + (SPLIT_T ? 0 : bh * NH) + j;
     if (b >= a.nb) break;
-    const double2 v = make_double2(acc[j].x * r.sign, acc[j].y * r.sign);
+    const double2 v = make_double2(acc[j].x * sl, acc[j].y * sl);
     a.dst[(int64_t)b * a.ds + (int64_t)l * l + l + m] = cmul_(v, wt);
   }
 }
