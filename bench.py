@@ -78,12 +78,16 @@ def args_():
     ap.add_argument("--N", type=int, default=4)
     ap.add_argument("--B", type=float, default=2.0)
     ap.add_argument("--J_min", type=int, default=2)
-    ap.add_argument("--workload", default="metric", choices=["metric", "spin2", "sparsity", "uneven", "L2048"],
+    ap.add_argument("--workload", default="metric",
+                    choices=["metric", "spin2", "sparsity", "uneven", "L2048", "axisym", "harmonic"],
                     help="metric: the headline (real maps, L=1024, N=4); spin2: complex spin-2 maps, "
                          "L=1024, N=5, J_min=3, error per scale; sparsity: differentiable wavelet-sparsity "
                          "loss, 32 real maps at L=256, forward + backward; uneven: 256 maps of their own L, N "
                          "and spin in one graph-replayed call against a call-per-map loop; L2048: one real map "
-                         "at L=2048, N=4 with recomputed Wigner tables")
+                         "at L=2048, N=4 with recomputed Wigner tables; axisym: axisymmetric lm and MW "
+                         "transforms of one real map at L=128, J_min=0, full resolution, through the drop-in "
+                         "calls (the oracle timed beside them); harmonic: lm2wav + wav2lm of one real map at "
+                         "L=1024, N=4 through the drop-in calls, split precision against FP64")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -417,6 +421,8 @@ def run_workload(a, world, rank, local):
     clocks = ClockSampler(local)
     if a.workload in ("uneven", "L2048"):
         return run_recompute_workload(a, world, rank, local)
+    if a.workload in ("axisym", "harmonic"):
+        return run_host_call_workload(a, world, rank)
     out = {"n_gpus": world, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "data": "synthetic"}
     if a.workload == "spin2":
@@ -517,6 +523,100 @@ def step_breakdown(lib, fn, sync):
     lib.s2let_gpu_timing_report(rep, 9)
     lib.s2let_gpu_timing_enable(0)
     return {c: round(rep[4 * i + 1], 2) for i, c in ALL_CATS.items() if rep[4 * i]}
+
+
+def run_host_call_workload(a, world, rank):
+    """One map through the drop-in host calls, timed on the wall clock (every
+    call synchronous, host buffers, copies included)."""
+    import s2let_gb300
+    from oracle import oracle
+    from s2let_gb300.capi import make_parameters, ptr
+
+    api = s2let_gb300.api()
+    lib = api.lib
+    port = oracle.port()
+    rng = np.random.default_rng(replica_seed(rank))
+
+    def wall(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            fn()
+        return (time.perf_counter() - t0) / steps
+
+    rel = lambda x, y: float(np.abs(np.asarray(x) - np.asarray(y)).max() / max(np.abs(np.asarray(y)).max(), 1e-300))
+    out = {"n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "data": "synthetic", "unit": "maps/s"}
+    if a.workload == "axisym":
+        L = 128
+        p = make_parameters(L, 2.0, 0, 1, 0, 1)
+        flm = power_law_real_flm(rng, L)
+        f = api.alm2map(flm, L, real=True)
+        res = {}
+        for name, impl in (("gpu", api), ("oracle", port)):
+            def lm_round():
+                fw, fs = impl.axisym_lm_analysis(flm, p)
+                return fw, fs, impl.axisym_lm_synthesis(fw, fs, p)
+
+            def mw_round():
+                w_, s_ = impl.axisym("analysis", [f], p, real=True)
+                return w_, s_, impl.axisym("synthesis", [w_, s_], p, real=True)
+
+            steps = a.steps if name == "gpu" else 1
+            res[name] = {"lm": (wall(lm_round, steps, 1 if name == "gpu" else 0), lm_round()),
+                         "mw": (wall(mw_round, steps, 1 if name == "gpu" else 0), mw_round())}
+        g, o = res["gpu"], res["oracle"]
+        out.update({
+            "metric": "axisymmetric lm wavelet analysis+synthesis maps/s at L=128, J_min=0, full resolution "
+                      "(drop-in host calls)",
+            "value": 1.0 / g["lm"][0], "ms_per_step": 1e3 * g["lm"][0], "dtype": "f64",
+            "config": {"workload": "one real map, L=128, B=2, J_min=0, N=1, spin=0, upsample=1, MW, power-law flm "
+                                   "(f_00 = 0); s2let_transform_axisym_lm_wav_analysis + _synthesis"},
+            "max_rel_err_vs_oracle": {"f_wav_lm": rel(g["lm"][1][0], o["lm"][1][0]),
+                                      "f_scal_lm": rel(g["lm"][1][1], o["lm"][1][1]),
+                                      "flm": rel(g["lm"][1][2], o["lm"][1][2])},
+            "round_trip_rel_err": rel(g["lm"][1][2], flm),
+            "oracle_cpu": {"value": 1.0 / o["lm"][0], "unit": "maps/s", "cores": os.cpu_count(), "kind": "port"},
+            "mw": {"value": 1.0 / g["mw"][0], "ms_per_step": 1e3 * g["mw"][0],
+                   "api": "s2let_transform_axisym_wav_analysis_mw_real + _synthesis_mw_real",
+                   "max_rel_err_vs_oracle": {"f_wav": rel(g["mw"][1][0], o["mw"][1][0]),
+                                             "f": rel(g["mw"][1][2], o["mw"][1][2])},
+                   "oracle_cpu_maps_per_s": 1.0 / o["mw"][0]},
+        })
+    else:
+        L = 1024
+        p = make_parameters(L, 2.0, 2, 4, 0, 0)
+        flm = power_law_real_flm(rng, L)
+        sz = api.sizes(p)
+        res = {}
+        for prec in (1, 0):
+            lib.s2let_gpu_set_precision(prec)
+
+            def round_trip():
+                w_ = np.zeros(sz["n_wav"])
+                s_ = np.zeros(sz["n_scal"])
+                lib.s2let_analysis_lm2wav_real(ptr(w_), ptr(s_), ptr(flm), C.byref(p))
+                r_ = np.zeros(L * L, np.complex128)
+                lib.s2let_synthesis_wav2lm_real(ptr(r_), ptr(w_), ptr(s_), C.byref(p))
+                return w_, s_, r_
+
+            t = wall(round_trip, a.steps, 1)
+            res[prec] = (t, round_trip())
+        lib.s2let_gpu_set_precision(0)
+        s2let_gb300.check(lib, "harmonic drop-in calls")
+        out.update({
+            "metric": "lm2wav+wav2lm maps/s at L=1024, N=4 (drop-in host calls, split precision)",
+            "value": 1.0 / res[1][0], "ms_per_step": 1e3 * res[1][0], "dtype": "bf16-split/f32-acc/f64",
+            "config": {"workload": "one real map's flm, L=1024, N=4, B=2, J_min=2, upsample=0; "
+                                   "s2let_analysis_lm2wav_real + s2let_synthesis_wav2lm_real"},
+            "fp64_path": {"value": 1.0 / res[0][0], "ms_per_step": 1e3 * res[0][0]},
+            "max_rel_err_vs_fp64": {"f_wav": rel(res[1][1][0], res[0][1][0]), "flm": rel(res[1][1][2], res[0][1][2])},
+            "round_trip_rel_err": rel(res[1][1][2], flm),
+            "note": "one map per call re-streams every Wigner table of the plan (the reference API takes one map)",
+        })
+    if rank == 0:
+        print(json.dumps(out), flush=True)
 
 
 def uneven_parameters(rng, n):
