@@ -415,10 +415,33 @@ const char *s2let_gpu_last_error_string(void);
 
 /* Arithmetic used by subsequent calls of this thread.
  *   0 = FP64 throughout (default);
- *   1 = mixed: FP64 Wigner tables and tiling, split-precision tensor-core Legendre
- *       contraction with FP32 accumulation and FP64 combination. */
+ *   1 = split precision (within 1e-10 of the FP64 path): on stored Wigner
+ *       tables the Legendre/Wigner contraction of batches of two maps or
+ *       more runs on the tensor cores (bf16 digit slices, FP32 accumulation,
+ *       FP64 combination); one-map calls (s2let_gpu_set_df_max_maps) and
+ *       band-limits below 128 contract in double-float arithmetic on the FP32
+ *       pipe; recomputed tables regenerate and contract in double-float; ring
+ *       and gamma DFTs in double-float. */
 int s2let_gpu_set_precision(int mode);
 int s2let_gpu_get_precision(void);
+
+/* Double-float copies of the stored Wigner tables for the double-float
+ * contractions of the split-precision path (1 = default): built on first use,
+ * the same size as the FP64 tables, skipped when they would leave less than
+ * 4 GiB of device memory free; 0 = split the FP64 values as they are read
+ * (slower, no extra memory).  Process-wide; copies are freed by
+ * s2let_gpu_release_plans.  Returns the status. */
+int s2let_gpu_set_split_tables(int on);
+int s2let_gpu_get_split_tables(void);
+
+/* Split precision on stored tables: batches of at most `maps` maps (0-4,
+ * default 1, initially S2LET_GPU_DF_MAX_MAPS when set) contract in
+ * double-float on the FP64 tables (8 bytes per table entry streamed, two
+ * scales of one band-limit in one pass) instead of on the tensor cores (14
+ * bytes per entry); 0 keeps every batch on the tensor cores.  Process-wide.
+ * Returns the status. */
+int s2let_gpu_set_df_max_maps(int maps);
+int s2let_gpu_get_df_max_maps(void);
 
 /* Wigner tables used by plans built afterwards on this thread.
  *   0 = auto (default): stored D and Q tables while a plan's tables fit 60 % of
@@ -427,8 +450,8 @@ int s2let_gpu_get_precision(void);
  *   1 = stored tables always;
  *   2 = recomputed always: the kernels regenerate the Wigner d values from
  *       double-double checkpoints every 64 degrees (≈ 1/50 of the memory) and
- *       apply the forward quadrature as a separate FP64 operator.  FP64
- *       contraction (the split-precision setting applies to stored tables only).
+ *       apply the forward quadrature as a separate operator (FP64, or
+ *       double-float at split precision).
  * Returns the status. */
 int s2let_gpu_set_table_mode(int mode);
 int s2let_gpu_get_table_mode(void);

@@ -132,6 +132,10 @@ GPU_SIGNATURES = {
     "s2let_gpu_last_error": (I, []),
     "s2let_gpu_last_error_string": (C.c_char_p, []),
     "s2let_gpu_set_precision": (I, [I]),
+    "s2let_gpu_set_split_tables": (I, [I]),
+    "s2let_gpu_get_split_tables": (I, []),
+    "s2let_gpu_set_df_max_maps": (I, [I]),
+    "s2let_gpu_get_df_max_maps": (I, []),
     "s2let_gpu_get_precision": (I, []),
     "s2let_gpu_set_table_mode": (I, [I]),
     "s2let_gpu_get_table_mode": (I, []),

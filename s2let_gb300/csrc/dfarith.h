@@ -85,5 +85,11 @@ __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
   return make_float2(p, e);
 }
 
+// s += v x (double-float real times complex), the accumulator renormalised
+// after each add (for sums of many terms)
+__device__ __forceinline__ void df_mac(float4 &s, float2 v, float4 x) {
+  s = dmk(df_add_norm(dre(s), df_mul(v, dre(x))), df_add_norm(dim_(s), df_mul(v, dim_(x))));
+}
+
 }  // namespace
 }  // namespace s2g

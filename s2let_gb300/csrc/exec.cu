@@ -1525,10 +1525,31 @@ void s2let_gpu_release_plans(void) {
     }
     s2g::release_multi_graphs();
     s2g::release_sliced_tables();
+    s2g::release_df_tables();
     s2g::release_plans();
   });
 }
-size_t s2let_gpu_plan_bytes(void) { return s2g::plan_bytes() + s2g::sliced_table_bytes(); }
+size_t s2let_gpu_plan_bytes(void) {
+  return s2g::plan_bytes() + s2g::sliced_table_bytes() + s2g::df_table_bytes();
+}
+int s2let_gpu_set_split_tables(int on) {
+  if (on != 0 && on != 1) {
+    s2g::set_status(s2g::ERR_INVALID, "s2let_gpu_set_split_tables: 0 or 1");
+    return s2g::ERR_INVALID;
+  }
+  s2g::set_split_tables(on);
+  return 0;
+}
+int s2let_gpu_get_split_tables(void) { return s2g::get_split_tables(); }
+int s2let_gpu_set_df_max_maps(int maps) {
+  if (maps < 0 || maps > 4) {
+    s2g::set_status(s2g::ERR_INVALID, "s2let_gpu_set_df_max_maps: 0 to 4 maps");
+    return s2g::ERR_INVALID;
+  }
+  s2g::set_df_max_maps(maps);
+  return 0;
+}
+int s2let_gpu_get_df_max_maps(void) { return s2g::get_df_max_maps(); }
 int s2let_gpu_device_fault(void) {
   int v = 0;
   s2g::guarded("s2let_gpu_device_fault", [&] { v = s2g::mixed_error_flag_read_and_clear(); });

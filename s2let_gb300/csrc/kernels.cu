@@ -11,14 +11,20 @@
 //  k_merge     harmonic tiling merge (lmn -> lm) fused over scales/directions.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 #include <mutex>
+#include <type_traits>
 
 #include "autotune.h"
 #include "common.h"
 #include "dfarith.h"
 #include "dfconv.h"
+#include <cstdlib>
+
 #include "kernels.h"
 #include "mixed.h"
 #include "recompute.h"
@@ -548,6 +554,16 @@ int ring_threads(int P) { return P / 2 >= 512 ? 512 : (P / 2 >= 32 ? P / 2 : 32)
 
 constexpr int CT_M = 128;  // rows (t or l) per CTA
 constexpr int CT_K = 32;   // reduction tile
+// split precision: batches of at most this many maps contract in double-float
+// on the FP64 tables instead of streaming the tensor path's digit panels
+// (s2let_gpu_set_df_max_maps, initially S2LET_GPU_DF_MAX_MAPS or 1; 0 keeps
+// every batch on the tensor path)
+std::atomic<int> g_df_max_maps{[] {
+  const char *e = getenv("S2LET_GPU_DF_MAX_MAPS");
+  const int x = e ? atoi(e) : 1;
+  return (x >= 0 && x <= 4) ? x : 1;
+}()};
+int df_max_maps() { return g_df_max_maps.load(); }
 
 struct TableRef {
   int mi;       // m index inside the table
@@ -568,6 +584,7 @@ __device__ __forceinline__ TableRef table_ref(int mlo_table, int n, int m) {
 
 struct ContractArgs {
   const double *table;
+  const float2 *table_df;  // double-float copy of table (same offsets), or null
   const int64_t *off;
   int bl, nt, an, tmlo, n, mlo, lmin;  // nt: theta samples of the table
   const double2 *w;
@@ -583,6 +600,14 @@ struct ContractArgs {
   int64_t ds;
   int dw, d_mlo;  // l->t: spectrum row width / m of column 0
   int nb;
+  // double-float kernel: a second part on the same table and m range (another
+  // scale of the same band-limit and n) with its own source, destination,
+  // weights and lmin, contracted in the same pass over the table
+  int nparts;
+  const double2 *src2;
+  double2 *dst2;
+  const double2 *w2;
+  int lmin2;
 };
 
 __device__ __forceinline__ double2 weight_at(const ContractArgs &a, int l) {
@@ -702,9 +727,314 @@ __global__ void __launch_bounds__(CT_M) k_contract(ContractArgs a) {
   }
 }
 
+// The same contractions in double-float on the FP32 pipe (split-precision
+// path: every contraction the tensor-core kernel does not take, and batches of
+// one or two maps, for which streaming the tables' 7 bf16 digit panels (14 B
+// per entry) costs more than reading the FP64 tables (8 B per entry) and
+// multiplying in double-float).
+//
+// The CTA first splits its (m, map) coefficient columns over the whole
+// reduction range into double-float pairs in shared memory, one power-of-two
+// scale per map (|x| 2^-e < 1).  Table values (|d| <= 1) are split as they
+// are read (df_split_unit).  Products are summed as in Ogita, Rump and Oishi's
+// Dot2 (SIAM J. Sci. Comput. 26, 2005): a float sum s carried by TwoSum, its
+// rounding errors and the products' low parts gathered in a second float c,
+// so that s + c is the sum as if computed in twice the working precision;
+// (s + c) 2^e is widened to FP64 once per output.
+//   MODE 1, 3 (table contiguous along the output rows): one thread per row,
+//   each step of the reduction a coalesced warp-wide row of the table.
+//   MODE 0, 2 (table contiguous along the reduction axis): a warp takes
+//   DFC_R rows at a time with its lanes along the reduction axis (coalesced
+//   256-byte row segments, DFC_R loads in flight per lane), then reduces the
+//   lanes' partial sums by butterfly shuffles.
+
+// v (|v| <= 1 or zero) as hi + lo: the top 24 and next 23 significand bits
+// (truncated: |hi + lo - v| < 2^-46 |v|); |v| < 2^-103 gives 0
+__device__ __forceinline__ float2 df_split_unit(double v) {
+  const uint32_t wl = (uint32_t)__double2loint(v), wh = (uint32_t)__double2hiint(v);
+  const uint32_t mag = wh & 0x7FFFFFFFu;
+  const uint32_t eb = mag - 0x38000000u;  // float exponent field at bits 20..27
+  const uint32_t hb = __funnelshift_l(wl, eb, 3) | (wh & 0x80000000u);
+  const uint32_t base = (hb & 0xFF800000u) - (23u << 23);
+  const uint32_t lb = base | ((wl >> 6) & 0x7FFFFFu);
+  const bool ok = mag >= 0x39800000u;  // double exponent >= 1023 - 103
+  const float hi = __uint_as_float(hb);
+  const float lo = __fsub_rn(__uint_as_float(lb), __uint_as_float(base));
+  return ok ? make_float2(hi, lo) : make_float2(0.0f, 0.0f);
+}
+
+// table value as a double-float pair: split as read (FP64 table) or stored split
+__device__ __forceinline__ float2 unit_df(double v) { return df_split_unit(v); }
+__device__ __forceinline__ float2 unit_df(float2 v) { return v; }
+
+// Dot2 step: (s, c) += a * x, a and x double-float reals
+__device__ __forceinline__ void dot2_mac(float &s, float &c, float2 av, float xh, float xl) {
+  const float p = __fmul_rn(av.x, xh);
+  const float q = __fmaf_rn(av.x, xh, -p);
+  const float t = __fadd_rn(s, p);
+  const float v = __fsub_rn(t, s);
+  const float r = __fadd_rn(__fsub_rn(s, __fsub_rn(t, v)), __fsub_rn(p, v));
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(q, r));
+  c = __fmaf_rn(av.x, xl, c);
+  c = __fmaf_rn(av.y, xh, c);
+}
+// (s, c) += (s2, c2), symmetric in its two operands: TwoSum's error r is
+// exact and c + c2 commutes, so both lanes of a butterfly step get the same
+// bits (the lane that stores a sum then does not matter)
+__device__ __forceinline__ void dot2_add(float &s, float &c, float s2, float c2) {
+  const float t = __fadd_rn(s, s2);
+  const float v = __fsub_rn(t, s);
+  const float r = __fadd_rn(__fsub_rn(s, __fsub_rn(t, v)), __fsub_rn(s2, v));
+  s = t;
+  c = __fadd_rn(__fadd_rn(c, c2), r);
+}
+
+// complex product with explicit roundings: every instantiation of the
+// double-float kernel (maps per CTA, table element type) rounds the same way,
+// so that launch shapes chosen by the autotuner give identical bits
+__device__ __forceinline__ double2 cmul_rn(double2 a, double2 b) {
+  return make_double2(__fma_rn(a.x, b.x, __dmul_rn(-a.y, b.y)), __fma_rn(a.x, b.y, __dmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ double2 weight_at_part(const ContractArgs &a, int p, int l) {
+  const double2 *wp = p ? a.w2 : a.w;
+  double2 w = wp ? wp[l] : make_double2(1.0, 0.0);
+  if (a.wconj) w.y = -w.y;
+  return make_double2(__dmul_rn(w.x, a.wscale), __dmul_rn(w.y, a.wscale));
+}
+
+// coefficient k of map b of part p for column m (x(l = k, m) w(l) for l->t,
+// spectrum(t = k, m) for t->l)
+template <bool L2T>
+__device__ __forceinline__ double2 contract_coef(const ContractArgs &a, int p, int m, int am, int k, int b) {
+  const double2 *src = p ? a.src2 : a.src;
+  if (L2T) {
+    const int64_t base = (int64_t)b * a.ss + (int64_t)k * k + k;
+    double2 v;
+    if (a.x_half && m < 0) {
+      v = conj2(src[base - m]);
+      if (am & 1) v = scl2(v, -1.0);
+    } else {
+      v = src[base + m];
+    }
+    return cmul_rn(v, weight_at_part(a, p, k));
+  }
+  return src[(int64_t)b * a.ss + (int64_t)k * a.sw_or_xL + (m - a.s_mlo)];
+}
+
+// output of map b of part p at row (t for l->t, l - lst for t->l); t->l rows
+// below the part's first degree lstp are not written
+template <bool L2T>
+__device__ __forceinline__ void contract_store(const ContractArgs &a, int p, int b, int m, int row, int lst,
+                                               int lstp, double2 v) {
+  double2 *dst = p ? a.dst2 : a.dst;
+  if (L2T) {
+    dst[(int64_t)b * a.ds + (int64_t)row * a.dw + (m - a.d_mlo)] = v;
+  } else {
+    const int l = lst + row;
+    if (l < lstp) return;
+    dst[(int64_t)b * a.ds + (int64_t)l * l + l + m] = cmul_rn(v, weight_at_part(a, p, l));
+  }
+}
+
+constexpr int DFC_R = 8;    // rows per lane (MODE 0, 2; half that from 4 maps per CTA)
+constexpr int DFC_LPR = 8;  // lanes per row (MODE 0, 2)
+
+template <int MODE, int NBT, class E>
+__global__ void __launch_bounds__(CT_M) k_contract_df(ContractArgs a) {
+  extern __shared__ float4 sx[];  // [k - kbeg][b]
+  __shared__ int sxm[NBT];
+  const int m = a.mlo + blockIdx.x;
+  const int am = m < 0 ? -m : m;
+  const int l0 = am > a.an ? am : a.an;
+  const int bl = a.bl;
+  const int nl = bl - l0;
+  // columns: NBT = maps per CTA x parts (column c: part c / mpc, map b0 + c % mpc)
+  const int np = a.nparts == 2 ? 2 : 1;
+  const int mpc = NBT / np;
+  const int lmin_u = (np == 2 && a.lmin2 < a.lmin) ? a.lmin2 : a.lmin;
+  const int lst = l0 > lmin_u ? l0 : lmin_u;  // first degree of any part
+  constexpr bool L2T = (MODE == 0 || MODE == 1);
+  if (!L2T && lst >= bl) return;
+  const TableRef tr = table_ref(a.tmlo, a.n, m);
+  const E *T0;
+  if constexpr (std::is_same<E, double>::value)
+    T0 = a.table;
+  else
+    T0 = a.table_df;
+  const E *T = (lst < bl) ? T0 + a.off[tr.mi] : T0;
+  const int b0 = blockIdx.z * mpc;
+  const int row0 = blockIdx.y * CT_M;
+  const int nt = a.nt;
+  const int rows_total = L2T ? nt : (bl - lst);
+  if (row0 >= rows_total) return;
+  const int kbeg = L2T ? lst : 0, kend = L2T ? bl : nt;
+  const int K = kend > kbeg ? kend - kbeg : 0;
+
+  // coefficient columns: per-column scale, then the double-float split.  The
+  // stride CT_M is a multiple of NBT, so each thread serves one column.  l->t
+  // coefficients below a part's first degree are zero.
+  const int bt = threadIdx.x % NBT;
+  const int pt = bt / mpc, mt = b0 + bt % mpc;
+  const bool bon = mt < a.nb;
+  const int lpt = pt ? a.lmin2 : a.lmin;
+  const int lst_t = l0 > lpt ? l0 : lpt;
+  if (threadIdx.x < NBT) sxm[threadIdx.x] = 0;
+  __syncthreads();
+  int emax = 0;
+  if (bon)
+    for (int i = threadIdx.x; i < K * NBT; i += CT_M) {
+      const int k = kbeg + i / NBT;
+      if (L2T && k < lst_t) continue;
+      const double2 v = contract_coef<L2T>(a, pt, m, am, k, mt);
+      emax = max(emax, max(exp_field(v.x), exp_field(v.y)));
+    }
+  atomicMax(&sxm[bt], emax);
+  __syncthreads();
+  const int es = block_scale(sxm[bt]);
+  for (int i = threadIdx.x; i < K * NBT; i += CT_M) {
+    const int k = kbeg + i / NBT;
+    sx[i] = (bon && !(L2T && k < lst_t)) ? dc_split(contract_coef<L2T>(a, pt, m, am, k, mt), es)
+                                         : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncthreads();
+  int eo[NBT];
+#pragma unroll
+  for (int b = 0; b < NBT; ++b) eo[b] = block_scale(sxm[b]);
+
+  if (MODE == 1 || MODE == 3) {
+    const int row = row0 + threadIdx.x;
+    if (row >= rows_total) return;
+    // 32-bit element offsets from the CTA's table block
+    const uint32_t tstride = MODE == 1 ? (uint32_t)nt : (uint32_t)nl;
+    const uint32_t t0 = MODE == 1 ? (uint32_t)(kbeg - l0) * tstride + (uint32_t)row
+                                  : (uint32_t)kbeg * tstride + (uint32_t)(lst + row - l0);
+    float sre[NBT], cre[NBT], sim[NBT], cim[NBT];
+#pragma unroll
+    for (int b = 0; b < NBT; ++b) sre[b] = cre[b] = sim[b] = cim[b] = 0.f;
+    int k = 0;
+    for (; k + 8 <= K; k += 8) {
+      E tv[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) tv[j] = T[t0 + (uint32_t)(k + j) * tstride];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float2 av = unit_df(tv[j]);
+#pragma unroll
+        for (int b = 0; b < NBT; ++b) {
+          const float4 x = sx[(k + j) * NBT + b];
+          dot2_mac(sre[b], cre[b], av, x.x, x.y);
+          dot2_mac(sim[b], cim[b], av, x.z, x.w);
+        }
+      }
+    }
+    for (; k < K; ++k) {
+      const float2 av = unit_df(T[t0 + (uint32_t)k * tstride]);
+#pragma unroll
+      for (int b = 0; b < NBT; ++b) {
+        const float4 x = sx[k * NBT + b];
+        dot2_mac(sre[b], cre[b], av, x.x, x.y);
+        dot2_mac(sim[b], cim[b], av, x.z, x.w);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < NBT; ++c) {
+      const int p = c / mpc, b = b0 + c % mpc;
+      if (b >= a.nb) continue;
+      const int lp = p ? a.lmin2 : a.lmin;
+      const double2 v =
+          scl2(make_double2(join_scaled(sre[c], cre[c], eo[c]), join_scaled(sim[c], cim[c], eo[c])), tr.sign);
+      contract_store<L2T>(a, p, b, m, row, lst, l0 > lp ? l0 : lp, v);
+    }
+    return;
+  }
+
+  // MODE 0, 2: groups of DFC_LPR lanes along the reduction axis, one row per
+  // group and DFC_R rows per lane; the next step's table values are loaded
+  // before the current step's arithmetic
+  constexpr int R = NBT <= 2 ? DFC_R : DFC_R / 2;
+  constexpr int GPW = 32 / DFC_LPR;  // row groups per warp
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane % DFC_LPR, grp = lane / DFC_LPR;
+  const uint32_t rs = MODE == 0 ? (uint32_t)nl : (uint32_t)nt;  // table row stride
+  for (int g = 0; g < 32; g += GPW * R) {
+    const int rbase = row0 + warp * 32 + g;
+    if (rbase >= rows_total) break;
+    // rows of this lane: rbase + grp + GPW i (past the end: the last row, not stored)
+    uint32_t roff[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int row = min(rbase + grp + GPW * i, rows_total - 1);
+      roff[i] = MODE == 0 ? (uint32_t)row * rs + (uint32_t)(kbeg - l0) : (uint32_t)(lst + row - l0) * rs;
+    }
+    float sre[R][NBT], cre[R][NBT], sim[R][NBT], cim[R][NBT];
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+      for (int b = 0; b < NBT; ++b) sre[i][b] = cre[i][b] = sim[i][b] = cim[i][b] = 0.f;
+    // loads past the reduction range re-read its last entry (the value is not
+    // used); an empty range (l -> t with no admissible l) reads nothing
+    E cur[R] = {};
+    if (K > 0)
+#pragma unroll
+      for (int i = 0; i < R; ++i) cur[i] = T[roff[i] + (uint32_t)min(sub, K - 1)];
+    for (int k = sub; k < K + sub; k += DFC_LPR) {
+      const uint32_t kn = (uint32_t)min(k + DFC_LPR, K - 1);
+      E nxt[R];
+#pragma unroll
+      for (int i = 0; i < R; ++i) nxt[i] = T[roff[i] + kn];
+      if (k < K) {
+        float4 x[NBT];
+#pragma unroll
+        for (int b = 0; b < NBT; ++b) x[b] = sx[k * NBT + b];
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const float2 av = unit_df(cur[i]);
+#pragma unroll
+          for (int b = 0; b < NBT; ++b) {
+            dot2_mac(sre[i][b], cre[i][b], av, x[b].x, x[b].y);
+            dot2_mac(sim[i][b], cim[i][b], av, x[b].z, x[b].w);
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < R; ++i) cur[i] = nxt[i];
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+#pragma unroll
+      for (int b = 0; b < NBT; ++b) {
+#pragma unroll
+        for (int off = DFC_LPR / 2; off >= 1; off >>= 1) {
+          const float s2 = __shfl_xor_sync(0xFFFFFFFFu, sre[i][b], off);
+          const float c2 = __shfl_xor_sync(0xFFFFFFFFu, cre[i][b], off);
+          const float t2 = __shfl_xor_sync(0xFFFFFFFFu, sim[i][b], off);
+          const float d2 = __shfl_xor_sync(0xFFFFFFFFu, cim[i][b], off);
+          dot2_add(sre[i][b], cre[i][b], s2, c2);
+          dot2_add(sim[i][b], cim[i][b], t2, d2);
+        }
+      }
+      // lane sub = c of each group stores column c of the group's row
+      const int row = rbase + grp + GPW * i;
+      if (sub < NBT && row < rows_total) {
+#pragma unroll
+        for (int c = 0; c < NBT; ++c) {
+          const int p = c / mpc, b = b0 + c % mpc;
+          if (c != sub || b >= a.nb) continue;
+          const int lp = p ? a.lmin2 : a.lmin;
+          const double2 v = scl2(make_double2(join_scaled(sre[i][c], cre[i][c], eo[c]),
+                                              join_scaled(sim[i][c], cim[i][c], eo[c])),
+                                 tr.sign);
+          contract_store<L2T>(a, p, b, m, row, lst, l0 > lp ? l0 : lp, v);
+        }
+      }
+    }
+  }
+}
+
 // algorithmic work of one contraction launch: one complex x real MAC (4 flops)
 // per (l, m, t) per map; bytes = table entries read once + coefficient/spectrum I/O
-void contract_work(const ContractArgs &a, int nm, double *flops, double *bytes) {
+void contract_work(const ContractArgs &a, int nm, double *flops, double *bytes, double *table_bytes = nullptr) {
   double macs = 0, tab = 0, io = 0;
   for (int i = 0; i < nm; ++i) {
     const int m = a.mlo + i, am = m < 0 ? -m : m;
@@ -717,11 +1047,90 @@ void contract_work(const ContractArgs &a, int nm, double *flops, double *bytes) 
   }
   *flops = 4.0 * macs * a.nb;
   *bytes = 8.0 * tab + 16.0 * io * a.nb;
+  if (table_bytes) *table_bytes = 8.0 * tab;
+}
+
+constexpr size_t kDfcSmemMax = 200 * 1024;
+
+template <int MODE, int NBT, class E>
+void launch_contract_df_e(dim3 grid, size_t smem, const ContractArgs &a, cudaStream_t st) {
+  static bool attr = [] {
+    S2G_CUDA(cudaFuncSetAttribute(k_contract_df<MODE, NBT, E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kDfcSmemMax));
+    return true;
+  }();
+  (void)attr;
+  k_contract_df<MODE, NBT, E><<<grid, CT_M, smem, st>>>(a);
+}
+template <int MODE, int NBT>
+void launch_contract_df(dim3 grid, size_t smem, const ContractArgs &a, cudaStream_t st) {
+  if (a.table_df)
+    launch_contract_df_e<MODE, NBT, float2>(grid, smem, a, st);
+  else
+    launch_contract_df_e<MODE, NBT, double>(grid, smem, a, st);
+}
+
+// Double-float copies of stored Wigner tables for the double-float
+// contractions (same layout and offsets, hi + lo per entry: the same 8 bytes
+// as FP64, no splitting in the contraction loop).  Built on first use per
+// table while the device keeps kDftReserve bytes free after the copy, else
+// the contraction splits the FP64 values as it reads them.
+constexpr size_t kDftReserve = size_t(4) << 30;
+std::mutex g_dft_mu;
+std::map<const double *, float2 *> g_dft;
+size_t g_dft_bytes = 0;
+std::atomic<int> g_split_tables{1};
+
+__global__ void k_split_table(const double *__restrict__ in, float2 *__restrict__ out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = df_split(in[i], 0);
+}
+
+const float2 *df_table(const WignerTable &tb, bool q, cudaStream_t st) {
+  const double *src = q ? tb.Q : tb.D;
+  if (!src || !g_split_tables.load()) return nullptr;
+  std::lock_guard<std::mutex> lk(g_dft_mu);
+  auto it = g_dft.find(src);
+  if (it != g_dft.end()) return it->second;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  S2G_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (cap != cudaStreamCaptureStatusNone) return nullptr;  // no allocation inside a graph capture
+  const int64_t n = tb.elems();
+  const size_t by = sizeof(float2) * (size_t)(n > 0 ? n : 1);
+  size_t fr = 0, tot = 0;
+  S2G_CUDA(cudaMemGetInfo(&fr, &tot));
+  if (fr < by + kDftReserve) return nullptr;
+  float2 *p = nullptr;
+  S2G_CUDA(cudaMalloc(&p, by));
+  const int64_t blocks = std::min<int64_t>(ceil_div(n > 0 ? n : 1, 256), 152 * 16);
+  k_split_table<<<(unsigned)blocks, 256, 0, st>>>(src, p, n);
+  S2G_LAUNCHED();
+  S2G_CUDA(cudaStreamSynchronize(st));
+  g_dft.emplace(src, p);
+  g_dft_bytes += by;
+  return p;
 }
 
 template <int MODE>
 void launch_contract_nbt(const ContractArgs &a, int nm, int rows, int nbt, cudaStream_t st) {
   dim3 grid(nm, ceil_div(rows, CT_M), ceil_div(a.nb, nbt));
+  if (t_precision == 1) {  // split precision: the double-float kernel
+    // shared memory: the split coefficient columns over the reduction range
+    const int kmax = a.bl > a.nt ? a.bl : a.nt;
+    while (nbt > 1 && (size_t)kmax * nbt * sizeof(float4) > kDfcSmemMax) nbt /= 2;
+    S2G_REQUIRE((size_t)kmax * sizeof(float4) <= kDfcSmemMax, ERR_UNSUPPORTED,
+                "reduction range too long for the double-float contraction");
+    grid.z = ceil_div(a.nb, nbt);
+    const size_t smem = (size_t)kmax * nbt * sizeof(float4);
+    switch (nbt) {
+      case 8: launch_contract_df<MODE, 8>(grid, smem, a, st); break;
+      case 4: launch_contract_df<MODE, 4>(grid, smem, a, st); break;
+      case 2: launch_contract_df<MODE, 2>(grid, smem, a, st); break;
+      default: launch_contract_df<MODE, 1>(grid, smem, a, st); break;
+    }
+    S2G_LAUNCHED();
+    return;
+  }
   switch (nbt) {
   case 8: k_contract<MODE, 8><<<grid, CT_M, 0, st>>>(a); break;
   case 4: k_contract<MODE, 4><<<grid, CT_M, 0, st>>>(a); break;
@@ -737,12 +1146,41 @@ template <int MODE>
 void launch_contract(const ContractArgs &a, int nm, int rows, cudaStream_t st) {
   static const int kCand[4] = {1, 2, 4, 8};
   const int ncand = a.nb >= 8 ? 4 : (a.nb >= 4 ? 3 : (a.nb >= 2 ? 2 : 1));
-  const int c = tuned(TF_CONTRACT, MODE, tune_bucket(a.bl), tune_bucket(a.nb), ncand, ncand - 1, st,
-                      [&](int i) { launch_contract_nbt<MODE>(a, nm, rows, kCand[i], st); });
+  const int c = tuned(TF_CONTRACT, MODE + 4 * t_precision, tune_bucket(a.bl), tune_bucket(a.nb), ncand, ncand - 1,
+                      st, [&](int i) { launch_contract_nbt<MODE>(a, nm, rows, kCand[i], st); });
   double fl = 0, by = 0;
   if (timing_enabled()) contract_work(a, nm, &fl, &by);
   KTimer kt(KC_CONTRACT, st, fl, by);
   launch_contract_nbt<MODE>(a, nm, rows, kCand[c], st);
+}
+
+// two parts on one table (double-float kernel, split precision): columns =
+// 2 parts x nb maps, one pass over the table
+template <int MODE>
+void launch_contract_df_pair(const ContractArgs &a, int nm, int rows, cudaStream_t st) {
+  const int nbt = 2 * a.nb;
+  const int kmax = a.bl > a.nt ? a.bl : a.nt;
+  const size_t smem = (size_t)kmax * nbt * sizeof(float4);
+  S2G_REQUIRE(a.nb >= 1 && a.nb <= 4 && smem <= kDfcSmemMax, ERR_UNSUPPORTED,
+              "double-float contraction of two parts: at most 4 maps");
+  double fl = 0, by = 0;
+  if (timing_enabled()) {
+    ContractArgs b = a;
+    b.lmin = a.lmin2;
+    double f1 = 0, b1 = 0, t1 = 0;
+    contract_work(a, nm, &fl, &by);
+    contract_work(b, nm, &f1, &b1, &t1);
+    fl += f1;
+    by += b1 - t1;  // the table is read once for both parts
+  }
+  KTimer kt(KC_CONTRACT, st, fl, by);
+  const dim3 grid(nm, ceil_div(rows, CT_M), 1);
+  switch (nbt) {
+    case 8: launch_contract_df<MODE, 8>(grid, smem, a, st); break;
+    case 4: launch_contract_df<MODE, 4>(grid, smem, a, st); break;
+    default: launch_contract_df<MODE, 2>(grid, smem, a, st); break;
+  }
+  S2G_LAUNCHED();
 }
 
 // ---------------------------------------------------------------------------
@@ -1636,15 +2074,31 @@ void ring_inverse_c(const double2 *spec, int64_t spec_stride, int64_t spec_map_s
   run_ring_inverse(a, nrings, false, st);
 }
 
+void release_df_tables() {
+  std::lock_guard<std::mutex> lk(g_dft_mu);
+  for (auto &kv : g_dft) cudaFree(kv.second);
+  g_dft.clear();
+  g_dft_bytes = 0;
+}
+size_t df_table_bytes() {
+  std::lock_guard<std::mutex> lk(g_dft_mu);
+  return g_dft_bytes;
+}
+void set_split_tables(int on) { g_split_tables.store(on ? 1 : 0); }
+int get_split_tables() { return g_split_tables.load(); }
+void set_df_max_maps(int maps) { g_df_max_maps.store(maps); }
+int get_df_max_maps() { return g_df_max_maps.load(); }
+
 void contract_l2t(const L2T &p, cudaStream_t st) {
   if (p.nb <= 0 || p.mhi < p.mlo) return;
   if (p.tb->rc) {
     contract_l2t_rc(p, st);
     return;
   }
-  if (t_precision == 1 && contract_l2t_mixed(&p, 1, st)) return;
+  if (t_precision == 1 && p.nb > df_max_maps() && contract_l2t_mixed(&p, 1, st)) return;
   ContractArgs a{};
   a.table = p.use_q ? p.tb->Q : p.tb->D;
+  if (t_precision == 1) a.table_df = df_table(*p.tb, p.use_q, st);
   a.off = p.tb->d_off;
   a.bl = p.tb->bl;
   a.nt = p.tb->nt;
@@ -1678,9 +2132,10 @@ void contract_t2l(const T2L &p, cudaStream_t st) {
     contract_t2l_rc(p, st);
     return;
   }
-  if (t_precision == 1 && contract_t2l_mixed(&p, 1, st)) return;
+  if (t_precision == 1 && p.nb > df_max_maps() && contract_t2l_mixed(&p, 1, st)) return;
   ContractArgs a{};
   a.table = p.use_q ? p.tb->Q : p.tb->D;
+  if (t_precision == 1) a.table_df = df_table(*p.tb, p.use_q, st);
   a.off = p.tb->d_off;
   a.bl = p.tb->bl;
   a.nt = p.tb->nt;
@@ -1706,15 +2161,111 @@ void contract_t2l(const T2L &p, cudaStream_t st) {
     launch_contract<3>(a, nm, a.bl, st);
 }
 
+// split precision, two scales of one band-limit and n on a stored table, a
+// batch the double-float kernel takes: both parts in one pass over the table
+bool df_pair_l2t(const L2T *a, cudaStream_t st) {
+  const L2T &p = a[0], &q = a[1];
+  if (p.tb != q.tb || p.tb->rc || p.use_q != q.use_q || p.n != q.n || p.mlo != q.mlo || p.mhi != q.mhi ||
+      p.xs != q.xs || p.xL != q.xL || p.x_half != q.x_half || p.wscale != q.wscale || p.wconj != q.wconj ||
+      p.os != q.os || p.ow != q.ow || p.omlo != q.omlo || p.nb != q.nb || p.nb > 4 || p.nb < 1 || p.mhi < p.mlo)
+    return false;
+  ContractArgs c{};
+  c.table = p.use_q ? p.tb->Q : p.tb->D;
+  c.table_df = df_table(*p.tb, p.use_q, st);
+  c.off = p.tb->d_off;
+  c.bl = p.tb->bl;
+  c.nt = p.tb->nt;
+  c.an = p.tb->an;
+  c.tmlo = p.tb->mlo;
+  c.n = p.n;
+  c.mlo = p.mlo;
+  c.lmin = p.lmin;
+  c.w = p.w;
+  c.wscale = p.wscale;
+  c.wconj = p.wconj;
+  c.src = p.x;
+  c.ss = p.xs;
+  c.sw_or_xL = p.xL;
+  c.x_half = p.x_half;
+  c.dst = p.out;
+  c.ds = p.os;
+  c.dw = p.ow;
+  c.d_mlo = p.omlo;
+  c.nb = p.nb;
+  c.nparts = 2;
+  c.src2 = q.x;
+  c.dst2 = q.out;
+  c.w2 = q.w;
+  c.lmin2 = q.lmin;
+  const int nm = p.mhi - p.mlo + 1;
+  if (p.use_q)
+    launch_contract_df_pair<1>(c, nm, c.nt, st);
+  else
+    launch_contract_df_pair<0>(c, nm, c.nt, st);
+  return true;
+}
+
+bool df_pair_t2l(const T2L *a, cudaStream_t st) {
+  const T2L &p = a[0], &q = a[1];
+  if (p.tb != q.tb || p.tb->rc || p.use_q != q.use_q || p.n != q.n || p.mlo != q.mlo || p.mhi != q.mhi ||
+      p.is != q.is || p.iw != q.iw || p.imlo != q.imlo || p.wscale != q.wscale || p.wconj != q.wconj ||
+      p.ys != q.ys || p.nb != q.nb || p.nb > 4 || p.nb < 1 || p.mhi < p.mlo)
+    return false;
+  ContractArgs c{};
+  c.table = p.use_q ? p.tb->Q : p.tb->D;
+  c.table_df = df_table(*p.tb, p.use_q, st);
+  c.off = p.tb->d_off;
+  c.bl = p.tb->bl;
+  c.nt = p.tb->nt;
+  c.an = p.tb->an;
+  c.tmlo = p.tb->mlo;
+  c.n = p.n;
+  c.mlo = p.mlo;
+  c.lmin = p.lmin;
+  c.w = p.w;
+  c.wscale = p.wscale;
+  c.wconj = p.wconj;
+  c.src = p.in;
+  c.ss = p.is;
+  c.sw_or_xL = p.iw;
+  c.s_mlo = p.imlo;
+  c.dst = p.y;
+  c.ds = p.ys;
+  c.nb = p.nb;
+  c.nparts = 2;
+  c.src2 = q.in;
+  c.dst2 = q.y;
+  c.w2 = q.w;
+  c.lmin2 = q.lmin;
+  const int nm = p.mhi - p.mlo + 1;
+  if (p.use_q)
+    launch_contract_df_pair<2>(c, nm, c.bl, st);
+  else
+    launch_contract_df_pair<3>(c, nm, c.bl, st);
+  return true;
+}
+
 void contract_l2t_group(const L2T *a, int n, cudaStream_t st) {
   if (n <= 0) return;
-  if (t_precision == 1 && n <= 2 && !a[0].tb->rc && contract_l2t_mixed(a, n, st)) return;
+  if (t_precision == 1 && n <= 2 && !a[0].tb->rc) {
+    if (a[0].nb > df_max_maps()) {
+      if (contract_l2t_mixed(a, n, st)) return;
+    } else if (n == 2 && df_pair_l2t(a, st)) {
+      return;
+    }
+  }
   for (int i = 0; i < n; ++i) contract_l2t(a[i], st);
 }
 
 void contract_t2l_group(const T2L *a, int n, cudaStream_t st) {
   if (n <= 0) return;
-  if (t_precision == 1 && n <= 2 && !a[0].tb->rc && contract_t2l_mixed(a, n, st)) return;
+  if (t_precision == 1 && n <= 2 && !a[0].tb->rc) {
+    if (a[0].nb > df_max_maps()) {
+      if (contract_t2l_mixed(a, n, st)) return;
+    } else if (n == 2 && df_pair_t2l(a, st)) {
+      return;
+    }
+  }
   for (int i = 0; i < n; ++i) contract_t2l(a[i], st);
 }
 

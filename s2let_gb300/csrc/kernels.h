@@ -66,6 +66,17 @@ struct L2T {
   int omlo;    // m of column 0
   int nb;
 };
+// double-float copies of the stored Wigner tables (split-precision
+// contractions on the FP32 pipe): freed with the plans; on/off switch
+void release_df_tables();
+size_t df_table_bytes();
+void set_split_tables(int on);
+int get_split_tables();
+// split precision: batches of at most this many maps (0-4) contract in
+// double-float on the FP64 tables instead of on the tensor cores
+void set_df_max_maps(int maps);
+int get_df_max_maps();
+
 void contract_l2t(const L2T &a, cudaStream_t st);
 // n problems on the same table (same band-limit, n, m range and batch): one
 // table pass on the split-precision path when n <= 2, else one call each.

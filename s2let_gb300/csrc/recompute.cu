@@ -385,11 +385,7 @@ __device__ void rescale_segment(double2 *cn, double2 *cs, const double *c2, doub
   __syncthreads();
 }
 
-// s += v x (double-float real times complex), the accumulator renormalised
-// after each add (unnormalised sums of 64-128 terms lost about 6 bits)
-__device__ __forceinline__ void df_mac(float4 &s, float2 v, float4 x) {
-  s = dmk(df_add_norm(dre(s), df_mul(v, dre(x))), df_add_norm(dim_(s), df_mul(v, dim_(x))));
-}
+
 
 template <int NBT>
 __global__ void __launch_bounds__(kRcT) k_rc_l2t_df(RcArgs a) {

@@ -8,7 +8,7 @@
 namespace s2g {
 
 enum KCat {
-  KC_CONTRACT = 0,  // FP64 Wigner/Legendre contractions
+  KC_CONTRACT = 0,  // Wigner/Legendre contractions on stored tables (FP64; double-float at split precision)
   KC_RING = 1,      // Bluestein ring DFTs
   KC_GAMMA = 2,     // gamma DFTs
   KC_MERGE = 3,     // tiling merge / split / symmetrise

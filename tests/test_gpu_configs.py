@@ -9,7 +9,8 @@
 * Directional, real, L=512, N=4, B=2, J_min=2 (multiresolution), FP64:
   px2wav / wav2px and both adjoints against the oracle.
 * Complex spin-2, L=1024, N=5, B=2, J_min=3: FP64 against the oracle on one
-  map, and the split-precision path against the FP64 path scale by scale.
+  map, and the split-precision path against the FP64 path scale by scale, on
+  one map and on a host batch of three.
 
 Inputs follow the benchmark spectra: complex Gaussian flm with C_l = (l+1)^-2
 (spin 0, real-field symmetry, f_00 = 0) or l^-2 for l >= 2 (spin 2),
@@ -187,14 +188,30 @@ def test_spin2_L1024_N5(gpu, oracle_port):
     assert rel_err(w64, w_o) < TOL and rel_err(s64, s_o) < TOL
     assert rel_err(fr64, oracle_port.wav2px(w_o, s_o, p)) < TOL
     assert rel_err(fr64, f) < TOL
-    # split precision against the FP64 path, scale by scale; the timing report
-    # shows that the tensor-core contraction ran
-    rep = (__import__("ctypes").c_double * 36)()
+    # split precision against the FP64 path, scale by scale: one map (double-
+    # float contractions on the FP64 tables), then a host batch of three maps
+    # (f, -f, f/2), whose contractions the timing report shows on the tensor
+    # cores
+    import ctypes as C
+
+    from s2let_gb300.capi import ptr
+
+    rep = (C.c_double * 36)()
+    s = gpu.sizes(p)
+    fb = np.ascontiguousarray(np.stack([f, -f, 0.5 * f]))
+    scale = np.array([1.0, -1.0, 0.5])[:, None]
+    wb = np.zeros((3, s["n_wav"]), np.complex128)
+    sb = np.zeros((3, s["n_scal"]), np.complex128)
+    rb = np.zeros_like(fb)
+    wb64 = np.ascontiguousarray(w64[None, :] * scale)
+    sb64 = np.ascontiguousarray(s64[None, :] * scale)
     assert lib.s2let_gpu_set_precision(1) == 0
     try:
-        lib.s2let_gpu_timing_enable(1)
         wmx, smx = gpu.px2wav(f, p)
         frmx = gpu.wav2px(w64, s64, p)
+        lib.s2let_gpu_timing_enable(1)
+        assert lib.s2let_gpu_analysis_px2wav_host_batch(ptr(wb), ptr(sb), ptr(fb), 3, C.byref(p)) == 0
+        assert lib.s2let_gpu_synthesis_wav2px_host_batch(ptr(rb), ptr(wb64), ptr(sb64), 3, C.byref(p)) == 0
         lib.s2let_gpu_timing_report(rep, 9)
         lib.s2let_gpu_timing_enable(0)
     finally:
@@ -204,6 +221,12 @@ def test_spin2_L1024_N5(gpu, oracle_port):
     for j, off, n in _scales(gpu, p):
         e = rel_err(wmx[off:off + n], w64[off:off + n])
         assert e < TOL_MIXED, f"scale {j}: {e:.3e}"
+        for b in range(3):
+            e = rel_err(wb[b, off:off + n], wb64[b, off:off + n])
+            assert e < TOL_MIXED, f"map {b} scale {j}: {e:.3e}"
     assert rel_err(smx, s64) < TOL_MIXED
     assert rel_err(frmx, fr64) < TOL_MIXED
+    for b in range(3):
+        assert rel_err(sb[b], sb64[b]) < TOL_MIXED, b
+        assert rel_err(rb[b], fr64 * scale[b, 0]) < TOL_MIXED, b
     _release(gpu)

@@ -1,9 +1,10 @@
 """Ring DFTs fused with the gamma DFT (split-precision path).
 
-Below band-limit 128 the split-precision path keeps the FP64 contraction, so
-at these band-limits precision 1 and precision 0 differ only in the ring and
-gamma DFTs: double-float (the fused thread-block-cluster launch, one CTA per
-n-component) against FP64 (separate launches).  Every directional operator
+Below band-limit 128 the split-precision path contracts in double-float on
+the FP64 tables (no bf16 digits), so at these band-limits precision 1 and
+precision 0 differ in double-float arithmetic only: the ring and gamma DFTs
+(the fused thread-block-cluster launch, one CTA per n-component, against
+separate FP64 launches) and the contractions.  Every directional operator
 must agree to 1e-12 normwise relative max error.  The cases cover every
 cluster size (2-8 n-components), real signals with and without the n = 0
 component, complex signals of spin 0-2, full resolution and multiresolution,
