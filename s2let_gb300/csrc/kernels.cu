@@ -879,24 +879,24 @@ __global__ void __launch_bounds__(CT_M) k_contract_df(ContractArgs a) {
   const bool bon = mt < a.nb;
   const int lpt = pt ? a.lmin2 : a.lmin;
   const int lst_t = l0 > lpt ? l0 : lpt;
+  // The weighted FP64 values go to the same 16-byte slots first and are split
+  // in place once the column scale is known (each slot by the thread that
+  // wrote it), so the FP64 weighting runs once per coefficient.
   if (threadIdx.x < NBT) sxm[threadIdx.x] = 0;
   __syncthreads();
+  double2 *sxd = reinterpret_cast<double2 *>(sx);
   int emax = 0;
-  if (bon)
-    for (int i = threadIdx.x; i < K * NBT; i += CT_M) {
-      const int k = kbeg + i / NBT;
-      if (L2T && k < lst_t) continue;
-      const double2 v = contract_coef<L2T>(a, pt, m, am, k, mt);
-      emax = max(emax, max(exp_field(v.x), exp_field(v.y)));
-    }
+  for (int i = threadIdx.x; i < K * NBT; i += CT_M) {
+    const int k = kbeg + i / NBT;
+    double2 v = make_double2(0.0, 0.0);
+    if (bon && !(L2T && k < lst_t)) v = contract_coef<L2T>(a, pt, m, am, k, mt);
+    sxd[i] = v;
+    emax = max(emax, max(exp_field(v.x), exp_field(v.y)));
+  }
   atomicMax(&sxm[bt], emax);
   __syncthreads();
   const int es = block_scale(sxm[bt]);
-  for (int i = threadIdx.x; i < K * NBT; i += CT_M) {
-    const int k = kbeg + i / NBT;
-    sx[i] = (bon && !(L2T && k < lst_t)) ? dc_split(contract_coef<L2T>(a, pt, m, am, k, mt), es)
-                                         : make_float4(0.f, 0.f, 0.f, 0.f);
-  }
+  for (int i = threadIdx.x; i < K * NBT; i += CT_M) sx[i] = dc_split(sxd[i], es);
   __syncthreads();
   int eo[NBT];
 #pragma unroll

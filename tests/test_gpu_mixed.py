@@ -140,7 +140,7 @@ def test_mixed_host_batch(gpu, nb, df_max):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L,N,spin,real,ss", [(192, 4, 0, True, 0), (160, 3, 1, False, 1)])
+@pytest.mark.parametrize("L,N,spin,real,ss", [(192, 4, 0, True, 0), (160, 3, 1, False, 1), (320, 4, 0, True, 0)])
 def test_df_contraction_table_copies(gpu, L, N, spin, real, ss):
     """One-map calls at split precision contract in double-float on the FP32
     pipe: on double-float copies of the Wigner tables (the default), or
