@@ -729,24 +729,26 @@ __global__ void __launch_bounds__(CT_M) k_contract(ContractArgs a) {
 
 // The same contractions in double-float on the FP32 pipe (split-precision
 // path: every contraction the tensor-core kernel does not take, and batches of
-// one or two maps, for which streaming the tables' 7 bf16 digit panels (14 B
-// per entry) costs more than reading the FP64 tables (8 B per entry) and
+// at most df_max_maps() maps, for which streaming the tables' 7 bf16 digit
+// panels (14 B per entry) costs more than reading 8 B per entry and
 // multiplying in double-float).
 //
-// The CTA first splits its (m, map) coefficient columns over the whole
-// reduction range into double-float pairs in shared memory, one power-of-two
-// scale per map (|x| 2^-e < 1).  Table values (|d| <= 1) are split as they
-// are read (df_split_unit).  Products are summed as in Ogita, Rump and Oishi's
-// Dot2 (SIAM J. Sci. Comput. 26, 2005): a float sum s carried by TwoSum, its
-// rounding errors and the products' low parts gathered in a second float c,
-// so that s + c is the sum as if computed in twice the working precision;
-// (s + c) 2^e is widened to FP64 once per output.
+// A CTA owns one m and up to 128 output rows.  It first splits its coefficient
+// columns (maps x parts; a second part is another scale on the same table)
+// over the whole reduction range into double-float pairs in shared memory,
+// one power-of-two scale per column (|x| 2^-e < 1).  Table values (|d| <= 1)
+// come from the double-float copy of the table (df_table) or are split from
+// FP64 as they are read (df_split_unit).  Products are summed as in Ogita,
+// Rump and Oishi's Dot2 (SIAM J. Sci. Comput. 26, 2005): a float sum s carried
+// by TwoSum, its rounding errors and the products' low parts gathered in a
+// second float c, so that s + c is the sum as if computed in twice the working
+// precision; (s + c) 2^e is widened to FP64 once per output.
 //   MODE 1, 3 (table contiguous along the output rows): one thread per row,
 //   each step of the reduction a coalesced warp-wide row of the table.
-//   MODE 0, 2 (table contiguous along the reduction axis): a warp takes
-//   DFC_R rows at a time with its lanes along the reduction axis (coalesced
-//   256-byte row segments, DFC_R loads in flight per lane), then reduces the
-//   lanes' partial sums by butterfly shuffles.
+//   MODE 0, 2 (table contiguous along the reduction axis): groups of DFC_LPR
+//   lanes along the reduction axis, one row per group and several rows per
+//   lane, the next step's table loads issued before the current step's
+//   arithmetic; the groups' partial sums are reduced by butterfly shuffles.
 
 // v (|v| <= 1 or zero) as hi + lo: the top 24 and next 23 significand bits
 // (truncated: |hi + lo - v| < 2^-46 |v|); |v| < 2^-103 gives 0
