@@ -149,6 +149,27 @@ def test_precision_mode_switch(lib):
     assert lib.s2let_gpu_set_precision(0) == 0
 
 
+def test_double_float_contraction_switches(lib):
+    """The batch limit of the double-float contraction (0-4 maps) and the
+    double-float table copies (0/1): out-of-range values are refused with
+    S2LET_GPU_ERR_INVALID and leave the setting unchanged."""
+    old_max, old_tab = lib.s2let_gpu_get_df_max_maps(), lib.s2let_gpu_get_split_tables()
+    try:
+        for n in (0, 4, 2):
+            assert lib.s2let_gpu_set_df_max_maps(n) == 0
+            assert lib.s2let_gpu_get_df_max_maps() == n
+        assert lib.s2let_gpu_set_df_max_maps(5) == 1 and lib.s2let_gpu_set_df_max_maps(-1) == 1
+        assert lib.s2let_gpu_get_df_max_maps() == 2
+        for on in (0, 1):
+            assert lib.s2let_gpu_set_split_tables(on) == 0
+            assert lib.s2let_gpu_get_split_tables() == on
+        assert lib.s2let_gpu_set_split_tables(2) == 1
+        assert lib.s2let_gpu_get_split_tables() == 1
+    finally:
+        lib.s2let_gpu_set_df_max_maps(old_max)
+        lib.s2let_gpu_set_split_tables(old_tab)
+
+
 RELINK = r"""
 /* A caller written against the reference's API (s2let.h), relinked against
    libs2let_gpu: allocation helpers, sizes, the tiling, and a transform whose
