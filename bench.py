@@ -79,7 +79,7 @@ def args_():
     ap.add_argument("--B", type=float, default=2.0)
     ap.add_argument("--J_min", type=int, default=2)
     ap.add_argument("--workload", default="metric",
-                    choices=["metric", "spin2", "sparsity", "uneven", "L2048", "axisym", "harmonic"],
+                    choices=["metric", "spin2", "sparsity", "uneven", "L2048", "axisym", "harmonic", "batches"],
                     help="metric: the headline (real maps, L=1024, N=4); spin2: complex spin-2 maps, "
                          "L=1024, N=5, J_min=3, error per scale; sparsity: differentiable wavelet-sparsity "
                          "loss, 32 real maps at L=256, forward + backward; uneven: 256 maps of their own L, N "
@@ -87,7 +87,8 @@ def args_():
                          "at L=2048, N=4 with recomputed Wigner tables; axisym: axisymmetric lm and MW "
                          "transforms of one real map at L=128, J_min=0, full resolution, through the drop-in "
                          "calls (the oracle timed beside them); harmonic: lm2wav + wav2lm of one real map at "
-                         "L=1024, N=4 through the drop-in calls, split precision against FP64")
+                         "L=1024, N=4 through the drop-in calls, split precision against FP64; batches: the "
+                         "metric unit at batch sizes 1, 8 and 64, split precision and FP64")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -463,6 +464,45 @@ def run_workload(a, world, rank, local):
                           "ms_per_step": res["fp64"], "speedup_mixed_over_fp64": res["fp64"] / res["mixed"]},
             "max_rel_err_vs_fp64": {"f_wav_per_scale": per_scale, "f_scal": rel(s1, s0),
                                     "wav2px_round_trip": rel(r1, f)},
+            "clocks": clk,
+        })
+    elif a.workload == "batches":
+        # the metric unit at batch sizes 1, 8 and 64, both paths, inputs in HBM
+        L = a.L
+        p = make_parameters(L, a.B, a.J_min, a.N, 0, 0)
+        rng = np.random.default_rng(replica_seed(rank))
+        lib.s2let_gpu_set_precision(0)
+        base = np.stack([api.alm2map(power_law_real_flm(rng, L), L, real=True) for _ in range(8)])
+        by_batch, clk = {}, None
+        for nb in (1, 8, 64):
+            f = torch.tensor(np.concatenate([base] * (nb // 8 or 1))[:nb], device=dev)
+            row = {}
+            for prec in ("mixed", "fp64"):
+                def step():
+                    w, sc = T.px2wav(f, p, precision=prec)
+                    T.wav2px(w, sc, p, precision=prec)
+                for _ in range(a.warmup):
+                    step()
+                steps = a.steps if prec == "mixed" or nb <= 8 else max(1, min(a.steps, 3))
+                if prec == "mixed" and nb == 64:
+                    clocks.start()
+                ms = max_over_ranks(event_ms(step, steps), None)
+                if prec == "mixed" and nb == 64:
+                    clk = clocks.stop()
+                row[prec] = {"value": whole_job_rate(nb, world, ms * 1e-3), "ms_per_step": ms, "steps": steps}
+            row["speedup_mixed_over_fp64"] = row["fp64"]["ms_per_step"] / row["mixed"]["ms_per_step"]
+            by_batch[str(nb)] = row
+            del f
+            torch.cuda.empty_cache()
+        out.update({
+            "metric": f"px2wav+wav2px maps/s at L={L}, N={a.N} by batch size (1, 8, 64; split precision and FP64)",
+            "value": by_batch["64"]["mixed"]["value"], "unit": "maps/s",
+            "ms_per_step": by_batch["64"]["mixed"]["ms_per_step"], "dtype": "bf16-split/f32-acc/f64",
+            "config": {"workload": f"real spin-0 maps, L={L}, N={a.N}, B={a.B:g}, J_min={a.J_min}, upsample=0, MW; "
+                                   "value: batch 64, split precision; one map per call takes the double-float "
+                                   "contraction, batches of more the tensor cores",
+                       "l2": "f_wav of one map (34.2 M doubles at L=1024) exceeds L2"},
+            "by_batch": by_batch,
             "clocks": clk,
         })
     else:
